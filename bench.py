@@ -1,0 +1,386 @@
+"""Benchmark of the sketching hot path on GB300.
+
+Headline workload (one "step" = one sketch): B = S A with S a 4096 x 2^20 uniform dense
+operator (seed RNGState(3)) generated inside the kernel, A a 2^20 x 1024 FP32 row-major matrix
+with singular values decaying geometrically from 1 to 1e-6 (random orthogonal factors from a
+seeded QR), d = 4096.  Reported as TFLOP/s of 2*d*m*n, for the tensor-core path (S and A
+rounded to BF16, FP32 accumulation) when the library provides it, next to the plain FP32
+path on the same GPU.  Secondary: the 1024 x 2^20 SASO (8 nonzeros per column) sketch of a
+2^20 x 256 N(0,1) matrix, reported in GB/s against the measured HBM copy bandwidth.
+
+python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+Under torchrun (N > 1) every rank runs an independent replica (the path needs no exchange
+between GPUs); the line reports the max time over ranks and the aggregate throughput.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "S·A sketch time and roofline fraction: BF16-TC fused vs FP32 plain, same GPU"
+D_SK, M_SK, N_SK = 4096, 1 << 20, 1024
+SASO_D, SASO_M, SASO_N, SASO_K = 1024, 1 << 20, 256, 8
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return p["hbm_gbs"], p["bf16_tflops"], p.get("bf16_tflops_sustained"), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, 1900.0, 1700.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms while running."""
+
+    def __init__(self, index: int):
+        self.index = index
+        self.rows = []
+        self.proc = None
+
+    def __enter__(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={q}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 9:
+                self.rows.append(parts)
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in self.rows for i in range(4)
+                          if r[5 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
+                "samples": len(self.rows)}
+
+
+# ----------------------------------------------------------------------------- workload
+def make_precision_input(torch, device):
+    """A = U diag(sigma) V^T, 2^20 x 1024 FP32 row-major, sigma_i = 10^(-6 i / 1023)."""
+    g0 = torch.Generator(device=device).manual_seed(0)
+    g1 = torch.Generator(device=device).manual_seed(1)
+    U, _ = torch.linalg.qr(torch.randn(M_SK, N_SK, generator=g0, device=device))
+    V, _ = torch.linalg.qr(torch.randn(N_SK, N_SK, generator=g1, device=device,
+                                       dtype=torch.float64))
+    sigma = torch.logspace(0, -6, N_SK, dtype=torch.float64, device=device)
+    A = (U * sigma.float()) @ V.T.float()
+    return A.contiguous(), U
+
+
+def event_time(torch, fn, steps, warmup, stream):
+    for _ in range(warmup):
+        fn()
+    torch.cuda.synchronize()
+    start = torch.cuda.Event(enable_timing=True)
+    stop = torch.cuda.Event(enable_timing=True)
+    start.record(stream)
+    for _ in range(steps):
+        fn()
+    stop.record(stream)
+    torch.cuda.synchronize()
+    return start.elapsed_time(stop) / steps
+
+
+# ----------------------------------------------------------------------------- CPU baseline
+def cpu_precision_sample(rows: int, A_host):
+    """The reference's CPU path on a row block of the operator: the oracle's OpenMP port of
+    fill_dense_unpacked (the 4096 x 2^20 uniform operator, rows [0, rows)) followed by an
+    OpenBLAS SGEMM -- what the reference does (materialise the submatrix, blas::gemm)."""
+    import ctypes as C
+
+    import numpy as np
+
+    from oracle.oracle import Oracle, State, find_cblas
+    orc = Oracle()
+    blas, sgemm, _ = find_cblas()
+    t0 = time.perf_counter()
+    Sblk, _ = orc.fill_dense_unpacked(0, 1, D_SK, M_SK, 1, 1, rows, M_SK, 0, 0,
+                                      State.from_key(3))
+    B = np.zeros((rows, N_SK), np.float32)
+    if sgemm:
+        fn = C.CFUNCTYPE(None, C.c_int, C.c_int, C.c_int, C.c_int64, C.c_int64, C.c_int64,
+                         C.c_float, C.c_void_p, C.c_int64, C.c_void_p, C.c_int64, C.c_float,
+                         C.c_void_p, C.c_int64)(sgemm)
+        fn(101, 111, 111, rows, N_SK, M_SK, 1.0, Sblk.ctypes.data, M_SK, A_host.ctypes.data,
+           N_SK, 0.0, B.ctypes.data, N_SK)
+    else:
+        B[:] = Sblk.reshape(rows, M_SK) @ A_host
+    return time.perf_counter() - t0
+
+
+# ----------------------------------------------------------------------------- main
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--cpu-rows", type=int, default=128,
+                    help="operator rows of the bounded CPU-baseline sample")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+
+    if args.impl == "reference":
+        return run_reference(args, rank, world)
+
+    import torch
+    import torch.distributed as dist
+
+    torch.cuda.set_device(local)
+    if world > 1:
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    device = torch.device("cuda", local)
+    from randblas_gb300 import build as rbuild
+    if rank == 0:
+        rbuild.build()
+    if world > 1:
+        dist.barrier()
+    import randblas_gb300 as rb
+    from randblas_gb300 import lowp
+    stream = torch.cuda.current_stream()
+    hbm, bf16_burst, bf16_sus, peak_kind = peaks()
+
+    A, U = make_precision_input(torch, device)
+    S = rb.DenseSkOp(rb.DenseDist(D_SK, M_SK, rb.ScalarDist.Uniform), rb.RNGState(3))
+    B = torch.empty(D_SK, N_SK, device=device)
+    flops = 2.0 * D_SK * M_SK * N_SK
+
+    have_lowp = lowp.available()
+
+    def plain():
+        rb.sketch_general(rb.Layout.RowMajor, rb.Op.NoTrans, rb.Op.NoTrans, D_SK, N_SK, M_SK,
+                          1.0, S, A, N_SK, 0.0, B, N_SK)
+
+    def fused():
+        lowp.sketch_lowp(rb.Layout.RowMajor, rb.Op.NoTrans, rb.Op.NoTrans, D_SK, N_SK, M_SK,
+                         1.0, S, 0, 0, A, N_SK, 0.0, B, N_SK)
+
+    headline = fused if have_lowp else plain
+    # plain FP32 path on the same GPU (fewer steps: it is the slow arm)
+    plain_steps = max(1, min(args.steps, 3))
+    ms_plain = event_time(torch, plain, plain_steps, 1, stream)
+
+    lib = rb.lib()
+    rb.profile.enable(True)
+    launches0 = lib.rbg_kernel_launches()
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        ms = event_time(torch, headline, args.steps, args.warmup, stream)
+    launches = (lib.rbg_kernel_launches() - launches0)
+    prof = rb.profile.read()
+    rb.profile.enable(False)
+    per_step_launches = launches / (args.steps + args.warmup)
+    gpu_launches = int(round(per_step_launches * args.steps))
+
+    # accuracy of the headline result against an FP64 oracle on sampled row blocks
+    headline()
+    torch.cuda.synchronize()
+    err_num, err_den = 0.0, 0.0
+    for r0 in (0, 1024, 2048, 4032):
+        Sblk = torch.empty(64 * M_SK, dtype=torch.float64, device=device)
+        rb.fill_dense_unpacked(rb.Layout.RowMajor, S.dist, 64, M_SK, r0, 0, Sblk, S.seed_state)
+        ref = Sblk.view(64, M_SK) @ A.double()
+        err_num += float(torch.linalg.norm(B[r0:r0 + 64].double() - ref) ** 2)
+        err_den += float(torch.linalg.norm(ref) ** 2)
+        del Sblk, ref
+    rel_err = (err_num / err_den) ** 0.5
+
+    # roofline of the dominant kernel
+    main_kernel = max(prof, key=lambda k: prof[k]["ms"]) if prof else None
+    if main_kernel:
+        kms = prof[main_kernel]["ms"] / max(1, prof[main_kernel]["launches"])
+        achieved = flops / (kms * 1e-3) / 1e12
+    else:
+        kms, achieved = ms, flops / (ms * 1e-3) / 1e12
+    peak = bf16_burst if have_lowp else derived_fp32_peak(torch, clk.summary())
+    roofline = {"bound": "tensor", "achieved": round(achieved, 1), "peak": round(peak, 1),
+                "unit": "TFLOP/s", "frac": round(achieved / peak, 4), "traffic": None,
+                "kernel": main_kernel, "kernel_ms": round(kms, 4),
+                "peak_source": ("bf16 burst, " + peak_kind) if have_lowp else
+                "FP32 CUDA-core peak derived as SMs x 128 lanes x 2 x median SM clock"}
+
+    # secondary: SASO sketch (HBM-bound)
+    saso = bench_saso(torch, rb, device, args, stream, hbm)
+
+    # end to end through the C ABI with host buffers
+    e2e = None
+    A_host = None
+    if not args.no_e2e or (rank == 0 and not args.no_cpu):
+        A_host = A.cpu().pin_memory() if not args.no_e2e else A.cpu()
+    if not args.no_e2e:
+        e2e = bench_e2e(torch, rb, lowp, have_lowp, S, A_host, args, stream, flops, device)
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        t = cpu_precision_sample(args.cpu_rows, A_host.numpy())
+        full_s = t * D_SK / args.cpu_rows
+        cpu = {"value": round(flops / full_s / 1e12, 5), "unit": "TFLOP/s",
+               "cores": os.cpu_count(), "kind": "port",
+               "sample": f"operator rows [0,{args.cpu_rows}) of 4096 (oracle OpenMP fill + "
+                         f"OpenBLAS SGEMM), {t:.2f} s, scaled by {D_SK // args.cpu_rows}",
+               "ms_per_sketch": round(full_s * 1e3, 1)}
+
+    # aggregate over ranks
+    ms_max = ms
+    if world > 1:
+        tt = torch.tensor([ms], device=device)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        ms_max = float(tt.item())
+    value = world * flops / (ms_max * 1e-3) / 1e12
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": round(value, 2), "unit": "TFLOP/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_max, 4),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "bf16" if have_lowp else "f32", "data": "synthetic",
+            "config": {"workload": "uniform DenseDist 4096 x 2^20 (seed RNGState(3)) left sketch "
+                                   "of a 2^20 x 1024 FP32 row-major matrix, singular values "
+                                   "1 -> 1e-6",
+                       "d": D_SK, "m": M_SK, "n": N_SK,
+                       "path": "bf16 tensor-core fused" if have_lowp else "fp32 plain",
+                       "l2": "inputs larger than L2 (A is 4.3 GB)",
+                       "parallelism": f"replicas x{world}"},
+            "fp32_plain": {"ms_per_step": round(ms_plain, 3),
+                           "TFLOP/s": round(flops / (ms_plain * 1e-3) / 1e12, 2)},
+            "speedup_vs_fp32_plain": round(ms_plain / ms_max, 2),
+            "rel_frobenius_err_vs_fp64": rel_err,
+            "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
+            "gpu_launches": gpu_launches, "clocks": clk.summary(), "saso": saso,
+        }
+        print(json.dumps(line))
+    if world > 1:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+def derived_fp32_peak(torch, clocks):
+    props = torch.cuda.get_device_properties(torch.cuda.current_device())
+    mhz = clocks.get("sm_mhz") or 2070.0
+    return props.multi_processor_count * 128 * 2 * mhz * 1e6 / 1e12
+
+
+def bench_saso(torch, rb, device, args, stream, hbm):
+    m, d, n = SASO_M, SASO_D, SASO_N
+    A = torch.empty(m * n, dtype=torch.float32, device=device)
+    nxt = rb.fill_dense(rb.DenseDist(m, n, rb.ScalarDist.Gaussian, rb.Axis.Short), A,
+                        rb.RNGState(0))
+    S = rb.SparseSkOp(rb.SparseDist(d, m, SASO_K), nxt)
+    B = torch.empty(d * n, dtype=torch.float32, device=device)
+
+    def step():
+        rb.sketch_general(rb.Layout.RowMajor, rb.Op.NoTrans, rb.Op.NoTrans, d, n, m, 1.0, S, A,
+                          n, 0.0, B, n)
+    rb.profile.enable(True)
+    ms = event_time(torch, step, args.steps, args.warmup, stream)
+    prof = rb.profile.read()
+    rb.profile.enable(False)
+    algo = 4.0 * m * n + 4.0 * d * n
+    out = {"workload": "SASO 1024 x 2^20, 8 nnz/col, sampled in the sketch; A 2^20 x 256 FP32",
+           "ms_per_step": round(ms, 4), "GB/s": round(algo / (ms * 1e-3) / 1e9, 1),
+           "frac_of_hbm": round(algo / (ms * 1e-3) / 1e9 / hbm, 4),
+           "kernels_ms": {k: round(v["ms"] / max(1, v["launches"]), 4) for k, v in prof.items()}}
+    del A, B
+    return out
+
+
+def bench_e2e(torch, rb, lowp, have_lowp, S, A_host, args, stream, flops, device):
+    """Same sketch through the public API with host buffers: per step, copy A from pinned host
+    memory, sketch, copy B back."""
+    A_dev = torch.empty(M_SK, N_SK, device=device)
+    B_dev = torch.empty(D_SK, N_SK, device=device)
+    B_host = torch.empty(D_SK, N_SK, pin_memory=True)
+
+    def step():
+        A_dev.copy_(A_host, non_blocking=True)
+        if have_lowp:
+            lowp.sketch_lowp(rb.Layout.RowMajor, rb.Op.NoTrans, rb.Op.NoTrans, D_SK, N_SK, M_SK,
+                             1.0, S, 0, 0, A_dev, N_SK, 0.0, B_dev, N_SK)
+        else:
+            rb.sketch_general(rb.Layout.RowMajor, rb.Op.NoTrans, rb.Op.NoTrans, D_SK, N_SK, M_SK,
+                              1.0, S, A_dev, N_SK, 0.0, B_dev, N_SK)
+        B_host.copy_(B_dev, non_blocking=True)
+    steps = max(1, min(args.steps, 5))
+    ms = event_time(torch, step, steps, 1, stream)
+    return {"value": round(flops / (ms * 1e-3) / 1e12, 2), "unit": "TFLOP/s",
+            "ms_per_step": round(ms, 3), "h2d_bytes_per_step": M_SK * N_SK * 4,
+            "d2h_bytes_per_step": D_SK * N_SK * 4}
+
+
+def run_reference(args, rank, world):
+    """The reference's CPU path (the oracle's OpenMP port of the operator fill plus OpenBLAS
+    SGEMM, as RandBLAS materialises the submatrix and calls blas::gemm), each step a bounded
+    row block of the same workload, extrapolated to the full sketch."""
+    if rank != 0:
+        return
+    import numpy as np
+    rng = np.random.default_rng(0)
+    # the CPU arm needs A on the host; the exact singular spectrum does not change its cost
+    A_host = rng.standard_normal((M_SK, N_SK), dtype=np.float32)
+    for _ in range(max(0, min(args.warmup, 1))):
+        cpu_precision_sample(16, A_host)
+    times = [cpu_precision_sample(args.cpu_rows, A_host) for _ in range(args.steps)]
+    t = statistics.median(times)
+    full_s = t * D_SK / args.cpu_rows
+    flops = 2.0 * D_SK * M_SK * N_SK
+    value = flops / full_s / 1e12
+    line = {"impl": "reference", "metric": METRIC, "value": round(value, 5), "unit": "TFLOP/s",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": round(full_s * 1e3, 1), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "uniform DenseDist 4096 x 2^20 (seed RNGState(3)) left sketch "
+                                   "of a 2^20 x 1024 FP32 row-major matrix",
+                       "d": D_SK, "m": M_SK, "n": N_SK},
+            "cpu_baseline": {"value": round(value, 5), "unit": "TFLOP/s",
+                             "cores": os.cpu_count(), "kind": "port",
+                             "sample": f"operator rows [0,{args.cpu_rows}) per step, scaled by "
+                                       f"{D_SK // args.cpu_rows}"},
+            "e2e": {"value": round(value, 5), "unit": "TFLOP/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+if __name__ == "__main__":
+    main()

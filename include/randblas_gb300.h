@@ -1,0 +1,312 @@
+/*
+ * randblas_gb300.h -- C ABI of the GB300 (sm_103a) sketching library.
+ *
+ * This is the drop-in boundary for RandBLAS's sketching hot path.  Every entry point takes
+ * plain pointers and sizes; matrix/vector buffers are DEVICE pointers unless stated
+ * otherwise, and every call is asynchronous on the given CUDA stream (NULL = the legacy
+ * default stream) unless its comment says it synchronises.  Each declaration names the
+ * reference interface it replaces (paths relative to the RandBLAS source tree).
+ *
+ * Conventions (numeric values shared with the reference's enums' meaning):
+ *   layout  RBG_COL_MAJOR / RBG_ROW_MAJOR     blas::Layout
+ *   op      RBG_NO_TRANS / RBG_TRANS           blas::Op
+ *   family  RBG_GAUSSIAN / RBG_UNIFORM         RandBLAS::ScalarDist (RandBLAS/dense_skops.hh:215-224)
+ *   axis    RBG_AXIS_SHORT / RBG_AXIS_LONG     RandBLAS::Axis (RandBLAS/base.hh:306-312)
+ *   dtype   RBG_F32 / RBG_F64                  the template parameter T
+ *   itype   RBG_I32 / RBG_I64                  the template parameter sint_t
+ *
+ * Errors: every entry point returns RBG_SUCCESS (0) or a status code; rbg_last_error()
+ * returns a thread-local message.  Argument checks that the reference performs with
+ * randblas_require (RandBLAS/exceptions.hh:152-162) return RBG_ERROR_INVALID_ARGUMENT
+ * with the reference's message text "<cond> was required, but did not hold, in
+ * function <f>"; integer overflow of a size product (RandBLAS/base.hh:260-274) returns
+ * RBG_ERROR_OVERFLOW.
+ */
+#ifndef RANDBLAS_GB300_H
+#define RANDBLAS_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Same object as cudaStream_t; declared here so the header needs no CUDA include. */
+typedef struct CUstream_st *rbg_stream_t;
+
+enum { RBG_COL_MAJOR = 0, RBG_ROW_MAJOR = 1 };
+enum { RBG_NO_TRANS = 0, RBG_TRANS = 1 };
+enum { RBG_GAUSSIAN = 0, RBG_UNIFORM = 1 };
+enum { RBG_AXIS_SHORT = 0, RBG_AXIS_LONG = 1 };
+enum { RBG_F32 = 0, RBG_F64 = 1 };
+enum { RBG_I32 = 0, RBG_I64 = 1 };
+enum { RBG_COO = 0, RBG_CSR = 1, RBG_CSC = 2 };
+enum { RBG_PREC_BF16 = 0, RBG_PREC_FP8_E4M3 = 1 };
+
+enum {
+    RBG_SUCCESS = 0,
+    RBG_ERROR_INVALID_ARGUMENT = 1, /* RandBLAS::Error from randblas_require */
+    RBG_ERROR_OVERFLOW = 2,         /* std::overflow_error from safe_int_product */
+    RBG_ERROR_CUDA = 3,             /* a CUDA runtime call or kernel launch failed */
+    RBG_ERROR_TIMEOUT = 4,          /* a bounded device-side wait gave up */
+    RBG_ERROR_UNSUPPORTED = 5,      /* valid in the reference, not provided by this library */
+    RBG_ERROR_ALLOC = 6             /* device memory allocation failed */
+};
+
+/* RNGState<Philox4x32> (RandBLAS/base.hh:64-164): 128-bit counter as four little-endian
+ * 32-bit words and a 64-bit key as two. */
+typedef struct rbg_state {
+    uint32_t counter[4];
+    uint32_t key[2];
+} rbg_state;
+
+/* DenseDist (RandBLAS/dense_skops.hh:231-350). */
+typedef struct rbg_dense_dist {
+    int64_t n_rows;
+    int64_t n_cols;
+    int32_t family;     /* RBG_GAUSSIAN (default) or RBG_UNIFORM */
+    int32_t major_axis; /* RBG_AXIS_LONG (default) or RBG_AXIS_SHORT */
+} rbg_dense_dist;
+
+/* DenseSkOp<T> (RandBLAS/dense_skops.hh:357-478).  buff == NULL means "not materialised":
+ * sketching calls then generate the entries they need on the fly, inside the kernel. */
+typedef struct rbg_dense_skop {
+    rbg_dense_dist dist;
+    rbg_state seed_state;
+    rbg_state next_state;
+    int32_t dtype;  /* RBG_F32 / RBG_F64 */
+    int32_t layout; /* layout of buff; the dist's natural layout by default */
+    void *buff;     /* device pointer, n_rows * n_cols entries, or NULL */
+} rbg_dense_skop;
+
+/* SparseDist (RandBLAS/sparse_skops.hh:131-246). */
+typedef struct rbg_sparse_dist {
+    int64_t n_rows;
+    int64_t n_cols;
+    int64_t vec_nnz;    /* default 4 */
+    int32_t major_axis; /* RBG_AXIS_SHORT (SASO, default) or RBG_AXIS_LONG (LASO) */
+    int32_t reserved;
+} rbg_sparse_dist;
+
+/* SparseSkOp<T, RNG, sint_t> (RandBLAS/sparse_skops.hh:289-450).  nnz < 0 means "not
+ * sampled": sketching calls then sample it themselves (SASOs inside the kernel). */
+typedef struct rbg_sparse_skop {
+    rbg_sparse_dist dist;
+    rbg_state seed_state;
+    rbg_state next_state;
+    int64_t nnz;
+    int32_t dtype;
+    int32_t itype;
+    void *vals; /* device pointers, dist.vec_nnz * dim_minor entries each */
+    void *rows;
+    void *cols;
+} rbg_sparse_skop;
+
+/* COOMatrix / CSRMatrix / CSCMatrix views (RandBLAS/sparse_data/coo_matrix.hh:82-308,
+ * csr_matrix.hh:73-245, csc_matrix.hh:73-244), zero-based indices, device pointers.
+ *   COO: idx_a = rows (nnz),        idx_b = cols (nnz)
+ *   CSR: idx_a = rowptr (n_rows+1), idx_b = colidxs (nnz)
+ *   CSC: idx_a = colptr (n_cols+1), idx_b = rowidxs (nnz) */
+typedef struct rbg_spmat {
+    int32_t format; /* RBG_COO / RBG_CSR / RBG_CSC */
+    int32_t dtype;
+    int32_t itype;
+    int32_t reserved;
+    int64_t n_rows;
+    int64_t n_cols;
+    int64_t nnz;
+    const void *vals;
+    const void *idx_a;
+    const void *idx_b;
+} rbg_spmat;
+
+/* ------------------------------------------------------------------ library */
+
+/* Message of the last failed call on this host thread ("" if none). */
+const char *rbg_last_error(void);
+/* 10000 * major + 100 * minor + patch. */
+int rbg_version(void);
+/* Number of CUDA kernels this library has launched in this process (its own kernels; the
+ * radix-sort passes it delegates to CUB are not counted).  No reference counterpart. */
+uint64_t rbg_kernel_launches(void);
+/* Per-kernel timing, no reference counterpart.  While enabled, the library records CUDA events
+ * on the launching stream around its main kernels; rbg_profile_enable also clears what was
+ * recorded.  rbg_profile_entry synchronises on the recorded events. */
+int rbg_profile_enable(int on);
+int rbg_profile_count(int32_t *count);
+int rbg_profile_entry(int32_t index, char *name, int32_t name_cap, double *total_ms,
+                      int64_t *launches);
+
+/* ------------------------------------------------------------------ host-side logic */
+
+/* RNGState(uint64 k): counter 0, key k (RandBLAS/base.hh:119). */
+int rbg_state_from_key(uint64_t k, rbg_state *out);
+/* counter.incr(n) on a copy (Random123 r123array4x32::incr, RandBLAS/base.hh:84-97). */
+int rbg_state_incr(const rbg_state *in, uint64_t n, rbg_state *out);
+
+/* DenseDist constructor's derived fields (RandBLAS/dense_skops.hh:313-329). */
+int rbg_dense_dist_properties(const rbg_dense_dist *D, int64_t *dim_major, int64_t *dim_minor,
+                              int32_t *natural_layout, double *isometry_scale);
+/* dense::compute_next_state (RandBLAS/dense_skops.hh:172-185). */
+int rbg_dense_next_state(const rbg_dense_dist *D, const rbg_state *seed, rbg_state *next);
+/* DenseSkOp(dist, seed) (RandBLAS/dense_skops.hh:441-453): fills seed/next state, natural
+ * layout and buff = NULL. */
+int rbg_dense_skop_init(rbg_dense_skop *S, const rbg_dense_dist *D, const rbg_state *seed,
+                        int32_t dtype);
+
+/* SparseDist constructor's derived fields (RandBLAS/sparse_skops.hh:208-224). */
+int rbg_sparse_dist_properties(const rbg_sparse_dist *D, int64_t *dim_major,
+                               int64_t *dim_minor, int64_t *full_nnz, double *isometry_scale);
+/* compute_next_state(SparseDist, state) (RandBLAS/sparse_skops.hh:266-283). */
+int rbg_sparse_next_state(const rbg_sparse_dist *D, const rbg_state *seed, rbg_state *next);
+/* SparseSkOp(dist, seed) (RandBLAS/sparse_skops.hh:399-407): nnz = -1, no arrays. */
+int rbg_sparse_skop_init(rbg_sparse_skop *S, const rbg_sparse_dist *D, const rbg_state *seed,
+                         int32_t dtype, int32_t itype);
+
+/* ------------------------------------------------------------------ sampling */
+
+/* fill_dense_unpacked (RandBLAS/dense_skops.hh:563-606): write the n_rows x n_cols
+ * submatrix at (ro_s, co_s) of a matrix from D, in `layout`, packed, into buff.  *next gets
+ * the state the reference returns (seed + first counter used + rows * stride). */
+int rbg_fill_dense_unpacked(int32_t dtype, int32_t layout, const rbg_dense_dist *D,
+                            int64_t n_rows, int64_t n_cols, int64_t ro_s, int64_t co_s,
+                            void *buff, const rbg_state *seed, rbg_state *next,
+                            rbg_stream_t stream);
+/* fill_dense(D, buff, seed) (RandBLAS/dense_skops.hh:623-626), natural layout. */
+int rbg_fill_dense(int32_t dtype, const rbg_dense_dist *D, void *buff, const rbg_state *seed,
+                   rbg_state *next, rbg_stream_t stream);
+/* fill_dense(S) (RandBLAS/dense_skops.hh:649-658): S->buff must be a device buffer of
+ * n_rows * n_cols entries; written in S->layout. */
+int rbg_fill_dense_skop(rbg_dense_skop *S, rbg_stream_t stream);
+
+/* fill_sparse_unpacked_nosub (RandBLAS/sparse_skops.hh:515-565): sample into device COO
+ * arrays of length >= vec_nnz * dim_minor.  *nnz is written on return, which makes this
+ * call synchronise `stream` for LASOs (their nnz depends on duplicate merging); for SASOs
+ * nnz = vec_nnz * dim_minor and the call stays asynchronous.  LASO duplicates are merged
+ * as in the reference (sqrt(count) * first sign) and emitted in first-occurrence order
+ * (the reference's order there is std::unordered_map's, which is unspecified). */
+int rbg_fill_sparse_unpacked_nosub(int32_t dtype, int32_t itype, const rbg_sparse_dist *D,
+                                   int64_t *nnz, void *vals, void *rows, void *cols,
+                                   const rbg_state *seed, rbg_state *next, rbg_stream_t stream);
+/* fill_sparse(S) (RandBLAS/sparse_skops.hh:587-603): S->vals/rows/cols must be device
+ * buffers of full_nnz entries; sets S->nnz. */
+int rbg_fill_sparse(rbg_sparse_skop *S, rbg_stream_t stream);
+/* repeated_fisher_yates(k, n, r, samples, state) (RandBLAS/sparse_skops.hh:259-264):
+ * r independent k-subsets of {0..n-1}, int64 samples[k * r]. */
+int rbg_repeated_fisher_yates(int64_t k, int64_t n, int64_t r, int64_t *samples,
+                              const rbg_state *seed, rbg_state *next, rbg_stream_t stream);
+
+/* ------------------------------------------------------------------ dense operators */
+
+/* LSKGE3 / sketch_general left (RandBLAS/skge.hh:154-202, 756-821, 1073-1097):
+ *   B = alpha * op(submat(S)) * op(A) + beta * B,  op(submat(S)) d x m at (ro_s, co_s),
+ *   op(A) m x n, B d x n; A, B in `layout` with leading dims lda, ldb.
+ * T = S->dtype for A, B, alpha, beta.  beta == 0 does not read B; alpha == 0 does not read
+ * A.  Generated operators are never materialised: entries are produced in the GEMM. */
+int rbg_lskge3(int32_t layout, int32_t opS, int32_t opA, int64_t d, int64_t n, int64_t m,
+               double alpha, const rbg_dense_skop *S, int64_t ro_s, int64_t co_s,
+               const void *A, int64_t lda, double beta, void *B, int64_t ldb,
+               rbg_stream_t stream);
+/* RSKGE3 / sketch_general right (RandBLAS/skge.hh:307-355, 928-992, 1175-1199):
+ *   B = alpha * op(A) * op(submat(S)) + beta * B,  op(A) m x n, op(submat(S)) n x d. */
+int rbg_rskge3(int32_t layout, int32_t opA, int32_t opS, int64_t m, int64_t d, int64_t n,
+               double alpha, const void *A, int64_t lda, const rbg_dense_skop *S,
+               int64_t ro_s, int64_t co_s, double beta, void *B, int64_t ldb,
+               rbg_stream_t stream);
+/* sketch_vector (RandBLAS/skve.hh:140-164): y = alpha * op(submat(S)) * x + beta * y with
+ * strides incx, incy (>= 1); submat(S) is d x m. */
+int rbg_sketch_vector(int32_t opS, int64_t d, int64_t m, double alpha, const rbg_dense_skop *S,
+                      int64_t ro_s, int64_t co_s, const void *x, int64_t incx, double beta,
+                      void *y, int64_t incy, rbg_stream_t stream);
+
+/* ------------------------------------------------------------------ sparse operators */
+
+/* LSKGES / sketch_general left with a SparseSkOp (RandBLAS/skge.hh:465-492, 776-797).
+ * An unsampled SASO (nnz < 0) is sampled inside the sketch and never written out. */
+int rbg_lskges(int32_t layout, int32_t opS, int32_t opA, int64_t d, int64_t n, int64_t m,
+               double alpha, const rbg_sparse_skop *S, int64_t ro_s, int64_t co_s,
+               const void *A, int64_t lda, double beta, void *B, int64_t ldb,
+               rbg_stream_t stream);
+/* RSKGES / sketch_general right with a SparseSkOp (RandBLAS/skge.hh:598-626, 947-968).
+ * The reference's rskges has no `return` after sampling an unsampled operator
+ * (RandBLAS/skge.hh:616-620) and then fails; this call samples and applies once. */
+int rbg_rskges(int32_t layout, int32_t opA, int32_t opS, int64_t m, int64_t d, int64_t n,
+               double alpha, const void *A, int64_t lda, const rbg_sparse_skop *S,
+               int64_t ro_s, int64_t co_s, double beta, void *B, int64_t ldb,
+               rbg_stream_t stream);
+/* sketch_vector with a SparseSkOp (RandBLAS/skve.hh:140-164). */
+int rbg_sketch_vector_sparse(int32_t opS, int64_t d, int64_t m, double alpha,
+                             const rbg_sparse_skop *S, int64_t ro_s, int64_t co_s,
+                             const void *x, int64_t incx, double beta, void *y, int64_t incy,
+                             rbg_stream_t stream);
+
+/* ------------------------------------------------------------------ sparse data */
+
+/* LSKSP3 / sketch_sparse left (RandBLAS/sparse_data/sksp.hh:132-182, 418-437):
+ *   B = alpha * op(submat(S)) * op(A) + beta * B with dense S and sparse A (m x n). */
+int rbg_lsksp3(int32_t layout, int32_t opS, int32_t opA, int64_t d, int64_t n, int64_t m,
+               double alpha, const rbg_dense_skop *S, int64_t ro_s, int64_t co_s,
+               const rbg_spmat *A, double beta, void *B, int64_t ldb, rbg_stream_t stream);
+/* RSKSP3 / sketch_sparse right (RandBLAS/sparse_data/sksp.hh:277-326, 520-539):
+ *   B = alpha * op(A) * op(submat(S)) + beta * B with sparse A (op(A) m x n). */
+int rbg_rsksp3(int32_t layout, int32_t opA, int32_t opS, int64_t m, int64_t d, int64_t n,
+               double alpha, const rbg_spmat *A, const rbg_dense_skop *S, int64_t ro_s,
+               int64_t co_s, double beta, void *B, int64_t ldb, rbg_stream_t stream);
+/* left_spmm (RandBLAS/sparse_data/spmm_dispatch.hh:52-179):
+ *   C = alpha * op(submat(A)) * op(B) + beta * C, sparse A, dense B; (ro_a, co_a) are only
+ *   allowed for COO, as in the reference. */
+int rbg_left_spmm(int32_t layout, int32_t opA, int32_t opB, int64_t d, int64_t n, int64_t m,
+                  double alpha, const rbg_spmat *A, int64_t ro_a, int64_t co_a, const void *B,
+                  int64_t ldb, double beta, void *C, int64_t ldc, rbg_stream_t stream);
+/* right_spmm (RandBLAS/sparse_data/spmm_dispatch.hh:181-219):
+ *   C = alpha * op(A) * op(submat(B)) + beta * C, dense A, sparse B. */
+int rbg_right_spmm(int32_t layout, int32_t opA, int32_t opB, int64_t m, int64_t d, int64_t n,
+                   double alpha, const void *A, int64_t lda, const rbg_spmat *B, int64_t ro_b,
+                   int64_t co_b, double beta, void *C, int64_t ldc, rbg_stream_t stream);
+
+/* ------------------------------------------------------------------ precision path */
+
+/* Bytes of device workspace rbg_lskge3_lowp needs for these sizes. */
+int rbg_lskge3_lowp_workspace(int32_t precision, int64_t d, int64_t n, int64_t m,
+                              size_t *bytes);
+/* Left dense sketch on the tensor cores (no reference counterpart; same semantics as
+ * rbg_lskge3 with T = float): the entries of submat(S) are generated inside the kernel,
+ * rounded to `precision` (RBG_PREC_BF16, or RBG_PREC_FP8_E4M3 with one scale per 128
+ * entries along m), multiplied with A rounded the same way, accumulated in FP32 in tensor
+ * memory.  workspace: device buffer of rbg_lskge3_lowp_workspace bytes, or NULL to let the
+ * call allocate (stream-ordered) and free it. */
+int rbg_lskge3_lowp(int32_t precision, int32_t layout, int32_t opS, int32_t opA, int64_t d,
+                    int64_t n, int64_t m, float alpha, const rbg_dense_skop *S, int64_t ro_s,
+                    int64_t co_s, const float *A, int64_t lda, float beta, float *B,
+                    int64_t ldb, void *workspace, size_t workspace_bytes, rbg_stream_t stream);
+
+/* ------------------------------------------------------------------ batching path */
+
+/* One problem of a batch: B_i = alpha_i * submat(S_i) * A_i + beta_i * B_i (left sketch,
+ * op = NoTrans) for a generated dense operator S_i with its own state. */
+typedef struct rbg_batch_problem {
+    int64_t d, n, m;
+    rbg_dense_dist dist;
+    rbg_state seed;
+    int64_t ro_s, co_s;
+    const float *A;
+    int64_t lda;
+    float *B;
+    int64_t ldb;
+    float alpha, beta;
+} rbg_batch_problem;
+
+/* Sketch `count` independent problems (host array `problems`) in one persistent launch,
+ * all in `layout`, T = float.  tile_config: 0 = let the library choose; otherwise one of
+ * the configurations listed by rbg_batched_tile_configs. */
+int rbg_lskge3_batched(int32_t layout, const rbg_batch_problem *problems, int64_t count,
+                       int32_t tile_config, rbg_stream_t stream);
+/* Number of tile configurations the batched kernel offers (1-based ids). */
+int rbg_batched_tile_configs(int32_t *count);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* RANDBLAS_GB300_H */

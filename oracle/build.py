@@ -1,0 +1,67 @@
+"""Build the CPU oracle (test infrastructure only).
+
+Two artefacts:
+
+* ``oracle/liboracle.so`` -- the plain-C restatement in ``oracle/oracle.c``.  Builds
+  anywhere gcc exists (this container and the GPU host alike).
+* ``oracle/_ref/librbref.so`` -- the reference's own RandBLAS headers, compiled directly
+  with g++ (no CMake) against the project-written Random123 / BLAS++ stand-ins in
+  ``oracle/shim/`` plus ``oracle/ref_driver.cc``.  Built only where the reference source
+  tree is present (``RANDBLAS_REF_DIR``, default ``/root/reference``); used to pin the
+  restatement and to generate ``tests/golden/``.
+
+Nothing in the product imports this module.
+"""
+from __future__ import annotations
+
+import os
+import subprocess
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REF_DIR = os.environ.get("RANDBLAS_REF_DIR", "/root/reference")
+ORACLE_SO = os.path.join(HERE, "liboracle.so")
+REF_SO = os.path.join(HERE, "_ref", "librbref.so")
+
+
+def _newer(target: str, sources: list[str]) -> bool:
+    if not os.path.exists(target):
+        return False
+    t = os.path.getmtime(target)
+    return all(os.path.getmtime(s) <= t for s in sources if os.path.exists(s))
+
+
+def build_oracle(force: bool = False) -> str:
+    src = os.path.join(HERE, "oracle.c")
+    if force or not _newer(ORACLE_SO, [src]):
+        cmd = ["gcc", "-O2", "-std=gnu11", "-fPIC", "-shared", "-ffp-contract=off", "-fopenmp",
+               src, "-o", ORACLE_SO, "-lm"]
+        subprocess.run(cmd, check=True)
+    return ORACLE_SO
+
+
+def ref_available() -> bool:
+    return os.path.isfile(os.path.join(REF_DIR, "RandBLAS.hh"))
+
+
+def build_ref(force: bool = False) -> str | None:
+    """Compile the reference headers + shims; returns the .so path or None if no reference."""
+    if not ref_available():
+        return None
+    src = os.path.join(HERE, "ref_driver.cc")
+    shim = os.path.join(HERE, "shim")
+    deps = [src] + [os.path.join(dp, f) for dp, _, fs in os.walk(shim) for f in fs]
+    if force or not _newer(REF_SO, deps):
+        os.makedirs(os.path.dirname(REF_SO), exist_ok=True)
+        # -I order: the reference tree first (RandBLAS/*.hh), then the shims (Random123/*,
+        # blas.hh and the RandBLAS/config.h that CMake would otherwise generate).
+        cmd = ["g++", "-O2", "-std=c++20", "-fPIC", "-shared", "-fopenmp", "-ffp-contract=off",
+               "-w", "-I", REF_DIR, "-I", shim, src, "-o", REF_SO]
+        subprocess.run(cmd, check=True)
+    return REF_SO
+
+
+if __name__ == "__main__":
+    force = "--force" in sys.argv
+    print(build_oracle(force))
+    print(build_ref(force) or "reference tree not present: oracle/_ref not built")

@@ -1,0 +1,389 @@
+/*
+ * oracle.c -- CPU restatement of RandBLAS's sketching hot path.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This file is the checker for the CUDA library in
+ * randblas_gb300/.  Only tests/, __graft_entry__.smoke() and bench.py's CPU
+ * baseline leg may load it; the product never links, calls or falls back to it.
+ *
+ * Everything here is written from the reference's documented behaviour, one
+ * function per reference routine, each citing the reference file:line it
+ * restates (paths are relative to the RandBLAS source tree):
+ *
+ *   Philox4x32-10 ............ Random123 r123::Philox4x32 (used at RandBLAS/base.hh:53).
+ *                              Random123 is a third-party dependency that the reference
+ *                              does not vendor (CI clones HEAD, unpinned); the bijection is
+ *                              restated from its published description: Salmon, Moraes,
+ *                              Dror, Shaw, "Parallel Random Numbers: As Easy as 1, 2, 3",
+ *                              SC'11, section 4 (Philox-4x32 with R = 10 rounds).
+ *                              Pinned by test/test_basic_rng/r123_kat_vectors.txt:19-21.
+ *   128-bit counter increment  Random123 r123array4x32::incr(uint64), asserted by
+ *                              test/test_basic_rng/test_r123.cc:705-797.
+ *   uneg11 / u01 / boxmuller . Random123 uniform.hpp / boxmuller.hpp, as used by
+ *                              RandBLAS/random_gen.hh:60-137 (documented definitions:
+ *                              u01(x) = x*2^-32 + 2^-33, uneg11(x) = (int32)x*2^-31 + 2^-32,
+ *                              boxmuller = (sin(pi*uneg11(u0))*r, cos(pi*uneg11(u0))*r),
+ *                              r = sqrt(-2 log u01(u1))).
+ *   fill_dense_submat ........ RandBLAS/dense_skops.hh:96-170
+ *   fill_dense_unpacked ...... RandBLAS/dense_skops.hh:563-606
+ *   dense compute_next_state . RandBLAS/dense_skops.hh:172-185
+ *   natural_layout ........... RandBLAS/dense_skops.hh:187-199
+ *   repeated_fisher_yates .... RandBLAS/sparse_skops.hh:51-106
+ *   sample_indices_iid_uniform RandBLAS/util.hh:516-546
+ *   laso merge ............... RandBLAS/sparse_skops.hh:453-491 (duplicates merged to
+ *                              sqrt(count) * first sign; emitted in first-occurrence
+ *                              order -- the reference emits them in std::unordered_map
+ *                              order, which is implementation-defined, so only the set
+ *                              of (index, value) pairs per vector is comparable)
+ *   sparse compute_next_state  RandBLAS/sparse_skops.hh:266-283
+ *
+ * Build: gcc -O2 -std=c11 -fPIC -shared -ffp-contract=off -fopenmp (oracle/build.py).
+ */
+#include <math.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+
+#define ORC_COL_MAJOR 0
+#define ORC_ROW_MAJOR 1
+#define ORC_GAUSSIAN 0
+#define ORC_UNIFORM 1
+#define ORC_AXIS_SHORT 0
+#define ORC_AXIS_LONG 1
+#define ORC_F32 0
+#define ORC_F64 1
+#define ORC_I32 0
+#define ORC_I64 1
+
+typedef struct {
+    uint32_t counter[4];
+    uint32_t key[2];
+} orc_state;
+
+/* ---------------------------------------------------------------- Philox */
+
+/* Round multipliers and Weyl key increments of Philox-4x32 (SC'11, table 2 / sec. 4). */
+static const uint32_t kPhiloxMulA = 0xD2511F53u;
+static const uint32_t kPhiloxMulB = 0xCD9E8D57u;
+static const uint32_t kPhiloxWeylA = 0x9E3779B9u;
+static const uint32_t kPhiloxWeylB = 0xBB67AE85u;
+
+void orc_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]) {
+    uint32_t x0 = ctr[0], x1 = ctr[1], x2 = ctr[2], x3 = ctr[3];
+    uint32_t ka = key[0], kb = key[1];
+    for (int round = 0; round < 10; ++round) {
+        if (round > 0) {
+            ka += kPhiloxWeylA;
+            kb += kPhiloxWeylB;
+        }
+        uint64_t pa = (uint64_t)kPhiloxMulA * x0;
+        uint64_t pb = (uint64_t)kPhiloxMulB * x2;
+        uint32_t n0 = (uint32_t)(pb >> 32) ^ x1 ^ ka;
+        uint32_t n1 = (uint32_t)pb;
+        uint32_t n2 = (uint32_t)(pa >> 32) ^ x3 ^ kb;
+        uint32_t n3 = (uint32_t)pa;
+        x0 = n0; x1 = n1; x2 = n2; x3 = n3;
+    }
+    out[0] = x0; out[1] = x1; out[2] = x2; out[3] = x3;
+}
+
+/* counter <- counter + n, the counter read as a little-endian 128-bit integer. */
+void orc_ctr_add(uint32_t c[4], uint64_t n) {
+    uint64_t t = (uint64_t)c[0] + (n & 0xFFFFFFFFu);
+    c[0] = (uint32_t)t;
+    t = (uint64_t)c[1] + (n >> 32) + (t >> 32);
+    c[1] = (uint32_t)t;
+    t = (uint64_t)c[2] + (t >> 32);
+    c[2] = (uint32_t)t;
+    c[3] += (uint32_t)(t >> 32);
+}
+
+/* key <- key + k, the key read as a little-endian 64-bit integer (RNGState(k), base.hh:119). */
+void orc_key_from_u64(uint64_t k, uint32_t key[2]) {
+    key[0] = (uint32_t)k;
+    key[1] = (uint32_t)(k >> 32);
+}
+
+/* ------------------------------------------------------------ transforms */
+
+float orc_uneg11(uint32_t u) { return (float)(int32_t)u * 0x1p-31f + 0x1p-32f; }
+
+float orc_u01(uint32_t u) { return (float)u * 0x1p-32f + 0x1p-33f; }
+
+void orc_boxmuller(uint32_t u0, uint32_t u1, float *first, float *second) {
+    float s, c;
+    sincosf(3.14159265358979323846f * orc_uneg11(u0), &s, &c);
+    float r = sqrtf(-2.0f * logf(orc_u01(u1)));
+    *first = s * r;
+    *second = c * r;
+}
+
+/* The four floats one Philox call yields for a dense operator (random_gen.hh:85-137). */
+static void gen4(int family, const uint32_t ctr[4], const uint32_t key[2], float v[4]) {
+    uint32_t r[4];
+    orc_philox4x32_10(ctr, key, r);
+    if (family == ORC_GAUSSIAN) {
+        orc_boxmuller(r[0], r[1], &v[0], &v[1]);
+        orc_boxmuller(r[2], r[3], &v[2], &v[3]);
+    } else {
+        for (int l = 0; l < 4; ++l) v[l] = orc_uneg11(r[l]);
+    }
+}
+
+/* ----------------------------------------------------------- dense fills */
+
+int orc_natural_layout(int major_axis, int64_t n_rows, int64_t n_cols) {
+    int wide = n_rows < n_cols;
+    int is_long = major_axis == ORC_AXIS_LONG;
+    if (wide) return is_long ? ORC_ROW_MAJOR : ORC_COL_MAJOR;
+    return is_long ? ORC_COL_MAJOR : ORC_ROW_MAJOR;
+}
+
+int64_t orc_dim_major(int major_axis, int64_t n_rows, int64_t n_cols) {
+    int64_t mx = n_rows > n_cols ? n_rows : n_cols;
+    int64_t mn = n_rows > n_cols ? n_cols : n_rows;
+    return major_axis == ORC_AXIS_LONG ? mx : mn;
+}
+
+/*
+ * Row-major n_srows x n_scols block of the implicit row-major parent with n_cols
+ * columns, starting at linear offset ptr.  Row R of the parent owns counters
+ * [R*ceil(n_cols/4), (R+1)*ceil(n_cols/4)); column C sits in lane C%4 of counter C/4
+ * of its row.  Returns seed + (first counter used) + n_srows*ceil(n_cols/4)
+ * (dense_skops.hh:96-170).  No scaling, promotes float -> T.
+ */
+void orc_fill_dense_submat(int dtype, int family, int64_t n_cols, void *smat, int64_t n_srows,
+                           int64_t n_scols, int64_t ptr, const orc_state *seed, int64_t lda,
+                           orc_state *next) {
+    if (lda <= 0) lda = n_scols;
+    const int64_t stride = (n_cols + 3) / 4;
+    const int64_t r0 = ptr / n_cols, c0 = ptr % n_cols;
+    const int64_t blk_first = c0 / 4, blk_last = (c0 + n_scols - 1) / 4;
+#pragma omp parallel for schedule(static)
+    for (int64_t r = 0; r < n_srows; ++r) {
+        uint32_t row_ctr[4];
+        memcpy(row_ctr, seed->counter, sizeof row_ctr);
+        orc_ctr_add(row_ctr, (uint64_t)((r0 + r) * stride));
+        for (int64_t blk = blk_first; blk <= blk_last; ++blk) {
+            uint32_t c[4];
+            memcpy(c, row_ctr, sizeof c);
+            orc_ctr_add(c, (uint64_t)blk);
+            float v[4];
+            gen4(family, c, seed->key, v);
+            for (int l = 0; l < 4; ++l) {
+                int64_t col = blk * 4 + l - c0;
+                if (col < 0 || col >= n_scols) continue;
+                if (dtype == ORC_F32)
+                    ((float *)smat)[r * lda + col] = v[l];
+                else
+                    ((double *)smat)[r * lda + col] = (double)v[l];
+            }
+        }
+    }
+    *next = *seed;
+    orc_ctr_add(next->counter, (uint64_t)(r0 * stride + blk_first + n_srows * stride));
+}
+
+/* dense_skops.hh:563-606: fill an n_rows x n_cols submatrix at (ro_s, co_s) in `layout`. */
+int orc_fill_dense_unpacked(int dtype, int layout, int64_t D_rows, int64_t D_cols, int family,
+                            int major_axis, int64_t n_rows, int64_t n_cols, int64_t ro_s,
+                            int64_t co_s, void *buff, const orc_state *seed, orc_state *next) {
+    if (D_rows < n_rows + ro_s || D_cols < n_cols + co_s) return 1;
+    const int natural = orc_natural_layout(major_axis, D_rows, D_cols);
+    const int64_t ma_len = orc_dim_major(major_axis, D_rows, D_cols);
+    int64_t nr, nc, ptr;
+    if (natural == ORC_COL_MAJOR) {
+        nr = n_cols; nc = n_rows; ptr = ro_s + co_s * ma_len;
+    } else {
+        nr = n_rows; nc = n_cols; ptr = ro_s * ma_len + co_s;
+    }
+    orc_fill_dense_submat(dtype, family, ma_len, buff, nr, nc, ptr, seed, 0, next);
+    const int64_t size = nr * nc;
+    if (family == ORC_UNIFORM) {
+        if (dtype == ORC_F32) {
+            const float s3 = (float)sqrt(3.0);
+            for (int64_t i = 0; i < size; ++i) ((float *)buff)[i] *= s3;
+        } else {
+            const double s3 = sqrt(3.0);
+            for (int64_t i = 0; i < size; ++i) ((double *)buff)[i] *= s3;
+        }
+    }
+    if (layout != natural && size > 0) {
+        /* the packed natural-layout block is row-major nr x nc; the other layout is its transpose */
+        size_t esz = dtype == ORC_F32 ? 4 : 8;
+        char *tmp = (char *)malloc(size * esz);
+        if (!tmp) return 2;
+        memcpy(tmp, buff, size * esz);
+        for (int64_t i = 0; i < nr; ++i)
+            for (int64_t j = 0; j < nc; ++j)
+                memcpy((char *)buff + (j * nr + i) * esz, tmp + (i * nc + j) * esz, esz);
+        free(tmp);
+    }
+    return 0;
+}
+
+/* dense_skops.hh:172-185 */
+void orc_dense_next_state(int major_axis, int64_t D_rows, int64_t D_cols, const orc_state *seed,
+                          orc_state *next) {
+    int64_t ma = orc_dim_major(major_axis, D_rows, D_cols);
+    int64_t mi = D_rows + D_cols - ma;
+    *next = *seed;
+    orc_ctr_add(next->counter, (uint64_t)(((ma + 3) / 4) * mi));
+}
+
+/* ---------------------------------------------------------- sparse fills */
+
+static void put_idx(int itype, void *p, int64_t i, int64_t v) {
+    if (itype == ORC_I32) ((int32_t *)p)[i] = (int32_t)v;
+    else ((int64_t *)p)[i] = v;
+}
+static void put_val(int dtype, void *p, int64_t i, double v) {
+    if (dtype == ORC_F32) ((float *)p)[i] = (float)v;
+    else ((double *)p)[i] = v;
+}
+
+/*
+ * sparse_skops.hh:51-106.  For each minor index i, vec_nnz steps of a Fisher-Yates
+ * shuffle of the identity over [0, dim_major); step j of vector i uses counter
+ * seed + i*vec_nnz + j, draws ell = j + x0 mod (dim_major - j), and gives a sign from
+ * the parity of x1.  The shuffle is undone after each vector, so vectors are independent.
+ */
+int orc_repeated_fisher_yates(int dtype, int itype, const orc_state *seed, int64_t vec_nnz,
+                              int64_t dim_major, int64_t dim_minor, void *idxs_major,
+                              void *idxs_minor, void *vals, orc_state *next) {
+    if (vec_nnz > dim_major) return 1;
+    int64_t *perm = (int64_t *)malloc(sizeof(int64_t) * (size_t)dim_major);
+    int64_t *piv = (int64_t *)malloc(sizeof(int64_t) * (size_t)(vec_nnz > 0 ? vec_nnz : 1));
+    if (!perm || !piv) { free(perm); free(piv); return 2; }
+    for (int64_t t = 0; t < dim_major; ++t) perm[t] = t;
+    for (int64_t i = 0; i < dim_minor; ++i) {
+        for (int64_t j = 0; j < vec_nnz; ++j) {
+            uint32_t c[4], r[4];
+            memcpy(c, seed->counter, sizeof c);
+            orc_ctr_add(c, (uint64_t)(i * vec_nnz + j));
+            orc_philox4x32_10(c, seed->key, r);
+            int64_t ell = j + (int64_t)(r[0] % (uint64_t)(dim_major - j));
+            piv[j] = ell;
+            int64_t picked = perm[ell];
+            perm[ell] = perm[j];
+            perm[j] = picked;
+            put_idx(itype, idxs_major, i * vec_nnz + j, picked);
+            if (idxs_minor) put_idx(itype, idxs_minor, i * vec_nnz + j, i);
+            if (vals) put_val(dtype, vals, i * vec_nnz + j, (r[1] % 2 == 0) ? 1.0 : -1.0);
+        }
+        for (int64_t j = vec_nnz - 1; j >= 0; --j) {  /* undo the swaps, last first */
+            int64_t ell = piv[j];
+            int64_t t = perm[j];
+            perm[j] = perm[ell];
+            perm[ell] = t;
+        }
+    }
+    free(perm);
+    free(piv);
+    *next = *seed;
+    orc_ctr_add(next->counter, (uint64_t)(dim_minor * vec_nnz));
+    return 0;
+}
+
+/*
+ * util.hh:516-546 with Rademachers.  Sample j of a call uses counter state + j/2,
+ * lanes 2*(j%2) (index) and 2*(j%2)+1 (sign); the call consumes ceil(k/2) counters.
+ * index = trunc(n * ((double)uneg11(x) + 1) / 2); sign = +1 iff uneg11(x') >= 0.
+ */
+void orc_sample_indices_iid_uniform(int64_t n, int64_t k, int64_t *samples, double *signs,
+                                    const orc_state *state, orc_state *next) {
+    for (int64_t j = 0; j < k; ++j) {
+        uint32_t c[4], r[4];
+        memcpy(c, state->counter, sizeof c);
+        orc_ctr_add(c, (uint64_t)(j / 2));
+        orc_philox4x32_10(c, state->key, r);
+        int lane = 2 * (int)(j % 2);
+        double u = ((double)orc_uneg11(r[lane]) + 1.0) / 2.0;
+        samples[j] = (int64_t)((double)n * u);
+        if (signs) signs[j] = orc_uneg11(r[lane + 1]) >= 0.0f ? 1.0 : -1.0;
+    }
+    *next = *state;
+    orc_ctr_add(next->counter, (uint64_t)((k + 1) / 2));
+}
+
+/*
+ * LASO fill (sparse_skops.hh:515-565 long-axis branch + merge at :453-491): one
+ * long-axis vector per minor index i, vec_nnz iid samples each; duplicates inside a
+ * vector merge into one entry of value sqrt(count) * (sign of first occurrence).
+ * Writes nnz; returns the state after the last vector.
+ */
+int orc_fill_laso(int dtype, int itype, int64_t vec_nnz, int64_t dim_major, int64_t dim_minor,
+                  void *idxs_long, void *idxs_short, void *vals, int64_t *nnz,
+                  const orc_state *seed, orc_state *next) {
+    int64_t *smp = (int64_t *)malloc(sizeof(int64_t) * (size_t)vec_nnz);
+    double *sg = (double *)malloc(sizeof(double) * (size_t)vec_nnz);
+    int64_t *cnt = (int64_t *)malloc(sizeof(int64_t) * (size_t)vec_nnz);
+    if (!smp || !sg || !cnt) { free(smp); free(sg); free(cnt); return 2; }
+    orc_state st = *seed;
+    int64_t total = 0;
+    for (int64_t i = 0; i < dim_minor; ++i) {
+        orc_state nx;
+        orc_sample_indices_iid_uniform(dim_major, vec_nnz, smp, sg, &st, &nx);
+        st = nx;
+        int64_t distinct = 0;
+        for (int64_t j = 0; j < vec_nnz; ++j) {
+            int64_t found = -1;
+            for (int64_t q = 0; q < distinct; ++q)
+                if (smp[q] == smp[j]) { found = q; break; }
+            if (found >= 0) {
+                cnt[found] += 1;
+            } else {
+                smp[distinct] = smp[j];
+                sg[distinct] = sg[j];
+                cnt[distinct] = 1;
+                distinct += 1;
+            }
+        }
+        for (int64_t q = 0; q < distinct; ++q) {
+            double v;
+            if (dtype == ORC_F32) v = (double)(sqrtf((float)cnt[q]) * (float)sg[q]);
+            else v = sqrt((double)cnt[q]) * sg[q];
+            put_idx(itype, idxs_long, total + q, smp[q]);
+            put_idx(itype, idxs_short, total + q, i);
+            put_val(dtype, vals, total + q, v);
+        }
+        total += distinct;
+    }
+    free(smp);
+    free(sg);
+    free(cnt);
+    *nnz = total;
+    *next = st;
+    return 0;
+}
+
+/* sparse_skops.hh:266-283 */
+void orc_sparse_next_state(int major_axis, int64_t D_rows, int64_t D_cols, int64_t vec_nnz,
+                           const orc_state *seed, orc_state *next) {
+    int64_t mx = D_rows > D_cols ? D_rows : D_cols;
+    int64_t mn = D_rows > D_cols ? D_cols : D_rows;
+    int64_t incr = major_axis == ORC_AXIS_SHORT ? mx * vec_nnz : mn * ((vec_nnz + 1) / 2);
+    *next = *seed;
+    orc_ctr_add(next->counter, (uint64_t)incr);
+}
+
+/*
+ * fill_sparse (sparse_skops.hh:515-565, 587-603): SASO (Axis::Short) or LASO (Axis::Long)
+ * into COO arrays (rows, cols, vals) of length >= vec_nnz * dim_minor.  Short-axis indices
+ * go to `rows` when n_rows <= n_cols, else to `cols`.  Returns the state after sampling.
+ */
+int orc_fill_sparse(int dtype, int itype, int64_t D_rows, int64_t D_cols, int64_t vec_nnz,
+                    int major_axis, void *vals, void *rows, void *cols, int64_t *nnz,
+                    const orc_state *seed, orc_state *next) {
+    int64_t mx = D_rows > D_cols ? D_rows : D_cols;
+    int64_t mn = D_rows > D_cols ? D_cols : D_rows;
+    void *idxs_short = D_rows <= D_cols ? rows : cols;
+    void *idxs_long = D_rows <= D_cols ? cols : rows;
+    if (major_axis == ORC_AXIS_SHORT) {
+        int rc = orc_repeated_fisher_yates(dtype, itype, seed, vec_nnz, mn, mx, idxs_short,
+                                           idxs_long, vals, next);
+        *nnz = vec_nnz * mx;
+        return rc;
+    }
+    return orc_fill_laso(dtype, itype, vec_nnz, mx, mn, idxs_long, idxs_short, vals, nnz, seed,
+                         next);
+}

@@ -1,0 +1,29 @@
+// Project-written Box-Muller transform (test infrastructure), following the documented
+// Random123 definition used by RandBLAS/random_gen.hh:60-74: for 32-bit inputs (u0, u1),
+//   theta = pi * uneg11<float>(u0), r = sqrt(-2 log(u01<float>(u1))),
+//   result = (sin(theta) * r, cos(theta) * r), all in float.
+#pragma once
+#include <cmath>
+#include <cstdint>
+#include "uniform.hpp"
+
+namespace r123 {
+
+struct float2 { float x, y; };
+struct double2 { double x, y; };
+
+inline float2 boxmuller(std::uint32_t u0, std::uint32_t u1) {
+    float s, c;
+    ::sincosf(3.14159265358979323846f * uneg11<float>(u0), &s, &c);
+    float r = std::sqrt(-2.0f * std::log(u01<float>(u1)));
+    return float2{s * r, c * r};
+}
+
+inline double2 boxmuller(std::uint64_t u0, std::uint64_t u1) {
+    double s, c;
+    ::sincos(3.14159265358979323846 * uneg11<double>(u0), &s, &c);
+    double r = std::sqrt(-2.0 * std::log(u01<double>(u1)));
+    return double2{s * r, c * r};
+}
+
+}  // namespace r123

@@ -1,0 +1,16 @@
+"""randblas_gb300 -- RandBLAS's sketching hot path on one GB300 (sm_103a).
+
+The compute lives in ``librandblas_gb300.so`` (hand-written CUDA behind the C ABI of
+``include/randblas_gb300.h``); this package is the host-side mirror of the reference's API
+(:mod:`randblas_gb300.api`), the autograd front end (:mod:`randblas_gb300.autograd`) and the
+batching front end (:mod:`randblas_gb300.batched`).
+"""
+from . import profile  # noqa: F401
+from ._lib import RandBLASError, lib  # noqa: F401
+from .api import (  # noqa: F401
+    Axis, COOMatrix, CSCMatrix, CSRMatrix, DenseDist, DenseSkOp, Layout, Op, RNGState,
+    ScalarDist, SparseDist, SparseSkOp, fill_dense, fill_dense_unpacked, fill_sparse,
+    fill_sparse_unpacked_nosub, left_spmm, repeated_fisher_yates, right_spmm, sketch_general,
+    sketch_sparse, sketch_vector, spmm)
+
+__version__ = "1.1.0"

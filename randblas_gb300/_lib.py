@@ -1,0 +1,173 @@
+"""ctypes binding of the C ABI in ``include/randblas_gb300.h``.
+
+The shared library is loaded from the package directory (built in-tree by
+``randblas_gb300/build.py``).  There is no fallback: if the library is missing the import
+of :func:`lib` raises, so nothing can silently run on the CPU.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import threading
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "librandblas_gb300.so")
+
+# enums (values as in the header)
+COL_MAJOR, ROW_MAJOR = 0, 1
+NO_TRANS, TRANS = 0, 1
+GAUSSIAN, UNIFORM = 0, 1
+AXIS_SHORT, AXIS_LONG = 0, 1
+F32, F64 = 0, 1
+I32, I64 = 0, 1
+COO, CSR, CSC = 0, 1, 2
+PREC_BF16, PREC_FP8_E4M3 = 0, 1
+
+SUCCESS = 0
+ERROR_INVALID_ARGUMENT = 1
+ERROR_OVERFLOW = 2
+ERROR_CUDA = 3
+ERROR_TIMEOUT = 4
+ERROR_UNSUPPORTED = 5
+ERROR_ALLOC = 6
+
+
+class rbg_state(C.Structure):
+    _fields_ = [("counter", C.c_uint32 * 4), ("key", C.c_uint32 * 2)]
+
+
+class rbg_dense_dist(C.Structure):
+    _fields_ = [("n_rows", C.c_int64), ("n_cols", C.c_int64), ("family", C.c_int32),
+                ("major_axis", C.c_int32)]
+
+
+class rbg_dense_skop(C.Structure):
+    _fields_ = [("dist", rbg_dense_dist), ("seed_state", rbg_state), ("next_state", rbg_state),
+                ("dtype", C.c_int32), ("layout", C.c_int32), ("buff", C.c_void_p)]
+
+
+class rbg_sparse_dist(C.Structure):
+    _fields_ = [("n_rows", C.c_int64), ("n_cols", C.c_int64), ("vec_nnz", C.c_int64),
+                ("major_axis", C.c_int32), ("reserved", C.c_int32)]
+
+
+class rbg_sparse_skop(C.Structure):
+    _fields_ = [("dist", rbg_sparse_dist), ("seed_state", rbg_state), ("next_state", rbg_state),
+                ("nnz", C.c_int64), ("dtype", C.c_int32), ("itype", C.c_int32),
+                ("vals", C.c_void_p), ("rows", C.c_void_p), ("cols", C.c_void_p)]
+
+
+class rbg_spmat(C.Structure):
+    _fields_ = [("format", C.c_int32), ("dtype", C.c_int32), ("itype", C.c_int32),
+                ("reserved", C.c_int32), ("n_rows", C.c_int64), ("n_cols", C.c_int64),
+                ("nnz", C.c_int64), ("vals", C.c_void_p), ("idx_a", C.c_void_p),
+                ("idx_b", C.c_void_p)]
+
+
+class rbg_batch_problem(C.Structure):
+    _fields_ = [("d", C.c_int64), ("n", C.c_int64), ("m", C.c_int64), ("dist", rbg_dense_dist),
+                ("seed", rbg_state), ("ro_s", C.c_int64), ("co_s", C.c_int64),
+                ("A", C.c_void_p), ("lda", C.c_int64), ("B", C.c_void_p), ("ldb", C.c_int64),
+                ("alpha", C.c_float), ("beta", C.c_float)]
+
+
+P = C.c_void_p
+I64 = C.c_int64
+I32 = C.c_int32
+D = C.c_double
+PS = C.POINTER(rbg_state)
+
+# name -> argtypes (restype int unless noted)
+SIGNATURES = {
+    "rbg_last_error": ([], C.c_char_p),
+    "rbg_version": ([], C.c_int),
+    "rbg_kernel_launches": ([], C.c_uint64),
+    "rbg_profile_enable": ([C.c_int], C.c_int),
+    "rbg_profile_count": ([C.POINTER(I32)], C.c_int),
+    "rbg_profile_entry": ([I32, C.c_char_p, I32, C.POINTER(D), C.POINTER(I64)], C.c_int),
+    "rbg_state_from_key": ([C.c_uint64, PS], C.c_int),
+    "rbg_state_incr": ([PS, C.c_uint64, PS], C.c_int),
+    "rbg_dense_dist_properties": ([C.POINTER(rbg_dense_dist), C.POINTER(I64), C.POINTER(I64),
+                                   C.POINTER(I32), C.POINTER(D)], C.c_int),
+    "rbg_dense_next_state": ([C.POINTER(rbg_dense_dist), PS, PS], C.c_int),
+    "rbg_dense_skop_init": ([C.POINTER(rbg_dense_skop), C.POINTER(rbg_dense_dist), PS, I32],
+                            C.c_int),
+    "rbg_sparse_dist_properties": ([C.POINTER(rbg_sparse_dist), C.POINTER(I64), C.POINTER(I64),
+                                    C.POINTER(I64), C.POINTER(D)], C.c_int),
+    "rbg_sparse_next_state": ([C.POINTER(rbg_sparse_dist), PS, PS], C.c_int),
+    "rbg_sparse_skop_init": ([C.POINTER(rbg_sparse_skop), C.POINTER(rbg_sparse_dist), PS, I32,
+                              I32], C.c_int),
+    "rbg_fill_dense_unpacked": ([I32, I32, C.POINTER(rbg_dense_dist), I64, I64, I64, I64, P, PS,
+                                 PS, P], C.c_int),
+    "rbg_fill_dense": ([I32, C.POINTER(rbg_dense_dist), P, PS, PS, P], C.c_int),
+    "rbg_fill_dense_skop": ([C.POINTER(rbg_dense_skop), P], C.c_int),
+    "rbg_fill_sparse_unpacked_nosub": ([I32, I32, C.POINTER(rbg_sparse_dist), C.POINTER(I64), P,
+                                        P, P, PS, PS, P], C.c_int),
+    "rbg_fill_sparse": ([C.POINTER(rbg_sparse_skop), P], C.c_int),
+    "rbg_repeated_fisher_yates": ([I64, I64, I64, P, PS, PS, P], C.c_int),
+    "rbg_lskge3": ([I32, I32, I32, I64, I64, I64, D, C.POINTER(rbg_dense_skop), I64, I64, P, I64,
+                    D, P, I64, P], C.c_int),
+    "rbg_rskge3": ([I32, I32, I32, I64, I64, I64, D, P, I64, C.POINTER(rbg_dense_skop), I64, I64,
+                    D, P, I64, P], C.c_int),
+    "rbg_sketch_vector": ([I32, I64, I64, D, C.POINTER(rbg_dense_skop), I64, I64, P, I64, D, P,
+                           I64, P], C.c_int),
+    "rbg_lskges": ([I32, I32, I32, I64, I64, I64, D, C.POINTER(rbg_sparse_skop), I64, I64, P,
+                    I64, D, P, I64, P], C.c_int),
+    "rbg_rskges": ([I32, I32, I32, I64, I64, I64, D, P, I64, C.POINTER(rbg_sparse_skop), I64,
+                    I64, D, P, I64, P], C.c_int),
+    "rbg_sketch_vector_sparse": ([I32, I64, I64, D, C.POINTER(rbg_sparse_skop), I64, I64, P, I64,
+                                  D, P, I64, P], C.c_int),
+    "rbg_lsksp3": ([I32, I32, I32, I64, I64, I64, D, C.POINTER(rbg_dense_skop), I64, I64,
+                    C.POINTER(rbg_spmat), D, P, I64, P], C.c_int),
+    "rbg_rsksp3": ([I32, I32, I32, I64, I64, I64, D, C.POINTER(rbg_spmat),
+                    C.POINTER(rbg_dense_skop), I64, I64, D, P, I64, P], C.c_int),
+    "rbg_left_spmm": ([I32, I32, I32, I64, I64, I64, D, C.POINTER(rbg_spmat), I64, I64, P, I64, D,
+                       P, I64, P], C.c_int),
+    "rbg_right_spmm": ([I32, I32, I32, I64, I64, I64, D, P, I64, C.POINTER(rbg_spmat), I64, I64,
+                        D, P, I64, P], C.c_int),
+    "rbg_lskge3_lowp_workspace": ([I32, I64, I64, I64, C.POINTER(C.c_size_t)], C.c_int),
+    "rbg_lskge3_lowp": ([I32, I32, I32, I32, I64, I64, I64, C.c_float, C.POINTER(rbg_dense_skop),
+                         I64, I64, P, I64, C.c_float, P, I64, P, C.c_size_t, P], C.c_int),
+    "rbg_lskge3_batched": ([I32, C.POINTER(rbg_batch_problem), I64, I32, P], C.c_int),
+    "rbg_batched_tile_configs": ([C.POINTER(I32)], C.c_int),
+}
+
+_lock = threading.Lock()
+_lib = None
+
+
+class RandBLASError(RuntimeError):
+    """A failed call of the C ABI; ``code`` is the status, the message is rbg_last_error()."""
+
+    def __init__(self, code: int, message: str):
+        super().__init__(message)
+        self.code = code
+
+
+def lib() -> C.CDLL:
+    """The loaded library (raises if it was not built)."""
+    global _lib
+    if _lib is None:
+        with _lock:
+            if _lib is None:
+                if not os.path.exists(LIB_PATH):
+                    raise ImportError(
+                        f"{LIB_PATH} is missing: build it with `python randblas_gb300/build.py` "
+                        "(there is no CPU fallback)")
+                handle = C.CDLL(LIB_PATH)
+                for name, (args, res) in SIGNATURES.items():
+                    fn = getattr(handle, name)
+                    fn.argtypes = args
+                    fn.restype = res
+                _lib = handle
+    return _lib
+
+
+def check(rc: int) -> None:
+    if rc != SUCCESS:
+        msg = lib().rbg_last_error().decode(errors="replace")
+        raise RandBLASError(rc, msg)
+
+
+def call(name: str, *args) -> None:
+    check(getattr(lib(), name)(*args))

@@ -1,0 +1,242 @@
+// gemm_simt.cu -- the plain (FP32 / FP64) dense sketch: LSKGE3 / RSKGE3 semantics
+// (RandBLAS/skge.hh:154-202, 307-355) as one CUDA-core GEMM whose S operand is produced
+// tile by tile inside the kernel (or read from a materialised DenseSkOp buffer).
+//
+// Canonical problem: Out[M x N] = alpha * P[M x K] * Q[K x N] + beta * Out, with
+// P = op(submat(S)) (left sketch) or its transpose (right sketch, solved as B^T), Q a
+// strided view of op(A).  The reference materialises submat(S) with new[] and calls
+// blas::gemm; here S never touches HBM.  Accumulation is in T (float or double), like the
+// reference's BLAS call; K is split across CTAs when the output has too few tiles, with a
+// fixed-order reduction so results do not depend on timing.
+#include <algorithm>
+
+#include "rbg_internal.h"
+
+namespace rbg {
+namespace {
+
+constexpr int BM = 128, BN = 128, BK = 16, NT = 256;
+
+// P tile, k-major: Ps[k][i] for i in [0, BM), k in [0, BK).  Entries outside M x K are 0.
+template <typename T>
+__device__ __forceinline__ void gen_p_tile(T (*Ps)[BM + 4], const POperand &P, int64_t M,
+                                           int64_t K, int64_t i0, int64_t k0) {
+    const DenseGen &g = P.gen;
+    if (P.r_on_i) {
+        // R follows i, C follows k: each of the BM rows needs the counter blocks covering
+        // columns [c0 + k0, c0 + k0 + BK).
+        const int64_t cfirst = P.c0 + k0;
+        const int64_t b0 = cfirst / 4;
+        const int nb = (int)((cfirst + BK - 1) / 4 - b0 + 1);
+        for (int w = threadIdx.x; w < BM * nb; w += NT) {
+            const int i = w / nb, b = w % nb;
+            const bool row_ok = i0 + i < M;
+            float v[4] = {0.f, 0.f, 0.f, 0.f};
+            if (row_ok) gen4(g.family, g.counter_of(P.r0 + i0 + i, b0 + b), g.key, v);
+#pragma unroll
+            for (int l = 0; l < 4; ++l) {
+                const int64_t k = (b0 + b) * 4 + l - cfirst;
+                if (k >= 0 && k < BK)
+                    Ps[k][i] = (row_ok && k0 + k < K) ? finish_entry<T>(g.family, v[l]) : (T)0;
+            }
+        }
+    } else {
+        // R follows k, C follows i: each of the BK rows needs the blocks covering columns
+        // [c0 + i0, c0 + i0 + BM).
+        const int64_t cfirst = P.c0 + i0;
+        const int64_t b0 = cfirst / 4;
+        const int nb = (int)((cfirst + BM - 1) / 4 - b0 + 1);
+        for (int w = threadIdx.x; w < BK * nb; w += NT) {
+            const int k = w / nb, b = w % nb;
+            const bool k_ok = k0 + k < K;
+            float v[4] = {0.f, 0.f, 0.f, 0.f};
+            if (k_ok) gen4(g.family, g.counter_of(P.r0 + k0 + k, b0 + b), g.key, v);
+#pragma unroll
+            for (int l = 0; l < 4; ++l) {
+                const int64_t i = (b0 + b) * 4 + l - cfirst;
+                if (i >= 0 && i < BM)
+                    Ps[k][i] = (k_ok && i0 + i < M) ? finish_entry<T>(g.family, v[l]) : (T)0;
+            }
+        }
+    }
+}
+
+// Strided tile load into a k-major SMEM tile: dst[k][x] = src(k0 + k, x0 + x), x in [0, W).
+// Threads walk the unit-stride dimension when there is one.
+template <typename T, int W>
+__device__ __forceinline__ void load_tile(T (*dst)[W + 4], const T *__restrict__ src,
+                                          int64_t sk, int64_t sx, int64_t K, int64_t X,
+                                          int64_t k0, int64_t x0) {
+    if (sx == 1 || sk != 1) {
+        for (int w = threadIdx.x; w < BK * W; w += NT) {
+            const int k = w / W, x = w % W;
+            dst[k][x] = (k0 + k < K && x0 + x < X) ? src[(k0 + k) * sk + (x0 + x) * sx] : (T)0;
+        }
+    } else {
+        for (int w = threadIdx.x; w < BK * W; w += NT) {
+            const int x = w / BK, k = w % BK;
+            dst[k][x] = (k0 + k < K && x0 + x < X) ? src[(k0 + k) * sk + (x0 + x) * sx] : (T)0;
+        }
+    }
+}
+
+template <typename T, bool GEN>
+__global__ void __launch_bounds__(NT, sizeof(T) == 4 ? 2 : 1)
+    dense_sketch_kernel(int64_t M, int64_t N, int64_t K, POperand P, Strided Q, T alpha, T beta,
+                        T *__restrict__ out, int64_t os_i, int64_t os_j, int64_t kt_per_split,
+                        T *__restrict__ partial) {
+    __shared__ __align__(16) T Ps[BK][BM + 4];
+    __shared__ __align__(16) T Qs[BK][BN + 4];
+    const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
+    const int64_t tiles_n = (N + BN - 1) / BN;
+    const int64_t i0 = (blockIdx.x / tiles_n) * BM;
+    const int64_t j0 = (blockIdx.x % tiles_n) * BN;
+    const int64_t kt_total = (K + BK - 1) / BK;
+    const int64_t kt_begin = blockIdx.y * kt_per_split;
+    const int64_t kt_end = min(kt_total, kt_begin + kt_per_split);
+
+    T acc[8][8];
+#pragma unroll
+    for (int a = 0; a < 8; ++a)
+#pragma unroll
+        for (int b = 0; b < 8; ++b) acc[a][b] = (T)0;
+
+    const T *Qp = static_cast<const T *>(Q.ptr);
+    for (int64_t kt = kt_begin; kt < kt_end; ++kt) {
+        const int64_t k0 = kt * BK;
+        if constexpr (GEN) {
+            gen_p_tile<T>(Ps, P, M, K, i0, k0);
+        } else {
+            // P(i, k) = buff[base + i*si + k*sk]
+            load_tile<T, BM>(Ps, static_cast<const T *>(P.buff) + P.base, P.sk, P.si, K, M, k0,
+                             i0);
+        }
+        load_tile<T, BN>(Qs, Qp, Q.s0, Q.s1, K, N, k0, j0);
+        __syncthreads();
+#pragma unroll
+        for (int kk = 0; kk < BK; ++kk) {
+            T a[8], b[8];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                a[q] = Ps[kk][ty * 4 + q];
+                a[4 + q] = Ps[kk][64 + ty * 4 + q];
+                b[q] = Qs[kk][tx * 4 + q];
+                b[4 + q] = Qs[kk][64 + tx * 4 + q];
+            }
+#pragma unroll
+            for (int x = 0; x < 8; ++x)
+#pragma unroll
+                for (int y = 0; y < 8; ++y) acc[x][y] = fma(a[x], b[y], acc[x][y]);
+        }
+        __syncthreads();
+    }
+
+#pragma unroll
+    for (int x = 0; x < 8; ++x) {
+        const int64_t i = i0 + (x < 4 ? ty * 4 + x : 64 + ty * 4 + (x - 4));
+        if (i >= M) continue;
+#pragma unroll
+        for (int y = 0; y < 8; ++y) {
+            const int64_t j = j0 + (y < 4 ? tx * 4 + y : 64 + tx * 4 + (y - 4));
+            if (j >= N) continue;
+            if (partial) {
+                partial[((int64_t)blockIdx.y * M + i) * N + j] = acc[x][y];
+            } else {
+                T &o = out[i * os_i + j * os_j];
+                o = (beta == (T)0) ? alpha * acc[x][y] : fma(alpha, acc[x][y], beta * o);
+            }
+        }
+    }
+}
+
+// out = alpha * sum_s partial[s] + beta * out, splits summed in order 0..S-1.
+template <typename T>
+__global__ void reduce_splits_kernel(int64_t M, int64_t N, int splits, const T *partial, T alpha,
+                                     T beta, T *out, int64_t os_i, int64_t os_j) {
+    const int64_t total = M * N;
+    const bool j_fast = os_j <= os_i;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total;
+         t += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t i = j_fast ? t / N : t % M;
+        const int64_t j = j_fast ? t % N : t / M;
+        T sum = (T)0;
+        for (int s = 0; s < splits; ++s) sum += partial[((int64_t)s * M + i) * N + j];
+        T &o = out[i * os_i + j * os_j];
+        o = (beta == (T)0) ? alpha * sum : fma(alpha, sum, beta * o);
+    }
+}
+
+// Pick a split of K so that tiles * splits fills whole waves of resident CTAs.
+int choose_splits(int64_t tiles, int64_t kt_total, int64_t out_elems, size_t esz) {
+    const int64_t slots = (int64_t)num_sms() * 2;
+    if (tiles >= 4 * slots || kt_total < 16) return 1;
+    int best = 1;
+    double best_eff = -1.0;
+    for (int s = 1; s <= 64; ++s) {
+        if (kt_total / s < 8) break;
+        if ((double)s * out_elems * esz > (double)(1ll << 30)) break;
+        const int64_t ctas = tiles * s;
+        const int64_t waves = (ctas + slots - 1) / slots;
+        const double eff = (double)ctas / (double)(waves * slots) - 0.002 * s;
+        if (eff > best_eff + 1e-9) {
+            best_eff = eff;
+            best = s;
+        }
+    }
+    return best;
+}
+
+template <typename T>
+void run(int64_t M, int64_t N, int64_t K, double alpha, const POperand &P, const Strided &Q,
+         double beta, void *out, int64_t os_i, int64_t os_j, cudaStream_t s) {
+    const int64_t tiles = ((M + BM - 1) / BM) * ((N + BN - 1) / BN);
+    const int64_t kt_total = (K + BK - 1) / BK;
+    const int splits = choose_splits(tiles, kt_total, M * N, sizeof(T));
+    const int64_t kt_per_split = (kt_total + splits - 1) / splits;
+    Scratch ws;
+    T *partial = nullptr;
+    if (splits > 1) {
+        ws.alloc((size_t)splits * M * N * sizeof(T), s);
+        partial = ws.as<T>();
+    }
+    const dim3 grid((unsigned)tiles, (unsigned)splits);
+    {
+        ProfScope prof(P.buff ? "dense_sketch_simt_loaded" : "dense_sketch_simt_generated", s);
+        if (P.buff)
+            dense_sketch_kernel<T, false><<<grid, NT, 0, s>>>(M, N, K, P, Q, (T)alpha, (T)beta,
+                                                              (T *)out, os_i, os_j, kt_per_split,
+                                                              partial);
+        else
+            dense_sketch_kernel<T, true><<<grid, NT, 0, s>>>(M, N, K, P, Q, (T)alpha, (T)beta,
+                                                             (T *)out, os_i, os_j, kt_per_split,
+                                                             partial);
+        RBG_LAUNCHED();
+    }
+    if (splits > 1) {
+        const int64_t work = M * N;
+        const int grid_r = (int)std::max<int64_t>(
+            1, std::min<int64_t>((work + 255) / 256, (int64_t)num_sms() * 16));
+        reduce_splits_kernel<T><<<grid_r, 256, 0, s>>>(M, N, splits, partial, (T)alpha,
+                                                       (T)beta, (T *)out, os_i, os_j);
+        RBG_LAUNCHED();
+    }
+}
+
+}  // namespace
+
+void gemm_dense_sketch(int dtype, int64_t M, int64_t N, int64_t K, double alpha,
+                       const POperand &P, const Strided &Q, double beta, void *out,
+                       int64_t os_i, int64_t os_j, cudaStream_t s) {
+    if (M <= 0 || N <= 0) return;
+    if (K <= 0 || alpha == 0.0) {
+        // B = beta * B; A and S are not read (BLAS gemm semantics at alpha == 0).
+        launch_scale(dtype, M, N, os_i, os_j, beta, out, s);
+        return;
+    }
+    if (dtype == RBG_F32)
+        run<float>(M, N, K, alpha, P, Q, beta, out, os_i, os_j, s);
+    else
+        run<double>(M, N, K, alpha, P, Q, beta, out, os_i, os_j, s);
+}
+
+}  // namespace rbg

@@ -1,0 +1,142 @@
+// rbg_common.cuh -- device building blocks shared by every kernel of the library:
+// Philox4x32-10, 128-bit counter arithmetic, the float transforms RandBLAS applies to
+// Philox output, and the entry-generation rule of a dense sketching operator.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "randblas_gb300.h"
+
+namespace rbg {
+
+// ------------------------------------------------------------------ Philox4x32-10
+// Salmon, Moraes, Dror, Shaw, "Parallel Random Numbers: As Easy as 1, 2, 3" (SC'11),
+// section 4: Philox-4x32 with 10 rounds.  This is the generator behind RandBLAS's
+// DefaultRNG (RandBLAS/base.hh:53).
+constexpr uint32_t kMulA = 0xD2511F53u;
+constexpr uint32_t kMulB = 0xCD9E8D57u;
+constexpr uint32_t kWeylA = 0x9E3779B9u;
+constexpr uint32_t kWeylB = 0xBB67AE85u;
+
+__device__ __forceinline__ uint4 philox(uint4 c, uint2 k) {
+#pragma unroll
+    for (int round = 0; round < 10; ++round) {
+        if (round > 0) {
+            k.x += kWeylA;
+            k.y += kWeylB;
+        }
+        const uint32_t hi_a = __umulhi(kMulA, c.x), lo_a = kMulA * c.x;
+        const uint32_t hi_b = __umulhi(kMulB, c.z), lo_b = kMulB * c.z;
+        c = make_uint4(hi_b ^ c.y ^ k.x, lo_b, hi_a ^ c.w ^ k.y, lo_a);
+    }
+    return c;
+}
+
+// counter + n, the counter read as a little-endian 128-bit integer
+// (Random123's r123array4x32::incr, asserted by test/test_basic_rng/test_r123.cc:705-797).
+__host__ __device__ __forceinline__ uint4 ctr_add(uint4 c, uint64_t n) {
+    const uint64_t lo = ((uint64_t)c.y << 32 | c.x);
+    const uint64_t sum = lo + n;
+    const uint64_t carry = sum < lo ? 1u : 0u;
+    uint64_t hi = ((uint64_t)c.w << 32 | c.z) + carry;
+    return make_uint4((uint32_t)sum, (uint32_t)(sum >> 32), (uint32_t)hi, (uint32_t)(hi >> 32));
+}
+
+struct DevState {
+    uint4 ctr;
+    uint2 key;
+};
+
+__host__ __device__ __forceinline__ DevState to_dev(const rbg_state &s) {
+    return DevState{make_uint4(s.counter[0], s.counter[1], s.counter[2], s.counter[3]),
+                    make_uint2(s.key[0], s.key[1])};
+}
+
+// ------------------------------------------------------------------ transforms
+// Random123's documented transforms, as RandBLAS uses them (RandBLAS/random_gen.hh:60-137):
+//   uneg11(x) = (int32)x * 2^-31 + 2^-32, u01(x) = x * 2^-32 + 2^-33 (float),
+//   boxmuller(u0, u1) = (sin(pi*uneg11(u0)) * r, cos(pi*uneg11(u0)) * r),
+//   r = sqrt(-2 log(u01(u1))).
+// The products by powers of two are exact, so the single rounding of each transform does
+// not depend on FMA contraction.
+__device__ __forceinline__ float uneg11(uint32_t x) {
+    return __fadd_rn(__fmul_rn(__int2float_rn((int32_t)x), 0x1p-31f), 0x1p-32f);
+}
+
+__device__ __forceinline__ float u01(uint32_t x) {
+    return __fadd_rn(__fmul_rn(__uint2float_rn(x), 0x1p-32f), 0x1p-33f);
+}
+
+// CUDA's accurate (non-intrinsic) sincosf/logf/sqrtf; the products are rounded once each,
+// like the host code they mirror.  The results match glibc's to a few ulp (measured by
+// the parity tests), not bit for bit.
+__device__ __forceinline__ void boxmuller(uint32_t u0, uint32_t u1, float &first,
+                                          float &second) {
+    float s, c;
+    sincosf(__fmul_rn(3.14159265358979323846f, uneg11(u0)), &s, &c);
+    const float r = sqrtf(__fmul_rn(-2.0f, logf(u01(u1))));
+    first = __fmul_rn(s, r);
+    second = __fmul_rn(c, r);
+}
+
+// Four operator entries from one Philox call: Gaussian pairs (lanes 0,1) and (2,3), or
+// four uniforms on (-1, 1).  Uniform entries are NOT scaled here (see scale_uniform).
+__device__ __forceinline__ void gen4(int family, uint4 ctr, uint2 key, float v[4]) {
+    const uint4 r = philox(ctr, key);
+    if (family == RBG_GAUSSIAN) {
+        boxmuller(r.x, r.y, v[0], v[1]);
+        boxmuller(r.z, r.w, v[2], v[3]);
+    } else {
+        v[0] = uneg11(r.x);
+        v[1] = uneg11(r.y);
+        v[2] = uneg11(r.z);
+        v[3] = uneg11(r.w);
+    }
+}
+
+// RandBLAS scales uniform entries by (T)sqrt(3) in the operator's precision T after the
+// float transform (RandBLAS/dense_skops.hh:589).
+template <typename T>
+__device__ __forceinline__ T scale_uniform(float v);
+template <>
+__device__ __forceinline__ float scale_uniform<float>(float v) {
+    return __fmul_rn(v, 1.7320508075688772f);
+}
+template <>
+__device__ __forceinline__ double scale_uniform<double>(float v) {
+    return __dmul_rn((double)v, 1.7320508075688772);
+}
+
+template <typename T>
+__device__ __forceinline__ T finish_entry(int family, float v) {
+    return family == RBG_UNIFORM ? scale_uniform<T>(v) : (T)v;
+}
+
+// ------------------------------------------------------------------ dense operators
+// A dense operator entry S(x, y) (0 <= x < n_rows, 0 <= y < n_cols) lives at "natural"
+// coordinates (R, C): R = x, C = y when the natural layout is RowMajor, R = y, C = x when
+// it is ColMajor.  Row R owns counters seed + [R*stride, (R+1)*stride) with
+// stride = ceil(dim_major / 4); entry C is lane C % 4 of counter C / 4 of its row
+// (RandBLAS/dense_skops.hh:96-170, 563-606).
+struct DenseGen {
+    uint4 ctr;        // seed counter
+    uint2 key;        // seed key
+    int64_t stride;   // counters per natural row
+    int family;       // RBG_GAUSSIAN / RBG_UNIFORM
+    int natural_col;  // 1 when the natural layout is ColMajor
+
+    __device__ __forceinline__ uint4 counter_of(int64_t R, int64_t block) const {
+        return ctr_add(ctr, (uint64_t)(R * stride + block));
+    }
+};
+
+// Per-launch error word (device-side bounds checks and bounded waits report here).
+struct DevError {
+    int *flag;  // nullable
+    __device__ __forceinline__ void raise(int code) const {
+        if (flag) atomicCAS(flag, 0, code);
+    }
+};
+
+}  // namespace rbg

@@ -1,0 +1,436 @@
+// spmm.cu -- sparse sketching and sparse-times-dense products:
+//   LSKGES / RSKGES (RandBLAS/skge.hh:465-492, 598-626), left_spmm / right_spmm
+//   (RandBLAS/sparse_data/spmm_dispatch.hh:52-219) and the SpMM inside LSKSP3 / RSKSP3.
+//
+// Canonical problem: Out[M x N] = alpha * Sp[M x K] * Q[K x N] + beta * Out with Sp sparse.
+//
+// 1. Row lists.  The nonzeros of Sp (after the submatrix filter and the transpose that
+//    op() asks for) are sorted by (row, k) with a stable radix sort, giving CSR-like row
+//    lists whose entries are in increasing k.  A SASO that has not been sampled is sampled
+//    right here (Fisher-Yates per minor index, RandBLAS/sparse_skops.hh:51-106) and never
+//    written out as COO.
+// 2. SpMM.  A CTA owns 1024 output rows x 32 output columns x one K range.  It walks the K
+//    range in blocks: the block of Q (KB x 32) is staged in shared memory once, then each
+//    warp adds, for each of its 32 rows, the row's entries that fall in the block -- lane
+//    = output column, accumulators in registers, entries in k order.  Each CTA writes a
+//    partial result for its K range and a second kernel adds the ranges in a fixed order,
+//    so results are deterministic.  Reads of Q are coalesced and happen once per CTA.
+#include <cub/device/device_radix_sort.cuh>
+
+#include <algorithm>
+
+#include "rbg_internal.h"
+
+namespace rbg {
+namespace {
+
+constexpr int kSliceCols = 32;
+// Rows per warp: 32 accumulators per lane for float, 16 for double (register budget of a
+// 1024-thread CTA).
+template <typename T>
+constexpr int rows_per_warp() { return sizeof(T) == 4 ? 32 : 16; }
+
+int bits_for(uint64_t x) {  // bits needed to store values in [0, x]
+    int b = 0;
+    while (b < 64 && (x >> b) != 0) ++b;
+    return std::max(b, 1);
+}
+
+// ------------------------------------------------------------------ entry extraction
+// Writes one slot per potential nonzero: key = (row << kbits) | k (or row alone when the
+// entries are known to arrive in increasing k per row); entries outside the submatrix get
+// key M << kbits, which sorts after every valid key; kcol[slot] = k; val[slot] = value.
+struct KeySpec {
+    int64_t M, K, ro, co;
+    int trans;
+    int kbits;        // 0: key = row only
+};
+
+template <typename V>
+__device__ __forceinline__ void emit(const KeySpec &ks, int64_t slot, int64_t x, int64_t y, V v,
+                                     uint64_t *key, int32_t *kcol, V *val) {
+    // Sp(i, k) = X(ro + i, co + k), or X(ro + k, co + i) when transposed.
+    const int64_t i = ks.trans ? y - ks.co : x - ks.ro;
+    const int64_t k = ks.trans ? x - ks.ro : y - ks.co;
+    const bool ok = i >= 0 && i < ks.M && k >= 0 && k < ks.K;
+    key[slot] = ok ? (((uint64_t)i << ks.kbits) | (ks.kbits ? (uint64_t)k : 0ull))
+                   : ((uint64_t)ks.M << ks.kbits);
+    kcol[slot] = ok ? (int32_t)k : 0;
+    val[slot] = v;
+}
+
+// Generated SASO: same steps as the sampling kernel in fill.cu (vec_nnz Fisher-Yates steps
+// per minor index, counter seed + i*vec_nnz + j), emitted straight into sort slots.
+template <typename V>
+__global__ void saso_entries_kernel(DevState s, int64_t vec_nnz, int64_t dim_major,
+                                    int64_t dim_minor, int short_is_row, KeySpec ks,
+                                    uint64_t *key, int32_t *kcol, V *val) {
+    const int64_t tid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    const int64_t nthreads = (int64_t)gridDim.x * blockDim.x;
+    int64_t mp[64], mv[64];  // vec_nnz <= 64 on this path (checked by the host)
+    for (int64_t i = tid; i < dim_minor; i += nthreads) {
+        int msize = 0;
+        const int64_t off = i * vec_nnz;
+        for (int64_t j = 0; j < vec_nnz; ++j) {
+            const uint4 r = philox(ctr_add(s.ctr, (uint64_t)(off + j)), s.key);
+            const int64_t ell = j + (int64_t)((uint64_t)r.x % (uint64_t)(dim_major - j));
+            int64_t vj = j, vl = ell;
+            int sj = -1, sl = -1;
+            for (int q = 0; q < msize; ++q) {
+                if (mp[q] == j) { vj = mv[q]; sj = q; }
+                if (mp[q] == ell) { vl = mv[q]; sl = q; }
+            }
+            if (ell != j) {
+                if (sl >= 0) {
+                    mv[sl] = vj;
+                } else {
+                    mp[msize] = ell;
+                    mv[msize] = vj;
+                    ++msize;
+                }
+            }
+            if (sj >= 0) {
+                --msize;
+                mp[sj] = mp[msize];
+                mv[sj] = mv[msize];
+            }
+            const V v = (r.y % 2u == 0u) ? (V)1 : (V)-1;
+            const int64_t x = short_is_row ? vl : i;
+            const int64_t y = short_is_row ? i : vl;
+            emit(ks, off + j, x, y, v, key, kcol, val);
+        }
+    }
+}
+
+template <typename V, typename I>
+__global__ void coo_entries_kernel(int64_t nnz, const I *rows, const I *cols, const V *vals,
+                                   KeySpec ks, uint64_t *key, int32_t *kcol, V *val) {
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < nnz;
+         e += (int64_t)gridDim.x * blockDim.x)
+        emit(ks, e, (int64_t)rows[e], (int64_t)cols[e], vals[e], key, kcol, val);
+}
+
+// CSR (compressed over rows, by_rows = 1) or CSC (compressed over columns): one thread per
+// compressed line.
+template <typename V, typename I>
+__global__ void compressed_entries_kernel(int64_t lines, const I *ptr, const I *idx,
+                                          const V *vals, int by_rows, KeySpec ks, uint64_t *key,
+                                          int32_t *kcol, V *val) {
+    for (int64_t l = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; l < lines;
+         l += (int64_t)gridDim.x * blockDim.x) {
+        for (int64_t e = (int64_t)ptr[l]; e < (int64_t)ptr[l + 1]; ++e) {
+            const int64_t other = (int64_t)idx[e];
+            emit(ks, e, by_rows ? l : other, by_rows ? other : l, vals[e], key, kcol, val);
+        }
+    }
+}
+
+template <typename V>
+__global__ void gather_entries_kernel(int64_t n, const int32_t *perm, const int32_t *kcol_in,
+                                      const V *val_in, int32_t *kcol_out, V *val_out) {
+    for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < n;
+         p += (int64_t)gridDim.x * blockDim.x) {
+        const int32_t e = perm[p];
+        kcol_out[p] = kcol_in[e];
+        val_out[p] = val_in[e];
+    }
+}
+
+__global__ void iota_kernel(int64_t n, int32_t *p) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x)
+        p[i] = (int32_t)i;
+}
+
+// rowptr[r] = first sorted position whose row is >= r, for r in [0, M]; entries outside the
+// submatrix carry row M and sort last.
+__global__ void rowptr_kernel(int64_t n, const uint64_t *skey, int kbits, int64_t M,
+                              int64_t *rowptr) {
+    for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p <= n;
+         p += (int64_t)gridDim.x * blockDim.x) {
+        auto row_of = [&](int64_t q) -> int64_t {
+            if (q >= n) return M;
+            return (int64_t)(skey[q] >> kbits);
+        };
+        const int64_t hi = row_of(p);
+        const int64_t lo = p == 0 ? -1 : row_of(p - 1);
+        for (int64_t r = lo + 1; r <= hi && r <= M; ++r) rowptr[r] = p;
+    }
+}
+
+// ------------------------------------------------------------------ SpMM
+template <typename T>
+struct SpmmArgs {
+    int64_t M, N, K;
+    const int64_t *rowptr;
+    const int32_t *kcol;
+    const T *val;
+    const T *Q;
+    int64_t qs0, qs1;     // Q(k, c) = Q[k*qs0 + c*qs1]
+    int64_t k_per_split;  // multiple of KB
+    T *partial;           // [split][M][N], or nullptr when writing `out` directly
+    T *out;
+    int64_t os_i, os_j;
+    T alpha, beta;
+};
+
+template <typename T, int KB>
+__global__ void __launch_bounds__(1024, 1) spmm_rows_kernel(SpmmArgs<T> a) {
+    constexpr int RPW = rows_per_warp<T>();
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T(*Qs)[kSliceCols + 1] = reinterpret_cast<T(*)[kSliceCols + 1]>(smem_raw);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int64_t c0 = (int64_t)blockIdx.x * kSliceCols;
+    const int64_t row_base = (int64_t)blockIdx.y * (32 * RPW) + warp * RPW;
+    const int64_t ka = (int64_t)blockIdx.z * a.k_per_split;
+    const int64_t kz = min(a.K, ka + a.k_per_split);
+
+    // lane l < RPW tracks row row_base + l: cursor = first entry with k >= block start
+    const int64_t my_row = row_base + lane;
+    int64_t cur = 0, end = 0;
+    if (lane < RPW && my_row < a.M) {
+        int64_t lo = a.rowptr[my_row], hi = a.rowptr[my_row + 1];
+        end = hi;
+        while (lo < hi) {  // lower_bound of ka
+            const int64_t mid = (lo + hi) >> 1;
+            if (a.kcol[mid] < ka) lo = mid + 1;
+            else hi = mid;
+        }
+        cur = lo;
+    }
+
+    T acc[RPW];
+#pragma unroll
+    for (int r = 0; r < RPW; ++r) acc[r] = (T)0;
+    const int64_t col = c0 + lane;
+    const bool col_ok = col < a.N;
+
+    for (int64_t kb = ka; kb < kz; kb += KB) {
+        const int kn = (int)min((int64_t)KB, kz - kb);
+        __syncthreads();
+        if (a.qs1 == 1 || a.qs0 != 1) {
+            for (int w = threadIdx.x; w < KB * kSliceCols; w += blockDim.x) {
+                const int k = w / kSliceCols, c = w % kSliceCols;
+                Qs[k][c] = (k < kn && c0 + c < a.N) ? a.Q[(kb + k) * a.qs0 + (c0 + c) * a.qs1]
+                                                     : (T)0;
+            }
+        } else {
+            for (int w = threadIdx.x; w < KB * kSliceCols; w += blockDim.x) {
+                const int c = w / KB, k = w % KB;
+                Qs[k][c] = (k < kn && c0 + c < a.N) ? a.Q[(kb + k) * a.qs0 + (c0 + c) * a.qs1]
+                                                     : (T)0;
+            }
+        }
+        __syncthreads();
+        const int64_t kend = kb + kn;
+#pragma unroll
+        for (int r = 0; r < RPW; ++r) {
+            int64_t c = __shfl_sync(0xffffffffu, cur, r);
+            const int64_t e = __shfl_sync(0xffffffffu, end, r);
+            while (true) {
+                const int64_t idx = c + lane;
+                const bool valid = idx < e;
+                const int32_t kk = valid ? a.kcol[idx] : INT32_MAX;
+                const T vv = valid ? a.val[idx] : (T)0;
+                const unsigned in_blk = __ballot_sync(0xffffffffu, valid && kk < kend);
+                const int cnt = __popc(in_blk);  // entries are k-sorted: a prefix
+                for (int t = 0; t < cnt; ++t) {
+                    const int32_t kt = __shfl_sync(0xffffffffu, kk, t);
+                    const T vt = __shfl_sync(0xffffffffu, vv, t);
+                    acc[r] = fma(vt, Qs[kt - kb][lane], acc[r]);
+                }
+                c += cnt;
+                if (cnt < 32) break;
+            }
+            if (lane == r) cur = c;
+        }
+    }
+
+    if (!col_ok) return;
+#pragma unroll
+    for (int r = 0; r < RPW; ++r) {
+        const int64_t i = row_base + r;
+        if (i >= a.M) break;
+        if (a.partial) {
+            a.partial[((int64_t)blockIdx.z * a.M + i) * a.N + col] = acc[r];
+        } else {
+            T &o = a.out[i * a.os_i + col * a.os_j];
+            o = (a.beta == (T)0) ? a.alpha * acc[r] : fma(a.alpha, acc[r], a.beta * o);
+        }
+    }
+}
+
+template <typename T>
+__global__ void spmm_reduce_kernel(int64_t M, int64_t N, int splits, const T *partial, T alpha,
+                                   T beta, T *out, int64_t os_i, int64_t os_j) {
+    const int64_t total = M * N;
+    const bool j_fast = os_j <= os_i;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total;
+         t += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t i = j_fast ? t / N : t % M;
+        const int64_t j = j_fast ? t % N : t / M;
+        T sum = (T)0;
+        for (int s = 0; s < splits; ++s) sum += partial[((int64_t)s * M + i) * N + j];
+        T &o = out[i * os_i + j * os_j];
+        o = (beta == (T)0) ? alpha * sum : fma(alpha, sum, beta * o);
+    }
+}
+
+int grid1d(int64_t work, int threads) {
+    return (int)std::max<int64_t>(
+        1, std::min<int64_t>((work + threads - 1) / threads, (int64_t)num_sms() * 16));
+}
+
+template <typename T>
+void run(int64_t M, int64_t N, int64_t K, double alpha, const SparseOperand &Sp,
+         const Strided &Q, double beta, void *out, int64_t os_i, int64_t os_j, cudaStream_t s) {
+    if (K > INT32_MAX) fail(RBG_ERROR_UNSUPPORTED, "sparse sketch: inner dimension >= 2^31");
+    // ---- 1. entries into sort slots
+    int64_t slots = 0;
+    bool k_ordered = false;  // entries of each row already arrive in increasing k
+    if (Sp.kind == SparseOperand::SASO_GEN) {
+        slots = safe_mul(Sp.vec_nnz, Sp.dim_minor);
+        // minor index i runs over S's columns (short_is_row) or rows; within one row of Sp
+        // the entries then come in increasing k exactly when k follows the minor index.
+        k_ordered = (Sp.short_is_row && !Sp.trans) || (!Sp.short_is_row && Sp.trans);
+    } else {
+        slots = Sp.nnz;
+    }
+    if (slots > INT32_MAX) fail(RBG_ERROR_UNSUPPORTED, "sparse sketch: more than 2^31 nonzeros");
+    KeySpec ks{M, K, Sp.ro, Sp.co, Sp.trans, 0};
+    const int rbits = bits_for((uint64_t)M);
+    if (!k_ordered) ks.kbits = bits_for((uint64_t)K);
+    if (rbits + ks.kbits > 64) fail(RBG_ERROR_UNSUPPORTED, "sparse sketch: sort key too wide");
+    const int end_bit = rbits + ks.kbits;
+
+    Scratch keys(std::max<int64_t>(slots, 1) * 8, s), skeys(std::max<int64_t>(slots, 1) * 8, s);
+    Scratch kc(std::max<int64_t>(slots, 1) * 4, s), vv(std::max<int64_t>(slots, 1) * sizeof(T), s);
+    Scratch perm(std::max<int64_t>(slots, 1) * 4, s), sperm(std::max<int64_t>(slots, 1) * 4, s);
+    Scratch rowptr((M + 1) * 8, s);
+    const int th = 256;
+    ProfScope prof_lists("spmm_row_lists", s);
+    if (slots > 0) {
+        if (Sp.kind == SparseOperand::SASO_GEN) {
+            if (Sp.vec_nnz > 64)
+                fail(RBG_ERROR_UNSUPPORTED, "in-kernel SASO sampling needs vec_nnz <= 64");
+            saso_entries_kernel<T><<<grid1d(Sp.dim_minor, 128), 128, 0, s>>>(
+                Sp.seed, Sp.vec_nnz, Sp.dim_major, Sp.dim_minor, Sp.short_is_row, ks,
+                keys.as<uint64_t>(), kc.as<int32_t>(), vv.as<T>());
+        } else if (Sp.kind == SparseOperand::COO) {
+            if (Sp.itype == RBG_I32)
+                coo_entries_kernel<T, int32_t><<<grid1d(slots, th), th, 0, s>>>(
+                    slots, (const int32_t *)Sp.idx_a, (const int32_t *)Sp.idx_b,
+                    (const T *)Sp.vals, ks, keys.as<uint64_t>(), kc.as<int32_t>(), vv.as<T>());
+            else
+                coo_entries_kernel<T, int64_t><<<grid1d(slots, th), th, 0, s>>>(
+                    slots, (const int64_t *)Sp.idx_a, (const int64_t *)Sp.idx_b,
+                    (const T *)Sp.vals, ks, keys.as<uint64_t>(), kc.as<int32_t>(), vv.as<T>());
+        } else {
+            const int by_rows = Sp.kind == SparseOperand::CSR;
+            const int64_t lines = by_rows ? Sp.x_rows : Sp.x_cols;
+            if (Sp.itype == RBG_I32)
+                compressed_entries_kernel<T, int32_t><<<grid1d(lines, th), th, 0, s>>>(
+                    lines, (const int32_t *)Sp.idx_a, (const int32_t *)Sp.idx_b,
+                    (const T *)Sp.vals, by_rows, ks, keys.as<uint64_t>(), kc.as<int32_t>(),
+                    vv.as<T>());
+            else
+                compressed_entries_kernel<T, int64_t><<<grid1d(lines, th), th, 0, s>>>(
+                    lines, (const int64_t *)Sp.idx_a, (const int64_t *)Sp.idx_b,
+                    (const T *)Sp.vals, by_rows, ks, keys.as<uint64_t>(), kc.as<int32_t>(),
+                    vv.as<T>());
+        }
+        RBG_LAUNCHED();
+        iota_kernel<<<grid1d(slots, th), th, 0, s>>>(slots, perm.as<int32_t>());
+        RBG_LAUNCHED();
+        // ---- 2. stable sort by key (invalid keys have every bit set and sort last)
+        size_t tmp_bytes = 0;
+        RBG_CUDA(cub::DeviceRadixSort::SortPairs(nullptr, tmp_bytes, keys.as<uint64_t>(),
+                                                 skeys.as<uint64_t>(), perm.as<int32_t>(),
+                                                 sperm.as<int32_t>(), (int)slots, 0, end_bit,
+                                                 s));
+        Scratch tmp(tmp_bytes, s);
+        RBG_CUDA(cub::DeviceRadixSort::SortPairs(tmp.ptr, tmp_bytes, keys.as<uint64_t>(),
+                                                 skeys.as<uint64_t>(), perm.as<int32_t>(),
+                                                 sperm.as<int32_t>(), (int)slots, 0, end_bit,
+                                                 s));
+        // sorted entries go back into the `keys` buffer's neighbours: reuse perm/kc storage
+        gather_entries_kernel<T><<<grid1d(slots, th), th, 0, s>>>(
+            slots, sperm.as<int32_t>(), kc.as<int32_t>(), vv.as<T>(), perm.as<int32_t>(),
+            reinterpret_cast<T *>(keys.ptr));
+        RBG_LAUNCHED();
+    }
+    rowptr_kernel<<<grid1d(slots + 1, th), th, 0, s>>>(slots, skeys.as<uint64_t>(),
+                                                        ks.kbits, M, rowptr.as<int64_t>());
+    RBG_LAUNCHED();
+    prof_lists.finish();
+
+    // ---- 3. SpMM
+    constexpr int KB = sizeof(T) == 4 ? 1024 : 512;
+    const int64_t slices = (N + kSliceCols - 1) / kSliceCols;
+    constexpr int rows_per_cta = 32 * rows_per_warp<T>();
+    const int64_t rblocks = (M + rows_per_cta - 1) / rows_per_cta;
+    const int64_t kblocks = (K + KB - 1) / KB;
+    const int64_t base = slices * rblocks;
+    const int64_t sms = num_sms();
+    int64_t splits = 1;
+    if (base < sms) {
+        splits = std::max<int64_t>(1, sms / base);
+        splits = std::min<int64_t>(splits, kblocks);
+        while (splits > 1 && (double)splits * M * N * sizeof(T) > (double)(1ll << 30)) --splits;
+    }
+    const int64_t kb_per_split = (kblocks + splits - 1) / splits;
+    splits = (kblocks + kb_per_split - 1) / kb_per_split;
+    if (splits > 65535 || rblocks > 65535) fail(RBG_ERROR_UNSUPPORTED, "sparse sketch too large");
+    Scratch part;
+    SpmmArgs<T> args{};
+    args.M = M; args.N = N; args.K = K;
+    args.rowptr = rowptr.as<int64_t>();
+    args.kcol = perm.as<int32_t>();
+    args.val = reinterpret_cast<const T *>(keys.ptr);
+    args.Q = static_cast<const T *>(Q.ptr);
+    args.qs0 = Q.s0; args.qs1 = Q.s1;
+    args.k_per_split = kb_per_split * KB;
+    args.out = (T *)out; args.os_i = os_i; args.os_j = os_j;
+    args.alpha = (T)alpha; args.beta = (T)beta;
+    if (splits > 1) {
+        part.alloc((size_t)splits * M * N * sizeof(T), s);
+        args.partial = part.as<T>();
+    }
+    const size_t smem = (size_t)KB * (kSliceCols + 1) * sizeof(T);
+    static bool attr_set[2] = {false, false};
+    if (!attr_set[sizeof(T) == 8]) {
+        RBG_CUDA(cudaFuncSetAttribute(spmm_rows_kernel<T, KB>,
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        attr_set[sizeof(T) == 8] = true;
+    }
+    {
+        ProfScope prof("spmm_rows", s);
+        spmm_rows_kernel<T, KB><<<dim3((unsigned)slices, (unsigned)rblocks, (unsigned)splits),
+                                  1024, smem, s>>>(args);
+        RBG_LAUNCHED();
+    }
+    if (splits > 1) {
+        spmm_reduce_kernel<T><<<grid1d(M * N, 256), 256, 0, s>>>(M, N, (int)splits, args.partial,
+                                                                (T)alpha, (T)beta, (T *)out,
+                                                                os_i, os_j);
+        RBG_LAUNCHED();
+    }
+}
+
+}  // namespace
+
+void spmm_sketch(int dtype, int64_t M, int64_t N, int64_t K, double alpha,
+                 const SparseOperand &Sp, const Strided &Q, double beta, void *out,
+                 int64_t os_i, int64_t os_j, cudaStream_t s) {
+    if (M <= 0 || N <= 0) return;
+    if (K <= 0 || alpha == 0.0) {
+        launch_scale(dtype, M, N, os_i, os_j, beta, out, s);
+        return;
+    }
+    if (dtype == RBG_F32)
+        run<float>(M, N, K, alpha, Sp, Q, beta, out, os_i, os_j, s);
+    else
+        run<double>(M, N, K, alpha, Sp, Q, beta, out, os_i, os_j, s);
+}
+
+}  // namespace rbg

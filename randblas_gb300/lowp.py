@@ -1,0 +1,39 @@
+"""Tensor-core precision path (rbg_lskge3_lowp): the left dense sketch with the operator's
+entries generated in-kernel and rounded, together with A, to BF16 (or FP8 e4m3 with per-128
+scales), FP32 accumulation.  No reference counterpart; same argument meaning as
+sketch_general's left form with T = float."""
+from __future__ import annotations
+
+import ctypes as C
+
+import torch
+
+from . import _lib
+from ._lib import call
+from .api import DenseSkOp, Layout, Op, _ptr, _stream
+
+BF16 = _lib.PREC_BF16
+FP8_E4M3 = _lib.PREC_FP8_E4M3
+
+
+def available(precision: int = BF16) -> bool:
+    nbytes = C.c_size_t()
+    rc = _lib.lib().rbg_lskge3_lowp_workspace(precision, 128, 128, 128, C.byref(nbytes))
+    return rc == _lib.SUCCESS
+
+
+def workspace_bytes(precision: int, d: int, n: int, m: int) -> int:
+    nbytes = C.c_size_t()
+    call("rbg_lskge3_lowp_workspace", precision, d, n, m, C.byref(nbytes))
+    return nbytes.value
+
+
+def sketch_lowp(layout: Layout, opS: Op, opA: Op, d: int, n: int, m: int, alpha: float,
+                S: DenseSkOp, ro_s: int, co_s: int, A: torch.Tensor, lda: int, beta: float,
+                B: torch.Tensor, ldb: int, precision: int = BF16,
+                workspace: torch.Tensor | None = None) -> None:
+    ws = _ptr(workspace) if workspace is not None else None
+    wbytes = workspace.numel() * workspace.element_size() if workspace is not None else 0
+    call("rbg_lskge3_lowp", precision, int(layout), int(opS), int(opA), d, n, m, float(alpha),
+         C.byref(S._c()), ro_s, co_s, _ptr(A), lda, float(beta), _ptr(B), ldb, ws, wbytes,
+         _stream())

@@ -1,0 +1,292 @@
+"""Generate the golden fixtures in tests/golden/ from the reference itself.
+
+Run in a container that has the RandBLAS source tree (default /root/reference, override with
+RANDBLAS_REF_DIR).  It builds oracle/_ref/librbref.so -- the reference's own headers compiled
+against the project's Random123 / BLAS++ stand-ins -- and records:
+
+* philox_kat.json: the Philox4x32-10 known-answer rows of the reference's
+  test/test_basic_rng/r123_kat_vectors.txt (parsed from that file);
+* fill_dense.npz, fill_sparse.npz, sketch_*.npz: outputs of the reference's public functions on
+  small seeded cases (every layout / op / side / submatrix combination the parity tests use);
+* full_size.json: SHA-256 digests and next states of the full-size operators of the
+  benchmark workloads (the 200 x 10000 Gaussian FP64 operator and its 10000 x 50 uniform data
+  matrix; the 1024 x 2^20 SASO with 8 nonzeros per column), so the GPU tests can pin those
+  bit for bit without shipping the arrays.
+
+Usage: python tests/golden/make_golden.py
+"""
+from __future__ import annotations
+
+import hashlib
+import json
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+from oracle.oracle import RefLib, State  # noqa: E402
+from oracle import build as obuild  # noqa: E402
+
+import itertools  # noqa: E402
+
+CASES = os.path.join(HERE)
+
+
+def st(s: State):
+    return [list(s.counter), list(s.key)]
+
+
+def kat_rows():
+    path = os.path.join(obuild.REF_DIR, "test", "test_basic_rng", "r123_kat_vectors.txt")
+    rows = []
+    with open(path) as f:
+        for line in f:
+            parts = line.split()
+            if len(parts) == 12 and parts[0] == "philox4x32" and parts[1] == "10":
+                vals = [int(x, 16) for x in parts[2:]]
+                rows.append({"ctr": vals[0:4], "key": vals[4:6], "out": vals[6:10]})
+    return rows
+
+
+def dense_fill_cases():
+    cases = []
+    dims = [(7, 13), (13, 7), (37, 90), (90, 37), (5, 5), (64, 65)]
+    for (R, Cc), fam, ax, dt, lay in itertools.product(dims, (0, 1), (0, 1), (0, 1), (0, 1)):
+        subs = [(R, Cc, 0, 0), (max(1, R - 3), max(1, Cc - 5), min(2, R - 1), min(3, Cc - 1)),
+                (1, Cc, R - 1, 0), (R, 1, 0, Cc - 1)]
+        for (nr, nc, ro, co) in subs:
+            cases.append(dict(R=R, C=Cc, family=fam, axis=ax, dtype=dt, layout=lay, nr=nr, nc=nc,
+                              ro=ro, co=co, ctr=[11, 0, 7, 0], key=[2024, 3]))
+    return cases
+
+
+def main():
+    ref = RefLib()
+    out = {}
+
+    kat = kat_rows()
+    assert len(kat) == 3, kat
+    with open(os.path.join(HERE, "philox_kat.json"), "w") as f:
+        json.dump(kat, f, indent=1)
+
+    # ---- fill_dense_unpacked
+    cases = dense_fill_cases()
+    arrays = {}
+    meta = []
+    for i, c in enumerate(cases):
+        seed = State.make(c["ctr"], c["key"])
+        buf, nxt = ref.fill_dense_unpacked(c["dtype"], c["layout"], c["R"], c["C"], c["family"],
+                                           c["axis"], c["nr"], c["nc"], c["ro"], c["co"], seed)
+        arrays[f"c{i}"] = buf
+        meta.append(dict(c, next=st(nxt)))
+    np.savez_compressed(os.path.join(HERE, "fill_dense.npz"), meta=json.dumps(meta), **arrays)
+
+    # ---- fill_sparse (SASO and LASO; LASO stored as per-vector sorted triplets)
+    arrays, meta = {}, []
+    sp_cases = []
+    for (R, Cc, k), ax, dt, it in itertools.product(
+            [(10, 50, 3), (50, 10, 4), (64, 3000, 8), (16, 16, 16), (3, 100, 3), (100, 3, 2),
+             (7, 7, 1)], (0, 1), (0, 1), (0, 1)):
+        sp_cases.append(dict(R=R, C=Cc, vec_nnz=k, axis=ax, dtype=dt, itype=it, ctr=[3, 1, 0, 0],
+                             key=[77, 0]))
+    for i, c in enumerate(sp_cases):
+        seed = State.make(c["ctr"], c["key"])
+        vals, rows, cols, nnz, nxt = ref.fill_sparse(c["dtype"], c["itype"], c["R"], c["C"],
+                                                     c["vec_nnz"], c["axis"], seed)
+        if c["axis"] == 1:
+            order = np.lexsort((cols, rows))
+            vals, rows, cols = vals[order], rows[order], cols[order]
+        arrays[f"v{i}"], arrays[f"r{i}"], arrays[f"c{i}"] = vals, rows, cols
+        meta.append(dict(c, nnz=int(nnz), next=st(nxt)))
+    np.savez_compressed(os.path.join(HERE, "fill_sparse.npz"), meta=json.dumps(meta), **arrays)
+
+    # ---- dense sketches (left / right, all layouts and ops, submatrices, alpha / beta)
+    rng = np.random.default_rng(7)
+    arrays, meta = {}, []
+    i = 0
+    for side, lay, opS, opA, dt, fam, prefill in itertools.product(
+            (0, 1), (0, 1), (0, 1), (0, 1), (0, 1), (0, 1), (0, 1)):
+        if prefill and (opA == 1 or fam == 1):
+            continue
+        d, n, m = 9, 5, 37
+        # operator large enough to hold a shifted submatrix
+        if side == 0:
+            Sr, Sc = (d, m) if opS == 0 else (m, d)
+        else:
+            Sr, Sc = (n, d) if opS == 0 else (d, n)
+        ro, co = 2, 3
+        D_rows, D_cols = Sr + ro + 1, Sc + co + 2
+        # A dims
+        if side == 0:
+            ar, ac = (m, n) if opA == 0 else (n, m)
+            br, bc = d, n
+        else:
+            # right: op(A) is m x n in the reference's naming; here (d,n,m) passes (m,d,n)
+            ar, ac = (m, n) if opA == 0 else (n, m)
+            br, bc = m, d
+        if side == 1:
+            # reference right overload argument order: (m, d, n)
+            ar, ac = (m, n) if opA == 0 else (n, m)
+            Sr, Sc = (n, d) if opS == 0 else (d, n)
+            D_rows, D_cols = Sr + ro + 1, Sc + co + 2
+        lda = (ar if lay == 0 else ac) + 1
+        ldb = (br if lay == 0 else bc) + 2
+        npdt = np.float32 if dt == 0 else np.float64
+        A = rng.standard_normal((lda * (ac if lay == 0 else ar),)).astype(npdt)
+        B = rng.standard_normal((ldb * (bc if lay == 0 else br),)).astype(npdt)
+        alpha, beta = 1.5, (0.0 if i % 3 == 0 else -0.5)
+        seed = State.make([i, 0, 0, 0], [99, 1])
+        Bout = B.copy()
+        if prefill and (ro, co) != (0, 0):
+            pass
+        ref.sketch_dense(dt, side, lay, opS, opA, d if side == 0 else m, n if side == 0 else d,
+                         m if side == 0 else n, alpha, D_rows, D_cols, fam, 1, seed, ro, co, A,
+                         lda, beta, Bout, ldb, prefill=bool(prefill))
+        arrays[f"A{i}"], arrays[f"B{i}"], arrays[f"O{i}"] = A, B, Bout
+        meta.append(dict(side=side, layout=lay, opS=opS, opA=opA, dtype=dt, family=fam,
+                         prefill=prefill, d=d, n=n, m=m, D_rows=D_rows, D_cols=D_cols, ro=ro,
+                         co=co, lda=lda, ldb=ldb, alpha=alpha, beta=beta, ctr=[i, 0, 0, 0],
+                         key=[99, 1]))
+        i += 1
+    np.savez_compressed(os.path.join(HERE, "sketch_dense.npz"), meta=json.dumps(meta), **arrays)
+
+    # ---- sparse-operator sketches
+    arrays, meta = {}, []
+    i = 0
+    for side, lay, opS, opA, dt, ax in itertools.product((0, 1), (0, 1), (0, 1), (0, 1), (0, 1),
+                                                         (0, 1)):
+        d, n, m = 11, 6, 200
+        if side == 0:
+            Sr, Sc = (d, m) if opS == 0 else (m, d)
+            ar, ac = (m, n) if opA == 0 else (n, m)
+            br, bc = d, n
+        else:
+            Sr, Sc = (m, d) if opS == 0 else (d, m)  # right: op(S) is n x d with n := m here
+            ar, ac = (n, m) if opA == 0 else (m, n)
+            br, bc = n, d
+        ro, co = 1, 4
+        D_rows, D_cols = Sr + ro + 2, Sc + co + 3
+        vec_nnz = 3
+        lda = (ar if lay == 0 else ac) + 1
+        ldb = (br if lay == 0 else bc) + 1
+        npdt = np.float32 if dt == 0 else np.float64
+        A = rng.standard_normal((lda * (ac if lay == 0 else ar),)).astype(npdt)
+        B = rng.standard_normal((ldb * (bc if lay == 0 else br),)).astype(npdt)
+        alpha, beta = -0.75, (0.0 if i % 2 == 0 else 2.0)
+        seed = State.make([5 * i, 0, 0, 1], [123, 0])
+        Bout = B.copy()
+        if side == 0:
+            ref.sketch_saso(dt, 0, lay, opS, opA, d, n, m, alpha, D_rows, D_cols, vec_nnz, ax,
+                            seed, ro, co, A, lda, beta, Bout, ldb)
+        else:
+            # reference right overload: (m_rows_of_B, d, n_inner) = (n, d, m)
+            ref.sketch_saso(dt, 1, lay, opS, opA, n, d, m, alpha, D_rows, D_cols, vec_nnz, ax,
+                            seed, ro, co, A, lda, beta, Bout, ldb)
+        arrays[f"A{i}"], arrays[f"B{i}"], arrays[f"O{i}"] = A, B, Bout
+        meta.append(dict(side=side, layout=lay, opS=opS, opA=opA, dtype=dt, axis=ax, d=d, n=n,
+                         m=m, D_rows=D_rows, D_cols=D_cols, vec_nnz=vec_nnz, ro=ro, co=co,
+                         lda=lda, ldb=ldb, alpha=alpha, beta=beta, ctr=[5 * i, 0, 0, 1],
+                         key=[123, 0]))
+        i += 1
+    np.savez_compressed(os.path.join(HERE, "sketch_saso.npz"), meta=json.dumps(meta), **arrays)
+
+    # ---- sketch_vector
+    arrays, meta = {}, []
+    for i, (opS, dt, fam, incx, incy) in enumerate(itertools.product((0, 1), (0, 1), (0, 1),
+                                                                     (1, 3), (1, 2))):
+        d, m = 8, 50
+        ro, co = 1, 2
+        D_rows, D_cols = d + ro + 1, m + co + 1
+        xl = (m if opS == 0 else d)
+        yl = (d if opS == 0 else m)
+        npdt = np.float32 if dt == 0 else np.float64
+        x = rng.standard_normal(xl * incx).astype(npdt)
+        y = rng.standard_normal(yl * incy).astype(npdt)
+        yout = y.copy()
+        seed = State.make([i, 9, 0, 0], [5, 5])
+        ref.sketch_vector(dt, opS, d, m, 0.5, D_rows, D_cols, fam, 1, seed, ro, co, x, incx,
+                          (0.0 if i % 2 else 1.25), yout, incy)
+        arrays[f"x{i}"], arrays[f"y{i}"], arrays[f"o{i}"] = x, y, yout
+        meta.append(dict(opS=opS, dtype=dt, family=fam, incx=incx, incy=incy, d=d, m=m, ro=ro,
+                         co=co, D_rows=D_rows, D_cols=D_cols, alpha=0.5,
+                         beta=(0.0 if i % 2 else 1.25), ctr=[i, 9, 0, 0], key=[5, 5]))
+    np.savez_compressed(os.path.join(HERE, "sketch_vector.npz"), meta=json.dumps(meta), **arrays)
+
+    # ---- sketch_sparse (dense operator, sparse data in COO / CSR / CSC)
+    arrays, meta = {}, []
+    i = 0
+    for side, lay, opS, opA, dt, fmt in itertools.product((0, 1), (0, 1), (0, 1), (0, 1), (0, 1),
+                                                          (0, 1, 2)):
+        d, n, m = 7, 9, 60
+        if side == 0:
+            Sr, Sc = (d, m) if opS == 0 else (m, d)
+            Ar, Ac = (m, n) if opA == 0 else (n, m)
+            br, bc = d, n
+        else:
+            # right: B (n x d) = op(A) (n x m) op(S) (m x d)
+            Sr, Sc = (m, d) if opS == 0 else (d, m)
+            Ar, Ac = (n, m) if opA == 0 else (m, n)
+            br, bc = n, d
+        ro, co = 2, 1
+        D_rows, D_cols = Sr + ro + 1, Sc + co + 1
+        dense = rng.standard_normal((Ar, Ac)) * (rng.random((Ar, Ac)) < 0.2)
+        r_, c_ = np.nonzero(dense)
+        npdt = np.float32 if dt == 0 else np.float64
+        vals = dense[r_, c_].astype(npdt)
+        if fmt == 0:
+            perm = rng.permutation(len(vals))
+            a, b, v = r_[perm].astype(np.int64), c_[perm].astype(np.int64), vals[perm]
+        elif fmt == 1:
+            a = np.concatenate([[0], np.cumsum(np.bincount(r_, minlength=Ar))]).astype(np.int64)
+            b, v = c_.astype(np.int64), vals
+        else:
+            order = np.lexsort((r_, c_))
+            a = np.concatenate([[0], np.cumsum(np.bincount(c_, minlength=Ac))]).astype(np.int64)
+            b, v = r_[order].astype(np.int64), vals[order]
+        ldb = (br if lay == 0 else bc) + 1
+        B = rng.standard_normal((ldb * (bc if lay == 0 else br),)).astype(npdt)
+        Bout = B.copy()
+        alpha, beta = 0.625, (0.0 if i % 2 == 0 else 0.5)
+        seed = State.make([i, 0, 3, 0], [31, 4])
+        if side == 0:
+            ref.sketch_sparse(dt, 0, lay, opS, opA, d, n, m, alpha, D_rows, D_cols, 0, 1, seed, ro,
+                              co, fmt, Ar, Ac, len(v), v, a, b, beta, Bout, ldb)
+        else:
+            ref.sketch_sparse(dt, 1, lay, opS, opA, n, d, m, alpha, D_rows, D_cols, 0, 1, seed, ro,
+                              co, fmt, Ar, Ac, len(v), v, a, b, beta, Bout, ldb)
+        arrays[f"v{i}"], arrays[f"a{i}"], arrays[f"b{i}"] = v, a, b
+        arrays[f"B{i}"], arrays[f"O{i}"] = B, Bout
+        meta.append(dict(side=side, layout=lay, opS=opS, opA=opA, dtype=dt, fmt=fmt, d=d, n=n, m=m,
+                         Ar=Ar, Ac=Ac, D_rows=D_rows, D_cols=D_cols, ro=ro, co=co, ldb=ldb,
+                         alpha=alpha, beta=beta, ctr=[i, 0, 3, 0], key=[31, 4]))
+        i += 1
+    np.savez_compressed(os.path.join(HERE, "sketch_sparse.npz"), meta=json.dumps(meta), **arrays)
+
+    # ---- full-size operators of the benchmark workloads
+    full = {}
+    # 200 x 10000 Gaussian FP64 operator seeded after its data matrix (counter 125000, key 0):
+    # Gaussians are compared to within a few ulp, so keep every 97th entry, not a digest
+    S_dist = dict(n_rows=200, n_cols=10000, family=0, axis=1)
+    sbuf, snext = ref.fill_dense_unpacked(1, 1, 200, 10000, 0, 1, 200, 10000, 0, 0,
+                                          State.make([125000, 0, 0, 0], [0, 0]))
+    np.savez_compressed(os.path.join(HERE, "dense_200x10000_sample.npz"),
+                        idx=np.arange(0, sbuf.size, 97), vals=sbuf[::97])
+    full["dense_200x10000_f64"] = dict(dist=S_dist, seed=[[125000, 0, 0, 0], [0, 0]],
+                                       next=st(snext), layout=1, sample_every=97)
+    vals, rows, cols, nnz, nxt = ref.fill_sparse(0, 1, 1024, 1 << 20, 8, 0,
+                                                 State.make([7, 0, 0, 0], [0, 0]))
+    full["saso_1024x2^20_k8"] = dict(seed=[[7, 0, 0, 0], [0, 0]], nnz=int(nnz), next=st(nxt),
+                                     rows_sha256=hashlib.sha256(rows.tobytes()).hexdigest(),
+                                     cols_sha256=hashlib.sha256(cols.tobytes()).hexdigest(),
+                                     vals_sha256=hashlib.sha256(vals.tobytes()).hexdigest())
+    with open(os.path.join(HERE, "full_size.json"), "w") as f:
+        json.dump(full, f, indent=1)
+    print("golden fixtures written to", HERE)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,154 @@
+"""GPU sampling kernels against the reference's outputs (golden fixtures) and the oracle:
+dense operators (uniform entries bit-exact, Gaussians within a few ulp), SASO / LASO index
+sets and values, and every returned RNGState."""
+import hashlib
+
+import numpy as np
+import pytest
+
+from conftest import golden_json, load_golden
+from gpu_helpers import st_list, state_of, to_host, ulp_distance
+
+pytestmark = pytest.mark.gpu
+
+# Box-Muller runs on CUDA's accurate sincosf / logf / sqrtf; the reference's host build uses
+# glibc's.  Both are within about 1 ulp of the exact values; the products below may differ
+# by a few ulp.  Uniform entries involve only exact scalings and one rounding: bit-exact.
+GAUSS_ULP_MAX = 4
+GAUSS_ULP_TYPICAL = 2        # at least 99.9% of Gaussian entries within this
+GAUSS_FRAC_TYPICAL = 0.999
+
+
+def _fill(rb, c):
+    import torch
+    dt = torch.float32 if c["dtype"] == 0 else torch.float64
+    D = rb.DenseDist(c["R"], c["C"], rb.ScalarDist(c["family"]), rb.Axis(c["axis"]))
+    buf = torch.empty(c["nr"] * c["nc"], dtype=dt, device="cuda")
+    nxt = rb.fill_dense_unpacked(rb.Layout(c["layout"]), D, c["nr"], c["nc"], c["ro"], c["co"],
+                                 buf, state_of([c["ctr"], c["key"]]))
+    return to_host(buf), nxt
+
+
+def test_fill_dense_golden(rb):
+    meta, z = load_golden("fill_dense")
+    worst = 0
+    for i, c in enumerate(meta):
+        got, nxt = _fill(rb, c)
+        ref = z[f"c{i}"]
+        assert st_list(nxt) == c["next"], c
+        if c["family"] == 1:  # uniform: bit-exact
+            assert np.array_equal(got.view(np.uint8), ref.view(np.uint8)), c
+        else:
+            u = ulp_distance(got.astype(np.float32), ref.astype(np.float32))
+            worst = max(worst, int(u.max()))
+            assert u.max() <= GAUSS_ULP_MAX, (c, int(u.max()))
+            # FP64 operators hold float values promoted to double, as in the reference
+            assert np.array_equal(got.astype(np.float32).astype(got.dtype), got)
+    print("max Gaussian ulp distance on golden cases:", worst)
+
+
+def test_full_size_gaussian_operator(rb):
+    import torch
+    g = golden_json("full_size.json")["dense_200x10000_f64"]
+    _, z = load_golden("dense_200x10000_sample")
+    D = rb.DenseDist(200, 10000)
+    buf = torch.empty(200 * 10000, dtype=torch.float64, device="cuda")
+    nxt = rb.fill_dense(D, buf, state_of(g["seed"]))
+    assert st_list(nxt) == g["next"]
+    got = to_host(buf)[z["idx"]]
+    u = ulp_distance(got, z["vals"])
+    assert u.max() <= GAUSS_ULP_MAX
+    assert np.mean(u <= GAUSS_ULP_TYPICAL) >= GAUSS_FRAC_TYPICAL
+    print("200x10000 sample: exact", float(np.mean(u == 0)), "max ulp", int(u.max()))
+
+
+def test_uniform_large_block_bit_exact(rb, oracle):
+    """A 64 x 60000 block at an odd offset of a 4096 x 2^20 uniform operator."""
+    import torch
+    from oracle.oracle import State
+    D = rb.DenseDist(4096, 1 << 20, rb.ScalarDist.Uniform)
+    seed = rb.RNGState(3, counter=(5, 0, 0, 0))
+    for dt, npdt in ((torch.float32, np.float32), (torch.float64, np.float64)):
+        for lay in (rb.Layout.RowMajor, rb.Layout.ColMajor):
+            buf = torch.empty(64 * 60000, dtype=dt, device="cuda")
+            nxt = rb.fill_dense_unpacked(lay, D, 64, 60000, 1001, 12345, buf, seed)
+            ref, rnxt = oracle.fill_dense_unpacked(0 if dt == torch.float32 else 1, int(lay), 4096,
+                                                   1 << 20, 1, 1, 64, 60000, 1001, 12345,
+                                                   State.make((5, 0, 0, 0), (3, 0)))
+            assert np.array_equal(to_host(buf).view(np.uint8), ref.view(np.uint8))
+            assert st_list(nxt) == [list(rnxt.counter), list(rnxt.key)]
+
+
+def test_gaussian_ulp_statistics(rb, oracle):
+    """4M Gaussian entries against the oracle (glibc transforms)."""
+    import torch
+    from oracle.oracle import State
+    D = rb.DenseDist(1000, 4000)
+    buf = torch.empty(1000 * 4000, dtype=torch.float32, device="cuda")
+    rb.fill_dense(D, buf, rb.RNGState(11))
+    ref, _ = oracle.fill_dense_unpacked(0, 1, 1000, 4000, 0, 1, 1000, 4000, 0, 0,
+                                        State.from_key(11))
+    u = ulp_distance(to_host(buf), ref)
+    print("Gaussian ulp histogram:", np.bincount(np.minimum(u, 8)).tolist())
+    assert u.max() <= GAUSS_ULP_MAX
+    assert np.mean(u <= GAUSS_ULP_TYPICAL) >= GAUSS_FRAC_TYPICAL
+
+
+def test_fill_dense_skop_and_launch_invariance(rb):
+    """fill_dense(S) equals the submatrix fills that tile it (thread-count / launch-shape
+    invariance, test/test_datastructures/test_denseskop.cc:299-341, and slicing,
+    :162-296)."""
+    import torch
+    D = rb.DenseDist(300, 777, rb.ScalarDist.Uniform)
+    S = rb.DenseSkOp(D, rb.RNGState(9))
+    rb.fill_dense(S)
+    full = to_host(S.buff).reshape(300, 777)  # natural layout: wide & Long -> RowMajor
+    for (ro, co, nr, nc) in [(0, 0, 300, 777), (5, 3, 17, 401), (299, 0, 1, 777), (0, 776, 300, 1)]:
+        buf = torch.empty(nr * nc, dtype=torch.float32, device="cuda")
+        rb.fill_dense_unpacked(rb.Layout.RowMajor, D, nr, nc, ro, co, buf, rb.RNGState(9))
+        assert np.array_equal(to_host(buf).reshape(nr, nc), full[ro:ro + nr, co:co + nc])
+
+
+def test_fill_sparse_golden(rb):
+    import torch
+    meta, z = load_golden("fill_sparse")
+    for i, c in enumerate(meta):
+        dt = torch.float32 if c["dtype"] == 0 else torch.float64
+        it = torch.int32 if c["itype"] == 0 else torch.int64
+        D = rb.SparseDist(c["R"], c["C"], c["vec_nnz"], rb.Axis(c["axis"]))
+        S = rb.SparseSkOp(D, state_of([c["ctr"], c["key"]]), dtype=dt, index_dtype=it)
+        rb.fill_sparse(S)
+        assert S.nnz == c["nnz"], c
+        assert st_list(S.next_state) == c["next"]
+        vals = to_host(S.vals)[:S.nnz]
+        rows = to_host(S.rows)[:S.nnz]
+        cols = to_host(S.cols)[:S.nnz]
+        if c["axis"] == 1:
+            order = np.lexsort((cols, rows))
+            vals, rows, cols = vals[order], rows[order], cols[order]
+        assert np.array_equal(rows, z[f"r{i}"]) and np.array_equal(cols, z[f"c{i}"]), c
+        assert np.array_equal(vals, z[f"v{i}"]), c
+
+
+def test_full_size_saso_digest(rb):
+    import torch
+    g = golden_json("full_size.json")["saso_1024x2^20_k8"]
+    D = rb.SparseDist(1024, 1 << 20, 8)
+    S = rb.SparseSkOp(D, state_of(g["seed"]))
+    rb.fill_sparse(S)
+    torch.cuda.synchronize()
+    assert S.nnz == g["nnz"]
+    assert hashlib.sha256(to_host(S.rows).tobytes()).hexdigest() == g["rows_sha256"]
+    assert hashlib.sha256(to_host(S.cols).tobytes()).hexdigest() == g["cols_sha256"]
+    assert hashlib.sha256(to_host(S.vals).tobytes()).hexdigest() == g["vals_sha256"]
+
+
+def test_repeated_fisher_yates(rb, oracle):
+    import torch
+    from oracle.oracle import State
+    for (k, n, r) in [(8, 1024, 1000), (16, 16, 50), (1, 5, 7), (100, 300, 20)]:
+        smp = torch.empty(k * r, dtype=torch.int64, device="cuda")
+        nxt = rb.repeated_fisher_yates(k, n, r, smp, rb.RNGState(4))
+        idx, rn = oracle.repeated_fisher_yates(k, n, r, State.from_key(4))
+        assert np.array_equal(to_host(smp), idx)
+        assert nxt.counter == list(rn.counter)

@@ -1,0 +1,160 @@
+"""Sparse sketching on the GPU (LSKGES / RSKGES with SASO and LASO operators, sketch_sparse
+with COO / CSR / CSC data) against the reference's outputs (tests/golden) and, at the full
+1024 x 2^20 SASO size, against an FP64 product of the bit-exact operator.
+
+Criterion: the reference's componentwise bound (test/test_matmul_cores/linop_common.hh:
+260-266), |B - B_ref| <= |alpha| (2K + 16) eps (|op(S)| |op(A)|) + 2 eps |beta| |B_in|."""
+import numpy as np
+import pytest
+
+from conftest import load_golden
+from gpu_helpers import as_matrix, check_bound, state_of, to_dev, to_host
+
+pytestmark = pytest.mark.gpu
+
+F32_GAUSS = 8 * 2.0**-24
+
+
+def _eps(dt):
+    return np.finfo(np.float32 if dt == 0 else np.float64).eps
+
+
+def test_sparse_operator_sketch_golden(rb, oracle):
+    import torch
+    from oracle.oracle import State
+    meta, z = load_golden("sketch_saso")
+    for i, c in enumerate(meta):
+        dt = torch.float32 if c["dtype"] == 0 else torch.float64
+        D = rb.SparseDist(c["D_rows"], c["D_cols"], c["vec_nnz"], rb.Axis(c["axis"]))
+        S = rb.SparseSkOp(D, state_of([c["ctr"], c["key"]]), dtype=dt)
+        A, B0 = z[f"A{i}"], z[f"B{i}"]
+        B = to_dev(B0)
+        d, n, m, lay = c["d"], c["n"], c["m"], c["layout"]
+        full = oracle.sparse_dense_matrix(1, c["D_rows"], c["D_cols"], c["vec_nnz"], c["axis"],
+                                          State.make(c["ctr"], c["key"]))
+        if c["side"] == 0:
+            rb.sketch_general(rb.Layout(lay), rb.Op(c["opS"]), rb.Op(c["opA"]), d, n, m,
+                              c["alpha"], S, c["ro"], c["co"], to_dev(A), c["lda"], c["beta"], B,
+                              c["ldb"])
+            sr, sc = (d, m) if c["opS"] == 0 else (m, d)
+            Ssub = full[c["ro"]:c["ro"] + sr, c["co"]:c["co"] + sc]
+            opS = Ssub if c["opS"] == 0 else Ssub.T
+            ar, ac = (m, n) if c["opA"] == 0 else (n, m)
+            Am = as_matrix(A, ar, ac, lay, c["lda"])
+            prod = np.abs(opS) @ np.abs(Am if c["opA"] == 0 else Am.T)
+            br, bc, K = d, n, m
+        else:
+            # reference right overload: B (n x d) = op(A) (n x m) op(S) (m x d)
+            rb.sketch_general(rb.Layout(lay), rb.Op(c["opA"]), rb.Op(c["opS"]), n, d, m,
+                              c["alpha"], to_dev(A), c["lda"], S, c["ro"], c["co"], c["beta"], B,
+                              c["ldb"])
+            sr, sc = (m, d) if c["opS"] == 0 else (d, m)
+            Ssub = full[c["ro"]:c["ro"] + sr, c["co"]:c["co"] + sc]
+            opS = Ssub if c["opS"] == 0 else Ssub.T
+            ar, ac = (n, m) if c["opA"] == 0 else (m, n)
+            Am = as_matrix(A, ar, ac, lay, c["lda"])
+            prod = np.abs(Am if c["opA"] == 0 else Am.T) @ np.abs(opS)
+            br, bc, K = n, d, m
+        got = as_matrix(to_host(B), br, bc, lay, c["ldb"])
+        ref = as_matrix(z[f"O{i}"], br, bc, lay, c["ldb"])
+        bin_ = as_matrix(B0, br, bc, lay, c["ldb"])
+        eps = _eps(c["dtype"])
+        bound = abs(c["alpha"]) * (2 * K + 16) * eps * prod + \
+            2 * eps * abs(c["beta"]) * np.abs(bin_) + 1e-300
+        check_bound(got, ref, bound, c)
+
+
+def test_prefilled_sparse_operator_matches_unsampled(rb):
+    """Sampling inside the sketch and sketching with fill_sparse's COO give the same B."""
+    import torch
+    for ax in (rb.Axis.Short, rb.Axis.Long):
+        D = rb.SparseDist(64, 5000, 5, ax)
+        A = torch.randn(5000 * 33, device="cuda")
+        S1 = rb.SparseSkOp(D, rb.RNGState(21))
+        S2 = rb.SparseSkOp(D, rb.RNGState(21))
+        rb.fill_sparse(S2)
+        B1 = torch.zeros(64 * 33, device="cuda")
+        B2 = torch.zeros(64 * 33, device="cuda")
+        for S, B in ((S1, B1), (S2, B2)):
+            rb.sketch_general(rb.Layout.RowMajor, rb.Op.NoTrans, rb.Op.NoTrans, 64, 33, 5000, 1.0,
+                              S, A, 33, 0.0, B, 33)
+        assert torch.equal(B1, B2)
+
+
+def test_sketch_sparse_data_golden(rb, oracle):
+    import torch
+    from oracle.oracle import State
+    meta, z = load_golden("sketch_sparse")
+    for i, c in enumerate(meta):
+        dt = torch.float32 if c["dtype"] == 0 else torch.float64
+        D = rb.DenseDist(c["D_rows"], c["D_cols"], rb.ScalarDist.Gaussian, rb.Axis.Long)
+        S = rb.DenseSkOp(D, state_of([c["ctr"], c["key"]]), dtype=dt)
+        v, a, b = z[f"v{i}"], z[f"a{i}"], z[f"b{i}"]
+        Ar, Ac = c["Ar"], c["Ac"]
+        if c["fmt"] == 0:
+            Amat = rb.COOMatrix(Ar, Ac, to_dev(v), to_dev(a), to_dev(b))
+            dense = np.zeros((Ar, Ac))
+            np.add.at(dense, (a, b), v.astype(np.float64))
+        elif c["fmt"] == 1:
+            Amat = rb.CSRMatrix(Ar, Ac, to_dev(v), to_dev(a), to_dev(b))
+            rows = np.repeat(np.arange(Ar), np.diff(a))
+            dense = np.zeros((Ar, Ac))
+            np.add.at(dense, (rows, b), v.astype(np.float64))
+        else:
+            Amat = rb.CSCMatrix(Ar, Ac, to_dev(v), to_dev(b), to_dev(a))
+            cols = np.repeat(np.arange(Ac), np.diff(a))
+            dense = np.zeros((Ar, Ac))
+            np.add.at(dense, (b, cols), v.astype(np.float64))
+        B0 = z[f"B{i}"]
+        B = to_dev(B0)
+        d, n, m, lay = c["d"], c["n"], c["m"], c["layout"]
+        opA = dense if c["opA"] == 0 else dense.T
+        if c["side"] == 0:
+            rb.sketch_sparse(rb.Layout(lay), rb.Op(c["opS"]), rb.Op(c["opA"]), d, n, m,
+                             c["alpha"], S, c["ro"], c["co"], Amat, c["beta"], B, c["ldb"])
+            sr, sc = (d, m) if c["opS"] == 0 else (m, d)
+            Ssub = oracle.dense_matrix(1, c["D_rows"], c["D_cols"], 0, 1,
+                                       State.make(c["ctr"], c["key"]), sr, sc, c["ro"], c["co"])
+            prod = np.abs(Ssub if c["opS"] == 0 else Ssub.T) @ np.abs(opA)
+            br, bc, K = d, n, m
+        else:
+            rb.sketch_sparse(rb.Layout(lay), rb.Op(c["opA"]), rb.Op(c["opS"]), n, d, m,
+                             c["alpha"], Amat, S, c["ro"], c["co"], c["beta"], B, c["ldb"])
+            sr, sc = (m, d) if c["opS"] == 0 else (d, m)
+            Ssub = oracle.dense_matrix(1, c["D_rows"], c["D_cols"], 0, 1,
+                                       State.make(c["ctr"], c["key"]), sr, sc, c["ro"], c["co"])
+            prod = np.abs(opA) @ np.abs(Ssub if c["opS"] == 0 else Ssub.T)
+            br, bc, K = n, d, m
+        got = as_matrix(to_host(B), br, bc, lay, c["ldb"])
+        ref = as_matrix(z[f"O{i}"], br, bc, lay, c["ldb"])
+        bin_ = as_matrix(B0, br, bc, lay, c["ldb"])
+        eps = _eps(c["dtype"])
+        bound = abs(c["alpha"]) * ((2 * K + 16) * eps + F32_GAUSS) * prod + \
+            2 * eps * abs(c["beta"]) * np.abs(bin_) + 1e-300
+        check_bound(got, ref, bound, c)
+
+
+def test_full_size_saso_sketch(rb):
+    """1024 x 2^20 SASO (8 nonzeros per column) times a 2^20 x 256 row-major N(0,1) FP32
+    matrix: relative Frobenius error <= 1e-6 against an FP64 product of the same operator,
+    and bitwise-identical results on a second run (fixed-order reductions)."""
+    import torch
+    m, d, n = 1 << 20, 1024, 256
+    A = torch.empty(m * n, dtype=torch.float32, device="cuda")
+    nxt = rb.fill_dense(rb.DenseDist(m, n, rb.ScalarDist.Gaussian, rb.Axis.Short), A,
+                        rb.RNGState(0))
+    S = rb.SparseSkOp(rb.SparseDist(d, m, 8), nxt)
+    B = torch.empty(d * n, dtype=torch.float32, device="cuda")
+    rb.sketch_general(rb.Layout.RowMajor, rb.Op.NoTrans, rb.Op.NoTrans, d, n, m, 1.0, S, A, n,
+                      0.0, B, n)
+    B_again = torch.empty_like(B)
+    rb.sketch_general(rb.Layout.RowMajor, rb.Op.NoTrans, rb.Op.NoTrans, d, n, m, 1.0, S, A, n,
+                      0.0, B_again, n)
+    assert torch.equal(B, B_again)
+    Sf = rb.SparseSkOp(rb.SparseDist(d, m, 8), nxt)
+    rb.fill_sparse(Sf)
+    idx = torch.stack([Sf.rows, Sf.cols])
+    Ssp = torch.sparse_coo_tensor(idx, Sf.vals.double(), (d, m)).coalesce()
+    ref = torch.sparse.mm(Ssp, A.view(m, n).double())
+    rel = (torch.linalg.norm(B.view(d, n).double() - ref) / torch.linalg.norm(ref)).item()
+    assert rel <= 1e-6, rel
