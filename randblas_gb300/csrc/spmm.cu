@@ -237,7 +237,8 @@ __global__ void __launch_bounds__(1024, 1) spmm_rows_kernel(SpmmArgs<T> a) {
                 for (int t = 0; t < cnt; ++t) {
                     const int32_t kt = __shfl_sync(0xffffffffu, kk, t);
                     const T vt = __shfl_sync(0xffffffffu, vv, t);
-                    acc[r] = fma(vt, Qs[kt - kb][lane], acc[r]);
+                    const int64_t off = kt - kb;  // in [0, kn) for k-sorted lists
+                    if ((uint64_t)off < (uint64_t)kn) acc[r] = fma(vt, Qs[off][lane], acc[r]);
                 }
                 c += cnt;
                 if (cnt < 32) break;
