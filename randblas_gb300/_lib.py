@@ -72,9 +72,9 @@ class rbg_batch_problem(C.Structure):
 
 
 P = C.c_void_p
-I64 = C.c_int64
-I32 = C.c_int32
-D = C.c_double
+CI64 = C.c_int64
+CI32 = C.c_int32
+CD = C.c_double
 PS = C.POINTER(rbg_state)
 
 # name -> argtypes (restype int unless noted)
@@ -83,53 +83,53 @@ SIGNATURES = {
     "rbg_version": ([], C.c_int),
     "rbg_kernel_launches": ([], C.c_uint64),
     "rbg_profile_enable": ([C.c_int], C.c_int),
-    "rbg_profile_count": ([C.POINTER(I32)], C.c_int),
-    "rbg_profile_entry": ([I32, C.c_char_p, I32, C.POINTER(D), C.POINTER(I64)], C.c_int),
+    "rbg_profile_count": ([C.POINTER(CI32)], C.c_int),
+    "rbg_profile_entry": ([CI32, C.c_char_p, CI32, C.POINTER(CD), C.POINTER(CI64)], C.c_int),
     "rbg_state_from_key": ([C.c_uint64, PS], C.c_int),
     "rbg_state_incr": ([PS, C.c_uint64, PS], C.c_int),
-    "rbg_dense_dist_properties": ([C.POINTER(rbg_dense_dist), C.POINTER(I64), C.POINTER(I64),
-                                   C.POINTER(I32), C.POINTER(D)], C.c_int),
+    "rbg_dense_dist_properties": ([C.POINTER(rbg_dense_dist), C.POINTER(CI64), C.POINTER(CI64),
+                                   C.POINTER(CI32), C.POINTER(CD)], C.c_int),
     "rbg_dense_next_state": ([C.POINTER(rbg_dense_dist), PS, PS], C.c_int),
-    "rbg_dense_skop_init": ([C.POINTER(rbg_dense_skop), C.POINTER(rbg_dense_dist), PS, I32],
+    "rbg_dense_skop_init": ([C.POINTER(rbg_dense_skop), C.POINTER(rbg_dense_dist), PS, CI32],
                             C.c_int),
-    "rbg_sparse_dist_properties": ([C.POINTER(rbg_sparse_dist), C.POINTER(I64), C.POINTER(I64),
-                                    C.POINTER(I64), C.POINTER(D)], C.c_int),
+    "rbg_sparse_dist_properties": ([C.POINTER(rbg_sparse_dist), C.POINTER(CI64), C.POINTER(CI64),
+                                    C.POINTER(CI64), C.POINTER(CD)], C.c_int),
     "rbg_sparse_next_state": ([C.POINTER(rbg_sparse_dist), PS, PS], C.c_int),
-    "rbg_sparse_skop_init": ([C.POINTER(rbg_sparse_skop), C.POINTER(rbg_sparse_dist), PS, I32,
-                              I32], C.c_int),
-    "rbg_fill_dense_unpacked": ([I32, I32, C.POINTER(rbg_dense_dist), I64, I64, I64, I64, P, PS,
+    "rbg_sparse_skop_init": ([C.POINTER(rbg_sparse_skop), C.POINTER(rbg_sparse_dist), PS, CI32,
+                              CI32], C.c_int),
+    "rbg_fill_dense_unpacked": ([CI32, CI32, C.POINTER(rbg_dense_dist), CI64, CI64, CI64, CI64, P, PS,
                                  PS, P], C.c_int),
-    "rbg_fill_dense": ([I32, C.POINTER(rbg_dense_dist), P, PS, PS, P], C.c_int),
+    "rbg_fill_dense": ([CI32, C.POINTER(rbg_dense_dist), P, PS, PS, P], C.c_int),
     "rbg_fill_dense_skop": ([C.POINTER(rbg_dense_skop), P], C.c_int),
-    "rbg_fill_sparse_unpacked_nosub": ([I32, I32, C.POINTER(rbg_sparse_dist), C.POINTER(I64), P,
+    "rbg_fill_sparse_unpacked_nosub": ([CI32, CI32, C.POINTER(rbg_sparse_dist), C.POINTER(CI64), P,
                                         P, P, PS, PS, P], C.c_int),
     "rbg_fill_sparse": ([C.POINTER(rbg_sparse_skop), P], C.c_int),
-    "rbg_repeated_fisher_yates": ([I64, I64, I64, P, PS, PS, P], C.c_int),
-    "rbg_lskge3": ([I32, I32, I32, I64, I64, I64, D, C.POINTER(rbg_dense_skop), I64, I64, P, I64,
-                    D, P, I64, P], C.c_int),
-    "rbg_rskge3": ([I32, I32, I32, I64, I64, I64, D, P, I64, C.POINTER(rbg_dense_skop), I64, I64,
-                    D, P, I64, P], C.c_int),
-    "rbg_sketch_vector": ([I32, I64, I64, D, C.POINTER(rbg_dense_skop), I64, I64, P, I64, D, P,
-                           I64, P], C.c_int),
-    "rbg_lskges": ([I32, I32, I32, I64, I64, I64, D, C.POINTER(rbg_sparse_skop), I64, I64, P,
-                    I64, D, P, I64, P], C.c_int),
-    "rbg_rskges": ([I32, I32, I32, I64, I64, I64, D, P, I64, C.POINTER(rbg_sparse_skop), I64,
-                    I64, D, P, I64, P], C.c_int),
-    "rbg_sketch_vector_sparse": ([I32, I64, I64, D, C.POINTER(rbg_sparse_skop), I64, I64, P, I64,
-                                  D, P, I64, P], C.c_int),
-    "rbg_lsksp3": ([I32, I32, I32, I64, I64, I64, D, C.POINTER(rbg_dense_skop), I64, I64,
-                    C.POINTER(rbg_spmat), D, P, I64, P], C.c_int),
-    "rbg_rsksp3": ([I32, I32, I32, I64, I64, I64, D, C.POINTER(rbg_spmat),
-                    C.POINTER(rbg_dense_skop), I64, I64, D, P, I64, P], C.c_int),
-    "rbg_left_spmm": ([I32, I32, I32, I64, I64, I64, D, C.POINTER(rbg_spmat), I64, I64, P, I64, D,
-                       P, I64, P], C.c_int),
-    "rbg_right_spmm": ([I32, I32, I32, I64, I64, I64, D, P, I64, C.POINTER(rbg_spmat), I64, I64,
-                        D, P, I64, P], C.c_int),
-    "rbg_lskge3_lowp_workspace": ([I32, I64, I64, I64, C.POINTER(C.c_size_t)], C.c_int),
-    "rbg_lskge3_lowp": ([I32, I32, I32, I32, I64, I64, I64, C.c_float, C.POINTER(rbg_dense_skop),
-                         I64, I64, P, I64, C.c_float, P, I64, P, C.c_size_t, P], C.c_int),
-    "rbg_lskge3_batched": ([I32, C.POINTER(rbg_batch_problem), I64, I32, P], C.c_int),
-    "rbg_batched_tile_configs": ([C.POINTER(I32)], C.c_int),
+    "rbg_repeated_fisher_yates": ([CI64, CI64, CI64, P, PS, PS, P], C.c_int),
+    "rbg_lskge3": ([CI32, CI32, CI32, CI64, CI64, CI64, CD, C.POINTER(rbg_dense_skop), CI64, CI64, P, CI64,
+                    CD, P, CI64, P], C.c_int),
+    "rbg_rskge3": ([CI32, CI32, CI32, CI64, CI64, CI64, CD, P, CI64, C.POINTER(rbg_dense_skop), CI64, CI64,
+                    CD, P, CI64, P], C.c_int),
+    "rbg_sketch_vector": ([CI32, CI64, CI64, CD, C.POINTER(rbg_dense_skop), CI64, CI64, P, CI64, CD, P,
+                           CI64, P], C.c_int),
+    "rbg_lskges": ([CI32, CI32, CI32, CI64, CI64, CI64, CD, C.POINTER(rbg_sparse_skop), CI64, CI64, P,
+                    CI64, CD, P, CI64, P], C.c_int),
+    "rbg_rskges": ([CI32, CI32, CI32, CI64, CI64, CI64, CD, P, CI64, C.POINTER(rbg_sparse_skop), CI64,
+                    CI64, CD, P, CI64, P], C.c_int),
+    "rbg_sketch_vector_sparse": ([CI32, CI64, CI64, CD, C.POINTER(rbg_sparse_skop), CI64, CI64, P, CI64,
+                                  CD, P, CI64, P], C.c_int),
+    "rbg_lsksp3": ([CI32, CI32, CI32, CI64, CI64, CI64, CD, C.POINTER(rbg_dense_skop), CI64, CI64,
+                    C.POINTER(rbg_spmat), CD, P, CI64, P], C.c_int),
+    "rbg_rsksp3": ([CI32, CI32, CI32, CI64, CI64, CI64, CD, C.POINTER(rbg_spmat),
+                    C.POINTER(rbg_dense_skop), CI64, CI64, CD, P, CI64, P], C.c_int),
+    "rbg_left_spmm": ([CI32, CI32, CI32, CI64, CI64, CI64, CD, C.POINTER(rbg_spmat), CI64, CI64, P, CI64, CD,
+                       P, CI64, P], C.c_int),
+    "rbg_right_spmm": ([CI32, CI32, CI32, CI64, CI64, CI64, CD, P, CI64, C.POINTER(rbg_spmat), CI64, CI64,
+                        CD, P, CI64, P], C.c_int),
+    "rbg_lskge3_lowp_workspace": ([CI32, CI64, CI64, CI64, C.POINTER(C.c_size_t)], C.c_int),
+    "rbg_lskge3_lowp": ([CI32, CI32, CI32, CI32, CI64, CI64, CI64, C.c_float, C.POINTER(rbg_dense_skop),
+                         CI64, CI64, P, CI64, C.c_float, P, CI64, P, C.c_size_t, P], C.c_int),
+    "rbg_lskge3_batched": ([CI32, C.POINTER(rbg_batch_problem), CI64, CI32, P], C.c_int),
+    "rbg_batched_tile_configs": ([C.POINTER(CI32)], C.c_int),
 }
 
 _lock = threading.Lock()

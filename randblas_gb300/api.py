@@ -321,7 +321,7 @@ def sketch_general(layout: Layout, op1: Op, op2: Op, a: int, b: int, c: int, alp
     st = _stream()
     if _is_skop(args[0]):  # left
         S = args[0]
-        if len(args) == 7:
+        if len(args) == 8:
             ro_s, co_s, A, lda, beta, B, ldb = args[1:]
         else:
             A, lda, beta, B, ldb = args[1:]

@@ -68,25 +68,47 @@ __device__ __forceinline__ float u01(uint32_t x) {
     return __fadd_rn(__fmul_rn(__uint2float_rn(x), 0x1p-32f), 0x1p-33f);
 }
 
-// CUDA's accurate (non-intrinsic) sincosf/logf/sqrtf; the products are rounded once each,
-// like the host code they mirror.  The results match glibc's to a few ulp (measured by
-// the parity tests), not bit for bit.
+// Box-Muller for the plain paths and the explicit fills: sin, cos and log are evaluated in
+// double precision (CUDA's sincos / log) and rounded once to float, which gives the correctly
+// rounded float value except in vanishingly rare cases; then r = sqrtf(-2 * log) and the two
+// products are rounded in float exactly as the reference's host code does.  Against glibc's
+// float sinf / cosf / logf (max errors about 0.6 and 0.8 ulp) the results agree except where
+// glibc rounds the other way, and then by one or two ulp.
 __device__ __forceinline__ void boxmuller(uint32_t u0, uint32_t u1, float &first,
                                           float &second) {
+    const float theta = __fmul_rn(3.14159265358979323846f, uneg11(u0));
+    double s, c;
+    sincos((double)theta, &s, &c);
+    const float l = __double2float_rn(log((double)u01(u1)));
+    const float r = __fsqrt_rn(__fmul_rn(-2.0f, l));
+    first = __fmul_rn(__double2float_rn(s), r);
+    second = __fmul_rn(__double2float_rn(c), r);
+}
+
+// Box-Muller for the reduced-precision tensor-core paths, whose entries are rounded to BF16 /
+// FP8 afterwards: CUDA's float sincosf / logf (a few ulp in float, far below a BF16 ulp).
+__device__ __forceinline__ void boxmuller_fast(uint32_t u0, uint32_t u1, float &first,
+                                               float &second) {
     float s, c;
     sincosf(__fmul_rn(3.14159265358979323846f, uneg11(u0)), &s, &c);
-    const float r = sqrtf(__fmul_rn(-2.0f, logf(u01(u1))));
+    const float r = __fsqrt_rn(__fmul_rn(-2.0f, logf(u01(u1))));
     first = __fmul_rn(s, r);
     second = __fmul_rn(c, r);
 }
 
 // Four operator entries from one Philox call: Gaussian pairs (lanes 0,1) and (2,3), or
 // four uniforms on (-1, 1).  Uniform entries are NOT scaled here (see scale_uniform).
+template <bool kFast = false>
 __device__ __forceinline__ void gen4(int family, uint4 ctr, uint2 key, float v[4]) {
     const uint4 r = philox(ctr, key);
     if (family == RBG_GAUSSIAN) {
-        boxmuller(r.x, r.y, v[0], v[1]);
-        boxmuller(r.z, r.w, v[2], v[3]);
+        if (kFast) {
+            boxmuller_fast(r.x, r.y, v[0], v[1]);
+            boxmuller_fast(r.z, r.w, v[2], v[3]);
+        } else {
+            boxmuller(r.x, r.y, v[0], v[1]);
+            boxmuller(r.z, r.w, v[2], v[3]);
+        }
     } else {
         v[0] = uneg11(r.x);
         v[1] = uneg11(r.y);
