@@ -281,6 +281,11 @@ int rbg_lskge3_lowp(int32_t precision, int32_t layout, int32_t opS, int32_t opA,
                     int64_t co_s, const float *A, int64_t lda, float beta, float *B,
                     int64_t ldb, void *workspace, size_t workspace_bytes, rbg_stream_t stream);
 
+/* Device-side status of the precision path (no reference counterpart): RBG_SUCCESS, or
+ * RBG_ERROR_TIMEOUT if a bounded wait inside a tensor-core kernel gave up since the last call
+ * of this function.  Synchronises the device and clears the status. */
+int rbg_lowp_status(int32_t *code);
+
 /* ------------------------------------------------------------------ batching path */
 
 /* One problem of a batch: B_i = alpha_i * submat(S_i) * A_i + beta_i * B_i (left sketch,

@@ -128,6 +128,7 @@ SIGNATURES = {
     "rbg_lskge3_lowp_workspace": ([CI32, CI64, CI64, CI64, C.POINTER(C.c_size_t)], C.c_int),
     "rbg_lskge3_lowp": ([CI32, CI32, CI32, CI32, CI64, CI64, CI64, C.c_float, C.POINTER(rbg_dense_skop),
                          CI64, CI64, P, CI64, C.c_float, P, CI64, P, C.c_size_t, P], C.c_int),
+    "rbg_lowp_status": ([C.POINTER(CI32)], C.c_int),
     "rbg_lskge3_batched": ([CI32, C.POINTER(rbg_batch_problem), CI64, CI32, P], C.c_int),
     "rbg_batched_tile_configs": ([C.POINTER(CI32)], C.c_int),
 }

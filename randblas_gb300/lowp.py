@@ -37,3 +37,11 @@ def sketch_lowp(layout: Layout, opS: Op, opA: Op, d: int, n: int, m: int, alpha:
     call("rbg_lskge3_lowp", precision, int(layout), int(opS), int(opA), d, n, m, float(alpha),
          C.byref(S._c()), ro_s, co_s, _ptr(A), lda, float(beta), _ptr(B), ldb, ws, wbytes,
          _stream())
+
+
+def status() -> int:
+    """Device-side status of the tensor-core kernels since the last call (0 = fine,
+    4 = a bounded wait timed out); synchronises the device."""
+    code = C.c_int32()
+    call("rbg_lowp_status", C.byref(code))
+    return code.value

@@ -1,0 +1,89 @@
+"""The tensor-core precision path (rbg_lskge3_lowp): BF16 operands, FP32 accumulation.
+
+1. Exactness of the tensor-core mapping: the result equals an FP64 product of the same
+   BF16-rounded operands up to FP32 accumulation error (relative Frobenius <= 2e-5).
+2. Accuracy: relative Frobenius error against the FP64 product of the unrounded operator and
+   data <= 1e-2 (the target stated for this path).
+Covers tails in every dimension, submatrix offsets (aligned and not), both operator
+orientations, both layouts, alpha / beta, uniform and Gaussian operators."""
+import numpy as np
+import pytest
+
+from gpu_helpers import to_dev, to_host
+
+pytestmark = pytest.mark.gpu
+
+CASES = [
+    # d, n, m, ro_s, co_s, opS, layout, family, alpha, beta
+    (128, 512, 256, 0, 0, 0, 1, 1, 1.0, 0.0),
+    (300, 130, 5000, 3, 8, 0, 1, 1, 1.0, 0.0),
+    (256, 1024, 6400, 0, 0, 0, 1, 0, 0.5, 0.0),
+    (200, 77, 3001, 5, 6, 0, 0, 1, 1.0, 2.0),
+    (140, 600, 1000, 7, 1, 1, 1, 1, -1.0, 0.0),
+    (96, 40, 777, 0, 3, 1, 0, 0, 1.0, 0.5),
+]
+
+
+def _bf16(x):
+    import torch
+    return torch.as_tensor(x).to(torch.bfloat16).to(torch.float64)
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_lowp_bf16(rb, oracle, case):
+    import torch
+    from oracle.oracle import State
+    from randblas_gb300 import lowp
+    d, n, m, ro, co, opS, lay, fam, alpha, beta = case
+    rows, cols = (d, m) if opS == 0 else (m, d)
+    Dr, Dc = rows + ro + 2, cols + co + 3
+    D = rb.DenseDist(Dr, Dc, rb.ScalarDist(fam))
+    seed = rb.RNGState(17, counter=(9, 0, 0, 0))
+    S = rb.DenseSkOp(D, seed)
+    g = torch.Generator(device="cuda").manual_seed(3)
+    Am = torch.randn(m, n, device="cuda", generator=g)        # op(A), m x n
+    A = Am.contiguous() if lay == 1 else Am.T.contiguous()   # row-major / col-major storage
+    lda = n if lay == 1 else m
+    B0 = torch.randn(d, n, device="cuda", generator=g)
+    B = B0.clone() if lay == 1 else B0.T.contiguous()
+    ldb = n if lay == 1 else d
+    lowp.sketch_lowp(rb.Layout(lay), rb.Op(opS), rb.Op.NoTrans, d, n, m, alpha, S, ro, co, A,
+                     lda, beta, B, ldb)
+    assert lowp.status() == 0
+    got = (B if lay == 1 else B.T).double().cpu()
+    Ssub = torch.from_numpy(oracle.dense_matrix(0, Dr, Dc, fam, 1, State.make((9, 0, 0, 0),
+                                                (17, 0)), rows, cols, ro, co))
+    opSm = Ssub if opS == 0 else Ssub.T
+    A64 = Am.double().cpu()
+    exact_rounded = alpha * (_bf16(opSm) @ _bf16(A64)) + beta * B0.double().cpu()
+    exact = alpha * (opSm.double() @ A64) + beta * B0.double().cpu()
+    r1 = float(torch.linalg.norm(got - exact_rounded) / torch.linalg.norm(exact_rounded))
+    r2 = float(torch.linalg.norm(got - exact) / torch.linalg.norm(exact))
+    assert r1 <= 2e-5, (case, r1)
+    assert r2 <= 1e-2, (case, r2)
+
+
+def test_lowp_workspace_and_errors(rb):
+    import torch
+    from randblas_gb300 import lowp
+    D = rb.DenseDist(256, 4096, rb.ScalarDist.Uniform)
+    S = rb.DenseSkOp(D, rb.RNGState(1))
+    A = torch.randn(4096, 64, device="cuda")
+    need = lowp.workspace_bytes(lowp.BF16, 256, 64, 4096)
+    ws = torch.empty(need + 1024, dtype=torch.uint8, device="cuda")
+    off = (-ws.data_ptr()) % 1024
+    ws_al = ws[off:off + need]
+    B1 = torch.empty(256, 64, device="cuda")
+    B2 = torch.empty(256, 64, device="cuda")
+    lowp.sketch_lowp(rb.Layout.RowMajor, rb.Op.NoTrans, rb.Op.NoTrans, 256, 64, 4096, 1.0, S, 0,
+                     0, A, 64, 0.0, B1, 64, workspace=ws_al)
+    lowp.sketch_lowp(rb.Layout.RowMajor, rb.Op.NoTrans, rb.Op.NoTrans, 256, 64, 4096, 1.0, S, 0,
+                     0, A, 64, 0.0, B2, 64)
+    assert torch.equal(B1, B2)  # deterministic, caller workspace or not
+    with pytest.raises(rb.RandBLASError):
+        lowp.sketch_lowp(rb.Layout.RowMajor, rb.Op.NoTrans, rb.Op.NoTrans, 256, 64, 4096, 1.0, S,
+                         0, 0, A, 63, 0.0, B1, 64)
+    with pytest.raises(rb.RandBLASError):
+        lowp.sketch_lowp(rb.Layout.RowMajor, rb.Op.NoTrans, rb.Op.NoTrans, 256, 64, 4096, 1.0, S,
+                         0, 0, A, 64, 0.0, B1, 64, workspace=ws_al[:need - 1024])
+    assert lowp.status() == 0
