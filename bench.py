@@ -155,6 +155,10 @@ def main():
                     help="operator rows of the bounded CPU-baseline sample")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--case", default="full",
+                    choices=["full", "lowp-small", "plain-small", "saso", "convert-small"],
+                    help="full: the benchmark line; the others run one kernel family on a "
+                         "smaller case (for profilers) and print a short JSON line")
     args = ap.parse_args()
 
     rank = int(os.environ.get("RANK", "0"))
@@ -163,6 +167,8 @@ def main():
 
     if args.impl == "reference":
         return run_reference(args, rank, world)
+    if args.case != "full":
+        return run_case(args)
 
     import torch
     import torch.distributed as dist
@@ -347,6 +353,51 @@ def bench_e2e(torch, rb, lowp, have_lowp, S, A_host, args, stream, flops, device
     return {"value": round(flops / (ms * 1e-3) / 1e12, 2), "unit": "TFLOP/s",
             "ms_per_step": round(ms, 3), "h2d_bytes_per_step": M_SK * N_SK * 4,
             "d2h_bytes_per_step": D_SK * N_SK * 4}
+
+
+def run_case(args):
+    """One kernel family on a smaller case: 4096 x 2^17 uniform operator against a
+    2^17 x 1024 FP32 matrix (512 MiB, larger than L2) for the dense paths; the full SASO
+    workload for the sparse path."""
+    import torch
+
+    import randblas_gb300 as rb
+    from randblas_gb300 import build as rbuild
+    from randblas_gb300 import lowp
+    rbuild.build()
+    torch.cuda.set_device(0)
+    dev = torch.device("cuda", 0)
+    stream = torch.cuda.current_stream()
+    out = {"case": args.case}
+    if args.case == "saso":
+        out.update(bench_saso(torch, rb, dev, args, stream, peaks()[0]))
+    else:
+        m = 1 << 17
+        S = rb.DenseSkOp(rb.DenseDist(D_SK, m, rb.ScalarDist.Uniform), rb.RNGState(3))
+        A = torch.randn(m, N_SK, device=dev)
+        B = torch.empty(D_SK, N_SK, device=dev)
+        if args.case == "lowp-small":
+            def step():
+                lowp.sketch_lowp(rb.Layout.RowMajor, rb.Op.NoTrans, rb.Op.NoTrans, D_SK, N_SK, m,
+                                 1.0, S, 0, 0, A, N_SK, 0.0, B, N_SK)
+        elif args.case == "convert-small":
+            def step():
+                # the same call with a 1-row operator: the A conversion dominates
+                lowp.sketch_lowp(rb.Layout.RowMajor, rb.Op.NoTrans, rb.Op.NoTrans, 1, N_SK, m,
+                                 1.0, S, 0, 0, A, N_SK, 0.0, B, N_SK)
+        else:
+            def step():
+                rb.sketch_general(rb.Layout.RowMajor, rb.Op.NoTrans, rb.Op.NoTrans, D_SK, N_SK, m,
+                                  1.0, S, A, N_SK, 0.0, B, N_SK)
+        rb.profile.enable(True)
+        ms = event_time(torch, step, args.steps, args.warmup, stream)
+        prof = rb.profile.read()
+        rb.profile.enable(False)
+        out.update({"d": D_SK, "m": m, "n": N_SK, "ms_per_step": round(ms, 4),
+                    "TFLOP/s": round(2.0 * D_SK * m * N_SK / (ms * 1e-3) / 1e12, 1),
+                    "kernels_ms": {k: round(v["ms"] / max(1, v["launches"]), 4)
+                                   for k, v in prof.items()}})
+    print(json.dumps(out))
 
 
 def run_reference(args, rank, world):
