@@ -214,6 +214,19 @@ int rbg_rskge3(int32_t layout, int32_t opA, int32_t opS, int64_t m, int64_t d, i
                double alpha, const void *A, int64_t lda, const rbg_dense_skop *S,
                int64_t ro_s, int64_t co_s, double beta, void *B, int64_t ldb,
                rbg_stream_t stream);
+/* Allocation-free variant of rbg_lskge3 -- no counterpart in the reference.  Same arguments
+ * and result; it never allocates device memory (no cudaMalloc, cudaMallocAsync or
+ * cudaFree), for callers that cannot: code capturing a CUDA graph with a fixed memory plan,
+ * or hosts that forbid allocation after start-up.  Its split-K partial sums live in a fixed
+ * 32 MiB device array inside the library, which every GPU that loads the library holds until
+ * exit; d * n * sizeof(T) may be at most 16 MiB, larger sizes return
+ * RBG_ERROR_INVALID_ARGUMENT.  The first call on a device looks up that array's address, so
+ * make it before any stream capture.  All calls share the array: calls whose kernels can
+ * overlap on the GPU race on it. */
+int rbg_lskge3_noalloc(int32_t layout, int32_t opS, int32_t opA, int64_t d, int64_t n, int64_t m,
+                       double alpha, const rbg_dense_skop *S, int64_t ro_s, int64_t co_s,
+                       const void *A, int64_t lda, double beta, void *B, int64_t ldb,
+                       rbg_stream_t stream);
 /* sketch_vector (RandBLAS/skve.hh:140-164): y = alpha * op(submat(S)) * x + beta * y with
  * strides incx, incy (>= 1); submat(S) is d x m. */
 int rbg_sketch_vector(int32_t opS, int64_t d, int64_t m, double alpha, const rbg_dense_skop *S,

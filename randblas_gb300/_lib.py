@@ -109,6 +109,8 @@ SIGNATURES = {
                     CD, P, CI64, P], C.c_int),
     "rbg_rskge3": ([CI32, CI32, CI32, CI64, CI64, CI64, CD, P, CI64, C.POINTER(rbg_dense_skop), CI64, CI64,
                     CD, P, CI64, P], C.c_int),
+    "rbg_lskge3_noalloc": ([CI32, CI32, CI32, CI64, CI64, CI64, CD, C.POINTER(rbg_dense_skop),
+                            CI64, CI64, P, CI64, CD, P, CI64, P], C.c_int),
     "rbg_sketch_vector": ([CI32, CI64, CI64, CD, C.POINTER(rbg_dense_skop), CI64, CI64, P, CI64, CD, P,
                            CI64, P], C.c_int),
     "rbg_lskges": ([CI32, CI32, CI32, CI64, CI64, CI64, CD, C.POINTER(rbg_sparse_skop), CI64, CI64, P,

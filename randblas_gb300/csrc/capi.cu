@@ -748,6 +748,48 @@ void rsksp3_impl(int32_t layout, int32_t opA, int32_t opS, int64_t m, int64_t d,
 
 }  // namespace
 
+namespace rbg {
+
+bool prepare_dense_left(int32_t layout, int32_t opS, int32_t opA, int64_t d, int64_t n,
+                        int64_t m, double alpha, const rbg_dense_skop *S, int64_t ro_s,
+                        int64_t co_s, const void *A, int64_t lda, double beta, void *B,
+                        int64_t ldb, DenseLeftProblem *out) {
+    check_layout(layout);
+    check_op(opS);
+    check_op(opA);
+    validate_dense_skop(S);
+    const Dims sub = dims_before_op(d, m, opS);
+    RBG_REQUIRE("lskge3", S->dist.n_rows >= sub.rows + ro_s);
+    RBG_REQUIRE("lskge3", S->dist.n_cols >= sub.cols + co_s);
+    RBG_REQUIRE("lskge3", ro_s >= 0 && co_s >= 0 && d >= 0 && n >= 0 && m >= 0);
+    const Dims a = dims_before_op(m, n, opA);
+    if (layout == RBG_COL_MAJOR) {
+        RBG_REQUIRE("lskge3", lda >= a.rows);
+        RBG_REQUIRE("lskge3", ldb >= d);
+    } else {
+        RBG_REQUIRE("lskge3", lda >= a.cols);
+        RBG_REQUIRE("lskge3", ldb >= n);
+    }
+    if (d == 0 || n == 0) return false;
+    check_nonnull(B, "B");
+    if (alpha != 0.0 && m > 0) check_nonnull(A, "A");
+    const Strides b = strides_of(layout, ldb);
+    out->dtype = S->dtype;
+    out->M = d;
+    out->N = n;
+    out->K = m;
+    out->alpha = alpha;
+    out->beta = beta;
+    out->P = make_p(*S, opS == RBG_TRANS, ro_s, co_s);
+    out->Q = q_of(A, layout, lda, opA);
+    out->out = B;
+    out->os_i = b.rs;
+    out->os_j = b.cs;
+    return true;
+}
+
+}  // namespace rbg
+
 extern "C" {
 
 const char *rbg_last_error(void) { return g_last_error.c_str(); }

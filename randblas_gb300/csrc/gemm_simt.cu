@@ -9,6 +9,8 @@
 // reference's BLAS call; K is split across CTAs when the output has too few tiles, with a
 // fixed-order reduction so results do not depend on timing.
 #include <algorithm>
+#include <exception>
+#include <mutex>
 
 #include "rbg_internal.h"
 
@@ -240,3 +242,103 @@ void gemm_dense_sketch(int dtype, int64_t M, int64_t N, int64_t K, double alpha,
 }
 
 }  // namespace rbg
+
+// ------------------------------------------------------------------ allocation-free variant
+// For callers that cannot allocate device memory -- code running inside a CUDA graph being
+// captured with a fixed memory plan, an allocator hook, or a host that forbids allocation
+// after start-up -- rbg_lskge3_noalloc runs the left dense sketch above with its split-K
+// partial sums in this file-scope device array instead of stream-ordered allocations.
+// Every GPU that loads this library holds the array until the process exits.
+namespace rbg {
+namespace {
+
+constexpr size_t kNoallocScratchBytes = size_t(32) << 20;  // 32 MiB
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoallocScratchBytes];
+
+// Device address of g_noalloc_scratch, looked up once per device (with that device current).
+void *noalloc_scratch_address() {
+    static std::mutex mu;
+    static void *addr[64] = {nullptr};
+    int dev = 0;
+    RBG_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 64) fail(RBG_ERROR_UNSUPPORTED, "device ordinal out of range");
+    std::lock_guard<std::mutex> g(mu);
+    if (!addr[dev]) {
+        void *p = nullptr;
+        RBG_CUDA(cudaGetSymbolAddress(&p, g_noalloc_scratch));
+        addr[dev] = p;
+    }
+    return addr[dev];
+}
+
+template <typename T>
+void run_noalloc(const DenseLeftProblem &pb, cudaStream_t s) {
+    const int64_t M = pb.M, N = pb.N, K = pb.K;
+    const size_t slice = (size_t)M * (size_t)N * sizeof(T);
+    if (slice > kNoallocScratchBytes / 2)
+        fail(RBG_ERROR_INVALID_ARGUMENT,
+             "rbg_lskge3_noalloc: d * n * sizeof(T) = " + std::to_string(slice) +
+                 " bytes exceeds its limit of " + std::to_string(kNoallocScratchBytes / 2) +
+                 " bytes (half of its fixed 32 MiB scratch); use rbg_lskge3");
+    const int64_t tiles = ((M + BM - 1) / BM) * ((N + BN - 1) / BN);
+    const int64_t kt_total = (K + BK - 1) / BK;
+    int splits = choose_splits(tiles, kt_total, M * N, sizeof(T));
+    while (splits > 1 && (size_t)splits * slice > kNoallocScratchBytes) --splits;
+    const int64_t kt_per_split = (kt_total + splits - 1) / splits;
+    T *partial = splits > 1 ? static_cast<T *>(noalloc_scratch_address()) : nullptr;
+    const dim3 grid((unsigned)tiles, (unsigned)splits);
+    // every partial element is written by exactly one CTA before the reduction reads it, so
+    // the scratch needs no clearing between calls
+    if (pb.P.buff)
+        dense_sketch_kernel<T, false><<<grid, NT, 0, s>>>(M, N, K, pb.P, pb.Q, (T)pb.alpha,
+                                                          (T)pb.beta, (T *)pb.out, pb.os_i,
+                                                          pb.os_j, kt_per_split, partial);
+    else
+        dense_sketch_kernel<T, true><<<grid, NT, 0, s>>>(M, N, K, pb.P, pb.Q, (T)pb.alpha,
+                                                         (T)pb.beta, (T *)pb.out, pb.os_i,
+                                                         pb.os_j, kt_per_split, partial);
+    RBG_LAUNCHED();
+    if (splits > 1) {
+        const int64_t work = M * N;
+        const int grid_r = (int)std::max<int64_t>(
+            1, std::min<int64_t>((work + 255) / 256, (int64_t)num_sms() * 16));
+        reduce_splits_kernel<T><<<grid_r, 256, 0, s>>>(M, N, splits, partial, (T)pb.alpha,
+                                                       (T)pb.beta, (T *)pb.out, pb.os_i, pb.os_j);
+        RBG_LAUNCHED();
+    }
+}
+
+}  // namespace
+}  // namespace rbg
+
+// The first call on a device looks up the scratch array's device address; make that first
+// call before capturing the stream into a CUDA graph.  Calls share the one array: two calls
+// whose kernels overlap on the GPU (different streams, no ordering) race on it.
+extern "C" int rbg_lskge3_noalloc(int32_t layout, int32_t opS, int32_t opA, int64_t d, int64_t n,
+                                  int64_t m, double alpha, const rbg_dense_skop *S, int64_t ro_s,
+                                  int64_t co_s, const void *A, int64_t lda, double beta, void *B,
+                                  int64_t ldb, rbg_stream_t stream) {
+    using namespace rbg;
+    try {
+        DenseLeftProblem pb{};
+        if (!prepare_dense_left(layout, opS, opA, d, n, m, alpha, S, ro_s, co_s, A, lda, beta, B,
+                                ldb, &pb))
+            return RBG_SUCCESS;
+        const cudaStream_t s = as_cuda(stream);
+        if (pb.K <= 0 || pb.alpha == 0.0) {
+            launch_scale(pb.dtype, pb.M, pb.N, pb.os_i, pb.os_j, pb.beta, pb.out, s);
+            return RBG_SUCCESS;
+        }
+        if (pb.dtype == RBG_F32)
+            run_noalloc<float>(pb, s);
+        else
+            run_noalloc<double>(pb, s);
+        return RBG_SUCCESS;
+    } catch (const Failure &e) {
+        set_last_error(e.msg);
+        return e.code;
+    } catch (const std::exception &e) {
+        set_last_error(e.what());
+        return RBG_ERROR_INVALID_ARGUMENT;
+    }
+}

@@ -113,6 +113,23 @@ void gemm_dense_sketch(int dtype, int64_t M, int64_t N, int64_t K, double alpha,
                        const POperand &P, const Strided &Q, double beta, void *out,
                        int64_t os_i, int64_t os_j, cudaStream_t s);
 
+// Argument checks and operand set-up of a left dense sketch (LSKGE3 semantics) for the
+// allocation-free entry point in gemm_simt.cu.  Returns false when there is nothing to
+// compute (d == 0 or n == 0); throws Failure on invalid arguments.
+struct DenseLeftProblem {
+    int dtype;
+    int64_t M, N, K;
+    double alpha, beta;
+    POperand P;
+    Strided Q;
+    void *out;
+    int64_t os_i, os_j;
+};
+bool prepare_dense_left(int32_t layout, int32_t opS, int32_t opA, int64_t d, int64_t n,
+                        int64_t m, double alpha, const rbg_dense_skop *S, int64_t ro_s,
+                        int64_t co_s, const void *A, int64_t lda, double beta, void *B,
+                        int64_t ldb, DenseLeftProblem *out);
+
 // --------------------------------------------------------------- sparse sketch (spmm.cu)
 // Sparse operand description for Out[M x N] = alpha * Sp[M x K] * Q[K x N] + beta * Out.
 struct SparseOperand {
