@@ -33,15 +33,19 @@ namespace {
 
 constexpr int BM = 128;          // rows of S per tile (tensor-memory lanes)
 constexpr int BN = 512;          // columns of A per tile (tensor-memory columns)
-constexpr int BK = 64;           // k per stage: 64 BF16 = one 128-byte swizzle row
-constexpr int STAGES = 2;
-constexpr int S_STAGE_BYTES = BM * BK * 2;  // 16 KiB
-constexpr int A_STAGE_BYTES = BN * BK * 2;  // 64 KiB
+constexpr int BK = 32;           // k per stage: 32 BF16 = one 64-byte swizzled row
+constexpr int ROW_BYTES = BK * 2;
+constexpr int CHUNKS = ROW_BYTES / 16;      // 16-byte chunks per row
+constexpr int STAGES = 5;
+constexpr int S_STAGE_BYTES = BM * BK * 2;  // 8 KiB
+constexpr int A_STAGE_BYTES = BN * BK * 2;  // 32 KiB
 constexpr int NUM_THREADS = 512;
 constexpr int EPI_WARP0 = 4;
 constexpr int GEN_WARP0 = 8;
 constexpr int GEN_WARPS = 8;
 constexpr int GEN_THREADS = GEN_WARPS * 32;
+constexpr int GEN_GROUPS = 2;                        // groups take alternate stages
+constexpr int GROUP_THREADS = GEN_THREADS / GEN_GROUPS;
 constexpr uint32_t TMEM_COLS = 512;
 constexpr int SMEM_BYTES = STAGES * (S_STAGE_BYTES + A_STAGE_BYTES) + 1024 /*align*/ + 256;
 
@@ -51,11 +55,11 @@ struct LowpParams {
     int64_t r0, c0;        // natural coordinates of submat(S)(0, 0)
     int r_on_i;            // 1: natural row follows the output row i
     int64_t k_steps;       // ceil(K / BK)
-    int64_t tiles_n;       // ceil(N / BN)
-    int64_t tiles;         // ceil(M / BM) * tiles_n
+    int64_t m_groups;      // row groups, each CM tiles of BM rows
+    int64_t n_groups;      // column groups, each CN tiles of BN columns
     int64_t ks_per_group;  // k-steps per K slice
-    int64_t units;         // tiles * groups
-    float *partial;        // [groups][M][N]
+    int64_t units;         // m_groups * n_groups * k_groups
+    float *partial;        // [k_groups][M][N]
     int *err;
 };
 
@@ -68,82 +72,127 @@ __device__ __forceinline__ uint32_t pack_bf16(float a, float b) {
     return *reinterpret_cast<const uint32_t *>(&h);
 }
 
-// Eight consecutive natural-column entries C = Cs .. Cs+7 of natural row R (transformed,
-// uniform entries scaled).  kAligned: Cs % 4 == 0 (two Philox calls instead of three).
-template <bool kAligned>
-__device__ __forceinline__ void gen8(const DenseGen &g, int64_t R, int64_t Cs, float out[8]) {
+// 128-bit counter + small increment (add with carry through all four words).
+__device__ __forceinline__ uint4 ctr_add_u32(uint4 c, uint32_t v) {
+    asm("add.cc.u32 %0, %0, %4;\n\t"
+        "addc.cc.u32 %1, %1, 0;\n\t"
+        "addc.cc.u32 %2, %2, 0;\n\t"
+        "addc.u32 %3, %3, 0;"
+        : "+r"(c.x), "+r"(c.y), "+r"(c.z), "+r"(c.w)
+        : "r"(v));
+    return c;
+}
+
+// uneg11 as one FMA: the product by 2^-31 is exact, so fma rounds once, like the reference.
+__device__ __forceinline__ float uneg11_fma(uint32_t x) {
+    return __fmaf_rn(__int2float_rn((int32_t)x), 0x1p-31f, 0x1p-32f);
+}
+
+// Eight consecutive natural-column entries starting at a block-aligned counter `c` (two
+// Philox calls), finished (uniform entries scaled) and packed to BF16.
+__device__ __forceinline__ uint4 gen8_aligned(int family, uint4 c, uint2 key) {
+    float v[8];
+    if (family == RBG_UNIFORM) {
+        const uint4 r0 = philox(c, key);
+        const uint4 r1 = philox(ctr_add_u32(c, 1u), key);
+        v[0] = uneg11_fma(r0.x); v[1] = uneg11_fma(r0.y);
+        v[2] = uneg11_fma(r0.z); v[3] = uneg11_fma(r0.w);
+        v[4] = uneg11_fma(r1.x); v[5] = uneg11_fma(r1.y);
+        v[6] = uneg11_fma(r1.z); v[7] = uneg11_fma(r1.w);
+#pragma unroll
+        for (int e = 0; e < 8; ++e) v[e] = __fmul_rn(v[e], 1.7320508075688772f);
+    } else {
+        gen4<true>(family, c, key, v);
+        gen4<true>(family, ctr_add_u32(c, 1u), key, v + 4);
+    }
+    return make_uint4(pack_bf16(v[0], v[1]), pack_bf16(v[2], v[3]), pack_bf16(v[4], v[5]),
+                      pack_bf16(v[6], v[7]));
+}
+
+// Eight consecutive natural-column entries C = Cs .. Cs+7 of natural row R, any alignment.
+__device__ __forceinline__ void gen8_any(const DenseGen &g, int64_t R, int64_t Cs, float out[8]) {
     const int64_t b0 = Cs >> 2;
+    const int sh = (int)(Cs & 3);
     float v[12];
     gen4<true>(g.family, g.counter_of(R, b0), g.key, v);
     gen4<true>(g.family, g.counter_of(R, b0 + 1), g.key, v + 4);
-    if (kAligned) {
+    if (sh) gen4<true>(g.family, g.counter_of(R, b0 + 2), g.key, v + 8);
 #pragma unroll
-        for (int e = 0; e < 8; ++e) out[e] = finish_bf16_input(g.family, v[e]);
-    } else {
-        const int sh = (int)(Cs & 3);
-        if (sh) gen4<true>(g.family, g.counter_of(R, b0 + 2), g.key, v + 8);
-#pragma unroll
-        for (int e = 0; e < 8; ++e) {
-            const float x = sh == 0 ? v[e] : sh == 1 ? v[e + 1] : sh == 2 ? v[e + 2] : v[e + 3];
-            out[e] = finish_bf16_input(g.family, x);
-        }
+    for (int e = 0; e < 8; ++e) {
+        const float x = sh == 0 ? v[e] : sh == 1 ? v[e + 1] : sh == 2 ? v[e + 2] : v[e + 3];
+        out[e] = finish_bf16_input(g.family, x);
     }
 }
 
-// S tile (BM rows x BK k, BF16, K-major, 128-byte swizzle) for rows i0.., k-step k0...
-// Row i occupies bytes [128 i, 128 i + 128); its 16-byte chunk c sits at chunk c ^ (i % 8).
-template <bool kAligned>
-__device__ __forceinline__ void produce_s_tile(uint8_t *tile, const LowpParams &p, int64_t i0,
-                                               int64_t k0, int gt) {
+// Byte offset of BF16 element (row i, k) in a BM x BK tile stored K-major with the 64-byte
+// swizzle: row i occupies bytes [64 i, 64 i + 64); its 16-byte chunk c sits at chunk
+// c ^ ((i / 2) % 4) (address bits 4-5 XOR bits 7-8).
+__device__ __forceinline__ uint32_t sw_offset(int i, int k) {
+    return (uint32_t)(i * ROW_BYTES + ((((k >> 3) ^ ((i >> 1) & 3))) << 4) + (k & 7) * 2);
+}
+
+// The part of one S stage this CTA produces: rows [row_lo, row_lo + rows) of the BM x BK
+// tile, by `nth` threads (thread index gt).  Generic path: any operator orientation and
+// submatrix offset.
+__device__ __forceinline__ void produce_s_generic(uint8_t *tile, const LowpParams &p, int64_t i0,
+                                                  int64_t k0, int row_lo, int rows, int gt,
+                                                  int nth) {
     if (p.r_on_i) {
-        // natural row follows i: thread unit = (row i, 8-wide k chunk c), one 16-byte store
-        for (int u = gt; u < BM * 8; u += GEN_THREADS) {
-            const int i = u >> 3, c = u & 7;
+        for (int u = gt; u < rows * CHUNKS; u += nth) {
+            const int i = row_lo + u / CHUNKS, c = u % CHUNKS;
             const int64_t gi = i0 + i, gk = k0 + 8 * c;
             uint4 w = make_uint4(0, 0, 0, 0);
             if (gi < p.M && gk < p.K) {
                 float v[8];
-                gen8<kAligned>(p.gen, p.r0 + gi, p.c0 + gk, v);
-                if (gk + 8 > p.K) {
+                gen8_any(p.gen, p.r0 + gi, p.c0 + gk, v);
 #pragma unroll
-                    for (int e = 0; e < 8; ++e)
-                        if (gk + e >= p.K) v[e] = 0.f;
-                }
+                for (int e = 0; e < 8; ++e)
+                    if (gk + e >= p.K) v[e] = 0.f;
                 w = make_uint4(pack_bf16(v[0], v[1]), pack_bf16(v[2], v[3]),
                                pack_bf16(v[4], v[5]), pack_bf16(v[6], v[7]));
             }
-            *reinterpret_cast<uint4 *>(tile + i * 128 + ((c ^ (i & 7)) << 4)) = w;
+            *reinterpret_cast<uint4 *>(tile + sw_offset(i, 8 * c)) = w;
         }
     } else {
-        // natural row follows k: thread unit = (k index kk, 8 consecutive rows i = 8q..8q+7)
-        for (int u = gt; u < BK * (BM / 8); u += GEN_THREADS) {
-            const int kk = u / (BM / 8), q = u % (BM / 8);
-            const int64_t gk = k0 + kk, gi = i0 + 8 * q;
+        for (int u = gt; u < BK * (rows / 8); u += nth) {
+            const int kk = u / (rows / 8), q = u % (rows / 8);
+            const int64_t gk = k0 + kk, gi = i0 + row_lo + 8 * q;
             float v[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
             if (gk < p.K && gi < p.M) {
-                gen8<kAligned>(p.gen, p.r0 + gk, p.c0 + gi, v);
+                gen8_any(p.gen, p.r0 + gk, p.c0 + gi, v);
 #pragma unroll
                 for (int e = 0; e < 8; ++e)
                     if (gi + e >= p.M) v[e] = 0.f;
             }
 #pragma unroll
-            for (int e = 0; e < 8; ++e) {
-                const int i = 8 * q + e;
-                *reinterpret_cast<__nv_bfloat16 *>(tile + i * 128 + (((kk >> 3) ^ (i & 7)) << 4) +
-                                                   (kk & 7) * 2) = __float2bfloat16_rn(v[e]);
-            }
+            for (int e = 0; e < 8; ++e)
+                *reinterpret_cast<__nv_bfloat16 *>(tile + sw_offset(row_lo + 8 * q + e, kk)) =
+                    __float2bfloat16_rn(v[e]);
         }
     }
 }
 
-template <bool kAligned>
+// One CTA computes a BM x BN output tile over one K slice per work unit.  The CTAs of a
+// cluster of CN x CM share work: the CN CTAs of a row group hold the same BM rows of S and
+// different BN-column tiles of A -- each produces BM / CN rows of every S stage and copies them
+// into its peers with a bulk shared-memory copy -- and the CM CTAs of a column group hold the
+// same A tile, which each loads a 1 / CM share of with a TMA multicast to all of them.
+// kFast: natural row follows i and the operator's column offset is a multiple of 4, so every
+// 8-wide k chunk starts on a counter block.
+template <int CN, int CM, bool kFast>
 __global__ void __launch_bounds__(NUM_THREADS, 1)
     sketch_bf16_kernel(const __grid_constant__ CUtensorMap tmap_a, LowpParams p) {
+    constexpr int CS = CN * CM;
+    constexpr int ROWS = BM / CN;                        // S rows this CTA produces per stage
+    constexpr uint32_t PART_BYTES = ROWS * ROW_BYTES;    // their bytes in a stage
+    constexpr int ROW_SLOTS = GROUP_THREADS / CHUNKS;    // rows a generator group covers at once
+    constexpr int FAST_ROWS = ROWS / ROW_SLOTS;          // rows per generator thread per stage
+    static_assert(ROWS % ROW_SLOTS == 0, "generator mapping");
     extern __shared__ uint8_t smem_raw[];
     uint8_t *smem = reinterpret_cast<uint8_t *>(
         (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
-    uint8_t *s_tiles = smem;                                 // STAGES x 16 KiB
-    uint8_t *a_tiles = smem + STAGES * S_STAGE_BYTES;        // STAGES x 64 KiB
+    uint8_t *s_tiles = smem;                                 // STAGES x S_STAGE_BYTES
+    uint8_t *a_tiles = smem + STAGES * S_STAGE_BYTES;        // STAGES x A_STAGE_BYTES
     uint64_t *bars = reinterpret_cast<uint64_t *>(a_tiles + STAGES * A_STAGE_BYTES);
     uint64_t *full_a = bars;
     uint64_t *full_s = bars + STAGES;
@@ -153,11 +202,15 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
     uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(acc_empty + 1);
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const uint32_t rank = CS > 1 ? tc::cluster_ctarank() : 0u;
+    const uint32_t n_idx = rank % CN, m_idx = rank / CN;
+    const int64_t cluster_id = blockIdx.x / CS;
+    const int64_t num_clusters = gridDim.x / CS;
     if (threadIdx.x == 0) {
         for (int s = 0; s < STAGES; ++s) {
             tc::mbar_init(&full_a[s], 1);
-            tc::mbar_init(&full_s[s], GEN_WARPS);
-            tc::mbar_init(&empty[s], 1);
+            tc::mbar_init(&full_s[s], 1);
+            tc::mbar_init(&empty[s], CS);
         }
         tc::mbar_init(acc_full, 1);
         tc::mbar_init(acc_empty, 4);
@@ -170,27 +223,45 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
     }
     tc::tc_fence_before();
     __syncthreads();
+    if (CS > 1) tc::cluster_sync();  // peers' barriers are initialised before any signal
     tc::tc_fence_after();
     const uint32_t tmem = *tmem_slot;
+
+    auto unit_tiles = [&](int64_t u, int64_t &m0, int64_t &n0, int64_t &ks0, int64_t &ks1) {
+        const int64_t mg = u % p.m_groups;
+        const int64_t ng = (u / p.m_groups) % p.n_groups;
+        const int64_t g = u / (p.m_groups * p.n_groups);
+        m0 = (mg * CM + m_idx) * BM;
+        n0 = (ng * CN + n_idx) * BN;
+        ks0 = g * p.ks_per_group;
+        ks1 = min(p.k_steps, ks0 + p.ks_per_group);
+        return g;
+    };
 
     if (warp == 0) {
         // ---------------- TMA producer
         if (lane == 0) {
             int64_t it = 0;
-            for (int64_t u = blockIdx.x; u < p.units; u += gridDim.x) {
-                const int64_t tile = u % p.tiles, g = u / p.tiles;
-                const int64_t n0 = (tile % p.tiles_n) * BN;
-                const int64_t ks0 = g * p.ks_per_group;
-                const int64_t ks1 = min(p.k_steps, ks0 + p.ks_per_group);
+            for (int64_t u = cluster_id; u < p.units; u += num_clusters) {
+                int64_t m0, n0, ks0, ks1;
+                unit_tiles(u, m0, n0, ks0, ks1);
                 for (int64_t ks = ks0; ks < ks1; ++ks, ++it) {
                     const int s = (int)(it % STAGES);
                     const uint32_t ph = (uint32_t)((it / STAGES) & 1);
-                    if (!tc::mbar_wait(&empty[s], ph ^ 1, p.err)) goto done;
+                    if (!tc::mbar_wait<(CS > 1)>(&empty[s], ph ^ 1, p.err)) goto done;
                     tc::mbar_arrive_expect_tx(&full_a[s], A_STAGE_BYTES);
                     uint8_t *dst = a_tiles + s * A_STAGE_BYTES;
-                    tc::tma_load_2d(dst, &tmap_a, &full_a[s], (int)(ks * BK), (int)n0);
-                    tc::tma_load_2d(dst + A_STAGE_BYTES / 2, &tmap_a, &full_a[s], (int)(ks * BK),
-                                    (int)(n0 + BN / 2));
+                    if (CM == 2) {
+                        // this CTA loads half h = m_idx of the tile for itself and its M-peer
+                        const uint16_t mask = (uint16_t)((1u << rank) | (1u << (rank ^ CN)));
+                        tc::tma_load_2d_multicast(dst + m_idx * (A_STAGE_BYTES / 2), &tmap_a,
+                                                  &full_a[s], (int)(ks * BK),
+                                                  (int)(n0 + m_idx * (BN / 2)), mask);
+                    } else {
+                        tc::tma_load_2d(dst, &tmap_a, &full_a[s], (int)(ks * BK), (int)n0);
+                        tc::tma_load_2d(dst + A_STAGE_BYTES / 2, &tmap_a, &full_a[s],
+                                        (int)(ks * BK), (int)(n0 + BN / 2));
+                    }
                 }
             }
         }
@@ -199,24 +270,23 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
         if (lane == 0) {
             constexpr uint32_t idesc = tc::idesc_bf16_f32(BM, BN / 2);
             int64_t it = 0, uc = 0;
-            for (int64_t u = blockIdx.x; u < p.units; u += gridDim.x, ++uc) {
-                const int64_t g = u / p.tiles;
-                const int64_t ks0 = g * p.ks_per_group;
-                const int64_t ks1 = min(p.k_steps, ks0 + p.ks_per_group);
-                if (!tc::mbar_wait(acc_empty, (uint32_t)((uc & 1) ^ 1), p.err)) goto done;
+            for (int64_t u = cluster_id; u < p.units; u += num_clusters, ++uc) {
+                int64_t m0, n0, ks0, ks1;
+                unit_tiles(u, m0, n0, ks0, ks1);
+                if (!tc::mbar_wait(acc_empty, (uint32_t)((uc & 1) ^ 1), p.err, 256)) goto done;
                 tc::tc_fence_after();
                 for (int64_t ks = ks0; ks < ks1; ++ks, ++it) {
                     const int s = (int)(it % STAGES);
                     const uint32_t ph = (uint32_t)((it / STAGES) & 1);
-                    if (!tc::mbar_wait(&full_a[s], ph, p.err)) goto done;
-                    if (!tc::mbar_wait(&full_s[s], ph, p.err)) goto done;
+                    if (!tc::mbar_wait<(CM > 1)>(&full_a[s], ph, p.err)) goto done;
+                    if (!tc::mbar_wait<(CN > 1)>(&full_s[s], ph, p.err)) goto done;
                     tc::tc_fence_after();
                     const uint64_t adesc =
-                        tc::sw128_kmajor_desc(tc::smem_addr(s_tiles + s * S_STAGE_BYTES));
+                        tc::kmajor_desc(tc::smem_addr(s_tiles + s * S_STAGE_BYTES), ROW_BYTES);
                     const uint64_t bdesc0 =
-                        tc::sw128_kmajor_desc(tc::smem_addr(a_tiles + s * A_STAGE_BYTES));
-                    const uint64_t bdesc1 = tc::sw128_kmajor_desc(
-                        tc::smem_addr(a_tiles + s * A_STAGE_BYTES + A_STAGE_BYTES / 2));
+                        tc::kmajor_desc(tc::smem_addr(a_tiles + s * A_STAGE_BYTES), ROW_BYTES);
+                    const uint64_t bdesc1 = tc::kmajor_desc(
+                        tc::smem_addr(a_tiles + s * A_STAGE_BYTES + A_STAGE_BYTES / 2), ROW_BYTES);
 #pragma unroll
                     for (int kk = 0; kk < BK / 16; ++kk) {
                         const uint32_t acc = (ks > ks0 || kk > 0) ? 1u : 0u;
@@ -224,19 +294,33 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
                         tc::mma_f16(tmem, adesc + 2 * kk, bdesc0 + 2 * kk, idesc, acc);
                         tc::mma_f16(tmem + BN / 2, adesc + 2 * kk, bdesc1 + 2 * kk, idesc, acc);
                     }
-                    tc::mma_commit(&empty[s]);
+                    // stage s of every CTA in the cluster may be rewritten by any of them, so
+                    // each CTA's MMA completion is signalled to all of them
+                    if (CS > 1)
+                        tc::mma_commit_multicast(&empty[s], (uint16_t)((1u << CS) - 1));
+                    else
+                        tc::mma_commit(&empty[s]);
                 }
                 tc::mma_commit(acc_full);
+            }
+            // wait until the last arrivals on this CTA's stage barriers -- including the
+            // peers' -- have landed, so nothing targets this CTA after it exits
+            const int64_t last = it;
+            for (int64_t j = 0; j < STAGES && j < last; ++j) {
+                const int64_t idx = last - 1 - j;
+                if (!tc::mbar_wait<(CS > 1)>(&empty[idx % STAGES],
+                                             (uint32_t)((idx / STAGES) & 1), p.err))
+                    goto done;
             }
         }
     } else if (warp >= EPI_WARP0 && warp < EPI_WARP0 + 4) {
         // ---------------- epilogue: tensor memory -> FP32 partial tile
         const int q = warp - EPI_WARP0;  // tensor-memory lanes 32q .. 32q+31
         int64_t uc = 0;
-        for (int64_t u = blockIdx.x; u < p.units; u += gridDim.x, ++uc) {
-            const int64_t tile = u % p.tiles, g = u / p.tiles;
-            const int64_t m0 = (tile / p.tiles_n) * BM, n0 = (tile % p.tiles_n) * BN;
-            if (!tc::mbar_wait(acc_full, (uint32_t)(uc & 1), p.err)) goto done;
+        for (int64_t u = cluster_id; u < p.units; u += num_clusters, ++uc) {
+            int64_t m0, n0, ks0, ks1;
+            const int64_t g = unit_tiles(u, m0, n0, ks0, ks1);
+            if (!tc::mbar_wait(acc_full, (uint32_t)(uc & 1), p.err, 512)) goto done;
             tc::tc_fence_after();
             const int64_t row = m0 + 32 * q + lane;
             float *dst = p.partial + (g * p.M + row) * p.N;
@@ -266,28 +350,73 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
             if (lane == 0) tc::mbar_arrive(acc_empty);
         }
     } else if (warp >= GEN_WARP0) {
-        // ---------------- S producers
-        const int gt = threadIdx.x - GEN_WARP0 * 32;
+        // ---------------- S producers: GEN_GROUPS groups, group gi takes stages it % G == gi
+        const int gi = (warp - GEN_WARP0) / (GEN_WARPS / GEN_GROUPS);
+        const int tg = threadIdx.x - GEN_WARP0 * 32 - gi * GROUP_THREADS;
+        const int row_lo = (int)n_idx * ROWS;
+        uint32_t peer_full_s[STAGES] = {};
+        uint32_t peer_tiles = 0;
+        if (CN > 1) {
+            for (int s = 0; s < STAGES; ++s)
+                peer_full_s[s] = tc::map_to_rank(tc::smem_addr(&full_s[s]), rank ^ 1u);
+            peer_tiles = tc::map_to_rank(tc::smem_addr(s_tiles), rank ^ 1u);
+        }
+        const int fc = tg % CHUNKS;
         int64_t it = 0;
-        for (int64_t u = blockIdx.x; u < p.units; u += gridDim.x) {
-            const int64_t tile = u % p.tiles, g = u / p.tiles;
-            const int64_t m0 = (tile / p.tiles_n) * BM;
-            const int64_t ks0 = g * p.ks_per_group;
-            const int64_t ks1 = min(p.k_steps, ks0 + p.ks_per_group);
+        for (int64_t u = cluster_id; u < p.units; u += num_clusters) {
+            int64_t m0, n0, ks0, ks1;
+            unit_tiles(u, m0, n0, ks0, ks1);
+            // fast path: counter offset of each owned row's chunk at k-step 0
+            int64_t base[FAST_ROWS > 0 ? FAST_ROWS : 1];
+            bool row_ok[FAST_ROWS > 0 ? FAST_ROWS : 1];
+            if (kFast) {
+#pragma unroll
+                for (int t = 0; t < FAST_ROWS; ++t) {
+                    const int64_t gi_row = m0 + row_lo + tg / CHUNKS + t * ROW_SLOTS;
+                    row_ok[t] = gi_row < p.M;
+                    base[t] = (p.r0 + gi_row) * p.gen.stride + p.c0 / 4 + 2 * fc;
+                }
+            }
             for (int64_t ks = ks0; ks < ks1; ++ks, ++it) {
+                if ((int)(it % GEN_GROUPS) != gi) continue;
                 const int s = (int)(it % STAGES);
                 const uint32_t ph = (uint32_t)((it / STAGES) & 1);
-                if (!tc::mbar_wait(&empty[s], ph ^ 1, p.err)) goto done;
-                produce_s_tile<kAligned>(s_tiles + s * S_STAGE_BYTES, p, m0, ks * BK, gt);
+                if (!tc::mbar_wait<(CS > 1)>(&empty[s], ph ^ 1, p.err)) goto done;
+                uint8_t *tile = s_tiles + s * S_STAGE_BYTES;
+                const int64_t gk = ks * BK + 8 * fc;
+                if (kFast && gk + 8 <= p.K) {
+#pragma unroll
+                    for (int t = 0; t < FAST_ROWS; ++t) {
+                        const int i = row_lo + tg / CHUNKS + t * ROW_SLOTS;
+                        const uint4 c = ctr_add(p.gen.ctr, (uint64_t)(base[t] + ks * (BK / 4)));
+                        const uint4 w = row_ok[t] ? gen8_aligned(p.gen.family, c, p.gen.key)
+                                                  : make_uint4(0, 0, 0, 0);
+                        *reinterpret_cast<uint4 *>(tile + sw_offset(i, 8 * fc)) = w;
+                    }
+                } else {
+                    produce_s_generic(tile, p, m0, ks * BK, row_lo, ROWS, tg, GROUP_THREADS);
+                }
                 tc::fence_proxy_async_smem();
-                __syncwarp();
-                if (lane == 0) tc::mbar_arrive(&full_s[s]);
+                tc::named_barrier(1 + gi, GROUP_THREADS);
+                if (tg == 0) {
+                    if (CN > 1) {
+                        // the peer's share of this stage arrives by bulk copy
+                        tc::mbar_arrive_expect_tx(&full_s[s], PART_BYTES);
+                        const uint32_t off = (uint32_t)(s * S_STAGE_BYTES + row_lo * ROW_BYTES);
+                        tc::bulk_copy_to_peer(peer_tiles + off, s_tiles + off, PART_BYTES,
+                                              peer_full_s[s]);
+                    } else {
+                        tc::mbar_arrive(&full_s[s]);
+                    }
+                }
             }
         }
     }
 done:
     tc::tc_fence_before();
+    __syncwarp();
     __syncthreads();
+    if (CS > 1) tc::cluster_sync();  // no CTA leaves while a peer may still signal it
     if (warp == 1) {
         __syncwarp();
         tc::tc_fence_after();
@@ -295,36 +424,81 @@ done:
     }
 }
 
-// op(A)(k, j) -> At[j * pitch + k] in BF16, through a 64 x 64 shared-memory tile.
-__global__ void convert_a_kernel(const float *__restrict__ A, int64_t sk, int64_t sj, int64_t K,
-                                 int64_t N, __nv_bfloat16 *__restrict__ At, int64_t pitch) {
-    __shared__ float tile[64][65];
-    const int64_t tk = (K + 63) / 64, tj = (N + 63) / 64;
+// op(A)(k, j) -> At[j * pitch + k] in BF16.  When j has unit stride the kernel transposes a
+// 64 (k) x 128 (j) tile through shared memory (float4 reads along j, 16-byte writes along k);
+// when k has unit stride it converts in place order (float4 reads, 8-byte writes).
+__global__ void __launch_bounds__(256) convert_a_kernel(const float *__restrict__ A, int64_t sk,
+                                                        int64_t sj, int64_t K, int64_t N,
+                                                        __nv_bfloat16 *__restrict__ At,
+                                                        int64_t pitch) {
+    __shared__ float tile[64][129];
+    if (sk == 1 && sj != 1) {
+        // direct: At[j][k] = A[j * sj + k]
+        const int64_t kq = (K + 3) / 4;
+        for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < kq * N;
+             t += (int64_t)gridDim.x * blockDim.x) {
+            const int64_t j = t / kq, k = (t % kq) * 4;
+            const float *src = A + j * sj + k;
+            float v[4];
+            if (k + 4 <= K && ((reinterpret_cast<uintptr_t>(src) & 15) == 0)) {
+                const float4 f = *reinterpret_cast<const float4 *>(src);
+                v[0] = f.x; v[1] = f.y; v[2] = f.z; v[3] = f.w;
+            } else {
+                for (int e = 0; e < 4; ++e) v[e] = k + e < K ? src[e] : 0.f;
+            }
+            __nv_bfloat16 *dst = At + j * pitch + k;
+            if (k + 4 <= K) {
+                uint2 w;
+                w.x = pack_bf16(v[0], v[1]);
+                w.y = pack_bf16(v[2], v[3]);
+                *reinterpret_cast<uint2 *>(dst) = w;
+            } else {
+                for (int e = 0; e < 4 && k + e < K; ++e) dst[e] = __float2bfloat16_rn(v[e]);
+            }
+        }
+        return;
+    }
+    const int64_t tk = (K + 63) / 64, tj = (N + 127) / 128;
+    const bool vec = sj == 1 && (N % 4) == 0 && (sk % 4) == 0 &&
+                     (reinterpret_cast<uintptr_t>(A) & 15) == 0;
     for (int64_t t = blockIdx.x; t < tk * tj; t += gridDim.x) {
-        const int64_t k0 = (t % tk) * 64, j0 = (t / tk) * 64;
-        if (sj == 1 || sk != 1) {
-            for (int w = threadIdx.x; w < 64 * 64; w += blockDim.x) {
-                const int kk = w / 64, jj = w % 64;
-                tile[kk][jj] = (k0 + kk < K && j0 + jj < N) ? A[(k0 + kk) * sk + (j0 + jj) * sj]
-                                                             : 0.f;
+        const int64_t k0 = (t % tk) * 64, j0 = (t / tk) * 128;
+        if (vec) {
+            // 32 float4 per k-row of the tile; 8 rows per pass of 256 threads
+            for (int w = threadIdx.x; w < 64 * 32; w += 256) {
+                const int kk = w / 32, jq = (w % 32) * 4;
+                float4 f = make_float4(0.f, 0.f, 0.f, 0.f);
+                if (k0 + kk < K && j0 + jq < N)
+                    f = *reinterpret_cast<const float4 *>(A + (k0 + kk) * sk + j0 + jq);
+                tile[kk][jq] = f.x;
+                tile[kk][jq + 1] = f.y;
+                tile[kk][jq + 2] = f.z;
+                tile[kk][jq + 3] = f.w;
             }
         } else {
-            for (int w = threadIdx.x; w < 64 * 64; w += blockDim.x) {
-                const int jj = w / 64, kk = w % 64;
+            for (int w = threadIdx.x; w < 64 * 128; w += 256) {
+                const int kk = w / 128, jj = w % 128;
                 tile[kk][jj] = (k0 + kk < K && j0 + jj < N) ? A[(k0 + kk) * sk + (j0 + jj) * sj]
                                                              : 0.f;
             }
         }
         __syncthreads();
-        // each thread writes two consecutive k (one 32-bit BF16 pair) of one row j
-        for (int w = threadIdx.x; w < 64 * 32; w += blockDim.x) {
-            const int jj = w / 32, kp = (w % 32) * 2;
-            if (j0 + jj < N && k0 + kp < K) {
-                const __nv_bfloat162 h = __floats2bfloat162_rn(tile[kp][jj], tile[kp + 1][jj]);
-                if (k0 + kp + 1 < K)
-                    *reinterpret_cast<__nv_bfloat162 *>(At + (j0 + jj) * pitch + k0 + kp) = h;
-                else
-                    At[(j0 + jj) * pitch + k0 + kp] = h.x;
+        // 128 rows j x 8 chunks of 8 k: one 16-byte store each
+        for (int w = threadIdx.x; w < 128 * 8; w += 256) {
+            const int jj = w / 8, c = w % 8;
+            if (j0 + jj >= N) continue;
+            const int64_t k = k0 + 8 * c;
+            if (k >= K) continue;
+            __nv_bfloat16 *dst = At + (j0 + jj) * pitch + k;
+            if (k + 8 <= K) {
+                uint4 q;
+                q.x = pack_bf16(tile[8 * c][jj], tile[8 * c + 1][jj]);
+                q.y = pack_bf16(tile[8 * c + 2][jj], tile[8 * c + 3][jj]);
+                q.z = pack_bf16(tile[8 * c + 4][jj], tile[8 * c + 5][jj]);
+                q.w = pack_bf16(tile[8 * c + 6][jj], tile[8 * c + 7][jj]);
+                *reinterpret_cast<uint4 *>(dst) = q;
+            } else {
+                for (int e = 0; k + e < K; ++e) dst[e] = __float2bfloat16_rn(tile[8 * c + e][jj]);
             }
         }
         __syncthreads();
@@ -351,26 +525,35 @@ __global__ void lowp_reduce_kernel(int64_t M, int64_t N, int64_t groups, const f
 __device__ int g_lowp_error = 0;
 
 struct Plan {
-    int64_t k_steps, tiles_n, tiles, groups, ks_per_group, units, pitch;
+    int64_t k_steps, tiles_m, tiles_n, m_groups, n_groups, groups, ks_per_group, units, pitch;
+    int cn, cm;
     size_t at_bytes, partial_bytes, total;
 };
 
-Plan make_plan(int64_t M, int64_t N, int64_t K, int sms) {
+int resident_clusters(int cs);
+
+Plan make_plan(int64_t M, int64_t N, int64_t K) {
     Plan pl{};
     pl.k_steps = (K + BK - 1) / BK;
+    pl.tiles_m = (M + BM - 1) / BM;
     pl.tiles_n = (N + BN - 1) / BN;
-    pl.tiles = ((M + BM - 1) / BM) * pl.tiles_n;
+    pl.cn = pl.tiles_n >= 2 ? 2 : 1;
+    pl.cm = pl.tiles_m >= 2 ? 2 : 1;
+    pl.m_groups = (pl.tiles_m + pl.cm - 1) / pl.cm;
+    pl.n_groups = (pl.tiles_n + pl.cn - 1) / pl.cn;
+    const int slots = std::max(1, resident_clusters(pl.cn * pl.cm));
     pl.pitch = (K + 7) / 8 * 8;  // TMA: row pitch a multiple of 16 bytes
-    // K slices: fill whole waves of one CTA per SM, keep slices >= 16 k-steps, bound the
+    // K slices: fill whole waves of resident clusters, keep slices >= 32 k-steps, bound the
     // partial buffer at 1 GiB
+    const int64_t tiles = pl.m_groups * pl.n_groups;
     int64_t best_g = 1;
     double best = -1.0;
-    const int64_t gmax = std::max<int64_t>(1, std::min<int64_t>(pl.k_steps / 16, 64));
+    const int64_t gmax = std::max<int64_t>(1, std::min<int64_t>(pl.k_steps / 32, 64));
     for (int64_t g = 1; g <= gmax; ++g) {
         if ((double)g * M * N * 4 > (double)(1ll << 30)) break;
-        const int64_t units = pl.tiles * g;
-        const int64_t waves = (units + sms - 1) / sms;
-        const double eff = (double)units / (double)(waves * sms) - 0.001 * (double)g;
+        const int64_t units = tiles * g;
+        const int64_t waves = (units + slots - 1) / slots;
+        const double eff = (double)units / (double)(waves * slots) - 0.001 * (double)g;
         if (eff > best + 1e-12) {
             best = eff;
             best_g = g;
@@ -378,11 +561,89 @@ Plan make_plan(int64_t M, int64_t N, int64_t K, int sms) {
     }
     pl.ks_per_group = (pl.k_steps + best_g - 1) / best_g;
     pl.groups = (pl.k_steps + pl.ks_per_group - 1) / pl.ks_per_group;
-    pl.units = pl.tiles * pl.groups;
+    pl.units = tiles * pl.groups;
     pl.at_bytes = ((size_t)N * pl.pitch * 2 + 1023) / 1024 * 1024;
     pl.partial_bytes = (size_t)pl.groups * M * N * 4;
     pl.total = pl.at_bytes + pl.partial_bytes;
     return pl;
+}
+
+template <int CN, int CM, bool kFast>
+void set_smem_attr() {
+    static bool done = false;
+    if (!done) {
+        RBG_CUDA(cudaFuncSetAttribute(sketch_bf16_kernel<CN, CM, kFast>,
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
+        done = true;
+    }
+}
+
+template <int CN, int CM>
+int query_resident_clusters() {
+    set_smem_attr<CN, CM, true>();
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(CN * CM * 256);
+    cfg.blockDim = dim3(NUM_THREADS);
+    cfg.dynamicSmemBytes = SMEM_BYTES;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = CN * CM;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    int n = 0;
+    const cudaError_t e =
+        cudaOccupancyMaxActiveClusters(&n, sketch_bf16_kernel<CN, CM, true>, &cfg);
+    if (e != cudaSuccess || n <= 0) {
+        cudaGetLastError();
+        n = num_sms() / (CN * CM);
+    }
+    return n;
+}
+
+// Clusters of `cs` CTAs (one CTA per SM) that fit on the current device at once.
+int resident_clusters(int cs) {
+    static std::mutex mu;
+    static int cached[64][5] = {};
+    int dev = 0;
+    RBG_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 64) dev = 0;
+    std::lock_guard<std::mutex> g(mu);
+    int &c = cached[dev][cs];
+    if (!c) c = cs == 1 ? query_resident_clusters<1, 1>()
+                : cs == 2 ? query_resident_clusters<2, 1>()
+                          : query_resident_clusters<2, 2>();
+    return c;
+}
+
+template <int CN, int CM, bool kFast>
+void launch_sketch(int clusters, const CUtensorMap &map, const LowpParams &p, cudaStream_t s) {
+    set_smem_attr<CN, CM, kFast>();
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)(clusters * CN * CM));
+    cfg.blockDim = dim3(NUM_THREADS);
+    cfg.dynamicSmemBytes = SMEM_BYTES;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = CN * CM;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    RBG_CUDA(cudaLaunchKernelEx(&cfg, sketch_bf16_kernel<CN, CM, kFast>, map, p));
+    RBG_LAUNCHED();
+}
+
+template <bool kFast>
+void launch_for(const Plan &pl, const CUtensorMap &map, const LowpParams &p, cudaStream_t s) {
+    const int clusters =
+        (int)std::min<int64_t>(pl.units, resident_clusters(pl.cn * pl.cm));
+    if (pl.cn == 2 && pl.cm == 2) launch_sketch<2, 2, kFast>(clusters, map, p, s);
+    else if (pl.cn == 2) launch_sketch<2, 1, kFast>(clusters, map, p, s);
+    else if (pl.cm == 2) launch_sketch<1, 2, kFast>(clusters, map, p, s);
+    else launch_sketch<1, 1, kFast>(clusters, map, p, s);
 }
 
 using EncodeFn = CUresult (*)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *,
@@ -409,7 +670,7 @@ void lowp_bf16(int64_t M, int64_t N, int64_t K, float alpha, const DenseGen &gen
                int64_t c0, int r_on_i, const Strided &Q, float beta, float *out, int64_t os_i,
                int64_t os_j, void *workspace, size_t ws_bytes, cudaStream_t s) {
     const int sms = num_sms();
-    const Plan pl = make_plan(M, N, K, sms);
+    const Plan pl = make_plan(M, N, K);
     Scratch own;
     uint8_t *ws = static_cast<uint8_t *>(workspace);
     if (!ws) {
@@ -425,10 +686,8 @@ void lowp_bf16(int64_t M, int64_t N, int64_t K, float alpha, const DenseGen &gen
 
     {
         ProfScope prof("lowp_convert_a", s);
-        const int64_t tiles = ((K + 63) / 64) * ((N + 63) / 64);
-        const int grid = (int)std::min<int64_t>(tiles, (int64_t)sms * 16);
-        convert_a_kernel<<<grid, 256, 0, s>>>(static_cast<const float *>(Q.ptr), Q.s0, Q.s1, K, N,
-                                              At, pl.pitch);
+        convert_a_kernel<<<sms * 8, 256, 0, s>>>(static_cast<const float *>(Q.ptr), Q.s0, Q.s1,
+                                                 K, N, At, pl.pitch);
         RBG_LAUNCHED();
     }
 
@@ -439,7 +698,7 @@ void lowp_bf16(int64_t M, int64_t N, int64_t K, float alpha, const DenseGen &gen
     const cuuint32_t estr[2] = {1, 1};
     const CUresult cr = encode_fn()(&map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, At, dims, strides,
                                     box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
-                                    CU_TENSOR_MAP_SWIZZLE_128B,
+                                    CU_TENSOR_MAP_SWIZZLE_64B,
                                     CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
                                     CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (cr != CUDA_SUCCESS) fail(RBG_ERROR_CUDA, "cuTensorMapEncodeTiled failed");
@@ -449,28 +708,14 @@ void lowp_bf16(int64_t M, int64_t N, int64_t K, float alpha, const DenseGen &gen
     LowpParams p{};
     p.M = M; p.N = N; p.K = K;
     p.gen = gen; p.r0 = r0; p.c0 = c0; p.r_on_i = r_on_i;
-    p.k_steps = pl.k_steps; p.tiles_n = pl.tiles_n; p.tiles = pl.tiles;
+    p.k_steps = pl.k_steps; p.m_groups = pl.m_groups; p.n_groups = pl.n_groups;
     p.ks_per_group = pl.ks_per_group; p.units = pl.units;
     p.partial = partial; p.err = err;
-    const bool aligned = (c0 % 4) == 0;
-    static bool attr[2] = {false, false};
-    if (!attr[aligned]) {
-        if (aligned)
-            RBG_CUDA(cudaFuncSetAttribute(sketch_bf16_kernel<true>,
-                                          cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
-        else
-            RBG_CUDA(cudaFuncSetAttribute(sketch_bf16_kernel<false>,
-                                          cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
-        attr[aligned] = true;
-    }
-    const int grid = (int)std::min<int64_t>(pl.units, sms);
+    const bool fast = r_on_i && (c0 % 4) == 0;
     {
         ProfScope prof("lowp_sketch_bf16_tc", s);
-        if (aligned)
-            sketch_bf16_kernel<true><<<grid, NUM_THREADS, SMEM_BYTES, s>>>(map, p);
-        else
-            sketch_bf16_kernel<false><<<grid, NUM_THREADS, SMEM_BYTES, s>>>(map, p);
-        RBG_LAUNCHED();
+        if (fast) launch_for<true>(pl, map, p, s);
+        else launch_for<false>(pl, map, p, s);
     }
     {
         ProfScope prof("lowp_reduce", s);
@@ -511,13 +756,7 @@ extern "C" int rbg_lskge3_lowp_workspace(int32_t precision, int64_t d, int64_t n
         if (precision != RBG_PREC_BF16)
             fail(RBG_ERROR_UNSUPPORTED, "only RBG_PREC_BF16 is provided");
         RBG_REQUIRE("lskge3_lowp", d > 0 && n > 0 && m > 0);
-        int sms = 148;
-        int dev = 0;
-        if (cudaGetDevice(&dev) == cudaSuccess)
-            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        else
-            cudaGetLastError();
-        *bytes = make_plan(d, n, m, sms).total;
+        *bytes = make_plan(d, n, m).total;
     });
 }
 

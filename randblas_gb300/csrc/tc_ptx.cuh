@@ -6,6 +6,8 @@
 #include <cuda.h>
 #include <cstdint>
 
+#include "randblas_gb300.h"
+
 namespace rbg {
 namespace tc {
 
@@ -45,14 +47,34 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
     return ok != 0;
 }
 
+// try_wait with acquire at cluster scope (the phase may have been completed by arrivals
+// from another CTA of the cluster).
+__device__ __forceinline__ bool mbar_try_wait_cluster(uint64_t *bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.acquire.cluster.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_addr(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
 // Wait for the phase with the given parity to complete, for at most ~`budget` clock cycles.
 // Returns false (after setting *err) on timeout or if another role already raised *err.
+// `backoff` > 0 sleeps that many nanoseconds between polls once the wait is long, so
+// waiting warps leave issue slots to the working ones.
+template <bool kCluster = false>
 __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, int *err,
+                                          unsigned backoff = 0,
                                           long long budget = 8000000000ll) {
     const long long t0 = clock64();
     uint32_t spins = 0;
-    while (!mbar_try_wait(bar, parity)) {
-        if ((++spins & 255u) == 0) {
+    while (!(kCluster ? mbar_try_wait_cluster(bar, parity) : mbar_try_wait(bar, parity))) {
+        ++spins;
+        if (backoff && spins > 8) __nanosleep(backoff);
+        if ((spins & 63u) == 0) {
             if (*(volatile int *)err) return false;
             if (clock64() - t0 > budget) {
                 atomicCAS(err, 0, RBG_ERROR_TIMEOUT);
@@ -61,6 +83,47 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, int *e
         }
     }
     return true;
+}
+
+// ------------------------------------------------------------------ clusters
+__device__ __forceinline__ uint32_t cluster_ctarank() {
+    uint32_t r;
+    asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+    return r;
+}
+
+__device__ __forceinline__ void cluster_sync() {
+    asm volatile("barrier.cluster.arrive.release.aligned;\n\t"
+                 "barrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+
+// Address of the same shared-memory location in CTA `rank` of the cluster.
+__device__ __forceinline__ uint32_t map_to_rank(uint32_t local, uint32_t rank) {
+    uint32_t r;
+    asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(local), "r"(rank));
+    return r;
+}
+
+__device__ __forceinline__ void st_cluster_v4(uint32_t addr, uint4 v) {
+    asm volatile("st.shared::cluster.v4.u32 [%0], {%1, %2, %3, %4};" ::"r"(addr), "r"(v.x),
+                 "r"(v.y), "r"(v.z), "r"(v.w)
+                 : "memory");
+}
+
+__device__ __forceinline__ void st_cluster_u16(uint32_t addr, uint16_t v) {
+    asm volatile("st.shared::cluster.u16 [%0], %1;" ::"r"(addr), "h"(v) : "memory");
+}
+
+// Arrive on an mbarrier of another CTA of the cluster (release at cluster scope).
+__device__ __forceinline__ void mbar_arrive_remote(uint32_t remote_bar) {
+    asm volatile("mbarrier.arrive.release.cluster.shared::cluster.b64 _, [%0];" ::"r"(remote_bar)
+                 : "memory");
+}
+
+// Make generic-proxy writes to this CTA's and peer CTAs' shared memory visible to the async
+// proxy.
+__device__ __forceinline__ void fence_proxy_async_cluster() {
+    asm volatile("fence.proxy.async.shared::cluster;" ::: "memory");
 }
 
 // ------------------------------------------------------------------ proxies / fences
@@ -78,6 +141,35 @@ __device__ __forceinline__ void tma_load_2d(void *dst, const CUtensorMap *map, u
         " [%0], [%1, {%3, %4}], [%2];" ::"r"(smem_addr(dst)),
         "l"(reinterpret_cast<uint64_t>(map)), "r"(smem_addr(bar)), "r"(x), "r"(y)
         : "memory");
+}
+
+// Tile load delivered to the same shared-memory offset of every CTA in `cta_mask`, each CTA's
+// mbarrier at `bar`'s offset receiving the byte count.
+__device__ __forceinline__ void tma_load_2d_multicast(void *dst, const CUtensorMap *map,
+                                                      uint64_t *bar, int x, int y,
+                                                      uint16_t cta_mask) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes"
+        ".multicast::cluster [%0], [%1, {%3, %4}], [%2], %5;" ::"r"(smem_addr(dst)),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(smem_addr(bar)), "r"(x), "r"(y),
+        "h"(cta_mask)
+        : "memory");
+}
+
+// Copy `bytes` (multiple of 16) of this CTA's shared memory to another CTA of the cluster;
+// the destination CTA's mbarrier `remote_bar` receives the byte count on completion.
+__device__ __forceinline__ void bulk_copy_to_peer(uint32_t remote_dst, const void *src,
+                                                  uint32_t bytes, uint32_t remote_bar) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.shared::cta.mbarrier::complete_tx::bytes"
+        " [%0], [%1], %2, [%3];" ::"r"(remote_dst),
+        "r"(smem_addr(src)), "r"(bytes), "r"(remote_bar)
+        : "memory");
+}
+
+// Named barrier over `count` threads (ids 1..15; 0 is __syncthreads).
+__device__ __forceinline__ void named_barrier(uint32_t id, uint32_t count) {
+    asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(count) : "memory");
 }
 
 __device__ __forceinline__ void prefetch_tensormap(const CUtensorMap *map) {
@@ -138,6 +230,15 @@ __device__ __forceinline__ void mma_commit(uint64_t *bar) {
         : "memory");
 }
 
+// Commit to the mbarrier at the same shared-memory offset in every CTA of `cta_mask`.
+__device__ __forceinline__ void mma_commit_multicast(uint64_t *bar, uint16_t cta_mask) {
+    asm volatile(
+        "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.multicast::cluster.b64"
+        " [%0], %1;" ::"r"(smem_addr(bar)),
+        "h"(cta_mask)
+        : "memory");
+}
+
 // 32 consecutive 32-bit columns of the calling lane's tensor-memory row.
 __device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
     asm volatile(
@@ -158,20 +259,24 @@ __device__ __forceinline__ void tmem_ld_wait() {
     asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 }
 
-// Shared-memory matrix descriptor for a K-major operand tile stored with the 128-byte
-// swizzle: rows of 128 bytes, groups of 8 rows 1024 bytes apart (stride byte offset), tile
-// base 1024-byte aligned.  Bit layout of the tcgen05 descriptor: start address >> 4 in
-// [0,14), leading byte offset >> 4 in [16,30) (unused for this layout), stride byte offset
-// >> 4 in [32,46), fixed version 1 in [46,48), base offset 0 in [49,52), swizzle mode 2
-// (128B) in [61,64).
-__device__ __forceinline__ uint64_t sw128_kmajor_desc(uint32_t saddr) {
+// Shared-memory matrix descriptor for a K-major operand tile stored with a swizzle of
+// `row_bytes` (128 or 64) bytes per row: groups of 8 rows are 8 * row_bytes apart (stride
+// byte offset); tile base aligned to that group size.  Bit layout of the tcgen05 descriptor:
+// start address >> 4 in [0,14), leading byte offset >> 4 in [16,30) (unused for these
+// layouts), stride byte offset >> 4 in [32,46), fixed version 1 in [46,48), base offset 0 in
+// [49,52), swizzle mode in [61,64): 2 = 128-byte, 4 = 64-byte.
+__device__ __forceinline__ uint64_t kmajor_desc(uint32_t saddr, uint32_t row_bytes) {
     uint64_t d = 0;
     d |= (uint64_t)((saddr & 0x3FFFFu) >> 4);
     d |= (uint64_t)1 << 16;
-    d |= (uint64_t)(1024u >> 4) << 32;
+    d |= (uint64_t)((8u * row_bytes) >> 4) << 32;
     d |= (uint64_t)1 << 46;
-    d |= (uint64_t)2 << 61;
+    d |= (uint64_t)(row_bytes == 128 ? 2 : 4) << 61;
     return d;
+}
+
+__device__ __forceinline__ uint64_t sw128_kmajor_desc(uint32_t saddr) {
+    return kmajor_desc(saddr, 128);
 }
 
 // Instruction descriptor for kind::f16 with FP32 accumulation, A and B in BF16, both
