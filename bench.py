@@ -41,7 +41,7 @@ def peaks():
 
 
 class ClockSampler:
-    """nvidia-smi clocks / throttle reasons sampled every 200 ms while running."""
+    """nvidia-smi clocks / throttle reasons sampled every 50 ms while running."""
 
     def __init__(self, index: int):
         self.index = index
@@ -55,7 +55,7 @@ class ClockSampler:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", f"--id={self.index}", f"--query-gpu={q}",
-                 "--format=csv,noheader,nounits", "-lms", "200"],
+                 "--format=csv,noheader,nounits", "-lms", "50"],
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.thread = threading.Thread(target=self._read, daemon=True)
             self.thread.start()
@@ -155,6 +155,8 @@ def main():
                     help="operator rows of the bounded CPU-baseline sample")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--m-log2", type=int, default=17,
+                    help="log2 of m for the dense small cases")
     ap.add_argument("--case", default="full",
                     choices=["full", "lowp-small", "plain-small", "saso", "convert-small"],
                     help="full: the benchmark line; the others run one kernel family on a "
@@ -356,9 +358,9 @@ def bench_e2e(torch, rb, lowp, have_lowp, S, A_host, args, stream, flops, device
 
 
 def run_case(args):
-    """One kernel family on a smaller case: 4096 x 2^17 uniform operator against a
-    2^17 x 1024 FP32 matrix (512 MiB, larger than L2) for the dense paths; the full SASO
-    workload for the sparse path."""
+    """One kernel family on a smaller case: 4096 x 2^m_log2 uniform operator against a
+    2^m_log2 x 1024 FP32 matrix (default 2^17: 512 MiB, larger than L2) for the dense paths;
+    the full SASO workload for the sparse path."""
     import torch
 
     import randblas_gb300 as rb
@@ -372,7 +374,7 @@ def run_case(args):
     if args.case == "saso":
         out.update(bench_saso(torch, rb, dev, args, stream, peaks()[0]))
     else:
-        m = 1 << 17
+        m = 1 << args.m_log2
         S = rb.DenseSkOp(rb.DenseDist(D_SK, m, rb.ScalarDist.Uniform), rb.RNGState(3))
         A = torch.randn(m, N_SK, device=dev)
         B = torch.empty(D_SK, N_SK, device=dev)

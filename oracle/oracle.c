@@ -36,8 +36,9 @@
  *                              of (index, value) pairs per vector is comparable)
  *   sparse compute_next_state  RandBLAS/sparse_skops.hh:266-283
  *
- * Build: gcc -O2 -std=c11 -fPIC -shared -ffp-contract=off -fopenmp (oracle/build.py).
+ * Build: gcc -O2 -std=gnu11 -fPIC -shared -ffp-contract=off -fopenmp (oracle/build.py).
  */
+#define _GNU_SOURCE 1 /* sincosf */
 #include <math.h>
 #include <stdint.h>
 #include <stdlib.h>

@@ -39,12 +39,12 @@ constexpr int CHUNKS = ROW_BYTES / 16;      // 16-byte chunks per row
 constexpr int STAGES = 5;
 constexpr int S_STAGE_BYTES = BM * BK * 2;  // 8 KiB
 constexpr int A_STAGE_BYTES = BN * BK * 2;  // 32 KiB
-constexpr int NUM_THREADS = 512;
+constexpr int NUM_THREADS = 640;
 constexpr int EPI_WARP0 = 4;
 constexpr int GEN_WARP0 = 8;
-constexpr int GEN_WARPS = 8;
+constexpr int GEN_WARPS = 12;
 constexpr int GEN_THREADS = GEN_WARPS * 32;
-constexpr int GEN_GROUPS = 2;                        // groups take alternate stages
+constexpr int GEN_GROUPS = 3;                        // groups take stages in turn
 constexpr int GROUP_THREADS = GEN_THREADS / GEN_GROUPS;
 constexpr uint32_t TMEM_COLS = 512;
 constexpr int SMEM_BYTES = STAGES * (S_STAGE_BYTES + A_STAGE_BYTES) + 1024 /*align*/ + 256;
@@ -59,6 +59,7 @@ struct LowpParams {
     int64_t n_groups;      // column groups, each CN tiles of BN columns
     int64_t ks_per_group;  // k-steps per K slice
     int64_t units;         // m_groups * n_groups * k_groups
+    int64_t npad;          // rows per k-block of the converted A (multiple of BN)
     float *partial;        // [k_groups][M][N]
     int *err;
 };
@@ -194,10 +195,11 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
     uint8_t *s_tiles = smem;                                 // STAGES x S_STAGE_BYTES
     uint8_t *a_tiles = smem + STAGES * S_STAGE_BYTES;        // STAGES x A_STAGE_BYTES
     uint64_t *bars = reinterpret_cast<uint64_t *>(a_tiles + STAGES * A_STAGE_BYTES);
-    uint64_t *full_a = bars;
-    uint64_t *full_s = bars + STAGES;
-    uint64_t *empty = bars + 2 * STAGES;
-    uint64_t *acc_full = bars + 3 * STAGES;
+    // full[s]: two arrivals (TMA thread, producing generator group) plus the bytes of the A
+    // tile and, with CN = 2, of the peer's S rows; empty[s]: one MMA commit per cluster CTA
+    uint64_t *full = bars;
+    uint64_t *empty = bars + STAGES;
+    uint64_t *acc_full = bars + 2 * STAGES;
     uint64_t *acc_empty = acc_full + 1;
     uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(acc_empty + 1);
 
@@ -208,8 +210,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
     const int64_t num_clusters = gridDim.x / CS;
     if (threadIdx.x == 0) {
         for (int s = 0; s < STAGES; ++s) {
-            tc::mbar_init(&full_a[s], 1);
-            tc::mbar_init(&full_s[s], 1);
+            tc::mbar_init(&full[s], 2);
             tc::mbar_init(&empty[s], CS);
         }
         tc::mbar_init(acc_full, 1);
@@ -248,19 +249,20 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
                 for (int64_t ks = ks0; ks < ks1; ++ks, ++it) {
                     const int s = (int)(it % STAGES);
                     const uint32_t ph = (uint32_t)((it / STAGES) & 1);
-                    if (!tc::mbar_wait<(CS > 1)>(&empty[s], ph ^ 1, p.err)) goto done;
-                    tc::mbar_arrive_expect_tx(&full_a[s], A_STAGE_BYTES);
+                    if (!tc::mbar_wait(&empty[s], ph ^ 1, p.err)) goto done;
+                    tc::mbar_arrive_expect_tx(&full[s], A_STAGE_BYTES);
                     uint8_t *dst = a_tiles + s * A_STAGE_BYTES;
+                    const int64_t row0 = ks * p.npad + n0;  // k-blocked layout
                     if (CM == 2) {
                         // this CTA loads half h = m_idx of the tile for itself and its M-peer
                         const uint16_t mask = (uint16_t)((1u << rank) | (1u << (rank ^ CN)));
                         tc::tma_load_2d_multicast(dst + m_idx * (A_STAGE_BYTES / 2), &tmap_a,
-                                                  &full_a[s], (int)(ks * BK),
-                                                  (int)(n0 + m_idx * (BN / 2)), mask);
+                                                  &full[s], 0,
+                                                  (int)(row0 + m_idx * (BN / 2)), mask);
                     } else {
-                        tc::tma_load_2d(dst, &tmap_a, &full_a[s], (int)(ks * BK), (int)n0);
-                        tc::tma_load_2d(dst + A_STAGE_BYTES / 2, &tmap_a, &full_a[s],
-                                        (int)(ks * BK), (int)(n0 + BN / 2));
+                        tc::tma_load_2d(dst, &tmap_a, &full[s], 0, (int)row0);
+                        tc::tma_load_2d(dst + A_STAGE_BYTES / 2, &tmap_a, &full[s], 0,
+                                        (int)(row0 + BN / 2));
                     }
                 }
             }
@@ -278,8 +280,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
                 for (int64_t ks = ks0; ks < ks1; ++ks, ++it) {
                     const int s = (int)(it % STAGES);
                     const uint32_t ph = (uint32_t)((it / STAGES) & 1);
-                    if (!tc::mbar_wait<(CM > 1)>(&full_a[s], ph, p.err)) goto done;
-                    if (!tc::mbar_wait<(CN > 1)>(&full_s[s], ph, p.err)) goto done;
+                    if (!tc::mbar_wait(&full[s], ph, p.err)) goto done;
                     tc::tc_fence_after();
                     const uint64_t adesc =
                         tc::kmajor_desc(tc::smem_addr(s_tiles + s * S_STAGE_BYTES), ROW_BYTES);
@@ -308,7 +309,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
             const int64_t last = it;
             for (int64_t j = 0; j < STAGES && j < last; ++j) {
                 const int64_t idx = last - 1 - j;
-                if (!tc::mbar_wait<(CS > 1)>(&empty[idx % STAGES],
+                if (!tc::mbar_wait(&empty[idx % STAGES],
                                              (uint32_t)((idx / STAGES) & 1), p.err))
                     goto done;
             }
@@ -350,15 +351,16 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
             if (lane == 0) tc::mbar_arrive(acc_empty);
         }
     } else if (warp >= GEN_WARP0) {
-        // ---------------- S producers: GEN_GROUPS groups, group gi takes stages it % G == gi
+        // ---------------- S producers: GEN_GROUPS groups, group gi takes the stages with
+        // it % GEN_GROUPS == gi
         const int gi = (warp - GEN_WARP0) / (GEN_WARPS / GEN_GROUPS);
         const int tg = threadIdx.x - GEN_WARP0 * 32 - gi * GROUP_THREADS;
         const int row_lo = (int)n_idx * ROWS;
-        uint32_t peer_full_s[STAGES] = {};
+        uint32_t peer_full[STAGES] = {};
         uint32_t peer_tiles = 0;
         if (CN > 1) {
             for (int s = 0; s < STAGES; ++s)
-                peer_full_s[s] = tc::map_to_rank(tc::smem_addr(&full_s[s]), rank ^ 1u);
+                peer_full[s] = tc::map_to_rank(tc::smem_addr(&full[s]), rank ^ 1u);
             peer_tiles = tc::map_to_rank(tc::smem_addr(s_tiles), rank ^ 1u);
         }
         const int fc = tg % CHUNKS;
@@ -381,7 +383,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
                 if ((int)(it % GEN_GROUPS) != gi) continue;
                 const int s = (int)(it % STAGES);
                 const uint32_t ph = (uint32_t)((it / STAGES) & 1);
-                if (!tc::mbar_wait<(CS > 1)>(&empty[s], ph ^ 1, p.err)) goto done;
+                if (!tc::mbar_wait(&empty[s], ph ^ 1, p.err)) goto done;
                 uint8_t *tile = s_tiles + s * S_STAGE_BYTES;
                 const int64_t gk = ks * BK + 8 * fc;
                 if (kFast && gk + 8 <= p.K) {
@@ -401,12 +403,12 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
                 if (tg == 0) {
                     if (CN > 1) {
                         // the peer's share of this stage arrives by bulk copy
-                        tc::mbar_arrive_expect_tx(&full_s[s], PART_BYTES);
+                        tc::mbar_arrive_expect_tx(&full[s], PART_BYTES);
                         const uint32_t off = (uint32_t)(s * S_STAGE_BYTES + row_lo * ROW_BYTES);
                         tc::bulk_copy_to_peer(peer_tiles + off, s_tiles + off, PART_BYTES,
-                                              peer_full_s[s]);
+                                              peer_full[s]);
                     } else {
-                        tc::mbar_arrive(&full_s[s]);
+                        tc::mbar_arrive(&full[s]);
                     }
                 }
             }
@@ -424,41 +426,44 @@ done:
     }
 }
 
-// op(A)(k, j) -> At[j * pitch + k] in BF16.  When j has unit stride the kernel transposes a
-// 64 (k) x 128 (j) tile through shared memory (float4 reads along j, 16-byte writes along k);
-// when k has unit stride it converts in place order (float4 reads, 8-byte writes).
+// op(A)(k, j) -> At in BF16, k-blocked: element (k, j) at ((k / BK) * npad + j) * BK + k % BK,
+// so the TMA box of a stage (BK consecutive k of 256 consecutive j) is one contiguous block.
+// Rows j in [N, npad) and k in [K, kpad) are written as zeros.  When j has unit stride the
+// kernel transposes a 64 (k) x 128 (j) tile through shared memory (float4 reads along j,
+// 16-byte writes along k); when k has unit stride it converts in order.
+__device__ __forceinline__ int64_t blocked_index(int64_t k, int64_t j, int64_t npad) {
+    return ((k / BK) * npad + j) * BK + (k % BK);
+}
+
 __global__ void __launch_bounds__(256) convert_a_kernel(const float *__restrict__ A, int64_t sk,
                                                         int64_t sj, int64_t K, int64_t N,
-                                                        __nv_bfloat16 *__restrict__ At,
-                                                        int64_t pitch) {
+                                                        int64_t kpad, int64_t npad,
+                                                        __nv_bfloat16 *__restrict__ At) {
     __shared__ float tile[64][129];
     if (sk == 1 && sj != 1) {
-        // direct: At[j][k] = A[j * sj + k]
-        const int64_t kq = (K + 3) / 4;
-        for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < kq * N;
+        // direct: 4 consecutive k of one row j per thread
+        const int64_t kq = kpad / 4;
+        for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < kq * npad;
              t += (int64_t)gridDim.x * blockDim.x) {
             const int64_t j = t / kq, k = (t % kq) * 4;
-            const float *src = A + j * sj + k;
-            float v[4];
-            if (k + 4 <= K && ((reinterpret_cast<uintptr_t>(src) & 15) == 0)) {
-                const float4 f = *reinterpret_cast<const float4 *>(src);
-                v[0] = f.x; v[1] = f.y; v[2] = f.z; v[3] = f.w;
-            } else {
-                for (int e = 0; e < 4; ++e) v[e] = k + e < K ? src[e] : 0.f;
+            float v[4] = {0.f, 0.f, 0.f, 0.f};
+            if (j < N) {
+                const float *src = A + j * sj + k;
+                if (k + 4 <= K && ((reinterpret_cast<uintptr_t>(src) & 15) == 0)) {
+                    const float4 f = *reinterpret_cast<const float4 *>(src);
+                    v[0] = f.x; v[1] = f.y; v[2] = f.z; v[3] = f.w;
+                } else {
+                    for (int e = 0; e < 4; ++e) v[e] = k + e < K ? src[e] : 0.f;
+                }
             }
-            __nv_bfloat16 *dst = At + j * pitch + k;
-            if (k + 4 <= K) {
-                uint2 w;
-                w.x = pack_bf16(v[0], v[1]);
-                w.y = pack_bf16(v[2], v[3]);
-                *reinterpret_cast<uint2 *>(dst) = w;
-            } else {
-                for (int e = 0; e < 4 && k + e < K; ++e) dst[e] = __float2bfloat16_rn(v[e]);
-            }
+            uint2 w;
+            w.x = pack_bf16(v[0], v[1]);
+            w.y = pack_bf16(v[2], v[3]);
+            *reinterpret_cast<uint2 *>(At + blocked_index(k, j, npad)) = w;
         }
         return;
     }
-    const int64_t tk = (K + 63) / 64, tj = (N + 127) / 128;
+    const int64_t tk = (kpad + 63) / 64, tj = (npad + 127) / 128;
     const bool vec = sj == 1 && (N % 4) == 0 && (sk % 4) == 0 &&
                      (reinterpret_cast<uintptr_t>(A) & 15) == 0;
     for (int64_t t = blockIdx.x; t < tk * tj; t += gridDim.x) {
@@ -483,23 +488,17 @@ __global__ void __launch_bounds__(256) convert_a_kernel(const float *__restrict_
             }
         }
         __syncthreads();
-        // 128 rows j x 8 chunks of 8 k: one 16-byte store each
+        // 128 rows j x 8 chunks of 8 k: one 16-byte store each (zeros outside K x N)
         for (int w = threadIdx.x; w < 128 * 8; w += 256) {
             const int jj = w / 8, c = w % 8;
-            if (j0 + jj >= N) continue;
             const int64_t k = k0 + 8 * c;
-            if (k >= K) continue;
-            __nv_bfloat16 *dst = At + (j0 + jj) * pitch + k;
-            if (k + 8 <= K) {
-                uint4 q;
-                q.x = pack_bf16(tile[8 * c][jj], tile[8 * c + 1][jj]);
-                q.y = pack_bf16(tile[8 * c + 2][jj], tile[8 * c + 3][jj]);
-                q.z = pack_bf16(tile[8 * c + 4][jj], tile[8 * c + 5][jj]);
-                q.w = pack_bf16(tile[8 * c + 6][jj], tile[8 * c + 7][jj]);
-                *reinterpret_cast<uint4 *>(dst) = q;
-            } else {
-                for (int e = 0; k + e < K; ++e) dst[e] = __float2bfloat16_rn(tile[8 * c + e][jj]);
-            }
+            if (j0 + jj >= npad || k >= kpad) continue;
+            uint4 q;
+            q.x = pack_bf16(tile[8 * c][jj], tile[8 * c + 1][jj]);
+            q.y = pack_bf16(tile[8 * c + 2][jj], tile[8 * c + 3][jj]);
+            q.z = pack_bf16(tile[8 * c + 4][jj], tile[8 * c + 5][jj]);
+            q.w = pack_bf16(tile[8 * c + 6][jj], tile[8 * c + 7][jj]);
+            *reinterpret_cast<uint4 *>(At + blocked_index(k, j0 + jj, npad)) = q;
         }
         __syncthreads();
     }
@@ -525,7 +524,8 @@ __global__ void lowp_reduce_kernel(int64_t M, int64_t N, int64_t groups, const f
 __device__ int g_lowp_error = 0;
 
 struct Plan {
-    int64_t k_steps, tiles_m, tiles_n, m_groups, n_groups, groups, ks_per_group, units, pitch;
+    int64_t k_steps, tiles_m, tiles_n, m_groups, n_groups, groups, ks_per_group, units, kpad,
+        npad;
     int cn, cm;
     size_t at_bytes, partial_bytes, total;
 };
@@ -542,7 +542,8 @@ Plan make_plan(int64_t M, int64_t N, int64_t K) {
     pl.m_groups = (pl.tiles_m + pl.cm - 1) / pl.cm;
     pl.n_groups = (pl.tiles_n + pl.cn - 1) / pl.cn;
     const int slots = std::max(1, resident_clusters(pl.cn * pl.cm));
-    pl.pitch = (K + 7) / 8 * 8;  // TMA: row pitch a multiple of 16 bytes
+    pl.kpad = pl.k_steps * BK;
+    pl.npad = pl.tiles_n * BN;
     // K slices: fill whole waves of resident clusters, keep slices >= 32 k-steps, bound the
     // partial buffer at 1 GiB
     const int64_t tiles = pl.m_groups * pl.n_groups;
@@ -562,7 +563,7 @@ Plan make_plan(int64_t M, int64_t N, int64_t K) {
     pl.ks_per_group = (pl.k_steps + best_g - 1) / best_g;
     pl.groups = (pl.k_steps + pl.ks_per_group - 1) / pl.ks_per_group;
     pl.units = tiles * pl.groups;
-    pl.at_bytes = ((size_t)N * pl.pitch * 2 + 1023) / 1024 * 1024;
+    pl.at_bytes = ((size_t)pl.npad * pl.kpad * 2 + 1023) / 1024 * 1024;
     pl.partial_bytes = (size_t)pl.groups * M * N * 4;
     pl.total = pl.at_bytes + pl.partial_bytes;
     return pl;
@@ -687,13 +688,14 @@ void lowp_bf16(int64_t M, int64_t N, int64_t K, float alpha, const DenseGen &gen
     {
         ProfScope prof("lowp_convert_a", s);
         convert_a_kernel<<<sms * 8, 256, 0, s>>>(static_cast<const float *>(Q.ptr), Q.s0, Q.s1,
-                                                 K, N, At, pl.pitch);
+                                                 K, N, pl.kpad, pl.npad, At);
         RBG_LAUNCHED();
     }
 
     CUtensorMap map;
-    const cuuint64_t dims[2] = {(cuuint64_t)K, (cuuint64_t)N};
-    const cuuint64_t strides[1] = {(cuuint64_t)pl.pitch * 2};
+    // rows of BK elements: row r = (k / BK) * npad + j
+    const cuuint64_t dims[2] = {(cuuint64_t)BK, (cuuint64_t)pl.npad * pl.k_steps};
+    const cuuint64_t strides[1] = {(cuuint64_t)BK * 2};
     const cuuint32_t box[2] = {(cuuint32_t)BK, (cuuint32_t)(BN / 2)};
     const cuuint32_t estr[2] = {1, 1};
     const CUresult cr = encode_fn()(&map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, At, dims, strides,
@@ -709,7 +711,7 @@ void lowp_bf16(int64_t M, int64_t N, int64_t K, float alpha, const DenseGen &gen
     p.M = M; p.N = N; p.K = K;
     p.gen = gen; p.r0 = r0; p.c0 = c0; p.r_on_i = r_on_i;
     p.k_steps = pl.k_steps; p.m_groups = pl.m_groups; p.n_groups = pl.n_groups;
-    p.ks_per_group = pl.ks_per_group; p.units = pl.units;
+    p.ks_per_group = pl.ks_per_group; p.units = pl.units; p.npad = pl.npad;
     p.partial = partial; p.err = err;
     const bool fast = r_on_i && (c0 % 4) == 0;
     {
@@ -812,8 +814,8 @@ extern "C" int rbg_lskge3_lowp(int32_t precision, int32_t layout, int32_t opS, i
             return;
         }
         if (!A) fail(RBG_ERROR_INVALID_ARGUMENT, "A must not be NULL");
-        if (m > (int64_t)INT32_MAX - 64 || n > (int64_t)INT32_MAX - BN)
-            fail(RBG_ERROR_UNSUPPORTED, "dimension too large for 32-bit TMA coordinates");
+        if ((double)((m + BK - 1) / BK) * (double)((n + BN - 1) / BN * BN) > (double)INT32_MAX)
+            fail(RBG_ERROR_UNSUPPORTED, "dimensions too large for 32-bit TMA coordinates");
         const int64_t ars = layout == RBG_COL_MAJOR ? 1 : lda;
         const int64_t acs = layout == RBG_COL_MAJOR ? lda : 1;
         const Strided Q = opA == RBG_NO_TRANS ? Strided{A, ars, acs} : Strided{A, acs, ars};

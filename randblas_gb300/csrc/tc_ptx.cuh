@@ -69,6 +69,7 @@ template <bool kCluster = false>
 __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, int *err,
                                           unsigned backoff = 0,
                                           long long budget = 8000000000ll) {
+    if (kCluster ? mbar_try_wait_cluster(bar, parity) : mbar_try_wait(bar, parity)) return true;
     const long long t0 = clock64();
     uint32_t spins = 0;
     while (!(kCluster ? mbar_try_wait_cluster(bar, parity) : mbar_try_wait(bar, parity))) {
