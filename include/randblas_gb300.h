@@ -40,6 +40,8 @@ enum { RBG_NO_TRANS = 0, RBG_TRANS = 1 };
 enum { RBG_GAUSSIAN = 0, RBG_UNIFORM = 1 };
 enum { RBG_AXIS_SHORT = 0, RBG_AXIS_LONG = 1 };
 enum { RBG_F32 = 0, RBG_F64 = 1 };
+/* Storage type of A accepted by rbg_lskge3_lowp_ex (precision path only). */
+enum { RBG_BF16 = 2 };
 enum { RBG_I32 = 0, RBG_I64 = 1 };
 enum { RBG_COO = 0, RBG_CSR = 1, RBG_CSC = 2 };
 enum { RBG_PREC_BF16 = 0, RBG_PREC_FP8_E4M3 = 1 };
@@ -294,6 +296,14 @@ int rbg_lskge3_lowp(int32_t precision, int32_t layout, int32_t opS, int32_t opA,
                     int64_t co_s, const float *A, int64_t lda, float beta, float *B,
                     int64_t ldb, void *workspace, size_t workspace_bytes, rbg_stream_t stream);
 
+/* rbg_lskge3_lowp with A stored as `a_dtype` (RBG_F32 or RBG_BF16); no reference
+ * counterpart.  BF16 data enters the tensor cores unchanged. */
+int rbg_lskge3_lowp_ex(int32_t precision, int32_t a_dtype, int32_t layout, int32_t opS,
+                       int32_t opA, int64_t d, int64_t n, int64_t m, float alpha,
+                       const rbg_dense_skop *S, int64_t ro_s, int64_t co_s, const void *A,
+                       int64_t lda, float beta, float *B, int64_t ldb, void *workspace,
+                       size_t workspace_bytes, rbg_stream_t stream);
+
 /* Device-side status of the precision path (no reference counterpart): RBG_SUCCESS, or
  * RBG_ERROR_TIMEOUT if a bounded wait inside a tensor-core kernel gave up since the last call
  * of this function.  Synchronises the device and clears the status. */
@@ -313,15 +323,34 @@ typedef struct rbg_batch_problem {
     float *B;
     int64_t ldb;
     float alpha, beta;
+    int32_t tile_config; /* 0: library's choice; else 1..rbg_batched_tile_configs() */
+    int32_t reserved;
 } rbg_batch_problem;
 
 /* Sketch `count` independent problems (host array `problems`) in one persistent launch,
- * all in `layout`, T = float.  tile_config: 0 = let the library choose; otherwise one of
- * the configurations listed by rbg_batched_tile_configs. */
+ * all in `layout`, T = float, stream-ordered (device memory for the work list comes from
+ * cudaMallocAsync on `stream`).  tile_config: 0 = each problem's own tile_config; otherwise
+ * one configuration for every problem.  Results do not depend on scheduling: K splits are
+ * summed in split order. */
 int rbg_lskge3_batched(int32_t layout, const rbg_batch_problem *problems, int64_t count,
                        int32_t tile_config, rbg_stream_t stream);
-/* Number of tile configurations the batched kernel offers (1-based ids). */
+/* Number of tile configurations the batched kernel offers (ids 1..count). */
 int rbg_batched_tile_configs(int32_t *count);
+/* Output tile width (columns) of configuration `config`; every configuration is 128 rows. */
+int rbg_batched_tile_width(int32_t config, int32_t *width);
+
+/* A reusable batch: validates the problems and uploads the work list once (synchronous);
+ * rbg_batched_plan_execute then only zeroes the plan's counters and launches the persistent
+ * kernel on `stream`, so it can be captured into a CUDA graph and replayed.  The problems'
+ * A and B pointers are baked into the plan. */
+typedef struct rbg_batched_plan_s *rbg_batched_plan;
+int rbg_batched_plan_create(int32_t layout, const rbg_batch_problem *problems, int64_t count,
+                            int32_t tile_config, rbg_batched_plan *plan);
+int rbg_batched_plan_execute(rbg_batched_plan plan, rbg_stream_t stream);
+/* Work items and device bytes of a plan (either pointer may be NULL). */
+int rbg_batched_plan_info(rbg_batched_plan plan, int64_t *work_items, int64_t *device_bytes);
+/* Frees the plan (synchronous; no launch of it may be pending). */
+int rbg_batched_plan_destroy(rbg_batched_plan plan);
 
 #ifdef __cplusplus
 }

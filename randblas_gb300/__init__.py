@@ -5,7 +5,7 @@ The compute lives in ``librandblas_gb300.so`` (hand-written CUDA behind the C AB
 (:mod:`randblas_gb300.api`), the autograd front end (:mod:`randblas_gb300.autograd`) and the
 batching front end (:mod:`randblas_gb300.batched`).
 """
-from . import profile  # noqa: F401
+from . import autograd, lowp, profile  # noqa: F401
 from ._lib import RandBLASError, lib  # noqa: F401
 from .api import (  # noqa: F401
     Axis, COOMatrix, CSCMatrix, CSRMatrix, DenseDist, DenseSkOp, Layout, Op, RNGState,

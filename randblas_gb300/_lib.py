@@ -19,6 +19,7 @@ NO_TRANS, TRANS = 0, 1
 GAUSSIAN, UNIFORM = 0, 1
 AXIS_SHORT, AXIS_LONG = 0, 1
 F32, F64 = 0, 1
+BF16 = 2  # storage type of A for rbg_lskge3_lowp_ex
 I32, I64 = 0, 1
 COO, CSR, CSC = 0, 1, 2
 PREC_BF16, PREC_FP8_E4M3 = 0, 1
@@ -130,6 +131,9 @@ SIGNATURES = {
     "rbg_lskge3_lowp_workspace": ([CI32, CI64, CI64, CI64, C.POINTER(C.c_size_t)], C.c_int),
     "rbg_lskge3_lowp": ([CI32, CI32, CI32, CI32, CI64, CI64, CI64, C.c_float, C.POINTER(rbg_dense_skop),
                          CI64, CI64, P, CI64, C.c_float, P, CI64, P, C.c_size_t, P], C.c_int),
+    "rbg_lskge3_lowp_ex": ([CI32, CI32, CI32, CI32, CI32, CI64, CI64, CI64, C.c_float,
+                            C.POINTER(rbg_dense_skop), CI64, CI64, P, CI64, C.c_float, P, CI64, P,
+                            C.c_size_t, P], C.c_int),
     "rbg_lowp_status": ([C.POINTER(CI32)], C.c_int),
     "rbg_lskge3_batched": ([CI32, C.POINTER(rbg_batch_problem), CI64, CI32, P], C.c_int),
     "rbg_batched_tile_configs": ([C.POINTER(CI32)], C.c_int),

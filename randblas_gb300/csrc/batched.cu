@@ -1,13 +1,477 @@
-// batched.cu -- placeholder translation unit, filled in by the batching path.
-#include "rbg_internal.h"
+// batched.cu -- the batching path: many independent left dense sketches
+// B_i = alpha_i * submat(S_i) * A_i + beta_i * B_i (LSKGE3 semantics, RandBLAS/skge.hh:154-202,
+// op = NoTrans, T = float) of uneven shapes in ONE persistent launch.  No reference
+// counterpart: the reference sketches problems one call at a time.
+//
+// Design.  The host turns the batch into a list of work items (problem, output tile, K split),
+// sorted by decreasing cost (longest-processing-time first), and uploads it with one
+// descriptor per problem.  A persistent grid of two CTAs per SM takes items from an atomic
+// counter.  Each item runs the CUDA-core tile of the plain path (simt_tiles.cuh: operator
+// entries generated from the RNG counters, data tile staged in shared memory, 8 x (BN/16)
+// FP32 accumulators per thread).  Problems with long K are split so no item dominates the
+// tail; the CTA that finishes a tile's last split (an atomic per tile, no waiting) sums the
+// splits' partial tiles in split order, so results do not depend on scheduling.
+// The tile width BN (128, 64 or 32) is chosen per problem -- by the caller (an autotuner),
+// or by a waste-based rule here.
+#include <algorithm>
+#include <cstring>
+#include <numeric>
+#include <vector>
 
-extern "C" int rbg_lskge3_batched(int32_t, const rbg_batch_problem *, int64_t, int32_t,
-                                  rbg_stream_t) {
-    rbg::set_last_error("batching path not built yet");
-    return RBG_ERROR_UNSUPPORTED;
+#include "rbg_internal.h"
+#include "simt_tiles.cuh"
+
+namespace rbg {
+namespace {
+
+using simt::BK;
+using simt::BM;
+using simt::NT;
+
+constexpr int kConfigs = 3;
+constexpr int kTileWidth[kConfigs + 1] = {0, 128, 64, 32};  // config id -> BN
+constexpr int kMaxSplits = 64;
+
+struct ProbDev {
+    POperand P;       // generated operator
+    Strided Q;        // Q(k, j) = A(k, j)
+    float *out;       // B(i, j) = out[i * os_i + j * os_j]
+    int64_t os_i, os_j;
+    int64_t M, N, K;  // d, n, m (K = 0 when alpha == 0 or m == 0)
+    float alpha, beta;
+    int32_t bn;       // tile width
+    int32_t splits;
+    int64_t kt_per_split;
+    int64_t tiles_n;
+    int64_t partial_off;  // floats into the partial buffer ([splits][M][N])
+    int64_t counter_off;  // ints into the tile counters
+};
+
+struct WorkItem {
+    int32_t prob;
+    int32_t split;
+    int64_t tile;
+};
+
+// One output tile (or one K split of it) of problem `pb`.  TN = columns per thread.
+template <int TN>
+__device__ __forceinline__ void batched_tile(const ProbDev &pb, int64_t tile, int split,
+                                             float (*Ps)[BM + 4], float *qs_raw, float *partial,
+                                             int *counters, int *s_flag) {
+    constexpr int BNT = TN * 16;
+    float(*Qs)[BNT + 4] = reinterpret_cast<float(*)[BNT + 4]>(qs_raw);
+    const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
+    const int64_t i0 = (tile / pb.tiles_n) * BM, j0 = (tile % pb.tiles_n) * BNT;
+    const int64_t kt_total = (pb.K + BK - 1) / BK;
+    const int64_t kb = (int64_t)split * pb.kt_per_split;
+    const int64_t ke = min(kt_total, kb + pb.kt_per_split);
+    const float *Qp = static_cast<const float *>(pb.Q.ptr);
+
+    float acc[8][TN];
+#pragma unroll
+    for (int a = 0; a < 8; ++a)
+#pragma unroll
+        for (int b = 0; b < TN; ++b) acc[a][b] = 0.f;
+
+    for (int64_t kt = kb; kt < ke; ++kt) {
+        const int64_t k0 = kt * BK;
+        simt::gen_p_tile<float>(Ps, pb.P, pb.M, pb.K, i0, k0);
+        simt::load_tile<float, BNT>(Qs, Qp, pb.Q.s0, pb.Q.s1, pb.K, pb.N, k0, j0);
+        __syncthreads();
+#pragma unroll
+        for (int kk = 0; kk < BK; ++kk) {
+            float a[8], b[TN];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                a[q] = Ps[kk][ty * 4 + q];
+                a[4 + q] = Ps[kk][64 + ty * 4 + q];
+            }
+#pragma unroll
+            for (int q = 0; q < TN / 2; ++q) {
+                b[q] = Qs[kk][tx * (TN / 2) + q];
+                b[TN / 2 + q] = Qs[kk][BNT / 2 + tx * (TN / 2) + q];
+            }
+#pragma unroll
+            for (int x = 0; x < 8; ++x)
+#pragma unroll
+                for (int y = 0; y < TN; ++y) acc[x][y] = fmaf(a[x], b[y], acc[x][y]);
+        }
+        __syncthreads();
+    }
+
+    auto row_of = [&](int x) { return i0 + (x < 4 ? ty * 4 + x : 64 + ty * 4 + (x - 4)); };
+    auto col_of = [&](int y) {
+        return j0 + (y < TN / 2 ? tx * (TN / 2) + y : BNT / 2 + tx * (TN / 2) + (y - TN / 2));
+    };
+    if (pb.splits == 1) {
+#pragma unroll
+        for (int x = 0; x < 8; ++x) {
+            const int64_t i = row_of(x);
+            if (i >= pb.M) continue;
+#pragma unroll
+            for (int y = 0; y < TN; ++y) {
+                const int64_t j = col_of(y);
+                if (j >= pb.N) continue;
+                float &o = pb.out[i * pb.os_i + j * pb.os_j];
+                o = pb.beta == 0.f ? pb.alpha * acc[x][y] : fmaf(pb.alpha, acc[x][y], pb.beta * o);
+            }
+        }
+        return;
+    }
+    // K split: publish this split's partial tile; the last split to finish reduces the tile
+    float *mine = partial + pb.partial_off + (int64_t)split * pb.M * pb.N;
+#pragma unroll
+    for (int x = 0; x < 8; ++x) {
+        const int64_t i = row_of(x);
+        if (i >= pb.M) continue;
+#pragma unroll
+        for (int y = 0; y < TN; ++y) {
+            const int64_t j = col_of(y);
+            if (j < pb.N) mine[i * pb.N + j] = acc[x][y];
+        }
+    }
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const int done = atomicAdd(counters + pb.counter_off + tile, 1);
+        *s_flag = done == pb.splits - 1;
+    }
+    __syncthreads();
+    if (!*s_flag) return;
+    __threadfence();
+    const float *base = partial + pb.partial_off;
+    for (int w = threadIdx.x; w < BM * BNT; w += NT) {
+        const int64_t i = i0 + w / BNT, j = j0 + w % BNT;
+        if (i >= pb.M || j >= pb.N) continue;
+        float sum = 0.f;
+        for (int s = 0; s < pb.splits; ++s) sum += __ldcg(base + ((int64_t)s * pb.M + i) * pb.N + j);
+        float &o = pb.out[i * pb.os_i + j * pb.os_j];
+        o = pb.beta == 0.f ? pb.alpha * sum : fmaf(pb.alpha, sum, pb.beta * o);
+    }
 }
 
+__global__ void __launch_bounds__(NT, 2)
+    batched_sketch_kernel(const ProbDev *__restrict__ probs, const WorkItem *__restrict__ items,
+                          int64_t n_items, unsigned long long *work_counter,
+                          float *__restrict__ partial, int *__restrict__ counters) {
+    __shared__ __align__(16) float Ps[BK][BM + 4];
+    __shared__ __align__(16) float Qs[BK * (128 + 4)];
+    __shared__ ProbDev s_pb;
+    __shared__ WorkItem s_item;
+    __shared__ int s_flag;
+    __shared__ unsigned long long s_w;
+    for (;;) {
+        if (threadIdx.x == 0) {
+            s_w = atomicAdd(work_counter, 1ull);
+            if (s_w < (unsigned long long)n_items) {
+                s_item = items[s_w];
+                s_pb = probs[s_item.prob];
+            }
+        }
+        __syncthreads();
+        if (s_w >= (unsigned long long)n_items) break;
+        const int64_t tile = s_item.tile;
+        const int split = s_item.split;
+        switch (s_pb.bn) {
+            case 128: batched_tile<8>(s_pb, tile, split, Ps, Qs, partial, counters, &s_flag); break;
+            case 64: batched_tile<4>(s_pb, tile, split, Ps, Qs, partial, counters, &s_flag); break;
+            default: batched_tile<2>(s_pb, tile, split, Ps, Qs, partial, counters, &s_flag); break;
+        }
+        __syncthreads();  // s_pb / s_item / s_w are rewritten by the next fetch
+    }
+}
+
+int resident_batched_ctas() {
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batched_sketch_kernel, NT, 0) !=
+            cudaSuccess ||
+        per_sm <= 0) {
+        cudaGetLastError();
+        per_sm = 1;
+    }
+    return per_sm * num_sms();
+}
+
+// Tile width by wasted columns: the widest tile whose padding stays small.
+int default_config(int64_t n) {
+    int best = 1;
+    double best_score = -1.0;
+    static const double eff[kConfigs + 1] = {0.0, 1.0, 0.88, 0.7};  // relative FLOP rates
+    for (int c = 1; c <= kConfigs; ++c) {
+        const int64_t bn = kTileWidth[c];
+        const double used = (double)n / (double)(((n + bn - 1) / bn) * bn);
+        const double score = used * eff[c];
+        if (score > best_score + 1e-12) {
+            best_score = score;
+            best = c;
+        }
+    }
+    return best;
+}
+
+}  // namespace
+}  // namespace rbg
+
+// The device memory and launch shape of one batch (the opaque rbg_batched_plan of the C ABI).
+struct rbg_batched_plan_s {
+    int64_t n_items = 0;
+    int grid = 0;
+    bool stream_ordered = false;  // memory from cudaMallocAsync (freed on a stream)
+    void *mem = nullptr;
+    rbg::ProbDev *probs = nullptr;
+    rbg::WorkItem *items = nullptr;
+    unsigned long long *work_counter = nullptr;  // followed by the tile counters
+    int *counters = nullptr;
+    size_t counter_bytes = 0;  // work counter + tile counters, zeroed before each run
+    float *partial = nullptr;
+    size_t bytes = 0;
+};
+
+namespace rbg {
+namespace {
+using BatchedPlan = rbg_batched_plan_s;
+
+size_t align256(size_t x) { return (x + 255) / 256 * 256; }
+
+// Validate the problems and build the descriptors and the sorted work list (host only).
+void build_plan(int32_t layout, const rbg_batch_problem *problems, int64_t count,
+                int32_t tile_config, std::vector<ProbDev> &descs, std::vector<WorkItem> &items,
+                int64_t &partial_floats, int64_t &tile_counters, int grid) {
+    if (layout != RBG_COL_MAJOR && layout != RBG_ROW_MAJOR)
+        fail(RBG_ERROR_INVALID_ARGUMENT, "layout must be RBG_COL_MAJOR or RBG_ROW_MAJOR");
+    if (count < 0) fail(RBG_ERROR_INVALID_ARGUMENT, "count must be >= 0");
+    if (count > 0 && !problems) fail(RBG_ERROR_INVALID_ARGUMENT, "problems must not be NULL");
+    if (count > INT32_MAX) fail(RBG_ERROR_INVALID_ARGUMENT, "too many problems");
+    if (tile_config < 0 || tile_config > kConfigs)
+        fail(RBG_ERROR_INVALID_ARGUMENT, "tile_config must be 0 or a listed configuration");
+    descs.clear();
+    items.clear();
+    partial_floats = 0;
+    tile_counters = 0;
+    std::vector<int64_t> kt(count, 0);
+    double total_cost = 0.0;
+    descs.resize(count);
+    for (int64_t p = 0; p < count; ++p) {
+        const rbg_batch_problem &q = problems[p];
+        ProbDev &pd = descs[p];
+        std::memset(&pd, 0, sizeof pd);
+        RBG_REQUIRE("lskge3_batched", q.d >= 0 && q.n >= 0 && q.m >= 0);
+        RBG_REQUIRE("lskge3_batched", q.ro_s >= 0 && q.co_s >= 0);
+        RBG_REQUIRE("DenseDist", q.dist.n_rows > 0);
+        RBG_REQUIRE("DenseDist", q.dist.n_cols > 0);
+        if (q.dist.family != RBG_GAUSSIAN && q.dist.family != RBG_UNIFORM)
+            fail(RBG_ERROR_INVALID_ARGUMENT, "Unrecognized ScalarDist.");
+        RBG_REQUIRE("lskge3_batched", q.dist.n_rows >= q.d + q.ro_s);
+        RBG_REQUIRE("lskge3_batched", q.dist.n_cols >= q.m + q.co_s);
+        if (layout == RBG_COL_MAJOR) {
+            RBG_REQUIRE("lskge3_batched", q.lda >= q.m);
+            RBG_REQUIRE("lskge3_batched", q.ldb >= q.d);
+        } else {
+            RBG_REQUIRE("lskge3_batched", q.lda >= q.n);
+            RBG_REQUIRE("lskge3_batched", q.ldb >= q.n);
+        }
+        const int32_t cfg = tile_config ? tile_config : q.tile_config;
+        if (cfg < 0 || cfg > kConfigs)
+            fail(RBG_ERROR_INVALID_ARGUMENT, "tile_config must be 0 or a listed configuration");
+        pd.M = q.d;
+        pd.N = q.n;
+        pd.K = (q.alpha == 0.f) ? 0 : q.m;  // alpha == 0: A and S are not read
+        pd.alpha = q.alpha;
+        pd.beta = q.beta;
+        if (pd.M == 0 || pd.N == 0) continue;
+        if (!q.B) fail(RBG_ERROR_INVALID_ARGUMENT, "B must not be NULL");
+        if (pd.K > 0 && !q.A) fail(RBG_ERROR_INVALID_ARGUMENT, "A must not be NULL");
+        const DenseInfo info = dense_info(q.dist);
+        pd.P.gen = make_dense_gen(q.dist, q.seed);
+        if (info.natural_layout == RBG_ROW_MAJOR) {
+            pd.P.r_on_i = 1;
+            pd.P.r0 = q.ro_s;
+            pd.P.c0 = q.co_s;
+        } else {
+            pd.P.r_on_i = 0;
+            pd.P.r0 = q.co_s;
+            pd.P.c0 = q.ro_s;
+        }
+        pd.P.buff = nullptr;
+        pd.Q = layout == RBG_ROW_MAJOR ? Strided{q.A, q.lda, 1} : Strided{q.A, 1, q.lda};
+        pd.out = q.B;
+        pd.os_i = layout == RBG_ROW_MAJOR ? q.ldb : 1;
+        pd.os_j = layout == RBG_ROW_MAJOR ? 1 : q.ldb;
+        pd.bn = kTileWidth[cfg ? cfg : default_config(pd.N)];
+        pd.tiles_n = (pd.N + pd.bn - 1) / pd.bn;
+        kt[p] = (pd.K + BK - 1) / BK;
+        const int64_t tiles = ((pd.M + BM - 1) / BM) * pd.tiles_n;
+        total_cost += (double)tiles * (double)std::max<int64_t>(kt[p], 1) * pd.bn;
+    }
+    // split long K so that no item costs more than ~1/8 of a CTA's fair share
+    const double cap = std::max(total_cost / (8.0 * std::max(grid, 1)), 128.0 * 64.0);
+    for (int64_t p = 0; p < count; ++p) {
+        ProbDev &pd = descs[p];
+        if (pd.M == 0 || pd.N == 0) continue;
+        const int64_t tiles = ((pd.M + BM - 1) / BM) * pd.tiles_n;
+        const int64_t cap_kt = std::max<int64_t>(32, (int64_t)(cap / pd.bn));
+        int64_t splits = kt[p] > 0 ? (kt[p] + cap_kt - 1) / cap_kt : 1;
+        splits = std::min<int64_t>(splits, kMaxSplits);
+        pd.kt_per_split = kt[p] > 0 ? (kt[p] + splits - 1) / splits : 0;
+        splits = kt[p] > 0 ? (kt[p] + pd.kt_per_split - 1) / pd.kt_per_split : 1;
+        pd.splits = (int32_t)splits;
+        if (splits > 1) {
+            pd.partial_off = partial_floats;
+            partial_floats += splits * pd.M * pd.N;
+            pd.counter_off = tile_counters;
+            tile_counters += tiles;
+        }
+        for (int64_t t = 0; t < tiles; ++t)
+            for (int64_t s = 0; s < splits; ++s) items.push_back(WorkItem{(int32_t)p, (int32_t)s, t});
+    }
+    // longest processing time first; ties keep problem order
+    std::stable_sort(items.begin(), items.end(), [&](const WorkItem &a, const WorkItem &b) {
+        const ProbDev &pa = descs[a.prob], &pb = descs[b.prob];
+        return (double)pa.kt_per_split * pa.bn > (double)pb.kt_per_split * pb.bn;
+    });
+}
+
+void execute_plan(const BatchedPlan &pl, cudaStream_t s) {
+    if (pl.n_items == 0) return;
+    RBG_CUDA(cudaMemsetAsync(pl.work_counter, 0, pl.counter_bytes, s));
+    ProfScope prof("batched_sketch", s);
+    batched_sketch_kernel<<<pl.grid, NT, 0, s>>>(pl.probs, pl.items, pl.n_items,
+                                                 pl.work_counter, pl.partial, pl.counters);
+    RBG_LAUNCHED();
+}
+
+// Lay the plan's device memory out and upload descriptors and items.
+void upload_plan(BatchedPlan &pl, const std::vector<ProbDev> &descs,
+                 const std::vector<WorkItem> &items, int64_t partial_floats,
+                 int64_t tile_counters, cudaStream_t s, bool stream_ordered) {
+    const size_t probs_b = align256(descs.size() * sizeof(ProbDev));
+    const size_t items_b = align256(items.size() * sizeof(WorkItem));
+    const size_t ctr_b = align256(sizeof(unsigned long long) + (size_t)tile_counters * sizeof(int));
+    const size_t part_b = align256((size_t)partial_floats * sizeof(float));
+    pl.bytes = probs_b + items_b + ctr_b + part_b;
+    pl.stream_ordered = stream_ordered;
+    if (stream_ordered)
+        RBG_CUDA(cudaMallocAsync(&pl.mem, std::max<size_t>(pl.bytes, 256), s));
+    else
+        RBG_CUDA(cudaMalloc(&pl.mem, std::max<size_t>(pl.bytes, 256)));
+    uint8_t *base = static_cast<uint8_t *>(pl.mem);
+    pl.probs = reinterpret_cast<ProbDev *>(base);
+    pl.items = reinterpret_cast<WorkItem *>(base + probs_b);
+    pl.work_counter = reinterpret_cast<unsigned long long *>(base + probs_b + items_b);
+    pl.counters = reinterpret_cast<int *>(pl.work_counter + 1);
+    pl.counter_bytes = sizeof(unsigned long long) + (size_t)tile_counters * sizeof(int);
+    pl.partial = reinterpret_cast<float *>(base + probs_b + items_b + ctr_b);
+    pl.n_items = (int64_t)items.size();
+    if (!descs.empty())
+        RBG_CUDA(cudaMemcpyAsync(pl.probs, descs.data(), descs.size() * sizeof(ProbDev),
+                                 cudaMemcpyHostToDevice, s));
+    if (!items.empty())
+        RBG_CUDA(cudaMemcpyAsync(pl.items, items.data(), items.size() * sizeof(WorkItem),
+                                 cudaMemcpyHostToDevice, s));
+    if (!stream_ordered) RBG_CUDA(cudaStreamSynchronize(s));
+}
+
+template <typename F>
+int guarded_batched(F &&f) {
+    try {
+        f();
+        return RBG_SUCCESS;
+    } catch (const Failure &e) {
+        set_last_error(e.msg);
+        return e.code;
+    } catch (const std::exception &e) {
+        set_last_error(e.what());
+        return RBG_ERROR_ALLOC;
+    }
+}
+
+}  // namespace
+}  // namespace rbg
+
+using namespace rbg;
+
 extern "C" int rbg_batched_tile_configs(int32_t *count) {
-    if (count) *count = 0;
+    if (!count) {
+        set_last_error("count must not be NULL");
+        return RBG_ERROR_INVALID_ARGUMENT;
+    }
+    *count = kConfigs;
     return RBG_SUCCESS;
+}
+
+extern "C" int rbg_batched_tile_width(int32_t config, int32_t *width) {
+    return guarded_batched([&] {
+        if (!width) fail(RBG_ERROR_INVALID_ARGUMENT, "width must not be NULL");
+        if (config < 1 || config > kConfigs)
+            fail(RBG_ERROR_INVALID_ARGUMENT, "config must be one of the listed configurations");
+        *width = kTileWidth[config];
+    });
+}
+
+extern "C" int rbg_batched_plan_create(int32_t layout, const rbg_batch_problem *problems,
+                                       int64_t count, int32_t tile_config,
+                                       rbg_batched_plan *plan) {
+    return guarded_batched([&] {
+        if (!plan) fail(RBG_ERROR_INVALID_ARGUMENT, "plan must not be NULL");
+        *plan = nullptr;
+        std::vector<ProbDev> descs;
+        std::vector<WorkItem> items;
+        int64_t partial_floats = 0, tile_counters = 0;
+        const int grid = resident_batched_ctas();
+        build_plan(layout, problems, count, tile_config, descs, items, partial_floats,
+                   tile_counters, grid);
+        auto *pl = new BatchedPlan();
+        pl->grid = grid;
+        try {
+            upload_plan(*pl, descs, items, partial_floats, tile_counters, nullptr, false);
+        } catch (...) {
+            if (pl->mem) cudaFree(pl->mem);
+            delete pl;
+            throw;
+        }
+        *plan = pl;
+    });
+}
+
+extern "C" int rbg_batched_plan_execute(rbg_batched_plan plan, rbg_stream_t stream) {
+    return guarded_batched([&] {
+        if (!plan) fail(RBG_ERROR_INVALID_ARGUMENT, "plan must not be NULL");
+        execute_plan(*plan, as_cuda(stream));
+    });
+}
+
+extern "C" int rbg_batched_plan_info(rbg_batched_plan plan, int64_t *work_items,
+                                     int64_t *device_bytes) {
+    return guarded_batched([&] {
+        if (!plan) fail(RBG_ERROR_INVALID_ARGUMENT, "plan must not be NULL");
+        if (work_items) *work_items = plan->n_items;
+        if (device_bytes) *device_bytes = (int64_t)plan->bytes;
+    });
+}
+
+extern "C" int rbg_batched_plan_destroy(rbg_batched_plan plan) {
+    return guarded_batched([&] {
+        if (!plan) return;
+        if (plan->mem) RBG_CUDA(cudaFree(plan->mem));
+        delete plan;
+    });
+}
+
+extern "C" int rbg_lskge3_batched(int32_t layout, const rbg_batch_problem *problems,
+                                  int64_t count, int32_t tile_config, rbg_stream_t stream) {
+    return guarded_batched([&] {
+        const cudaStream_t s = as_cuda(stream);
+        std::vector<ProbDev> descs;
+        std::vector<WorkItem> items;
+        int64_t partial_floats = 0, tile_counters = 0;
+        const int grid = resident_batched_ctas();
+        build_plan(layout, problems, count, tile_config, descs, items, partial_floats,
+                   tile_counters, grid);
+        if (items.empty()) return;
+        BatchedPlan pl;
+        pl.grid = grid;
+        upload_plan(pl, descs, items, partial_floats, tile_counters, s, true);
+        execute_plan(pl, s);
+        RBG_CUDA(cudaFreeAsync(pl.mem, s));
+    });
 }

@@ -13,74 +13,17 @@
 #include <mutex>
 
 #include "rbg_internal.h"
+#include "simt_tiles.cuh"
 
 namespace rbg {
 namespace {
 
-constexpr int BM = 128, BN = 128, BK = 16, NT = 256;
-
-// P tile, k-major: Ps[k][i] for i in [0, BM), k in [0, BK).  Entries outside M x K are 0.
-template <typename T>
-__device__ __forceinline__ void gen_p_tile(T (*Ps)[BM + 4], const POperand &P, int64_t M,
-                                           int64_t K, int64_t i0, int64_t k0) {
-    const DenseGen &g = P.gen;
-    if (P.r_on_i) {
-        // R follows i, C follows k: each of the BM rows needs the counter blocks covering
-        // columns [c0 + k0, c0 + k0 + BK).
-        const int64_t cfirst = P.c0 + k0;
-        const int64_t b0 = cfirst / 4;
-        const int nb = (int)((cfirst + BK - 1) / 4 - b0 + 1);
-        for (int w = threadIdx.x; w < BM * nb; w += NT) {
-            const int i = w / nb, b = w % nb;
-            const bool row_ok = i0 + i < M;
-            float v[4] = {0.f, 0.f, 0.f, 0.f};
-            if (row_ok) gen4(g.family, g.counter_of(P.r0 + i0 + i, b0 + b), g.key, v);
-#pragma unroll
-            for (int l = 0; l < 4; ++l) {
-                const int64_t k = (b0 + b) * 4 + l - cfirst;
-                if (k >= 0 && k < BK)
-                    Ps[k][i] = (row_ok && k0 + k < K) ? finish_entry<T>(g.family, v[l]) : (T)0;
-            }
-        }
-    } else {
-        // R follows k, C follows i: each of the BK rows needs the blocks covering columns
-        // [c0 + i0, c0 + i0 + BM).
-        const int64_t cfirst = P.c0 + i0;
-        const int64_t b0 = cfirst / 4;
-        const int nb = (int)((cfirst + BM - 1) / 4 - b0 + 1);
-        for (int w = threadIdx.x; w < BK * nb; w += NT) {
-            const int k = w / nb, b = w % nb;
-            const bool k_ok = k0 + k < K;
-            float v[4] = {0.f, 0.f, 0.f, 0.f};
-            if (k_ok) gen4(g.family, g.counter_of(P.r0 + k0 + k, b0 + b), g.key, v);
-#pragma unroll
-            for (int l = 0; l < 4; ++l) {
-                const int64_t i = (b0 + b) * 4 + l - cfirst;
-                if (i >= 0 && i < BM)
-                    Ps[k][i] = (k_ok && i0 + i < M) ? finish_entry<T>(g.family, v[l]) : (T)0;
-            }
-        }
-    }
-}
-
-// Strided tile load into a k-major SMEM tile: dst[k][x] = src(k0 + k, x0 + x), x in [0, W).
-// Threads walk the unit-stride dimension when there is one.
-template <typename T, int W>
-__device__ __forceinline__ void load_tile(T (*dst)[W + 4], const T *__restrict__ src,
-                                          int64_t sk, int64_t sx, int64_t K, int64_t X,
-                                          int64_t k0, int64_t x0) {
-    if (sx == 1 || sk != 1) {
-        for (int w = threadIdx.x; w < BK * W; w += NT) {
-            const int k = w / W, x = w % W;
-            dst[k][x] = (k0 + k < K && x0 + x < X) ? src[(k0 + k) * sk + (x0 + x) * sx] : (T)0;
-        }
-    } else {
-        for (int w = threadIdx.x; w < BK * W; w += NT) {
-            const int x = w / BK, k = w % BK;
-            dst[k][x] = (k0 + k < K && x0 + x < X) ? src[(k0 + k) * sk + (x0 + x) * sx] : (T)0;
-        }
-    }
-}
+using simt::BM;
+using simt::BN;
+using simt::BK;
+using simt::NT;
+using simt::gen_p_tile;
+using simt::load_tile;
 
 template <typename T, bool GEN>
 __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? 2 : 1)

@@ -39,13 +39,34 @@ constexpr int CHUNKS = ROW_BYTES / 16;      // 16-byte chunks per row
 constexpr int STAGES = 5;
 constexpr int S_STAGE_BYTES = BM * BK * 2;  // 8 KiB
 constexpr int A_STAGE_BYTES = BN * BK * 2;  // 32 KiB
-constexpr int NUM_THREADS = 640;
+// Warp roles: 0 TMA, 1 MMA, 4-7 epilogue (one per tensor-memory lane quarter), generator
+// warps from 8 on.  A warp runs on sub-partition id % 4.  With GEN_SKIP_MMA_SP the generators
+// avoid the MMA issuer's sub-partition (id % 4 == 1), whose warps above 8 then stay idle.
+#ifndef RBG_GEN_WARPS
+#define RBG_GEN_WARPS 16
+#endif
+#ifndef RBG_GEN_GROUPS
+#define RBG_GEN_GROUPS 4
+#endif
+#ifndef RBG_GEN_SKIP_MMA_SP
+#define RBG_GEN_SKIP_MMA_SP 0
+#endif
 constexpr int EPI_WARP0 = 4;
 constexpr int GEN_WARP0 = 8;
-constexpr int GEN_WARPS = 12;
+constexpr int GEN_WARPS = RBG_GEN_WARPS;
+constexpr bool GEN_SKIP_MMA_SP = RBG_GEN_SKIP_MMA_SP != 0;
+constexpr int NUM_THREADS = 32 * (GEN_WARP0 + (GEN_SKIP_MMA_SP ? GEN_WARPS / 3 * 4 : GEN_WARPS));
 constexpr int GEN_THREADS = GEN_WARPS * 32;
-constexpr int GEN_GROUPS = 3;                        // groups take stages in turn
+constexpr int GEN_GROUPS = RBG_GEN_GROUPS;           // groups take stages in turn
 constexpr int GROUP_THREADS = GEN_THREADS / GEN_GROUPS;
+static_assert(!GEN_SKIP_MMA_SP || GEN_WARPS % 3 == 0, "generator warp layout");
+static_assert(GEN_THREADS % GEN_GROUPS == 0 && GROUP_THREADS % 32 == 0, "generator groups");
+// A group's previous stage (it - GEN_GROUPS) guarantees only that the MMAs up to
+// it - GEN_GROUPS - STAGES have completed.  Its parity wait on the empty barrier of stage it
+// is unambiguous only if the phase before the awaited one (the MMAs of it - STAGES) is
+// already complete, so GEN_GROUPS must not exceed STAGES; with more groups a wait can pass a
+// phase early, merging two phases of the stage's barriers.
+static_assert(GEN_GROUPS <= STAGES, "generator groups must not outnumber the stages");
 constexpr uint32_t TMEM_COLS = 512;
 constexpr int SMEM_BYTES = STAGES * (S_STAGE_BYTES + A_STAGE_BYTES) + 1024 /*align*/ + 256;
 
@@ -350,11 +371,14 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
             __syncwarp();
             if (lane == 0) tc::mbar_arrive(acc_empty);
         }
-    } else if (warp >= GEN_WARP0) {
+    } else if (warp >= GEN_WARP0 && (!GEN_SKIP_MMA_SP || (warp & 3) != 1)) {
         // ---------------- S producers: GEN_GROUPS groups, group gi takes the stages with
         // it % GEN_GROUPS == gi
-        const int gi = (warp - GEN_WARP0) / (GEN_WARPS / GEN_GROUPS);
-        const int tg = threadIdx.x - GEN_WARP0 * 32 - gi * GROUP_THREADS;
+        const int gw = GEN_SKIP_MMA_SP
+                           ? ((warp - GEN_WARP0) >> 2) * 3 + ((warp & 3) == 0 ? 0 : (warp & 3) - 1)
+                           : warp - GEN_WARP0;
+        const int gi = gw / (GEN_WARPS / GEN_GROUPS);
+        const int tg = (gw % (GEN_WARPS / GEN_GROUPS)) * 32 + lane;
         const int row_lo = (int)n_idx * ROWS;
         uint32_t peer_full[STAGES] = {};
         uint32_t peer_tiles = 0;
@@ -435,10 +459,26 @@ __device__ __forceinline__ int64_t blocked_index(int64_t k, int64_t j, int64_t n
     return ((k / BK) * npad + j) * BK + (k % BK);
 }
 
-__global__ void __launch_bounds__(256) convert_a_kernel(const float *__restrict__ A, int64_t sk,
+// Loads of A in its storage type (FP32 or BF16), widened to float.
+__device__ __forceinline__ float load_a(const float *p) { return *p; }
+__device__ __forceinline__ float load_a(const __nv_bfloat16 *p) { return __bfloat162float(*p); }
+
+// Four consecutive elements; `p` must be 16-byte (FP32) or 8-byte (BF16) aligned.
+__device__ __forceinline__ float4 load_a4(const float *p) {
+    return *reinterpret_cast<const float4 *>(p);
+}
+__device__ __forceinline__ float4 load_a4(const __nv_bfloat16 *p) {
+    const uint2 w = *reinterpret_cast<const uint2 *>(p);
+    return make_float4(__uint_as_float(w.x << 16), __uint_as_float(w.x & 0xFFFF0000u),
+                       __uint_as_float(w.y << 16), __uint_as_float(w.y & 0xFFFF0000u));
+}
+
+template <typename TA>
+__global__ void __launch_bounds__(256) convert_a_kernel(const TA *__restrict__ A, int64_t sk,
                                                         int64_t sj, int64_t K, int64_t N,
                                                         int64_t kpad, int64_t npad,
                                                         __nv_bfloat16 *__restrict__ At) {
+    constexpr uintptr_t VEC_ALIGN = 4 * sizeof(TA) - 1;
     __shared__ float tile[64][129];
     if (sk == 1 && sj != 1) {
         // direct: 4 consecutive k of one row j per thread
@@ -448,12 +488,12 @@ __global__ void __launch_bounds__(256) convert_a_kernel(const float *__restrict_
             const int64_t j = t / kq, k = (t % kq) * 4;
             float v[4] = {0.f, 0.f, 0.f, 0.f};
             if (j < N) {
-                const float *src = A + j * sj + k;
-                if (k + 4 <= K && ((reinterpret_cast<uintptr_t>(src) & 15) == 0)) {
-                    const float4 f = *reinterpret_cast<const float4 *>(src);
+                const TA *src = A + j * sj + k;
+                if (k + 4 <= K && ((reinterpret_cast<uintptr_t>(src) & VEC_ALIGN) == 0)) {
+                    const float4 f = load_a4(src);
                     v[0] = f.x; v[1] = f.y; v[2] = f.z; v[3] = f.w;
                 } else {
-                    for (int e = 0; e < 4; ++e) v[e] = k + e < K ? src[e] : 0.f;
+                    for (int e = 0; e < 4; ++e) v[e] = k + e < K ? load_a(src + e) : 0.f;
                 }
             }
             uint2 w;
@@ -465,16 +505,15 @@ __global__ void __launch_bounds__(256) convert_a_kernel(const float *__restrict_
     }
     const int64_t tk = (kpad + 63) / 64, tj = (npad + 127) / 128;
     const bool vec = sj == 1 && (N % 4) == 0 && (sk % 4) == 0 &&
-                     (reinterpret_cast<uintptr_t>(A) & 15) == 0;
+                     (reinterpret_cast<uintptr_t>(A) & VEC_ALIGN) == 0;
     for (int64_t t = blockIdx.x; t < tk * tj; t += gridDim.x) {
         const int64_t k0 = (t % tk) * 64, j0 = (t / tk) * 128;
         if (vec) {
-            // 32 float4 per k-row of the tile; 8 rows per pass of 256 threads
+            // 32 groups of 4 per k-row of the tile; 8 rows per pass of 256 threads
             for (int w = threadIdx.x; w < 64 * 32; w += 256) {
                 const int kk = w / 32, jq = (w % 32) * 4;
                 float4 f = make_float4(0.f, 0.f, 0.f, 0.f);
-                if (k0 + kk < K && j0 + jq < N)
-                    f = *reinterpret_cast<const float4 *>(A + (k0 + kk) * sk + j0 + jq);
+                if (k0 + kk < K && j0 + jq < N) f = load_a4(A + (k0 + kk) * sk + j0 + jq);
                 tile[kk][jq] = f.x;
                 tile[kk][jq + 1] = f.y;
                 tile[kk][jq + 2] = f.z;
@@ -483,8 +522,9 @@ __global__ void __launch_bounds__(256) convert_a_kernel(const float *__restrict_
         } else {
             for (int w = threadIdx.x; w < 64 * 128; w += 256) {
                 const int kk = w / 128, jj = w % 128;
-                tile[kk][jj] = (k0 + kk < K && j0 + jj < N) ? A[(k0 + kk) * sk + (j0 + jj) * sj]
-                                                             : 0.f;
+                tile[kk][jj] = (k0 + kk < K && j0 + jj < N)
+                                   ? load_a(A + (k0 + kk) * sk + (j0 + jj) * sj)
+                                   : 0.f;
             }
         }
         __syncthreads();
@@ -668,8 +708,8 @@ EncodeFn encode_fn() {
 }
 
 void lowp_bf16(int64_t M, int64_t N, int64_t K, float alpha, const DenseGen &gen, int64_t r0,
-               int64_t c0, int r_on_i, const Strided &Q, float beta, float *out, int64_t os_i,
-               int64_t os_j, void *workspace, size_t ws_bytes, cudaStream_t s) {
+               int64_t c0, int r_on_i, const Strided &Q, bool a_bf16, float beta, float *out,
+               int64_t os_i, int64_t os_j, void *workspace, size_t ws_bytes, cudaStream_t s) {
     const int sms = num_sms();
     const Plan pl = make_plan(M, N, K);
     Scratch own;
@@ -687,8 +727,12 @@ void lowp_bf16(int64_t M, int64_t N, int64_t K, float alpha, const DenseGen &gen
 
     {
         ProfScope prof("lowp_convert_a", s);
-        convert_a_kernel<<<sms * 8, 256, 0, s>>>(static_cast<const float *>(Q.ptr), Q.s0, Q.s1,
-                                                 K, N, pl.kpad, pl.npad, At);
+        if (a_bf16)
+            convert_a_kernel<<<sms * 8, 256, 0, s>>>(static_cast<const __nv_bfloat16 *>(Q.ptr),
+                                                     Q.s0, Q.s1, K, N, pl.kpad, pl.npad, At);
+        else
+            convert_a_kernel<<<sms * 8, 256, 0, s>>>(static_cast<const float *>(Q.ptr), Q.s0,
+                                                     Q.s1, K, N, pl.kpad, pl.npad, At);
         RBG_LAUNCHED();
     }
 
@@ -773,14 +817,16 @@ extern "C" int rbg_lowp_status(int32_t *code) {
     });
 }
 
-extern "C" int rbg_lskge3_lowp(int32_t precision, int32_t layout, int32_t opS, int32_t opA,
-                               int64_t d, int64_t n, int64_t m, float alpha,
-                               const rbg_dense_skop *S, int64_t ro_s, int64_t co_s, const float *A,
-                               int64_t lda, float beta, float *B, int64_t ldb, void *workspace,
-                               size_t workspace_bytes, rbg_stream_t stream) {
+namespace {
+int lowp_entry(int32_t precision, int32_t a_dtype, int32_t layout, int32_t opS, int32_t opA,
+               int64_t d, int64_t n, int64_t m, float alpha, const rbg_dense_skop *S,
+               int64_t ro_s, int64_t co_s, const void *A, int64_t lda, float beta, float *B,
+               int64_t ldb, void *workspace, size_t workspace_bytes, rbg_stream_t stream) {
     return guarded_lowp([&] {
         if (precision != RBG_PREC_BF16)
             fail(RBG_ERROR_UNSUPPORTED, "only RBG_PREC_BF16 is provided");
+        if (a_dtype != RBG_F32 && a_dtype != RBG_BF16)
+            fail(RBG_ERROR_INVALID_ARGUMENT, "a_dtype must be RBG_F32 or RBG_BF16");
         if (layout != RBG_COL_MAJOR && layout != RBG_ROW_MAJOR)
             fail(RBG_ERROR_INVALID_ARGUMENT, "layout must be RBG_COL_MAJOR or RBG_ROW_MAJOR");
         if ((opS != RBG_NO_TRANS && opS != RBG_TRANS) || (opA != RBG_NO_TRANS && opA != RBG_TRANS))
@@ -833,7 +879,27 @@ extern "C" int rbg_lskge3_lowp(int32_t precision, int32_t layout, int32_t opS, i
             r0 = co_s;
             c0 = ro_s;
         }
-        lowp_bf16(d, n, m, alpha, make_dense_gen(S->dist, S->seed_state), r0, c0, r_on_i, Q, beta,
-                  B, brs, bcs, workspace, workspace_bytes, s);
+        lowp_bf16(d, n, m, alpha, make_dense_gen(S->dist, S->seed_state), r0, c0, r_on_i, Q,
+                  a_dtype == RBG_BF16, beta, B, brs, bcs, workspace, workspace_bytes, s);
     });
+}
+}  // namespace
+
+extern "C" int rbg_lskge3_lowp(int32_t precision, int32_t layout, int32_t opS, int32_t opA,
+                               int64_t d, int64_t n, int64_t m, float alpha,
+                               const rbg_dense_skop *S, int64_t ro_s, int64_t co_s, const float *A,
+                               int64_t lda, float beta, float *B, int64_t ldb, void *workspace,
+                               size_t workspace_bytes, rbg_stream_t stream) {
+    return lowp_entry(precision, RBG_F32, layout, opS, opA, d, n, m, alpha, S, ro_s, co_s, A, lda,
+                      beta, B, ldb, workspace, workspace_bytes, stream);
+}
+
+extern "C" int rbg_lskge3_lowp_ex(int32_t precision, int32_t a_dtype, int32_t layout,
+                                  int32_t opS, int32_t opA, int64_t d, int64_t n, int64_t m,
+                                  float alpha, const rbg_dense_skop *S, int64_t ro_s,
+                                  int64_t co_s, const void *A, int64_t lda, float beta, float *B,
+                                  int64_t ldb, void *workspace, size_t workspace_bytes,
+                                  rbg_stream_t stream) {
+    return lowp_entry(precision, a_dtype, layout, opS, opA, d, n, m, alpha, S, ro_s, co_s, A, lda,
+                      beta, B, ldb, workspace, workspace_bytes, stream);
 }

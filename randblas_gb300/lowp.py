@@ -32,11 +32,17 @@ def sketch_lowp(layout: Layout, opS: Op, opA: Op, d: int, n: int, m: int, alpha:
                 S: DenseSkOp, ro_s: int, co_s: int, A: torch.Tensor, lda: int, beta: float,
                 B: torch.Tensor, ldb: int, precision: int = BF16,
                 workspace: torch.Tensor | None = None) -> None:
+    """B = alpha * op(submat(S)) * op(A) + beta * B on the tensor cores.  A is FP32 or BF16
+    (BF16 data enters the tensor cores unchanged); B is FP32."""
     ws = _ptr(workspace) if workspace is not None else None
     wbytes = workspace.numel() * workspace.element_size() if workspace is not None else 0
-    call("rbg_lskge3_lowp", precision, int(layout), int(opS), int(opA), d, n, m, float(alpha),
-         C.byref(S._c()), ro_s, co_s, _ptr(A), lda, float(beta), _ptr(B), ldb, ws, wbytes,
-         _stream())
+    a_dtype = {torch.float32: _lib.F32, torch.bfloat16: _lib.BF16}.get(A.dtype)
+    if a_dtype is None:
+        raise _lib.RandBLASError(_lib.ERROR_INVALID_ARGUMENT,
+                                 "the precision path takes FP32 or BF16 A")
+    call("rbg_lskge3_lowp_ex", precision, a_dtype, int(layout), int(opS), int(opA), d, n, m,
+         float(alpha), C.byref(S._c()), ro_s, co_s, _ptr(A), lda, float(beta), _ptr(B), ldb, ws,
+         wbytes, _stream())
 
 
 def status() -> int:

@@ -57,3 +57,13 @@ def rb():
     import randblas_gb300
     randblas_gb300.lib()
     return randblas_gb300
+
+
+@pytest.fixture(scope="session")
+def rb_host():
+    """The package with its CUDA library built and loaded, for host-only calls (no GPU)."""
+    from randblas_gb300 import build as rbuild
+    rbuild.build()
+    import randblas_gb300
+    randblas_gb300.lib()
+    return randblas_gb300
