@@ -158,7 +158,8 @@ def main():
     ap.add_argument("--m-log2", type=int, default=17,
                     help="log2 of m for the dense small cases")
     ap.add_argument("--case", default="full",
-                    choices=["full", "lowp-small", "plain-small", "saso", "convert-small"],
+                    choices=["full", "lowp-small", "plain-small", "saso", "convert-small",
+                             "batched"],
                     help="full: the benchmark line; the others run one kernel family on a "
                          "smaller case (for profilers) and print a short JSON line")
     args = ap.parse_args()
@@ -334,6 +335,62 @@ def bench_saso(torch, rb, device, args, stream, hbm):
     return out
 
 
+def batched_workload(torch, rb, device, count=512):
+    """512 left sketches: m log-uniform in [2^12, 2^18], n uniform in [16, 512], d = 4n
+    (numpy default_rng(0)); A_i N(0,1) FP32 row-major from fill_dense with key 1000 + i;
+    Gaussian operators with chained states starting at RNGState(4)."""
+    import numpy as np
+    from randblas_gb300 import batched
+    rng = np.random.default_rng(0)
+    ms = np.round(2.0 ** rng.uniform(12, 18, count)).astype(int)
+    ns = rng.integers(16, 513, count)
+    probs, state = [], rb.RNGState(4)
+    for i in range(count):
+        d, n, m = 4 * int(ns[i]), int(ns[i]), int(ms[i])
+        A = torch.empty(m, n, device=device)
+        rb.fill_dense(rb.DenseDist(m, n, rb.ScalarDist.Gaussian, rb.Axis.Short), A.view(-1),
+                      rb.RNGState(1000 + i))
+        S = rb.DenseSkOp(rb.DenseDist(d, m, rb.ScalarDist.Gaussian), state)
+        state = S.next_state
+        probs.append(batched.BatchProblem(S, A, torch.empty(d, n, device=device), d, n, m))
+    return probs
+
+
+def bench_batched(torch, rb, device, args, stream):
+    import tempfile
+    from randblas_gb300 import batched
+    probs = batched_workload(torch, rb, device)
+    flops = sum(2.0 * p.d * p.n * p.m for p in probs)
+
+    def separate():
+        for p in probs:
+            rb.sketch_general(rb.Layout.RowMajor, rb.Op.NoTrans, rb.Op.NoTrans, p.d, p.n, p.m,
+                              1.0, p.S, p.A, p.n, 0.0, p.B, p.n)
+    steps = max(1, min(args.steps, 3))
+    ms_sep = event_time(torch, separate, steps, 1, stream)
+    res = {"workload": "512 Gaussian left sketches, m log-uniform [2^12, 2^18], n uniform "
+                       "[16, 512], d = 4n, FP32", "gflop": round(flops / 1e9, 1),
+           "separate_plain_launches": {"ms": round(ms_sep, 2),
+                                       "TFLOP/s": round(flops / ms_sep / 1e9, 2)}}
+    for name, tuner in (("default_tiles", None),
+                        ("autotuned", batched.Autotuner(
+                            cache_path=os.path.join(tempfile.gettempdir(), "rbg_tiles.json")))):
+        for p in probs:
+            p.tile_config = 0
+        plan = batched.BatchedPlan(probs, tuner=tuner)
+        graph = plan.capture()
+        ms = event_time(torch, graph.replay, steps, 1, stream)
+        res[name] = {"ms": round(ms, 2), "TFLOP/s": round(flops / ms / 1e9, 2),
+                     "speedup_vs_separate": round(ms_sep / ms, 2),
+                     "work_items": plan.info()["work_items"]}
+        if tuner is not None:
+            res[name]["tile_widths"] = {str(w): sum(1 for p in probs if
+                                                    batched.tile_width(p.tile_config) == w)
+                                        for w in (128, 64, 32)}
+        plan.close()
+    return res
+
+
 def bench_e2e(torch, rb, lowp, have_lowp, S, A_host, args, stream, flops, device):
     """Same sketch through the public API with host buffers: per step, copy A from pinned host
     memory, sketch, copy B back."""
@@ -373,6 +430,8 @@ def run_case(args):
     out = {"case": args.case}
     if args.case == "saso":
         out.update(bench_saso(torch, rb, dev, args, stream, peaks()[0]))
+    elif args.case == "batched":
+        out.update(bench_batched(torch, rb, dev, args, stream))
     else:
         m = 1 << args.m_log2
         S = rb.DenseSkOp(rb.DenseDist(D_SK, m, rb.ScalarDist.Uniform), rb.RNGState(3))

@@ -69,7 +69,8 @@ class rbg_batch_problem(C.Structure):
     _fields_ = [("d", C.c_int64), ("n", C.c_int64), ("m", C.c_int64), ("dist", rbg_dense_dist),
                 ("seed", rbg_state), ("ro_s", C.c_int64), ("co_s", C.c_int64),
                 ("A", C.c_void_p), ("lda", C.c_int64), ("B", C.c_void_p), ("ldb", C.c_int64),
-                ("alpha", C.c_float), ("beta", C.c_float)]
+                ("alpha", C.c_float), ("beta", C.c_float), ("tile_config", C.c_int32),
+                ("reserved", C.c_int32)]
 
 
 P = C.c_void_p
@@ -137,6 +138,12 @@ SIGNATURES = {
     "rbg_lowp_status": ([C.POINTER(CI32)], C.c_int),
     "rbg_lskge3_batched": ([CI32, C.POINTER(rbg_batch_problem), CI64, CI32, P], C.c_int),
     "rbg_batched_tile_configs": ([C.POINTER(CI32)], C.c_int),
+    "rbg_batched_tile_width": ([CI32, C.POINTER(CI32)], C.c_int),
+    "rbg_batched_plan_create": ([CI32, C.POINTER(rbg_batch_problem), CI64, CI32,
+                                 C.POINTER(P)], C.c_int),
+    "rbg_batched_plan_execute": ([P, P], C.c_int),
+    "rbg_batched_plan_info": ([P, C.POINTER(CI64), C.POINTER(CI64)], C.c_int),
+    "rbg_batched_plan_destroy": ([P], C.c_int),
 }
 
 _lock = threading.Lock()

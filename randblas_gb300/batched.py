@@ -1,0 +1,245 @@
+"""Batching path: many independent left dense sketches of uneven shapes,
+
+    B_i = alpha_i * submat(S_i) * A_i + beta_i * B_i      (LSKGE3 semantics, T = float),
+
+in one persistent launch of the library's batched kernel (rbg_lskge3_batched /
+rbg_batched_plan_*).  No reference counterpart: the reference sketches one problem per call
+(RandBLAS/skge.hh:154-202).  Each problem has its own generated operator S_i (its own
+RNGState), data A_i and output B_i, all row-major or all column-major CUDA tensors.
+
+* :func:`sketch_batched` -- one stream-ordered call.
+* :class:`BatchedPlan` -- validate and upload once, then :meth:`BatchedPlan.execute` (a memset
+  and one kernel launch, capturable) or :meth:`BatchedPlan.capture` into a CUDA graph.
+* :class:`Autotuner` -- picks each problem's tile width (128, 64 or 32 columns) per shape
+  class by timing the candidates on the device, and caches the choices as JSON.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import json
+import math
+import os
+import threading
+from dataclasses import dataclass
+from typing import Callable, Dict, List, Optional, Sequence
+
+import torch
+
+from . import _lib
+from ._lib import ERROR_INVALID_ARGUMENT, RandBLASError, call
+from .api import DenseSkOp, Layout, _stream
+
+
+@dataclass
+class BatchProblem:
+    """One left sketch of a batch; lda / ldb default to the tight leading dimensions."""
+    S: DenseSkOp
+    A: torch.Tensor
+    B: torch.Tensor
+    d: int
+    n: int
+    m: int
+    alpha: float = 1.0
+    beta: float = 0.0
+    ro_s: int = 0
+    co_s: int = 0
+    lda: Optional[int] = None
+    ldb: Optional[int] = None
+    tile_config: int = 0
+
+
+def tile_configs() -> List[int]:
+    n = C.c_int32()
+    call("rbg_batched_tile_configs", C.byref(n))
+    return list(range(1, n.value + 1))
+
+
+def tile_width(config: int) -> int:
+    w = C.c_int32()
+    call("rbg_batched_tile_width", int(config), C.byref(w))
+    return w.value
+
+
+def _c_problems(problems: Sequence[BatchProblem], layout: Layout):
+    arr = (_lib.rbg_batch_problem * max(len(problems), 1))()
+    for i, p in enumerate(problems):
+        for t, what in ((p.A, "A"), (p.B, "B")):
+            if not t.is_cuda or t.dtype != torch.float32:
+                raise RandBLASError(ERROR_INVALID_ARGUMENT, f"{what} must be an FP32 CUDA tensor")
+        if p.S.dtype != torch.float32 or p.S.buff is not None:
+            raise RandBLASError(ERROR_INVALID_ARGUMENT,
+                                "batched operators are FP32 and generated (unfilled)")
+        row = Layout(layout) == Layout.RowMajor
+        lda = p.lda if p.lda is not None else (p.n if row else p.m)
+        ldb = p.ldb if p.ldb is not None else (p.n if row else p.d)
+        q = arr[i]
+        q.d, q.n, q.m = p.d, p.n, p.m
+        q.dist = p.S.dist._c()
+        q.seed = p.S.seed_state._c()
+        q.ro_s, q.co_s = p.ro_s, p.co_s
+        q.A, q.lda = p.A.data_ptr(), lda
+        q.B, q.ldb = p.B.data_ptr(), ldb
+        q.alpha, q.beta = float(p.alpha), float(p.beta)
+        q.tile_config = int(p.tile_config)
+    return arr
+
+
+def sketch_batched(problems: Sequence[BatchProblem], layout: Layout = Layout.RowMajor,
+                   tile_config: int = 0, tuner: Optional["Autotuner"] = None) -> None:
+    """All problems in one persistent launch on the current stream (stream-ordered)."""
+    if tuner is not None:
+        tuner.assign(problems)
+    arr = _c_problems(problems, layout)
+    call("rbg_lskge3_batched", int(layout), arr, len(problems), int(tile_config), _stream())
+
+
+class BatchedPlan:
+    """A batch validated and uploaded once; execute() is a memset plus one kernel launch on
+    the current stream.  The plan keeps references to the problems' tensors."""
+
+    def __init__(self, problems: Sequence[BatchProblem], layout: Layout = Layout.RowMajor,
+                 tile_config: int = 0, tuner: Optional["Autotuner"] = None):
+        if tuner is not None:
+            tuner.assign(problems)
+        self._keep = [(p.A, p.B) for p in problems]
+        arr = _c_problems(problems, layout)
+        h = C.c_void_p()
+        call("rbg_batched_plan_create", int(layout), arr, len(problems), int(tile_config),
+             C.byref(h))
+        self._h = h
+        self.flops = sum(2.0 * p.d * p.n * p.m for p in problems)
+
+    def execute(self) -> None:
+        if self._h is None:
+            raise RandBLASError(ERROR_INVALID_ARGUMENT, "plan is closed")
+        call("rbg_batched_plan_execute", self._h, _stream())
+
+    def info(self):
+        items, nbytes = C.c_int64(), C.c_int64()
+        call("rbg_batched_plan_info", self._h, C.byref(items), C.byref(nbytes))
+        return {"work_items": items.value, "device_bytes": nbytes.value}
+
+    def capture(self) -> torch.cuda.CUDAGraph:
+        """A CUDA graph holding one execute(); replay() reruns the whole batch."""
+        side = torch.cuda.Stream()
+        side.wait_stream(torch.cuda.current_stream())
+        with torch.cuda.stream(side):
+            self.execute()  # warm-up outside the capture
+        torch.cuda.current_stream().wait_stream(side)
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g):
+            self.execute()
+        return g
+
+    def close(self) -> None:
+        if self._h is not None:
+            torch.cuda.synchronize()
+            call("rbg_batched_plan_destroy", self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            if self._h is not None and _lib is not None:
+                _lib.lib().rbg_batched_plan_destroy(self._h)
+        except Exception:
+            pass
+
+
+def _default_cache_path() -> str:
+    env = os.environ.get("RBG_AUTOTUNE_CACHE")
+    if env:
+        return env
+    return os.path.join(os.path.expanduser("~"), ".cache", "randblas_gb300", "batched_tiles.json")
+
+
+class Autotuner:
+    """Per-shape-class choice of the batched kernel's tile width.
+
+    A problem's class is (n rounded up to a power of two, round(log2 m)); d does not enter
+    because the tile is always 128 rows.  The first time a class is seen on a device, every
+    tile configuration runs a synthetic batch of that class (problems enough to fill the
+    device, Gaussian operators, N(0,1) data) and the fastest is kept.  Choices are stored in
+    a JSON file keyed by device name, so later processes reuse them.
+    ``measure(config, d, n, m) -> seconds`` can replace the device timing (tests)."""
+
+    def __init__(self, cache_path: Optional[str] = None,
+                 measure: Optional[Callable[[int, int, int, int], float]] = None,
+                 m_cap: int = 1 << 15):
+        self.cache_path = cache_path or _default_cache_path()
+        self._measure = measure or self._time_config
+        self.m_cap = m_cap
+        self._lock = threading.Lock()
+        self.cache: Dict[str, Dict[str, int]] = {}
+        if os.path.exists(self.cache_path):
+            try:
+                with open(self.cache_path) as f:
+                    self.cache = json.load(f)
+            except (OSError, ValueError):
+                self.cache = {}
+
+    @staticmethod
+    def shape_class(d: int, n: int, m: int) -> str:
+        nb = 16
+        while nb < n:
+            nb *= 2
+        mb = int(round(math.log2(max(m, 1))))
+        return f"n{nb}_m{mb}"
+
+    def _device_key(self) -> str:
+        if self._measure is not self._time_config:
+            return "external"
+        p = torch.cuda.get_device_properties(torch.cuda.current_device())
+        return f"{p.name}/{p.multi_processor_count}sm"
+
+    def choose(self, d: int, n: int, m: int) -> int:
+        key = self.shape_class(d, n, m)
+        dev = self._device_key()
+        with self._lock:
+            hit = self.cache.get(dev, {}).get(key)
+        if hit is not None:
+            return int(hit)
+        times = {c: self._measure(c, d, n, m) for c in tile_configs()}
+        best = min(times, key=lambda c: (times[c], c))
+        with self._lock:
+            self.cache.setdefault(dev, {})[key] = best
+            self._save()
+        return best
+
+    def assign(self, problems: Sequence[BatchProblem]) -> None:
+        for p in problems:
+            if p.tile_config == 0:
+                p.tile_config = self.choose(p.d, p.n, p.m)
+
+    def _save(self) -> None:
+        try:
+            os.makedirs(os.path.dirname(self.cache_path) or ".", exist_ok=True)
+            tmp = self.cache_path + ".tmp"
+            with open(tmp, "w") as f:
+                json.dump(self.cache, f, indent=1, sort_keys=True)
+            os.replace(tmp, self.cache_path)
+        except OSError:
+            pass
+
+    def _time_config(self, config: int, d: int, n: int, m: int) -> float:
+        from .api import DenseDist, RNGState, ScalarDist
+        m = min(m, self.m_cap)
+        sms = torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
+        tiles = math.ceil(d / 128) * math.ceil(n / tile_width(config))
+        count = max(2, min(64, math.ceil(2 * sms / max(tiles, 1))))
+        g = torch.Generator(device="cuda").manual_seed(0)
+        probs = []
+        for i in range(count):
+            S = DenseSkOp(DenseDist(d, m, ScalarDist.Gaussian), RNGState(i))
+            A = torch.randn(m, n, device="cuda", generator=g)
+            B = torch.empty(d, n, device="cuda")
+            probs.append(BatchProblem(S, A, B, d, n, m, tile_config=config))
+        plan = BatchedPlan(probs)
+        plan.execute()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(3):
+            plan.execute()
+        e1.record()
+        torch.cuda.synchronize()
+        plan.close()
+        return e0.elapsed_time(e1) / 3e3

@@ -236,7 +236,7 @@ size_t align256(size_t x) { return (x + 255) / 256 * 256; }
 // Validate the problems and build the descriptors and the sorted work list (host only).
 void build_plan(int32_t layout, const rbg_batch_problem *problems, int64_t count,
                 int32_t tile_config, std::vector<ProbDev> &descs, std::vector<WorkItem> &items,
-                int64_t &partial_floats, int64_t &tile_counters, int grid) {
+                int64_t &partial_floats, int64_t &tile_counters, int &grid) {
     if (layout != RBG_COL_MAJOR && layout != RBG_ROW_MAJOR)
         fail(RBG_ERROR_INVALID_ARGUMENT, "layout must be RBG_COL_MAJOR or RBG_ROW_MAJOR");
     if (count < 0) fail(RBG_ERROR_INVALID_ARGUMENT, "count must be >= 0");
@@ -303,7 +303,9 @@ void build_plan(int32_t layout, const rbg_batch_problem *problems, int64_t count
         const int64_t tiles = ((pd.M + BM - 1) / BM) * pd.tiles_n;
         total_cost += (double)tiles * (double)std::max<int64_t>(kt[p], 1) * pd.bn;
     }
-    // split long K so that no item costs more than ~1/8 of a CTA's fair share
+    // split long K so that no item costs more than ~1/8 of a CTA's fair share (the device is
+    // queried only after every argument has been checked)
+    grid = resident_batched_ctas();
     const double cap = std::max(total_cost / (8.0 * std::max(grid, 1)), 128.0 * 64.0);
     for (int64_t p = 0; p < count; ++p) {
         ProbDev &pd = descs[p];
@@ -417,7 +419,7 @@ extern "C" int rbg_batched_plan_create(int32_t layout, const rbg_batch_problem *
         std::vector<ProbDev> descs;
         std::vector<WorkItem> items;
         int64_t partial_floats = 0, tile_counters = 0;
-        const int grid = resident_batched_ctas();
+        int grid = 0;
         build_plan(layout, problems, count, tile_config, descs, items, partial_floats,
                    tile_counters, grid);
         auto *pl = new BatchedPlan();
@@ -464,7 +466,7 @@ extern "C" int rbg_lskge3_batched(int32_t layout, const rbg_batch_problem *probl
         std::vector<ProbDev> descs;
         std::vector<WorkItem> items;
         int64_t partial_floats = 0, tile_counters = 0;
-        const int grid = resident_batched_ctas();
+        int grid = 0;
         build_plan(layout, problems, count, tile_config, descs, items, partial_floats,
                    tile_counters, grid);
         if (items.empty()) return;

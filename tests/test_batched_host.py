@@ -1,0 +1,60 @@
+"""Host side of the batching path (no GPU): tile configuration listing, argument checks that
+fire before any device work, and the autotuner's choice and JSON cache."""
+import json
+
+import pytest
+
+
+def test_tile_configs(rb_host):
+    from randblas_gb300 import batched
+    cfgs = batched.tile_configs()
+    assert cfgs == [1, 2, 3]
+    assert [batched.tile_width(c) for c in cfgs] == [128, 64, 32]
+    with pytest.raises(rb_host.RandBLASError):
+        batched.tile_width(4)
+
+
+def test_batched_argument_checks(rb_host):
+    import ctypes as C
+    from randblas_gb300 import _lib
+    lib = _lib.lib()
+    arr = (_lib.rbg_batch_problem * 1)()
+    q = arr[0]
+    q.d, q.n, q.m = 8, 4, 100
+    q.dist = _lib.rbg_dense_dist(8, 50, _lib.GAUSSIAN, _lib.AXIS_LONG)
+    q.lda, q.ldb = 4, 4
+    q.alpha = 1.0
+    h = C.c_void_p()
+    # S too small for m = 100 columns
+    rc = lib.rbg_batched_plan_create(1, arr, 1, 0, C.byref(h))
+    assert rc == _lib.ERROR_INVALID_ARGUMENT
+    assert b"was required, but did not hold, in function lskge3_batched" in lib.rbg_last_error()
+    q.dist = _lib.rbg_dense_dist(8, 100, _lib.GAUSSIAN, _lib.AXIS_LONG)
+    q.lda = 3  # < n for row-major
+    assert lib.rbg_batched_plan_create(1, arr, 1, 0, C.byref(h)) == _lib.ERROR_INVALID_ARGUMENT
+    assert lib.rbg_batched_plan_create(7, arr, 1, 0, C.byref(h)) == _lib.ERROR_INVALID_ARGUMENT
+    assert lib.rbg_batched_plan_create(1, arr, 1, 9, C.byref(h)) == _lib.ERROR_INVALID_ARGUMENT
+
+
+def test_autotuner_choice_and_cache(rb_host, tmp_path):
+    from randblas_gb300 import batched
+    calls = []
+
+    def measure(cfg, d, n, m):
+        calls.append((cfg, n))
+        # pretend narrow problems like narrow tiles
+        return {1: 3.0, 2: 2.0, 3: 1.0}[cfg] if n <= 32 else {1: 1.0, 2: 2.0, 3: 3.0}[cfg]
+
+    path = str(tmp_path / "tiles.json")
+    t = batched.Autotuner(cache_path=path, measure=measure)
+    assert t.choose(64, 16, 5000) == 3
+    assert t.choose(512, 128, 1 << 16) == 1
+    n_calls = len(calls)
+    assert t.choose(100, 20, 4800) == 3  # same class (n16.. rounds to 32? no: 20 -> 32)
+    assert batched.Autotuner.shape_class(64, 16, 5000) == "n16_m12"
+    assert batched.Autotuner.shape_class(100, 20, 4800) == "n32_m12"
+    saved = json.load(open(path))
+    assert saved["external"]["n16_m12"] == 3 and saved["external"]["n128_m16"] == 1
+    t2 = batched.Autotuner(cache_path=path, measure=lambda *a: pytest.fail("re-tuned"))
+    assert t2.choose(64, 16, 5000) == 3
+    assert len(calls) >= n_calls
