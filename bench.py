@@ -383,10 +383,12 @@ def bench_batched(torch, rb, device, args, stream):
         res[name] = {"ms": round(ms, 2), "TFLOP/s": round(flops / ms / 1e9, 2),
                      "speedup_vs_separate": round(ms_sep / ms, 2),
                      "work_items": plan.info()["work_items"]}
-        if tuner is not None:
-            res[name]["tile_widths"] = {str(w): sum(1 for p in probs if
-                                                    batched.tile_width(p.tile_config) == w)
-                                        for w in (128, 64, 32)}
+        shapes = {}
+        for p in probs:
+            key = "x".join(map(str, batched.tile_shape(p.tile_config))) if p.tile_config \
+                else "library"
+            shapes[key] = shapes.get(key, 0) + 1
+        res[name]["tiles"] = shapes
         plan.close()
     return res
 

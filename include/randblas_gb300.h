@@ -132,6 +132,12 @@ int rbg_version(void);
 /* Number of CUDA kernels this library has launched in this process (its own kernels; the
  * radix-sort passes it delegates to CUB are not counted).  No reference counterpart. */
 uint64_t rbg_kernel_launches(void);
+/* Reproducibility switch, no reference counterpart (process-wide).  On: every path adds in a
+ * fixed order, so results are bitwise reproducible run to run.  Off (default): the fused SASO
+ * left sketch accumulates with shared-memory reductions whose order depends on scheduling
+ * (results agree to FP32 rounding).  rbg_get_deterministic returns the current setting. */
+int rbg_set_deterministic(int on);
+int rbg_get_deterministic(void);
 /* Per-kernel timing, no reference counterpart.  While enabled, the library records CUDA events
  * on the launching stream around its main kernels; rbg_profile_enable also clears what was
  * recorded.  rbg_profile_entry synchronises on the recorded events. */
@@ -336,8 +342,8 @@ int rbg_lskge3_batched(int32_t layout, const rbg_batch_problem *problems, int64_
                        int32_t tile_config, rbg_stream_t stream);
 /* Number of tile configurations the batched kernel offers (ids 1..count). */
 int rbg_batched_tile_configs(int32_t *count);
-/* Output tile width (columns) of configuration `config`; every configuration is 128 rows. */
-int rbg_batched_tile_width(int32_t config, int32_t *width);
+/* Output tile shape (rows x columns) of configuration `config`. */
+int rbg_batched_tile_shape(int32_t config, int32_t *rows, int32_t *cols);
 
 /* A reusable batch: validates the problems and uploads the work list once (synchronous);
  * rbg_batched_plan_execute then only zeroes the plan's counters and launches the persistent

@@ -9,8 +9,8 @@ from . import autograd, lowp, profile  # noqa: F401
 from ._lib import RandBLASError, lib  # noqa: F401
 from .api import (  # noqa: F401
     Axis, COOMatrix, CSCMatrix, CSRMatrix, DenseDist, DenseSkOp, Layout, Op, RNGState,
-    ScalarDist, SparseDist, SparseSkOp, fill_dense, fill_dense_unpacked, fill_sparse,
+    ScalarDist, SparseDist, SparseSkOp, deterministic, fill_dense, fill_dense_unpacked, fill_sparse,
     fill_sparse_unpacked_nosub, left_spmm, repeated_fisher_yates, right_spmm, sketch_general,
-    sketch_sparse, sketch_vector, spmm)
+    set_deterministic, sketch_sparse, sketch_vector, spmm)
 
 __version__ = "1.1.0"

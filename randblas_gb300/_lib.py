@@ -83,6 +83,8 @@ PS = C.POINTER(rbg_state)
 SIGNATURES = {
     "rbg_last_error": ([], C.c_char_p),
     "rbg_version": ([], C.c_int),
+    "rbg_set_deterministic": ([C.c_int], C.c_int),
+    "rbg_get_deterministic": ([], C.c_int),
     "rbg_kernel_launches": ([], C.c_uint64),
     "rbg_profile_enable": ([C.c_int], C.c_int),
     "rbg_profile_count": ([C.POINTER(CI32)], C.c_int),
@@ -138,7 +140,7 @@ SIGNATURES = {
     "rbg_lowp_status": ([C.POINTER(CI32)], C.c_int),
     "rbg_lskge3_batched": ([CI32, C.POINTER(rbg_batch_problem), CI64, CI32, P], C.c_int),
     "rbg_batched_tile_configs": ([C.POINTER(CI32)], C.c_int),
-    "rbg_batched_tile_width": ([CI32, C.POINTER(CI32)], C.c_int),
+    "rbg_batched_tile_shape": ([CI32, C.POINTER(CI32), C.POINTER(CI32)], C.c_int),
     "rbg_batched_plan_create": ([CI32, C.POINTER(rbg_batch_problem), CI64, CI32,
                                  C.POINTER(P)], C.c_int),
     "rbg_batched_plan_execute": ([P, P], C.c_int),

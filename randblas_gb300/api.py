@@ -56,6 +56,17 @@ def _ptr(t: Optional[torch.Tensor]):
     return C.c_void_p(t.data_ptr())
 
 
+def set_deterministic(on: bool) -> None:
+    """Process-wide reproducibility switch (no reference counterpart): when on, every path
+    adds in a fixed order; when off (default) the fused SASO sketch may vary in its last bits
+    between runs."""
+    call("rbg_set_deterministic", 1 if on else 0)
+
+
+def deterministic() -> bool:
+    return bool(_lib.lib().rbg_get_deterministic())
+
+
 # ------------------------------------------------------------------------- RNGState
 class RNGState:
     """RNGState<Philox4x32> (RandBLAS/base.hh:64-164): 128-bit counter, 64-bit key."""

@@ -10,8 +10,9 @@ RNGState), data A_i and output B_i, all row-major or all column-major CUDA tenso
 * :func:`sketch_batched` -- one stream-ordered call.
 * :class:`BatchedPlan` -- validate and upload once, then :meth:`BatchedPlan.execute` (a memset
   and one kernel launch, capturable) or :meth:`BatchedPlan.capture` into a CUDA graph.
-* :class:`Autotuner` -- picks each problem's tile width (128, 64 or 32 columns) per shape
-  class by timing the candidates on the device, and caches the choices as JSON.
+* :class:`Autotuner` -- picks each problem's output tile (128 x 128, 128 x 64, 128 x 32 or
+  64 x 256) per shape class by timing every candidate on the same synthetic batch on the
+  device, and caches the choices as JSON.
 """
 from __future__ import annotations
 
@@ -54,10 +55,11 @@ def tile_configs() -> List[int]:
     return list(range(1, n.value + 1))
 
 
-def tile_width(config: int) -> int:
-    w = C.c_int32()
-    call("rbg_batched_tile_width", int(config), C.byref(w))
-    return w.value
+def tile_shape(config: int):
+    """(rows, columns) of the output tile of a configuration."""
+    r, c = C.c_int32(), C.c_int32()
+    call("rbg_batched_tile_shape", int(config), C.byref(r), C.byref(c))
+    return r.value, c.value
 
 
 def _c_problems(problems: Sequence[BatchProblem], layout: Layout):
@@ -153,20 +155,20 @@ def _default_cache_path() -> str:
 
 
 class Autotuner:
-    """Per-shape-class choice of the batched kernel's tile width.
+    """Per-shape-class choice of the batched kernel's output tile.
 
-    A problem's class is (n rounded up to a power of two, round(log2 m)); d does not enter
-    because the tile is always 128 rows.  The first time a class is seen on a device, every
-    tile configuration runs a synthetic batch of that class (problems enough to fill the
-    device, Gaussian operators, N(0,1) data) and the fastest is kept.  Choices are stored in
-    a JSON file keyed by device name, so later processes reuse them.
-    ``measure(config, d, n, m) -> seconds`` can replace the device timing (tests)."""
+    A problem's class is (operator family, d, n rounded up to powers of two, round(log2 m)).
+    The first time a class is seen on a device, one synthetic batch of that class (problems
+    enough to fill the device, N(0,1) data) runs once per tile configuration and the fastest
+    is kept.  Choices are stored in a JSON file keyed by device name, so later processes
+    reuse them.  ``measure(config, d, n, m, family) -> seconds`` can replace the device
+    timing (tests)."""
 
     def __init__(self, cache_path: Optional[str] = None,
-                 measure: Optional[Callable[[int, int, int, int], float]] = None,
-                 m_cap: int = 1 << 15):
+                 measure: Optional[Callable[[int, int, int, int, int], float]] = None,
+                 m_cap: int = 1 << 16):
         self.cache_path = cache_path or _default_cache_path()
-        self._measure = measure or self._time_config
+        self._external = measure
         self.m_cap = m_cap
         self._lock = threading.Lock()
         self.cache: Dict[str, Dict[str, int]] = {}
@@ -178,27 +180,34 @@ class Autotuner:
                 self.cache = {}
 
     @staticmethod
-    def shape_class(d: int, n: int, m: int) -> str:
-        nb = 16
-        while nb < n:
-            nb *= 2
+    def _pow2(x: int, lo: int) -> int:
+        b = lo
+        while b < x:
+            b *= 2
+        return b
+
+    @classmethod
+    def shape_class(cls, d: int, n: int, m: int, family: int = 0) -> str:
         mb = int(round(math.log2(max(m, 1))))
-        return f"n{nb}_m{mb}"
+        return f"f{int(family)}_d{cls._pow2(d, 16)}_n{cls._pow2(n, 16)}_m{mb}"
 
     def _device_key(self) -> str:
-        if self._measure is not self._time_config:
+        if self._external is not None:
             return "external"
         p = torch.cuda.get_device_properties(torch.cuda.current_device())
         return f"{p.name}/{p.multi_processor_count}sm"
 
-    def choose(self, d: int, n: int, m: int) -> int:
-        key = self.shape_class(d, n, m)
+    def choose(self, d: int, n: int, m: int, family: int = 0) -> int:
+        key = self.shape_class(d, n, m, family)
         dev = self._device_key()
         with self._lock:
             hit = self.cache.get(dev, {}).get(key)
         if hit is not None:
             return int(hit)
-        times = {c: self._measure(c, d, n, m) for c in tile_configs()}
+        if self._external is not None:
+            times = {c: self._external(c, d, n, m, family) for c in tile_configs()}
+        else:
+            times = self._time_all(d, n, m, family)
         best = min(times, key=lambda c: (times[c], c))
         with self._lock:
             self.cache.setdefault(dev, {})[key] = best
@@ -208,7 +217,7 @@ class Autotuner:
     def assign(self, problems: Sequence[BatchProblem]) -> None:
         for p in problems:
             if p.tile_config == 0:
-                p.tile_config = self.choose(p.d, p.n, p.m)
+                p.tile_config = self.choose(p.d, p.n, p.m, int(p.S.dist.family))
 
     def _save(self) -> None:
         try:
@@ -220,26 +229,31 @@ class Autotuner:
         except OSError:
             pass
 
-    def _time_config(self, config: int, d: int, n: int, m: int) -> float:
+    def _time_all(self, d: int, n: int, m: int, family: int) -> Dict[int, float]:
+        """Seconds per run of one synthetic batch of the class, for every configuration."""
         from .api import DenseDist, RNGState, ScalarDist
         m = min(m, self.m_cap)
         sms = torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
-        tiles = math.ceil(d / 128) * math.ceil(n / tile_width(config))
-        count = max(2, min(64, math.ceil(2 * sms / max(tiles, 1))))
+        tiles = math.ceil(d / 128) * math.ceil(n / 128)
+        count = max(2, min(64, math.ceil(4 * sms / max(tiles, 1))))
         g = torch.Generator(device="cuda").manual_seed(0)
         probs = []
         for i in range(count):
-            S = DenseSkOp(DenseDist(d, m, ScalarDist.Gaussian), RNGState(i))
+            S = DenseSkOp(DenseDist(d, m, ScalarDist(family)), RNGState(i))
             A = torch.randn(m, n, device="cuda", generator=g)
-            B = torch.empty(d, n, device="cuda")
-            probs.append(BatchProblem(S, A, B, d, n, m, tile_config=config))
-        plan = BatchedPlan(probs)
-        plan.execute()
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record()
-        for _ in range(3):
+            probs.append(BatchProblem(S, A, torch.empty(d, n, device="cuda"), d, n, m))
+        times = {}
+        for c in tile_configs():
+            for p in probs:
+                p.tile_config = c
+            plan = BatchedPlan(probs)
             plan.execute()
-        e1.record()
-        torch.cuda.synchronize()
-        plan.close()
-        return e0.elapsed_time(e1) / 3e3
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            for _ in range(3):
+                plan.execute()
+            e1.record()
+            torch.cuda.synchronize()
+            plan.close()
+            times[c] = e0.elapsed_time(e1) / 3e3
+        return times

@@ -28,9 +28,15 @@ using simt::BK;
 using simt::BM;
 using simt::NT;
 
-constexpr int kConfigs = 3;
-constexpr int kTileWidth[kConfigs + 1] = {0, 128, 64, 32};  // config id -> BN
+constexpr int kConfigs = 4;
+// config id -> output tile (rows x columns); every configuration is 256 threads with 8 x TN
+// accumulators each.  The operator tile (rows x 16 per k step) is generated once per output
+// tile, so wider tiles spend less on generation per FLOP and narrower ones waste less on
+// padding columns.
+constexpr int kTileRows[kConfigs + 1] = {0, 128, 128, 128, 64};
+constexpr int kTileWidth[kConfigs + 1] = {0, 128, 64, 32, 256};
 constexpr int kMaxSplits = 64;
+constexpr int kQsFloats = BK * (256 + 4);
 
 struct ProbDev {
     POperand P;       // generated operator
@@ -39,7 +45,7 @@ struct ProbDev {
     int64_t os_i, os_j;
     int64_t M, N, K;  // d, n, m (K = 0 when alpha == 0 or m == 0)
     float alpha, beta;
-    int32_t bn;       // tile width
+    int32_t bm, bn;   // output tile rows and columns
     int32_t splits;
     int64_t kt_per_split;
     int64_t tiles_n;
@@ -53,15 +59,17 @@ struct WorkItem {
     int64_t tile;
 };
 
-// One output tile (or one K split of it) of problem `pb`.  TN = columns per thread.
-template <int TN>
+// One output tile (or one K split of it) of problem `pb`: BMT x BNT, TN columns per thread.
+template <int BMT, int BNT, int TN>
 __device__ __forceinline__ void batched_tile(const ProbDev &pb, int64_t tile, int split,
-                                             float (*Ps)[BM + 4], float *qs_raw, float *partial,
+                                             float *ps_raw, float *qs_raw, float *partial,
                                              int *counters, int *s_flag) {
-    constexpr int BNT = TN * 16;
+    constexpr int TX = BNT / TN;  // thread columns
+    static_assert(TX * (BMT / 8) == NT, "one 8 x TN block per thread");
+    float(*Ps)[BMT + 4] = reinterpret_cast<float(*)[BMT + 4]>(ps_raw);
     float(*Qs)[BNT + 4] = reinterpret_cast<float(*)[BNT + 4]>(qs_raw);
-    const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
-    const int64_t i0 = (tile / pb.tiles_n) * BM, j0 = (tile % pb.tiles_n) * BNT;
+    const int tx = threadIdx.x % TX, ty = threadIdx.x / TX;
+    const int64_t i0 = (tile / pb.tiles_n) * BMT, j0 = (tile % pb.tiles_n) * BNT;
     const int64_t kt_total = (pb.K + BK - 1) / BK;
     const int64_t kb = (int64_t)split * pb.kt_per_split;
     const int64_t ke = min(kt_total, kb + pb.kt_per_split);
@@ -75,7 +83,7 @@ __device__ __forceinline__ void batched_tile(const ProbDev &pb, int64_t tile, in
 
     for (int64_t kt = kb; kt < ke; ++kt) {
         const int64_t k0 = kt * BK;
-        simt::gen_p_tile<float>(Ps, pb.P, pb.M, pb.K, i0, k0);
+        simt::gen_p_tile<float, BMT>(Ps, pb.P, pb.M, pb.K, i0, k0);
         simt::load_tile<float, BNT>(Qs, Qp, pb.Q.s0, pb.Q.s1, pb.K, pb.N, k0, j0);
         __syncthreads();
 #pragma unroll
@@ -84,7 +92,7 @@ __device__ __forceinline__ void batched_tile(const ProbDev &pb, int64_t tile, in
 #pragma unroll
             for (int q = 0; q < 4; ++q) {
                 a[q] = Ps[kk][ty * 4 + q];
-                a[4 + q] = Ps[kk][64 + ty * 4 + q];
+                a[4 + q] = Ps[kk][BMT / 2 + ty * 4 + q];
             }
 #pragma unroll
             for (int q = 0; q < TN / 2; ++q) {
@@ -99,7 +107,7 @@ __device__ __forceinline__ void batched_tile(const ProbDev &pb, int64_t tile, in
         __syncthreads();
     }
 
-    auto row_of = [&](int x) { return i0 + (x < 4 ? ty * 4 + x : 64 + ty * 4 + (x - 4)); };
+    auto row_of = [&](int x) { return i0 + (x < 4 ? ty * 4 + x : BMT / 2 + ty * 4 + (x - 4)); };
     auto col_of = [&](int y) {
         return j0 + (y < TN / 2 ? tx * (TN / 2) + y : BNT / 2 + tx * (TN / 2) + (y - TN / 2));
     };
@@ -140,7 +148,7 @@ __device__ __forceinline__ void batched_tile(const ProbDev &pb, int64_t tile, in
     if (!*s_flag) return;
     __threadfence();
     const float *base = partial + pb.partial_off;
-    for (int w = threadIdx.x; w < BM * BNT; w += NT) {
+    for (int w = threadIdx.x; w < BMT * BNT; w += NT) {
         const int64_t i = i0 + w / BNT, j = j0 + w % BNT;
         if (i >= pb.M || j >= pb.N) continue;
         float sum = 0.f;
@@ -154,8 +162,8 @@ __global__ void __launch_bounds__(NT, 2)
     batched_sketch_kernel(const ProbDev *__restrict__ probs, const WorkItem *__restrict__ items,
                           int64_t n_items, unsigned long long *work_counter,
                           float *__restrict__ partial, int *__restrict__ counters) {
-    __shared__ __align__(16) float Ps[BK][BM + 4];
-    __shared__ __align__(16) float Qs[BK * (128 + 4)];
+    __shared__ __align__(16) float Ps[BK * (BM + 4)];
+    __shared__ __align__(16) float Qs[kQsFloats];
     __shared__ ProbDev s_pb;
     __shared__ WorkItem s_item;
     __shared__ int s_flag;
@@ -172,11 +180,14 @@ __global__ void __launch_bounds__(NT, 2)
         if (s_w >= (unsigned long long)n_items) break;
         const int64_t tile = s_item.tile;
         const int split = s_item.split;
-        switch (s_pb.bn) {
-            case 128: batched_tile<8>(s_pb, tile, split, Ps, Qs, partial, counters, &s_flag); break;
-            case 64: batched_tile<4>(s_pb, tile, split, Ps, Qs, partial, counters, &s_flag); break;
-            default: batched_tile<2>(s_pb, tile, split, Ps, Qs, partial, counters, &s_flag); break;
-        }
+        if (s_pb.bm == 64)
+            batched_tile<64, 256, 8>(s_pb, tile, split, Ps, Qs, partial, counters, &s_flag);
+        else if (s_pb.bn == 128)
+            batched_tile<128, 128, 8>(s_pb, tile, split, Ps, Qs, partial, counters, &s_flag);
+        else if (s_pb.bn == 64)
+            batched_tile<128, 64, 4>(s_pb, tile, split, Ps, Qs, partial, counters, &s_flag);
+        else
+            batched_tile<128, 32, 2>(s_pb, tile, split, Ps, Qs, partial, counters, &s_flag);
         __syncthreads();  // s_pb / s_item / s_w are rewritten by the next fetch
     }
 }
@@ -192,17 +203,20 @@ int resident_batched_ctas() {
     return per_sm * num_sms();
 }
 
-// Tile width by wasted columns: the widest tile whose padding stays small.
-int default_config(int64_t n) {
+// Tile by a cost model, per k step of 16 and in thread instructions: FMAs over the whole
+// (padded) tile, plus generating its operator rows (Gaussian entries cost about ten times
+// uniform ones), plus staging the data tile.
+int default_config(int64_t m_rows, int64_t n, int family) {
+    const double gen = family == RBG_GAUSSIAN ? 100.0 : 10.0;
     int best = 1;
-    double best_score = -1.0;
-    static const double eff[kConfigs + 1] = {0.0, 1.0, 0.88, 0.7};  // relative FLOP rates
+    double best_cost = 0.0;
     for (int c = 1; c <= kConfigs; ++c) {
-        const int64_t bn = kTileWidth[c];
-        const double used = (double)n / (double)(((n + bn - 1) / bn) * bn);
-        const double score = used * eff[c];
-        if (score > best_score + 1e-12) {
-            best_score = score;
+        const double bm = kTileRows[c], bn = kTileWidth[c];
+        const double tiles = (double)((m_rows + kTileRows[c] - 1) / kTileRows[c]) *
+                             (double)((n + kTileWidth[c] - 1) / kTileWidth[c]);
+        const double cost = tiles * (bm * bn + bm * gen + 2.0 * bn);
+        if (c == 1 || cost < best_cost * 0.999) {
+            best_cost = cost;
             best = c;
         }
     }
@@ -297,21 +311,23 @@ void build_plan(int32_t layout, const rbg_batch_problem *problems, int64_t count
         pd.out = q.B;
         pd.os_i = layout == RBG_ROW_MAJOR ? q.ldb : 1;
         pd.os_j = layout == RBG_ROW_MAJOR ? 1 : q.ldb;
-        pd.bn = kTileWidth[cfg ? cfg : default_config(pd.N)];
+        const int c = cfg ? cfg : default_config(pd.M, pd.N, q.dist.family);
+        pd.bm = kTileRows[c];
+        pd.bn = kTileWidth[c];
         pd.tiles_n = (pd.N + pd.bn - 1) / pd.bn;
         kt[p] = (pd.K + BK - 1) / BK;
-        const int64_t tiles = ((pd.M + BM - 1) / BM) * pd.tiles_n;
-        total_cost += (double)tiles * (double)std::max<int64_t>(kt[p], 1) * pd.bn;
+        const int64_t tiles = ((pd.M + pd.bm - 1) / pd.bm) * pd.tiles_n;
+        total_cost += (double)tiles * (double)std::max<int64_t>(kt[p], 1) * pd.bm * pd.bn;
     }
     // split long K so that no item costs more than ~1/8 of a CTA's fair share (the device is
     // queried only after every argument has been checked)
     grid = resident_batched_ctas();
-    const double cap = std::max(total_cost / (8.0 * std::max(grid, 1)), 128.0 * 64.0);
+    const double cap = std::max(total_cost / (8.0 * std::max(grid, 1)), 128.0 * 128.0 * 64.0);
     for (int64_t p = 0; p < count; ++p) {
         ProbDev &pd = descs[p];
         if (pd.M == 0 || pd.N == 0) continue;
-        const int64_t tiles = ((pd.M + BM - 1) / BM) * pd.tiles_n;
-        const int64_t cap_kt = std::max<int64_t>(32, (int64_t)(cap / pd.bn));
+        const int64_t tiles = ((pd.M + pd.bm - 1) / pd.bm) * pd.tiles_n;
+        const int64_t cap_kt = std::max<int64_t>(32, (int64_t)(cap / ((double)pd.bm * pd.bn)));
         int64_t splits = kt[p] > 0 ? (kt[p] + cap_kt - 1) / cap_kt : 1;
         splits = std::min<int64_t>(splits, kMaxSplits);
         pd.kt_per_split = kt[p] > 0 ? (kt[p] + splits - 1) / splits : 0;
@@ -329,7 +345,7 @@ void build_plan(int32_t layout, const rbg_batch_problem *problems, int64_t count
     // longest processing time first; ties keep problem order
     std::stable_sort(items.begin(), items.end(), [&](const WorkItem &a, const WorkItem &b) {
         const ProbDev &pa = descs[a.prob], &pb = descs[b.prob];
-        return (double)pa.kt_per_split * pa.bn > (double)pb.kt_per_split * pb.bn;
+        return (double)pa.kt_per_split * pa.bm * pa.bn > (double)pb.kt_per_split * pb.bm * pb.bn;
     });
 }
 
@@ -401,12 +417,13 @@ extern "C" int rbg_batched_tile_configs(int32_t *count) {
     return RBG_SUCCESS;
 }
 
-extern "C" int rbg_batched_tile_width(int32_t config, int32_t *width) {
+extern "C" int rbg_batched_tile_shape(int32_t config, int32_t *rows, int32_t *cols) {
     return guarded_batched([&] {
-        if (!width) fail(RBG_ERROR_INVALID_ARGUMENT, "width must not be NULL");
+        if (!rows || !cols) fail(RBG_ERROR_INVALID_ARGUMENT, "rows and cols must not be NULL");
         if (config < 1 || config > kConfigs)
             fail(RBG_ERROR_INVALID_ARGUMENT, "config must be one of the listed configurations");
-        *width = kTileWidth[config];
+        *rows = kTileRows[config];
+        *cols = kTileWidth[config];
     });
 }
 

@@ -788,11 +788,24 @@ bool prepare_dense_left(int32_t layout, int32_t opS, int32_t opA, int64_t d, int
     return true;
 }
 
+namespace {
+std::atomic<int> g_deterministic{0};
+}  // namespace
+
+bool deterministic_mode() { return g_deterministic.load(std::memory_order_relaxed) != 0; }
+
 }  // namespace rbg
 
 extern "C" {
 
 const char *rbg_last_error(void) { return g_last_error.c_str(); }
+
+int rbg_set_deterministic(int on) {
+    rbg::g_deterministic.store(on ? 1 : 0, std::memory_order_relaxed);
+    return RBG_SUCCESS;
+}
+
+int rbg_get_deterministic(void) { return rbg::deterministic_mode() ? 1 : 0; }
 
 int rbg_version(void) { return 10100; }
 

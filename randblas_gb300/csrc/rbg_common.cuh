@@ -7,6 +7,7 @@
 #include <cuda_runtime.h>
 
 #include "randblas_gb300.h"
+#include "rbg_ffmath.cuh"
 
 namespace rbg {
 
@@ -69,20 +70,21 @@ __device__ __forceinline__ float u01(uint32_t x) {
 }
 
 // Box-Muller for the plain paths and the explicit fills: sin, cos and log are evaluated in
-// double precision (CUDA's sincos / log) and rounded once to float, which gives the correctly
-// rounded float value except in vanishingly rare cases; then r = sqrtf(-2 * log) and the two
-// products are rounded in float exactly as the reference's host code does.  Against glibc's
-// float sinf / cosf / logf (max errors about 0.6 and 0.8 ulp) the results agree except where
-// glibc rounds the other way, and then by one or two ulp.
+// float-float arithmetic (rbg_ffmath.cuh: FP32 instructions only) and rounded once to float,
+// which gives the correctly rounded float except in vanishingly rare cases; then
+// r = sqrtf(-2 * log) and the two products are rounded in float exactly as the reference's
+// host code does.  Against glibc's float sincosf / logf (which are not correctly rounded) the
+// results agree bit for bit in about 98.5% of cases and otherwise by one or two ulp (three in
+// about 7 of 10^6, when the sine and the logarithm both round the other way).
 __device__ __forceinline__ void boxmuller(uint32_t u0, uint32_t u1, float &first,
                                           float &second) {
     const float theta = __fmul_rn(3.14159265358979323846f, uneg11(u0));
-    double s, c;
-    sincos((double)theta, &s, &c);
-    const float l = __double2float_rn(log((double)u01(u1)));
+    float s, c;
+    ff::sincosf_ff(theta, s, c);
+    const float l = ff::logf_ff(u01(u1));
     const float r = __fsqrt_rn(__fmul_rn(-2.0f, l));
-    first = __fmul_rn(__double2float_rn(s), r);
-    second = __fmul_rn(__double2float_rn(c), r);
+    first = __fmul_rn(s, r);
+    second = __fmul_rn(c, r);
 }
 
 // Box-Muller for the reduced-precision tensor-core paths, whose entries are rounded to BF16 /

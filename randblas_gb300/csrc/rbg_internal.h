@@ -132,6 +132,10 @@ bool prepare_dense_left(int32_t layout, int32_t opS, int32_t opA, int64_t d, int
 
 // --------------------------------------------------------------- sparse sketch (spmm.cu)
 // Sparse operand description for Out[M x N] = alpha * Sp[M x K] * Q[K x N] + beta * Out.
+// rbg_set_deterministic: when on, every path sums in a fixed order (bitwise reproducible);
+// when off (the default) the fused SASO sketch may add in a scheduling-dependent order.
+bool deterministic_mode();
+
 struct SparseOperand {
     enum Kind { SASO_GEN, COO, CSR, CSC } kind;
     // SASO_GEN: S generated in-kernel; Sp = op(submat(S)).

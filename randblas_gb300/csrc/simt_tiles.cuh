@@ -10,18 +10,18 @@ namespace simt {
 
 constexpr int BM = 128, BN = 128, BK = 16, NT = 256;  // tile M, max tile N, k step, threads
 
-// P tile, k-major: Ps[k][i] for i in [0, BM), k in [0, BK).  Entries outside M x K are 0.
-template <typename T>
-__device__ __forceinline__ void gen_p_tile(T (*Ps)[BM + 4], const POperand &P, int64_t M,
+// P tile, k-major: Ps[k][i] for i in [0, TM), k in [0, BK).  Entries outside M x K are 0.
+template <typename T, int TM = BM>
+__device__ __forceinline__ void gen_p_tile(T (*Ps)[TM + 4], const POperand &P, int64_t M,
                                            int64_t K, int64_t i0, int64_t k0) {
     const DenseGen &g = P.gen;
     if (P.r_on_i) {
-        // R follows i, C follows k: each of the BM rows needs the counter blocks covering
+        // R follows i, C follows k: each of the TM rows needs the counter blocks covering
         // columns [c0 + k0, c0 + k0 + BK).
         const int64_t cfirst = P.c0 + k0;
         const int64_t b0 = cfirst / 4;
         const int nb = (int)((cfirst + BK - 1) / 4 - b0 + 1);
-        for (int w = threadIdx.x; w < BM * nb; w += NT) {
+        for (int w = threadIdx.x; w < TM * nb; w += NT) {
             const int i = w / nb, b = w % nb;
             const bool row_ok = i0 + i < M;
             float v[4] = {0.f, 0.f, 0.f, 0.f};
@@ -35,10 +35,10 @@ __device__ __forceinline__ void gen_p_tile(T (*Ps)[BM + 4], const POperand &P, i
         }
     } else {
         // R follows k, C follows i: each of the BK rows needs the blocks covering columns
-        // [c0 + i0, c0 + i0 + BM).
+        // [c0 + i0, c0 + i0 + TM).
         const int64_t cfirst = P.c0 + i0;
         const int64_t b0 = cfirst / 4;
-        const int nb = (int)((cfirst + BM - 1) / 4 - b0 + 1);
+        const int nb = (int)((cfirst + TM - 1) / 4 - b0 + 1);
         for (int w = threadIdx.x; w < BK * nb; w += NT) {
             const int k = w / nb, b = w % nb;
             const bool k_ok = k0 + k < K;
@@ -47,7 +47,7 @@ __device__ __forceinline__ void gen_p_tile(T (*Ps)[BM + 4], const POperand &P, i
 #pragma unroll
             for (int l = 0; l < 4; ++l) {
                 const int64_t i = (b0 + b) * 4 + l - cfirst;
-                if (i >= 0 && i < BM)
+                if (i >= 0 && i < TM)
                     Ps[k][i] = (k_ok && i0 + i < M) ? finish_entry<T>(g.family, v[l]) : (T)0;
             }
         }

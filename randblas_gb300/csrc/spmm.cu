@@ -282,6 +282,216 @@ int grid1d(int64_t work, int threads) {
         1, std::min<int64_t>((work + threads - 1) / threads, (int64_t)num_sms() * 16));
 }
 
+// ------------------------------------------------------------------ fused SASO scatter
+// Left sketch by a SASO operator whose sparse vectors are the columns of S (short axis =
+// columns, no transpose), the shape RandBLAS's LSKGES gives a wide SparseDist
+// (RandBLAS/sparse_skops.hh:131-246, skge.hh:465-492):  B(r, :) += S(r, k) op(A)(k, :).
+// Instead of building row lists, a pre-pass samples each column's vec_nnz (row, sign) pairs
+// once into 16-bit words ((row << 1) | negative; 0xFFFF = outside submat(S)); then every CTA
+// keeps a d x 32 slice of B in shared memory and streams its share of A's rows exactly once,
+// adding each row into the vec_nnz rows of the slice with shared-memory reductions, and the
+// chunks' slices are summed in chunk order.  Additions into one slice entry arrive in a
+// scheduling-dependent order, so the last bits can vary between runs;
+// rbg_set_deterministic(1) selects the row-list path instead.
+#ifndef RBG_FUSED_THREADS
+#define RBG_FUSED_THREADS 1024
+#endif
+constexpr int kFusedCols = 32;
+constexpr int kFusedThreads = RBG_FUSED_THREADS;
+constexpr int kFusedMaxNnz = 16;
+
+// Column c of submat(S) (minor index co + c): the partial Fisher-Yates shuffle of
+// sparse_skops.hh:51-106 with 32-bit arithmetic (exact: dim_major < 2^32, x0 % span < span).
+__global__ void saso_pack_kernel(DevState s, int vec_nnz, int kp, uint32_t dim_major,
+                                 int64_t co, int64_t K, int64_t ro, int64_t M,
+                                 uint16_t *__restrict__ packed) {
+    const int64_t tid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    const int64_t nthreads = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t c = tid; c < K; c += nthreads) {
+        uint32_t mp[kFusedMaxNnz], mv[kFusedMaxNnz];
+        uint16_t w[kFusedMaxNnz];
+        int msize = 0;
+        const uint64_t off = (uint64_t)(co + c) * (uint64_t)vec_nnz;
+        for (int j = 0; j < vec_nnz; ++j) {
+            const uint4 r = philox(ctr_add(s.ctr, off + (uint64_t)j), s.key);
+            const uint32_t ell = (uint32_t)j + r.x % (dim_major - (uint32_t)j);
+            uint32_t vj = (uint32_t)j, vl = ell;
+            int sj = -1, sl = -1;
+            for (int q = 0; q < msize; ++q) {
+                if (mp[q] == (uint32_t)j) { vj = mv[q]; sj = q; }
+                if (mp[q] == ell) { vl = mv[q]; sl = q; }
+            }
+            if (ell != (uint32_t)j) {
+                if (sl >= 0) {
+                    mv[sl] = vj;
+                } else {
+                    mp[msize] = ell;
+                    mv[msize] = vj;
+                    ++msize;
+                }
+            }
+            if (sj >= 0) {
+                --msize;
+                mp[sj] = mp[msize];
+                mv[sj] = mv[msize];
+            }
+            const int64_t row = (int64_t)vl - ro;
+            w[j] = (row >= 0 && row < M) ? (uint16_t)((row << 1) | (r.y & 1u)) : (uint16_t)0xFFFF;
+        }
+        for (int j = vec_nnz; j < kp; ++j) w[j] = 0xFFFF;
+        uint4 *dst = reinterpret_cast<uint4 *>(packed + c * kp);
+        for (int q = 0; q < kp / 8; ++q)
+            dst[q] = make_uint4(w[8 * q] | ((uint32_t)w[8 * q + 1] << 16),
+                                w[8 * q + 2] | ((uint32_t)w[8 * q + 3] << 16),
+                                w[8 * q + 4] | ((uint32_t)w[8 * q + 5] << 16),
+                                w[8 * q + 6] | ((uint32_t)w[8 * q + 7] << 16));
+    }
+}
+
+__device__ __forceinline__ void red_shared_add(float *addr, float v) {
+    asm volatile("red.shared.add.f32 [%0], %1;" ::"r"((uint32_t)__cvta_generic_to_shared(addr)),
+                 "f"(v)
+                 : "memory");
+}
+
+// static staging buffer of saso_scatter_kernel<kp> and the dynamic bytes left beside it
+constexpr size_t fused_stage_bytes(int kp) { return (size_t)(kFusedThreads / 32) * 32 * 2 * kp; }
+constexpr size_t fused_max_dynamic(int kp) { return (size_t)220 * 1024 - fused_stage_bytes(kp); }
+
+// grid (ceil(N / 32), chunks); dynamic shared memory: M x 32 floats.
+template <int KP>
+__global__ void __launch_bounds__(kFusedThreads, 1)
+    saso_scatter_kernel(int64_t M, int64_t N, int64_t K, const uint16_t *__restrict__ packed,
+                        const float *__restrict__ Q, int64_t qs0, int64_t qs1, int64_t k_per_chunk,
+                        float alpha, float beta, float *out, int64_t os_i, int64_t os_j,
+                        float *partial) {
+    extern __shared__ float bs[];
+    __shared__ uint4 stage[kFusedThreads / 32][32][KP / 8];
+    static_assert(sizeof(stage) == fused_stage_bytes(KP), "staging size");
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int64_t j0 = (int64_t)blockIdx.x * kFusedCols;
+    const int64_t k_begin = (int64_t)blockIdx.y * k_per_chunk;
+    const int64_t k_end = min(K, k_begin + k_per_chunk);
+    for (int64_t t = threadIdx.x; t < M * kFusedCols; t += kFusedThreads) bs[t] = 0.f;
+    __syncthreads();
+    const bool col_ok = j0 + lane < N;
+    const float *qcol = Q + (col_ok ? (j0 + lane) * qs1 : 0);
+    for (int64_t base = k_begin + (int64_t)warp * 32; base < k_end;
+         base += (int64_t)kFusedThreads) {
+        const int64_t kr = base + lane;
+#pragma unroll
+        for (int q = 0; q < KP / 8; ++q)
+            stage[warp][lane][q] = kr < k_end
+                                       ? reinterpret_cast<const uint4 *>(packed + kr * KP)[q]
+                                       : make_uint4(~0u, ~0u, ~0u, ~0u);
+        float a[32];
+#pragma unroll
+        for (int t = 0; t < 32; ++t)
+            a[t] = (col_ok && base + t < k_end) ? __ldcs(qcol + (base + t) * qs0) : 0.f;
+        __syncwarp();
+#pragma unroll
+        for (int t = 0; t < 32; ++t) {
+#pragma unroll
+            for (int q = 0; q < KP / 8; ++q) {
+                const uint4 w = stage[warp][t][q];
+                const uint32_t words[4] = {w.x, w.y, w.z, w.w};
+#pragma unroll
+                for (int h = 0; h < 8; ++h) {
+                    const uint32_t e = (h & 1) ? (words[h >> 1] >> 16) : (words[h >> 1] & 0xFFFFu);
+                    if (e != 0xFFFFu)
+                        red_shared_add(bs + (e >> 1) * kFusedCols + lane, (e & 1u) ? -a[t] : a[t]);
+                }
+            }
+        }
+        __syncwarp();
+    }
+    __syncthreads();
+    for (int64_t t = threadIdx.x; t < M * kFusedCols; t += kFusedThreads) {
+        const int64_t r = t / kFusedCols, j = j0 + t % kFusedCols;
+        if (j >= N) continue;
+        if (partial) {
+            partial[((int64_t)blockIdx.y * M + r) * N + j] = bs[t];
+        } else {
+            float &o = out[r * os_i + j * os_j];
+            o = beta == 0.f ? alpha * bs[t] : fmaf(alpha, bs[t], beta * o);
+        }
+    }
+}
+
+// The fused path applies: float data, SASO columns as the sparse vectors, no transpose, and
+// the B slice fits in shared memory next to the staging buffer.
+size_t fused_smem_bytes(int64_t M) { return (size_t)M * kFusedCols * sizeof(float); }
+
+bool fused_saso_applies(int dtype, int64_t M, int64_t K, const SparseOperand &Sp) {
+    if (deterministic_mode() || dtype != RBG_F32) return false;
+    if (Sp.kind != SparseOperand::SASO_GEN || !Sp.short_is_row || Sp.trans) return false;
+    if (Sp.vec_nnz < 1 || Sp.vec_nnz > kFusedMaxNnz || Sp.vec_nnz > Sp.dim_major) return false;
+    if (Sp.dim_major >= (int64_t)UINT32_MAX || M >= 32768 || K > INT32_MAX) return false;
+    return fused_smem_bytes(M) <= fused_max_dynamic(Sp.vec_nnz > 8 ? 16 : 8);
+}
+
+void fused_saso(int64_t M, int64_t N, int64_t K, double alpha, const SparseOperand &Sp,
+                const Strided &Q, double beta, float *out, int64_t os_i, int64_t os_j,
+                cudaStream_t s) {
+    const int kp = Sp.vec_nnz > 8 ? 16 : 8;
+    Scratch packed((size_t)K * kp * sizeof(uint16_t), s);
+    {
+        ProfScope prof("saso_pack", s);
+        saso_pack_kernel<<<grid1d(K, 128), 128, 0, s>>>(
+            Sp.seed, (int)Sp.vec_nnz, kp, (uint32_t)Sp.dim_major, Sp.co, K, Sp.ro, M,
+            packed.as<uint16_t>());
+        RBG_LAUNCHED();
+    }
+    const int64_t slices = (N + kFusedCols - 1) / kFusedCols;
+    const int64_t sms = num_sms();
+    int64_t chunks = std::max<int64_t>(1, sms / slices);
+    chunks = std::min<int64_t>(chunks, (K + 1023) / 1024);
+    while (chunks > 1 && (double)chunks * M * N * 4 > (double)(1ll << 30)) --chunks;
+    const int64_t k_per_chunk = (K + chunks - 1) / chunks;
+    chunks = (K + k_per_chunk - 1) / k_per_chunk;
+    if (slices > INT32_MAX || chunks > 65535) fail(RBG_ERROR_UNSUPPORTED, "sparse sketch too large");
+    Scratch part;
+    float *partial = nullptr;
+    if (chunks > 1) {
+        part.alloc((size_t)chunks * M * N * sizeof(float), s);
+        partial = part.as<float>();
+    }
+    const size_t smem = fused_smem_bytes(M);
+    static bool attr_set[2] = {false, false};
+    const dim3 grid((unsigned)slices, (unsigned)chunks);
+    {
+        ProfScope prof("saso_scatter", s);
+        if (kp == 8) {
+            if (!attr_set[0]) {
+                RBG_CUDA(cudaFuncSetAttribute(saso_scatter_kernel<8>,
+                                              cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                              (int)fused_max_dynamic(8)));
+                attr_set[0] = true;
+            }
+            saso_scatter_kernel<8><<<grid, kFusedThreads, smem, s>>>(
+                M, N, K, packed.as<uint16_t>(), static_cast<const float *>(Q.ptr), Q.s0, Q.s1,
+                k_per_chunk, (float)alpha, (float)beta, out, os_i, os_j, partial);
+        } else {
+            if (!attr_set[1]) {
+                RBG_CUDA(cudaFuncSetAttribute(saso_scatter_kernel<16>,
+                                              cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                              (int)fused_max_dynamic(16)));
+                attr_set[1] = true;
+            }
+            saso_scatter_kernel<16><<<grid, kFusedThreads, smem, s>>>(
+                M, N, K, packed.as<uint16_t>(), static_cast<const float *>(Q.ptr), Q.s0, Q.s1,
+                k_per_chunk, (float)alpha, (float)beta, out, os_i, os_j, partial);
+        }
+        RBG_LAUNCHED();
+    }
+    if (chunks > 1) {
+        spmm_reduce_kernel<float><<<grid1d(M * N, 256), 256, 0, s>>>(
+            M, N, (int)chunks, partial, (float)alpha, (float)beta, out, os_i, os_j);
+        RBG_LAUNCHED();
+    }
+}
+
+
 template <typename T>
 void run(int64_t M, int64_t N, int64_t K, double alpha, const SparseOperand &Sp,
          const Strided &Q, double beta, void *out, int64_t os_i, int64_t os_j, cudaStream_t s) {
@@ -428,7 +638,9 @@ void spmm_sketch(int dtype, int64_t M, int64_t N, int64_t K, double alpha,
         launch_scale(dtype, M, N, os_i, os_j, beta, out, s);
         return;
     }
-    if (dtype == RBG_F32)
+    if (fused_saso_applies(dtype, M, K, Sp))
+        fused_saso(M, N, K, alpha, Sp, Q, beta, static_cast<float *>(out), os_i, os_j, s);
+    else if (dtype == RBG_F32)
         run<float>(M, N, K, alpha, Sp, Q, beta, out, os_i, os_j, s);
     else
         run<double>(M, N, K, alpha, Sp, Q, beta, out, os_i, os_j, s);

@@ -8,10 +8,10 @@ import pytest
 def test_tile_configs(rb_host):
     from randblas_gb300 import batched
     cfgs = batched.tile_configs()
-    assert cfgs == [1, 2, 3]
-    assert [batched.tile_width(c) for c in cfgs] == [128, 64, 32]
+    assert cfgs == [1, 2, 3, 4]
+    assert [batched.tile_shape(c) for c in cfgs] == [(128, 128), (128, 64), (128, 32), (64, 256)]
     with pytest.raises(rb_host.RandBLASError):
-        batched.tile_width(4)
+        batched.tile_shape(5)
 
 
 def test_batched_argument_checks(rb_host):
@@ -40,21 +40,23 @@ def test_autotuner_choice_and_cache(rb_host, tmp_path):
     from randblas_gb300 import batched
     calls = []
 
-    def measure(cfg, d, n, m):
+    def measure(cfg, d, n, m, family):
         calls.append((cfg, n))
-        # pretend narrow problems like narrow tiles
-        return {1: 3.0, 2: 2.0, 3: 1.0}[cfg] if n <= 32 else {1: 1.0, 2: 2.0, 3: 3.0}[cfg]
+        # pretend narrow problems like narrow tiles, wide ones the 64 x 256 tile
+        return {1: 3.0, 2: 2.0, 3: 1.0, 4: 4.0}[cfg] if n <= 32 else \
+            {1: 2.0, 2: 3.0, 3: 4.0, 4: 1.0}[cfg]
 
     path = str(tmp_path / "tiles.json")
     t = batched.Autotuner(cache_path=path, measure=measure)
     assert t.choose(64, 16, 5000) == 3
-    assert t.choose(512, 128, 1 << 16) == 1
+    assert t.choose(512, 128, 1 << 16) == 4
     n_calls = len(calls)
-    assert t.choose(100, 20, 4800) == 3  # same class (n16.. rounds to 32? no: 20 -> 32)
-    assert batched.Autotuner.shape_class(64, 16, 5000) == "n16_m12"
-    assert batched.Autotuner.shape_class(100, 20, 4800) == "n32_m12"
+    assert t.choose(60, 15, 4800) == 3      # same class as (64, 16, 5000): no new timing
+    assert len(calls) == n_calls
+    assert batched.Autotuner.shape_class(64, 16, 5000) == "f0_d64_n16_m12"
+    assert batched.Autotuner.shape_class(100, 20, 4800, 1) == "f1_d128_n32_m12"
     saved = json.load(open(path))
-    assert saved["external"]["n16_m12"] == 3 and saved["external"]["n128_m16"] == 1
+    assert saved["external"]["f0_d64_n16_m12"] == 3
+    assert saved["external"]["f0_d512_n128_m16"] == 4
     t2 = batched.Autotuner(cache_path=path, measure=lambda *a: pytest.fail("re-tuned"))
     assert t2.choose(64, 16, 5000) == 3
-    assert len(calls) >= n_calls

@@ -24,7 +24,7 @@ SHAPES = [
     (300, 130, 20000, 0, 0, 0, 0.5, 0.0, 1),
     (128, 64, 60000, 1, 0, 1, 1.0, 1.5, 2),
     (200, 33, 777, 0, 3, 0, -1.0, 0.0, 0),
-    (1000, 250, 4096, 0, 0, 1, 1.0, 0.0, 0),
+    (1000, 250, 4096, 0, 0, 1, 1.0, 0.0, 4),
     (96, 512, 150000, 0, 0, 0, 1.0, 0.0, 0),
     (20, 40, 100, 0, 0, 0, 0.0, 2.0, 0),
     (129, 65, 33, 4, 4, 1, 1.0, -0.5, 2),

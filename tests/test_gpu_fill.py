@@ -11,12 +11,14 @@ from gpu_helpers import st_list, state_of, to_host, ulp_distance
 
 pytestmark = pytest.mark.gpu
 
-# Box-Muller runs on CUDA's accurate sincosf / logf / sqrtf; the reference's host build uses
-# glibc's.  Both are within about 1 ulp of the exact values; the products below may differ
-# by a few ulp.  Uniform entries involve only exact scalings and one rounding: bit-exact.
-GAUSS_ULP_MAX = 4
-GAUSS_ULP_TYPICAL = 2        # at least 99.9% of Gaussian entries within this
-GAUSS_FRAC_TYPICAL = 0.999
+# Box-Muller evaluates sin, cos and log to the correctly rounded float (float-float
+# arithmetic); the reference's host build uses glibc's sincosf / logf, which round the other
+# way in about 1% of cases, so Gaussian entries agree to within 2 ulp in all but a few per
+# million (3 ulp at most, when sine and logarithm both differ).  Uniform entries involve only
+# exact scalings and one rounding: bit-exact.
+GAUSS_ULP_MAX = 3
+GAUSS_ULP_TYPICAL = 2        # at least 99.99% of Gaussian entries within this
+GAUSS_FRAC_TYPICAL = 0.9999
 
 
 def _fill(rb, c):

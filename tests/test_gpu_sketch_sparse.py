@@ -65,7 +65,9 @@ def test_sparse_operator_sketch_golden(rb, oracle):
 
 
 def test_prefilled_sparse_operator_matches_unsampled(rb):
-    """Sampling inside the sketch and sketching with fill_sparse's COO give the same B."""
+    """Sampling inside the sketch and sketching with fill_sparse's COO give the same B: bitwise
+    in deterministic mode (both through fixed-order row lists), to FP32 rounding with the fused
+    SASO scatter (the default for short-axis operators)."""
     import torch
     for ax in (rb.Axis.Short, rb.Axis.Long):
         D = rb.SparseDist(64, 5000, 5, ax)
@@ -73,12 +75,21 @@ def test_prefilled_sparse_operator_matches_unsampled(rb):
         S1 = rb.SparseSkOp(D, rb.RNGState(21))
         S2 = rb.SparseSkOp(D, rb.RNGState(21))
         rb.fill_sparse(S2)
-        B1 = torch.zeros(64 * 33, device="cuda")
-        B2 = torch.zeros(64 * 33, device="cuda")
-        for S, B in ((S1, B1), (S2, B2)):
-            rb.sketch_general(rb.Layout.RowMajor, rb.Op.NoTrans, rb.Op.NoTrans, 64, 33, 5000, 1.0,
-                              S, A, 33, 0.0, B, 33)
-        assert torch.equal(B1, B2)
+        out = {}
+        for det in (True, False):
+            rb.set_deterministic(det)
+            try:
+                for name, S in (("sampled", S1), ("filled", S2)):
+                    B = torch.zeros(64 * 33, device="cuda")
+                    rb.sketch_general(rb.Layout.RowMajor, rb.Op.NoTrans, rb.Op.NoTrans, 64, 33,
+                                      5000, 1.0, S, A, 33, 0.0, B, 33)
+                    out[(det, name)] = B
+            finally:
+                rb.set_deterministic(False)
+        assert torch.equal(out[(True, "sampled")], out[(True, "filled")])
+        ref = out[(True, "filled")].double()
+        rel = float((out[(False, "sampled")].double() - ref).norm() / ref.norm())
+        assert rel <= 1e-6, (ax, rel)
 
 
 def test_sketch_sparse_data_golden(rb, oracle):
@@ -136,25 +147,33 @@ def test_sketch_sparse_data_golden(rb, oracle):
 
 def test_full_size_saso_sketch(rb):
     """1024 x 2^20 SASO (8 nonzeros per column) times a 2^20 x 256 row-major N(0,1) FP32
-    matrix: relative Frobenius error <= 1e-6 against an FP64 product of the same operator,
-    and bitwise-identical results on a second run (fixed-order reductions)."""
+    matrix: relative Frobenius error <= 1e-6 against an FP64 product of the same operator on
+    both paths (fused scatter, deterministic row lists), and bitwise-identical results on a
+    second deterministic run (fixed-order reductions)."""
     import torch
     m, d, n = 1 << 20, 1024, 256
     A = torch.empty(m * n, dtype=torch.float32, device="cuda")
     nxt = rb.fill_dense(rb.DenseDist(m, n, rb.ScalarDist.Gaussian, rb.Axis.Short), A,
                         rb.RNGState(0))
     S = rb.SparseSkOp(rb.SparseDist(d, m, 8), nxt)
-    B = torch.empty(d * n, dtype=torch.float32, device="cuda")
-    rb.sketch_general(rb.Layout.RowMajor, rb.Op.NoTrans, rb.Op.NoTrans, d, n, m, 1.0, S, A, n,
-                      0.0, B, n)
-    B_again = torch.empty_like(B)
-    rb.sketch_general(rb.Layout.RowMajor, rb.Op.NoTrans, rb.Op.NoTrans, d, n, m, 1.0, S, A, n,
-                      0.0, B_again, n)
-    assert torch.equal(B, B_again)
+
+    def sketch():
+        B = torch.empty(d * n, dtype=torch.float32, device="cuda")
+        rb.sketch_general(rb.Layout.RowMajor, rb.Op.NoTrans, rb.Op.NoTrans, d, n, m, 1.0, S, A,
+                          n, 0.0, B, n)
+        return B
+    B_fast = sketch()
+    rb.set_deterministic(True)
+    try:
+        B_det, B_again = sketch(), sketch()
+    finally:
+        rb.set_deterministic(False)
+    assert torch.equal(B_det, B_again)
     Sf = rb.SparseSkOp(rb.SparseDist(d, m, 8), nxt)
     rb.fill_sparse(Sf)
     idx = torch.stack([Sf.rows, Sf.cols])
     Ssp = torch.sparse_coo_tensor(idx, Sf.vals.double(), (d, m)).coalesce()
     ref = torch.sparse.mm(Ssp, A.view(m, n).double())
-    rel = (torch.linalg.norm(B.view(d, n).double() - ref) / torch.linalg.norm(ref)).item()
-    assert rel <= 1e-6, rel
+    for B in (B_fast, B_det):
+        rel = (torch.linalg.norm(B.view(d, n).double() - ref) / torch.linalg.norm(ref)).item()
+        assert rel <= 1e-6, rel
