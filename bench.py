@@ -91,13 +91,30 @@ class ClockSampler:
 
 
 # ----------------------------------------------------------------------------- workload
+def _cholesky_qr2(torch, G):
+    """Orthonormal columns spanning G (tall, well conditioned): CholeskyQR2 (Fukaya, Nakatsukasa,
+    Yanagisawa, Yamamoto 2014) -- Q = G R^-1 twice, with the small Gram matrix factored on the
+    host in FP64 and the products on the GPU in FP32 (TF32 off)."""
+    import numpy as np
+    Q = G
+    for _ in range(2):
+        W = (Q.T @ Q).double().cpu().numpy()
+        R = np.linalg.cholesky(W).T  # W = R^T R
+        Q = Q @ torch.from_numpy(np.linalg.inv(R)).to(device=Q.device, dtype=Q.dtype)
+    return Q
+
+
 def make_precision_input(torch, device):
-    """A = U diag(sigma) V^T, 2^20 x 1024 FP32 row-major, sigma_i = 10^(-6 i / 1023)."""
+    """A = U diag(sigma) V^T, 2^20 x 1024 FP32 row-major, sigma_i = 10^(-6 i / 1023); U from
+    CholeskyQR2 of a seeded 2^20 x 1024 Gaussian matrix (torch seed 0), V the Q factor of a
+    seeded 1024 x 1024 Gaussian matrix (torch seed 1, Householder QR in FP64 on the host)."""
+    import numpy as np
+    torch.backends.cuda.matmul.allow_tf32 = False
     g0 = torch.Generator(device=device).manual_seed(0)
     g1 = torch.Generator(device=device).manual_seed(1)
-    U, _ = torch.linalg.qr(torch.randn(M_SK, N_SK, generator=g0, device=device))
-    V, _ = torch.linalg.qr(torch.randn(N_SK, N_SK, generator=g1, device=device,
-                                       dtype=torch.float64))
+    U = _cholesky_qr2(torch, torch.randn(M_SK, N_SK, generator=g0, device=device))
+    Vh = torch.randn(N_SK, N_SK, generator=g1, device=device, dtype=torch.float64).cpu().numpy()
+    V = torch.from_numpy(np.linalg.qr(Vh)[0]).to(device)
     sigma = torch.logspace(0, -6, N_SK, dtype=torch.float64, device=device)
     A = (U * sigma.float()) @ V.T.float()
     return A.contiguous(), U
@@ -155,6 +172,8 @@ def main():
                     help="operator rows of the bounded CPU-baseline sample")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-batched", action="store_true",
+                    help="skip the 512-problem batching measurement (about 15 s)")
     ap.add_argument("--m-log2", type=int, default=17,
                     help="log2 of m for the dense small cases")
     ap.add_argument("--case", default="full",
@@ -232,10 +251,15 @@ def main():
         Sblk = torch.empty(64 * M_SK, dtype=torch.float64, device=device)
         rb.fill_dense_unpacked(rb.Layout.RowMajor, S.dist, 64, M_SK, r0, 0, Sblk, S.seed_state)
         ref = Sblk.view(64, M_SK) @ A.double()
-        err_num += float(torch.linalg.norm(B[r0:r0 + 64].double() - ref) ** 2)
-        err_den += float(torch.linalg.norm(ref) ** 2)
+        err_num += float((B[r0:r0 + 64].double() - ref).norm() ** 2)
+        err_den += float(ref.norm() ** 2)
         del Sblk, ref
     rel_err = (err_num / err_den) ** 0.5
+
+    # subspace-embedding distortion of the headline operator on range(A) = range(U):
+    # extreme singular values of S U / sqrt(d) (FP64 SVD on the host)
+    distortion = embedding_distortion(torch, rb, lowp, have_lowp, S, U, device)
+    del U
 
     # roofline of the dominant kernel
     main_kernel = max(prof, key=lambda k: prof[k]["ms"]) if prof else None
@@ -251,8 +275,13 @@ def main():
                 "peak_source": ("bf16 burst, " + peak_kind) if have_lowp else
                 "FP32 CUDA-core peak derived as SMs x 128 lanes x 2 x median SM clock"}
 
-    # secondary: SASO sketch (HBM-bound)
+    # secondary rows: SASO sketch (HBM-bound), the small FP64 dense sketch, the
+    # differentiation path and the batching path
     saso = bench_saso(torch, rb, device, args, stream, hbm)
+    small = bench_small_fp64(torch, rb, device, stream)
+    autograd_row = bench_autograd(torch, rb, device, stream, bf16_sus)
+    batched_row = None if args.no_batched else bench_batched(torch, rb, device, args, stream,
+                                                             tune=False)
 
     # end to end through the C ABI with host buffers
     e2e = None
@@ -296,13 +325,80 @@ def main():
                            "TFLOP/s": round(flops / (ms_plain * 1e-3) / 1e12, 2)},
             "speedup_vs_fp32_plain": round(ms_plain / ms_max, 2),
             "rel_frobenius_err_vs_fp64": rel_err,
+            "embedding_distortion": distortion,
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
             "gpu_launches": gpu_launches, "clocks": clk.summary(), "saso": saso,
+            "dense_fp64_small": small, "autograd": autograd_row, "batched": batched_row,
         }
         print(json.dumps(line))
     if world > 1:
         dist.barrier()
         dist.destroy_process_group()
+
+
+def embedding_distortion(torch, rb, lowp, have_lowp, S, U, device):
+    """max(sigma_max - 1, 1 - sigma_min) of S U / sqrt(d) for the headline path (and the plain
+    FP32 path): S is an approximate isometry on range(U) after the 1/sqrt(d) scaling (uniform
+    entries have unit variance)."""
+    import numpy as np
+    out = {}
+    paths = [("plain_fp32", False)] + ([("bf16_tc", True)] if have_lowp else [])
+    for name, fused in paths:
+        SU = torch.empty(D_SK, N_SK, device=device)
+        if fused:
+            lowp.sketch_lowp(rb.Layout.RowMajor, rb.Op.NoTrans, rb.Op.NoTrans, D_SK, N_SK, M_SK,
+                             1.0, S, 0, 0, U, N_SK, 0.0, SU, N_SK)
+        else:
+            rb.sketch_general(rb.Layout.RowMajor, rb.Op.NoTrans, rb.Op.NoTrans, D_SK, N_SK,
+                              M_SK, 1.0, S, U, N_SK, 0.0, SU, N_SK)
+        sv = np.linalg.svd(SU.double().cpu().numpy() / np.sqrt(D_SK), compute_uv=False)
+        out[name] = {"sigma_max": float(sv[0]), "sigma_min": float(sv[-1]),
+                     "distortion": float(max(sv[0] - 1.0, 1.0 - sv[-1]))}
+        del SU
+    return out
+
+
+def bench_small_fp64(torch, rb, device, stream):
+    """The reference's CPU-runnable dense case: Gaussian 200 x 10000 operator (seeded after a
+    10000 x 50 uniform A from Philox key 0), FP64, column-major; latency of one sketch."""
+    d, m, n = 200, 10000, 50
+    A = torch.empty(m * n, dtype=torch.float64, device=device)
+    nxt = rb.fill_dense_unpacked(rb.Layout.RowMajor, rb.DenseDist(50, 10000, rb.ScalarDist.Uniform),
+                                 50, 10000, 0, 0, A, rb.RNGState(0))
+    S = rb.DenseSkOp(rb.DenseDist(d, m), nxt, dtype=torch.float64)
+    B = torch.empty(d * n, dtype=torch.float64, device=device)
+
+    def step():
+        rb.sketch_general(rb.Layout.ColMajor, rb.Op.NoTrans, rb.Op.NoTrans, d, n, m, 1.0, S, A,
+                          m, 0.0, B, d)
+    ms = event_time(torch, step, 20, 3, stream)
+    return {"workload": "Gaussian 200 x 10000, A 10000 x 50 FP64 column-major",
+            "us_per_sketch": round(ms * 1e3, 1),
+            "GFLOP/s": round(2.0 * d * m * n / (ms * 1e-3) / 1e9, 1)}
+
+
+def bench_autograd(torch, rb, device, stream, bf16_peak):
+    """Forward + backward of ||S A - B||_F^2 through the autograd Function, Gaussian
+    2048 x 2^18 operator (RNGState(5)), A 2^18 x 512: FP32 plain path and BF16 tensor cores."""
+    from randblas_gb300 import autograd
+    d, m, n = 2048, 1 << 18, 512
+    S = rb.DenseSkOp(rb.DenseDist(d, m, rb.ScalarDist.Gaussian), rb.RNGState(5))
+    g = torch.Generator(device=device).manual_seed(5)
+    A0 = torch.randn(m, n, device=device, generator=g)
+    Bt = torch.randn(d, n, device=device, generator=g)
+    out = {"workload": "Gaussian 2048 x 2^18, A 2^18 x 512, loss ||S A - B||^2, fwd + bwd"}
+    flops = 2 * 2.0 * d * m * n
+    for name, prec, dt in (("fp32_plain", None, torch.float32), ("bf16_tc", "bf16", torch.float32),
+                           ("bf16_tc_bf16_input", "bf16", torch.bfloat16)):
+        A = A0.to(dt).requires_grad_(True)
+
+        def step():
+            A.grad = None
+            loss = ((autograd.sketch(S, A, precision=prec) - Bt) ** 2).sum()
+            loss.backward()
+        ms = event_time(torch, step, 3, 1, stream)
+        out[name] = {"ms_fwd_bwd": round(ms, 3), "TFLOP/s": round(flops / (ms * 1e-3) / 1e12, 1)}
+    return out
 
 
 def derived_fp32_peak(torch, clocks):
@@ -356,7 +452,7 @@ def batched_workload(torch, rb, device, count=512):
     return probs
 
 
-def bench_batched(torch, rb, device, args, stream):
+def bench_batched(torch, rb, device, args, stream, tune=True):
     import tempfile
     from randblas_gb300 import batched
     probs = batched_workload(torch, rb, device)
@@ -372,9 +468,11 @@ def bench_batched(torch, rb, device, args, stream):
                        "[16, 512], d = 4n, FP32", "gflop": round(flops / 1e9, 1),
            "separate_plain_launches": {"ms": round(ms_sep, 2),
                                        "TFLOP/s": round(flops / ms_sep / 1e9, 2)}}
-    for name, tuner in (("default_tiles", None),
-                        ("autotuned", batched.Autotuner(
-                            cache_path=os.path.join(tempfile.gettempdir(), "rbg_tiles.json")))):
+    variants = [("default_tiles", None)]
+    if tune:
+        variants.append(("autotuned", batched.Autotuner(
+            cache_path=os.path.join(tempfile.gettempdir(), "rbg_tiles.json"))))
+    for name, tuner in variants:
         for p in probs:
             p.tile_config = 0
         plan = batched.BatchedPlan(probs, tuner=tuner)
