@@ -287,29 +287,33 @@ int grid1d(int64_t work, int threads) {
 // columns, no transpose), the shape RandBLAS's LSKGES gives a wide SparseDist
 // (RandBLAS/sparse_skops.hh:131-246, skge.hh:465-492):  B(r, :) += S(r, k) op(A)(k, :).
 // Instead of building row lists, a pre-pass samples each column's vec_nnz (row, sign) pairs
-// once into 16-bit words ((row << 1) | negative; 0xFFFF = outside submat(S)); then every CTA
-// keeps a d x 32 slice of B in shared memory and streams its share of A's rows exactly once,
-// adding each row into the vec_nnz rows of the slice with shared-memory reductions, and the
-// chunks' slices are summed in chunk order.  Additions into one slice entry arrive in a
-// scheduling-dependent order, so the last bits can vary between runs;
+// once into 32-bit words that are ready to use in the scatter: the byte offset of the row in
+// the shared-memory B slice, with the sign in bit 31 (entries outside submat(S) point at a
+// spare row past the slice).  Every CTA then keeps a d x 32 slice of B in shared memory and
+// streams its share of A's rows exactly once, adding each row into the vec_nnz rows of the
+// slice with shared-memory reductions (one mask, one add, one sign flip and the reduction per
+// entry), and the chunks' slices are summed in chunk order.  Additions into one slice entry
+// arrive in a scheduling-dependent order, so the last bits can vary between runs;
 // rbg_set_deterministic(1) selects the row-list path instead.
 #ifndef RBG_FUSED_THREADS
 #define RBG_FUSED_THREADS 1024
 #endif
 constexpr int kFusedCols = 32;
+constexpr int kFusedRowBytes = kFusedCols * 4;
 constexpr int kFusedThreads = RBG_FUSED_THREADS;
 constexpr int kFusedMaxNnz = 16;
+constexpr uint32_t kSignBit = 0x80000000u;
 
 // Column c of submat(S) (minor index co + c): the partial Fisher-Yates shuffle of
 // sparse_skops.hh:51-106 with 32-bit arithmetic (exact: dim_major < 2^32, x0 % span < span).
 __global__ void saso_pack_kernel(DevState s, int vec_nnz, int kp, uint32_t dim_major,
                                  int64_t co, int64_t K, int64_t ro, int64_t M,
-                                 uint16_t *__restrict__ packed) {
+                                 uint32_t *__restrict__ packed) {
     const int64_t tid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     const int64_t nthreads = (int64_t)gridDim.x * blockDim.x;
+    const uint32_t spare = (uint32_t)M * kFusedRowBytes;
     for (int64_t c = tid; c < K; c += nthreads) {
-        uint32_t mp[kFusedMaxNnz], mv[kFusedMaxNnz];
-        uint16_t w[kFusedMaxNnz];
+        uint32_t mp[kFusedMaxNnz], mv[kFusedMaxNnz], w[kFusedMaxNnz];
         int msize = 0;
         const uint64_t off = (uint64_t)(co + c) * (uint64_t)vec_nnz;
         for (int j = 0; j < vec_nnz; ++j) {
@@ -336,71 +340,69 @@ __global__ void saso_pack_kernel(DevState s, int vec_nnz, int kp, uint32_t dim_m
                 mv[sj] = mv[msize];
             }
             const int64_t row = (int64_t)vl - ro;
-            w[j] = (row >= 0 && row < M) ? (uint16_t)((row << 1) | (r.y & 1u)) : (uint16_t)0xFFFF;
+            w[j] = (row >= 0 && row < M)
+                       ? ((uint32_t)row * kFusedRowBytes) | ((r.y & 1u) ? kSignBit : 0u)
+                       : spare;
         }
-        for (int j = vec_nnz; j < kp; ++j) w[j] = 0xFFFF;
+        for (int j = vec_nnz; j < kp; ++j) w[j] = spare;
         uint4 *dst = reinterpret_cast<uint4 *>(packed + c * kp);
-        for (int q = 0; q < kp / 8; ++q)
-            dst[q] = make_uint4(w[8 * q] | ((uint32_t)w[8 * q + 1] << 16),
-                                w[8 * q + 2] | ((uint32_t)w[8 * q + 3] << 16),
-                                w[8 * q + 4] | ((uint32_t)w[8 * q + 5] << 16),
-                                w[8 * q + 6] | ((uint32_t)w[8 * q + 7] << 16));
+        for (int q = 0; q < kp / 4; ++q)
+            dst[q] = make_uint4(w[4 * q], w[4 * q + 1], w[4 * q + 2], w[4 * q + 3]);
     }
 }
 
-__device__ __forceinline__ void red_shared_add(float *addr, float v) {
-    asm volatile("red.shared.add.f32 [%0], %1;" ::"r"((uint32_t)__cvta_generic_to_shared(addr)),
-                 "f"(v)
+__device__ __forceinline__ void red_shared_add_bits(uint32_t addr, uint32_t bits) {
+    asm volatile("red.shared.add.f32 [%0], %1;" ::"r"(addr), "f"(__uint_as_float(bits))
                  : "memory");
 }
 
-// static staging buffer of saso_scatter_kernel<kp> and the dynamic bytes left beside it
-constexpr size_t fused_stage_bytes(int kp) { return (size_t)(kFusedThreads / 32) * 32 * 2 * kp; }
-constexpr size_t fused_max_dynamic(int kp) { return (size_t)220 * 1024 - fused_stage_bytes(kp); }
+// staging buffer of saso_scatter_kernel<kp> (entry words of 32 rows per warp) and the
+// largest dynamic shared memory the kernel may use
+constexpr size_t fused_stage_bytes(int kp) { return (size_t)(kFusedThreads / 32) * 32 * 4 * kp; }
+constexpr size_t kFusedMaxDynamic = (size_t)220 * 1024;
 
-// grid (ceil(N / 32), chunks); dynamic shared memory: M x 32 floats.
+// grid (ceil(N / 32), chunks); dynamic shared memory: the (M + 1) x 32 float slice of B (the
+// last row absorbs entries outside submat(S)), then the staging buffer.
 template <int KP>
 __global__ void __launch_bounds__(kFusedThreads, 1)
-    saso_scatter_kernel(int64_t M, int64_t N, int64_t K, const uint16_t *__restrict__ packed,
+    saso_scatter_kernel(int64_t M, int64_t N, int64_t K, const uint32_t *__restrict__ packed,
                         const float *__restrict__ Q, int64_t qs0, int64_t qs1, int64_t k_per_chunk,
                         float alpha, float beta, float *out, int64_t os_i, int64_t os_j,
                         float *partial) {
     extern __shared__ float bs[];
-    __shared__ uint4 stage[kFusedThreads / 32][32][KP / 8];
-    static_assert(sizeof(stage) == fused_stage_bytes(KP), "staging size");
+    uint4 *stage = reinterpret_cast<uint4 *>(bs + (M + 1) * kFusedCols);  // 16-byte aligned
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int64_t j0 = (int64_t)blockIdx.x * kFusedCols;
     const int64_t k_begin = (int64_t)blockIdx.y * k_per_chunk;
     const int64_t k_end = min(K, k_begin + k_per_chunk);
-    for (int64_t t = threadIdx.x; t < M * kFusedCols; t += kFusedThreads) bs[t] = 0.f;
+    for (int64_t t = threadIdx.x; t < (M + 1) * kFusedCols; t += kFusedThreads) bs[t] = 0.f;
     __syncthreads();
+    const uint32_t lane_base = (uint32_t)__cvta_generic_to_shared(bs) + 4u * (uint32_t)lane;
     const bool col_ok = j0 + lane < N;
     const float *qcol = Q + (col_ok ? (j0 + lane) * qs1 : 0);
     for (int64_t base = k_begin + (int64_t)warp * 32; base < k_end;
          base += (int64_t)kFusedThreads) {
         const int64_t kr = base + lane;
 #pragma unroll
-        for (int q = 0; q < KP / 8; ++q)
-            stage[warp][lane][q] = kr < k_end
-                                       ? reinterpret_cast<const uint4 *>(packed + kr * KP)[q]
-                                       : make_uint4(~0u, ~0u, ~0u, ~0u);
-        float a[32];
+        for (int q = 0; q < KP / 4; ++q)
+            stage[(warp * 32 + lane) * (KP / 4) + q] =
+                kr < k_end ? reinterpret_cast<const uint4 *>(packed + kr * KP)[q]
+                           : make_uint4(0u, 0u, 0u, 0u);  // a zero row adds 0.0 to row 0
+        uint32_t a[32];
 #pragma unroll
         for (int t = 0; t < 32; ++t)
-            a[t] = (col_ok && base + t < k_end) ? __ldcs(qcol + (base + t) * qs0) : 0.f;
+            a[t] = (col_ok && base + t < k_end) ? __float_as_uint(__ldcs(qcol + (base + t) * qs0))
+                                                : 0u;
         __syncwarp();
 #pragma unroll
         for (int t = 0; t < 32; ++t) {
 #pragma unroll
-            for (int q = 0; q < KP / 8; ++q) {
-                const uint4 w = stage[warp][t][q];
-                const uint32_t words[4] = {w.x, w.y, w.z, w.w};
-#pragma unroll
-                for (int h = 0; h < 8; ++h) {
-                    const uint32_t e = (h & 1) ? (words[h >> 1] >> 16) : (words[h >> 1] & 0xFFFFu);
-                    if (e != 0xFFFFu)
-                        red_shared_add(bs + (e >> 1) * kFusedCols + lane, (e & 1u) ? -a[t] : a[t]);
-                }
+            for (int q = 0; q < KP / 4; ++q) {
+                const uint4 w = stage[(warp * 32 + t) * (KP / 4) + q];
+                red_shared_add_bits(lane_base + (w.x & ~kSignBit), a[t] ^ (w.x & kSignBit));
+                red_shared_add_bits(lane_base + (w.y & ~kSignBit), a[t] ^ (w.y & kSignBit));
+                red_shared_add_bits(lane_base + (w.z & ~kSignBit), a[t] ^ (w.z & kSignBit));
+                red_shared_add_bits(lane_base + (w.w & ~kSignBit), a[t] ^ (w.w & kSignBit));
             }
         }
         __syncwarp();
@@ -419,27 +421,27 @@ __global__ void __launch_bounds__(kFusedThreads, 1)
 }
 
 // The fused path applies: float data, SASO columns as the sparse vectors, no transpose, and
-// the B slice fits in shared memory next to the staging buffer.
-size_t fused_smem_bytes(int64_t M) { return (size_t)M * kFusedCols * sizeof(float); }
+// the B slice (plus the spare row) fits in shared memory next to the staging buffer.
+size_t fused_smem_bytes(int64_t M) { return (size_t)(M + 1) * kFusedCols * sizeof(float); }
 
 bool fused_saso_applies(int dtype, int64_t M, int64_t K, const SparseOperand &Sp) {
     if (deterministic_mode() || dtype != RBG_F32) return false;
     if (Sp.kind != SparseOperand::SASO_GEN || !Sp.short_is_row || Sp.trans) return false;
     if (Sp.vec_nnz < 1 || Sp.vec_nnz > kFusedMaxNnz || Sp.vec_nnz > Sp.dim_major) return false;
     if (Sp.dim_major >= (int64_t)UINT32_MAX || M >= 32768 || K > INT32_MAX) return false;
-    return fused_smem_bytes(M) <= fused_max_dynamic(Sp.vec_nnz > 8 ? 16 : 8);
+    return fused_smem_bytes(M) + fused_stage_bytes(Sp.vec_nnz > 8 ? 16 : 8) <= kFusedMaxDynamic;
 }
 
 void fused_saso(int64_t M, int64_t N, int64_t K, double alpha, const SparseOperand &Sp,
                 const Strided &Q, double beta, float *out, int64_t os_i, int64_t os_j,
                 cudaStream_t s) {
-    const int kp = Sp.vec_nnz > 8 ? 16 : 8;
-    Scratch packed((size_t)K * kp * sizeof(uint16_t), s);
+    const int kp = Sp.vec_nnz > 8 ? 16 : 8;  // entries per column, padded with spare-row words
+    Scratch packed((size_t)K * kp * sizeof(uint32_t), s);
     {
         ProfScope prof("saso_pack", s);
         saso_pack_kernel<<<grid1d(K, 128), 128, 0, s>>>(
             Sp.seed, (int)Sp.vec_nnz, kp, (uint32_t)Sp.dim_major, Sp.co, K, Sp.ro, M,
-            packed.as<uint16_t>());
+            packed.as<uint32_t>());
         RBG_LAUNCHED();
     }
     const int64_t slices = (N + kFusedCols - 1) / kFusedCols;
@@ -456,7 +458,7 @@ void fused_saso(int64_t M, int64_t N, int64_t K, double alpha, const SparseOpera
         part.alloc((size_t)chunks * M * N * sizeof(float), s);
         partial = part.as<float>();
     }
-    const size_t smem = fused_smem_bytes(M);
+    const size_t smem = fused_smem_bytes(M) + fused_stage_bytes(kp);
     static bool attr_set[2] = {false, false};
     const dim3 grid((unsigned)slices, (unsigned)chunks);
     {
@@ -465,21 +467,21 @@ void fused_saso(int64_t M, int64_t N, int64_t K, double alpha, const SparseOpera
             if (!attr_set[0]) {
                 RBG_CUDA(cudaFuncSetAttribute(saso_scatter_kernel<8>,
                                               cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                              (int)fused_max_dynamic(8)));
+                                              (int)kFusedMaxDynamic));
                 attr_set[0] = true;
             }
             saso_scatter_kernel<8><<<grid, kFusedThreads, smem, s>>>(
-                M, N, K, packed.as<uint16_t>(), static_cast<const float *>(Q.ptr), Q.s0, Q.s1,
+                M, N, K, packed.as<uint32_t>(), static_cast<const float *>(Q.ptr), Q.s0, Q.s1,
                 k_per_chunk, (float)alpha, (float)beta, out, os_i, os_j, partial);
         } else {
             if (!attr_set[1]) {
                 RBG_CUDA(cudaFuncSetAttribute(saso_scatter_kernel<16>,
                                               cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                              (int)fused_max_dynamic(16)));
+                                              (int)kFusedMaxDynamic));
                 attr_set[1] = true;
             }
             saso_scatter_kernel<16><<<grid, kFusedThreads, smem, s>>>(
-                M, N, K, packed.as<uint16_t>(), static_cast<const float *>(Q.ptr), Q.s0, Q.s1,
+                M, N, K, packed.as<uint32_t>(), static_cast<const float *>(Q.ptr), Q.s0, Q.s1,
                 k_per_chunk, (float)alpha, (float)beta, out, os_i, os_j, partial);
         }
         RBG_LAUNCHED();
