@@ -174,6 +174,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-batched", action="store_true",
                     help="skip the 512-problem batching measurement (about 15 s)")
+    ap.add_argument("--precision", default="bf16", choices=["bf16", "fp8"],
+                    help="tensor-core operand precision for the lowp-small case")
     ap.add_argument("--m-log2", type=int, default=17,
                     help="log2 of m for the dense small cases")
     ap.add_argument("--case", default="full",
@@ -538,9 +540,11 @@ def run_case(args):
         A = torch.randn(m, N_SK, device=dev)
         B = torch.empty(D_SK, N_SK, device=dev)
         if args.case == "lowp-small":
+            prec = lowp.FP8_E4M3 if args.precision == "fp8" else lowp.BF16
+
             def step():
                 lowp.sketch_lowp(rb.Layout.RowMajor, rb.Op.NoTrans, rb.Op.NoTrans, D_SK, N_SK, m,
-                                 1.0, S, 0, 0, A, N_SK, 0.0, B, N_SK)
+                                 1.0, S, 0, 0, A, N_SK, 0.0, B, N_SK, precision=prec)
         elif args.case == "convert-small":
             def step():
                 # the same call with a 1-row operator: the A conversion dominates

@@ -293,10 +293,13 @@ int rbg_lskge3_lowp_workspace(int32_t precision, int64_t d, int64_t n, int64_t m
                               size_t *bytes);
 /* Left dense sketch on the tensor cores (no reference counterpart; same semantics as
  * rbg_lskge3 with T = float): the entries of submat(S) are generated inside the kernel,
- * rounded to `precision` (RBG_PREC_BF16, or RBG_PREC_FP8_E4M3 with one scale per 128
- * entries along m), multiplied with A rounded the same way, accumulated in FP32 in tensor
- * memory.  workspace: device buffer of rbg_lskge3_lowp_workspace bytes, or NULL to let the
- * call allocate (stream-ordered) and free it. */
+ * rounded to `precision`, multiplied with A rounded the same way, accumulated in FP32 in
+ * tensor memory.  RBG_PREC_BF16: both operands BF16.  RBG_PREC_FP8_E4M3: S's entries enter
+ * as e4m3 unscaled (|uniform| <= sqrt(3), Gaussians far below e4m3's 448); A is divided, per
+ * column and per K slice of the work split, by the power-of-two scale that brings that tile's
+ * largest magnitude to <= 448, and the epilogue multiplies the product back (exact).
+ * workspace: device buffer of rbg_lskge3_lowp_workspace bytes, or NULL to let the call
+ * allocate (stream-ordered) and free it. */
 int rbg_lskge3_lowp(int32_t precision, int32_t layout, int32_t opS, int32_t opA, int64_t d,
                     int64_t n, int64_t m, float alpha, const rbg_dense_skop *S, int64_t ro_s,
                     int64_t co_s, const float *A, int64_t lda, float beta, float *B,

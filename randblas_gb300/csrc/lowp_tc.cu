@@ -1,18 +1,23 @@
 // lowp_tc.cu -- the tensor-core precision path: B = alpha * op(submat(S)) * op(A) + beta * B
-// with S's entries generated inside the kernel, rounded to BF16, and multiplied on the 5th
-// generation tensor cores (tcgen05.mma, FP32 accumulators in tensor memory).  No reference
-// counterpart: the reference's LSKGE3 (RandBLAS/skge.hh:154-202) materialises S in FP32/FP64
-// and calls blas::gemm; this path keeps its semantics with BF16 operands.
+// with S's entries generated inside the kernel, rounded to BF16 (or FP8 e4m3), and multiplied
+// on the 5th-generation tensor cores (tcgen05.mma, FP32 accumulators in tensor memory).  No
+// reference counterpart: the reference's LSKGE3 (RandBLAS/skge.hh:154-202) materialises S in
+// FP32/FP64 and calls blas::gemm; this path keeps its semantics with reduced-precision operands.
 //
-// Three launches per call:
-//  1. convert: op(A) (FP32, any layout) -> At, BF16, K-major ([n][m], m contiguous), the
-//     layout the tensor core reads through TMA with the 128-byte swizzle.
-//  2. sketch: persistent, one CTA per SM, 16 warps with fixed roles --
-//       warp 0      TMA producer: A tiles (512 n-rows x 64 k) into a 2-stage ring;
+// Three launches per call (four for FP8):
+//  0. (FP8) amax: the largest |op(A)(k, j)| of every column j within every K slice.
+//  1. convert: op(A) (FP32 or BF16, any layout) -> At, k-blocked ([k / 64 bytes][n][64 bytes]),
+//     so every stage's TMA box is one contiguous block; BF16, or e4m3 after dividing by the
+//     power-of-two scale of its (K slice, column).
+//  2. sketch: persistent clusters of CN x CM CTAs (one per SM), 24 warps with fixed roles --
+//       warp 0      TMA producer: A tiles (512 n-rows x 64 bytes of k) into a 5-stage ring,
+//                   multicast to the CTA's M-peer;
 //       warp 1      MMA issuer (one thread) and tensor-memory owner (512 columns);
 //       warps 4-7   epilogue: tensor memory -> registers -> FP32 partial tile in HBM;
-//       warps 8-15  S producers: Philox4x32-10 + transform for a 128 x 64 tile of S per stage,
-//                   written as BF16 in the same swizzled K-major layout.
+//       warps 8-23  S producers in 4 groups taking stages in turn: Philox4x32-10 + transform
+//                   for their half of a 128-row S stage (the N-peer makes the other half and
+//                   copies it over with a bulk shared-memory copy), stored in the 64-byte
+//                   swizzled K-major layout the tensor core reads.
 //     A work unit is one 128 x 512 output tile over one slice of the K range; every unit's
 //     partial goes to its own slot, so the final sum has a fixed order.  S is never written
 //     to HBM.
@@ -21,6 +26,7 @@
 // that the host reads through rbg_lowp_status().
 #include <cuda.h>
 #include <cuda_bf16.h>
+#include <cuda_fp8.h>
 
 #include <algorithm>
 #include <mutex>
@@ -33,12 +39,19 @@ namespace {
 
 constexpr int BM = 128;          // rows of S per tile (tensor-memory lanes)
 constexpr int BN = 512;          // columns of A per tile (tensor-memory columns)
-constexpr int BK = 32;           // k per stage: 32 BF16 = one 64-byte swizzled row
-constexpr int ROW_BYTES = BK * 2;
+constexpr int ROW_BYTES = 64;    // one swizzled row of a stage: 32 BF16 or 64 e4m3 values of k
 constexpr int CHUNKS = ROW_BYTES / 16;      // 16-byte chunks per row
 constexpr int STAGES = 5;
-constexpr int S_STAGE_BYTES = BM * BK * 2;  // 8 KiB
-constexpr int A_STAGE_BYTES = BN * BK * 2;  // 32 KiB
+constexpr int S_STAGE_BYTES = BM * ROW_BYTES;  // 8 KiB
+constexpr int A_STAGE_BYTES = BN * ROW_BYTES;  // 32 KiB
+
+// Element traits: k values per stage and per 16-byte chunk.
+template <bool kFp8>
+struct Elem {
+    static constexpr int BYTES = kFp8 ? 1 : 2;
+    static constexpr int BK = ROW_BYTES / BYTES;  // 32 (BF16) or 64 (e4m3)
+    static constexpr int PER_CHUNK = 16 / BYTES;  // 8 or 16
+};
 // Warp roles: 0 TMA, 1 MMA, 4-7 epilogue (one per tensor-memory lane quarter), generator
 // warps from 8 on.  A warp runs on sub-partition id % 4.  With GEN_SKIP_MMA_SP the generators
 // avoid the MMA issuer's sub-partition (id % 4 == 1), whose warps above 8 then stay idle.
@@ -75,13 +88,14 @@ struct LowpParams {
     DenseGen gen;          // operator entries
     int64_t r0, c0;        // natural coordinates of submat(S)(0, 0)
     int r_on_i;            // 1: natural row follows the output row i
-    int64_t k_steps;       // ceil(K / BK)
+    int64_t k_steps;       // ceil(K / k per stage)
     int64_t m_groups;      // row groups, each CM tiles of BM rows
     int64_t n_groups;      // column groups, each CN tiles of BN columns
     int64_t ks_per_group;  // k-steps per K slice
     int64_t units;         // m_groups * n_groups * k_groups
     int64_t npad;          // rows per k-block of the converted A (multiple of BN)
     float *partial;        // [k_groups][M][N]
+    const uint32_t *amax;  // FP8: [k_groups][npad] column maxima (float bits); else null
     int *err;
 };
 
@@ -110,25 +124,61 @@ __device__ __forceinline__ float uneg11_fma(uint32_t x) {
     return __fmaf_rn(__int2float_rn((int32_t)x), 0x1p-31f, 0x1p-32f);
 }
 
-// Eight consecutive natural-column entries starting at a block-aligned counter `c` (two
-// Philox calls), finished (uniform entries scaled) and packed to BF16.
-__device__ __forceinline__ uint4 gen8_aligned(int family, uint4 c, uint2 key) {
-    float v[8];
-    if (family == RBG_UNIFORM) {
-        const uint4 r0 = philox(c, key);
-        const uint4 r1 = philox(ctr_add_u32(c, 1u), key);
-        v[0] = uneg11_fma(r0.x); v[1] = uneg11_fma(r0.y);
-        v[2] = uneg11_fma(r0.z); v[3] = uneg11_fma(r0.w);
-        v[4] = uneg11_fma(r1.x); v[5] = uneg11_fma(r1.y);
-        v[6] = uneg11_fma(r1.z); v[7] = uneg11_fma(r1.w);
-#pragma unroll
-        for (int e = 0; e < 8; ++e) v[e] = __fmul_rn(v[e], 1.7320508075688772f);
-    } else {
-        gen4<true>(family, c, key, v);
-        gen4<true>(family, ctr_add_u32(c, 1u), key, v + 4);
-    }
+// Four e4m3 values (round to nearest, saturating to +-448) in one word, first value lowest.
+__device__ __forceinline__ uint32_t pack_e4m3x4(float a, float b, float c, float d) {
+    const uint32_t lo = __nv_cvt_float2_to_fp8x2(make_float2(a, b), __NV_SATFINITE, __NV_E4M3);
+    const uint32_t hi = __nv_cvt_float2_to_fp8x2(make_float2(c, d), __NV_SATFINITE, __NV_E4M3);
+    return lo | (hi << 16);
+}
+
+// Power-of-two scale of one (K slice, column) of A on the FP8 path: the smallest 2^e with
+// amax / 2^e <= 448 (the largest finite e4m3), from amax's float bits; 1 for an all-zero
+// column.  Dividing by it and multiplying the product back are exact.
+__device__ __forceinline__ float e4m3_scale(uint32_t amax_bits) {
+    const float amax = __uint_as_float(amax_bits);
+    if (!(amax > 0.f)) return 1.0f;
+    const uint32_t xb = __float_as_uint(__fdiv_rn(amax, 448.0f));
+    int e = (int)((xb >> 23) & 0xFFu) - 127;
+    if (e < -126) return 0x1p-126f;
+    if (xb & 0x7FFFFFu) ++e;
+    e = min(e, 127);
+    return __uint_as_float((uint32_t)(e + 127) << 23);
+}
+
+// One 16-byte chunk of Elem<kFp8>::PER_CHUNK finished entries.
+template <bool kFp8>
+__device__ __forceinline__ uint4 pack_chunk(const float *v) {
+    if (kFp8)
+        return make_uint4(pack_e4m3x4(v[0], v[1], v[2], v[3]), pack_e4m3x4(v[4], v[5], v[6], v[7]),
+                          pack_e4m3x4(v[8], v[9], v[10], v[11]),
+                          pack_e4m3x4(v[12], v[13], v[14], v[15]));
     return make_uint4(pack_bf16(v[0], v[1]), pack_bf16(v[2], v[3]), pack_bf16(v[4], v[5]),
                       pack_bf16(v[6], v[7]));
+}
+
+// PER_CHUNK consecutive natural-column entries starting at a block-aligned counter `c`
+// (PER_CHUNK / 4 Philox calls), finished (uniform entries scaled) and packed.
+template <bool kFp8>
+__device__ __forceinline__ uint4 gen_chunk_aligned(int family, uint4 c, uint2 key) {
+    constexpr int E = Elem<kFp8>::PER_CHUNK;
+    float v[E];
+    if (family == RBG_UNIFORM) {
+#pragma unroll
+        for (int q = 0; q < E / 4; ++q) {
+            const uint4 r = philox(q == 0 ? c : ctr_add_u32(c, (uint32_t)q), key);
+            v[4 * q] = uneg11_fma(r.x);
+            v[4 * q + 1] = uneg11_fma(r.y);
+            v[4 * q + 2] = uneg11_fma(r.z);
+            v[4 * q + 3] = uneg11_fma(r.w);
+        }
+#pragma unroll
+        for (int e = 0; e < E; ++e) v[e] = __fmul_rn(v[e], 1.7320508075688772f);
+    } else {
+#pragma unroll
+        for (int q = 0; q < E / 4; ++q)
+            gen4<true>(family, q == 0 ? c : ctr_add_u32(c, (uint32_t)q), key, v + 4 * q);
+    }
+    return pack_chunk<kFp8>(v);
 }
 
 // Eight consecutive natural-column entries C = Cs .. Cs+7 of natural row R, any alignment.
@@ -146,37 +196,40 @@ __device__ __forceinline__ void gen8_any(const DenseGen &g, int64_t R, int64_t C
     }
 }
 
-// Byte offset of BF16 element (row i, k) in a BM x BK tile stored K-major with the 64-byte
-// swizzle: row i occupies bytes [64 i, 64 i + 64); its 16-byte chunk c sits at chunk
-// c ^ ((i / 2) % 4) (address bits 4-5 XOR bits 7-8).
-__device__ __forceinline__ uint32_t sw_offset(int i, int k) {
-    return (uint32_t)(i * ROW_BYTES + ((((k >> 3) ^ ((i >> 1) & 3))) << 4) + (k & 7) * 2);
+// Byte offset of byte kb of row i in a BM-row tile stored K-major with the 64-byte swizzle:
+// row i occupies bytes [64 i, 64 i + 64); its 16-byte chunk c sits at chunk c ^ ((i / 2) % 4)
+// (address bits 4-5 XOR bits 7-8).
+__device__ __forceinline__ uint32_t sw_byte(int i, int kb) {
+    return (uint32_t)(i * ROW_BYTES + ((((kb >> 4) ^ ((i >> 1) & 3))) << 4) + (kb & 15));
 }
 
-// The part of one S stage this CTA produces: rows [row_lo, row_lo + rows) of the BM x BK
-// tile, by `nth` threads (thread index gt).  Generic path: any operator orientation and
-// submatrix offset.
+// The part of one S stage this CTA produces: rows [row_lo, row_lo + rows) of the stage, by
+// `nth` threads (thread index gt).  Generic path: any operator orientation and submatrix
+// offset.
+template <bool kFp8>
 __device__ __forceinline__ void produce_s_generic(uint8_t *tile, const LowpParams &p, int64_t i0,
                                                   int64_t k0, int row_lo, int rows, int gt,
                                                   int nth) {
+    constexpr int E = Elem<kFp8>::PER_CHUNK;
+    constexpr int BKE = Elem<kFp8>::BK;
     if (p.r_on_i) {
         for (int u = gt; u < rows * CHUNKS; u += nth) {
             const int i = row_lo + u / CHUNKS, c = u % CHUNKS;
-            const int64_t gi = i0 + i, gk = k0 + 8 * c;
+            const int64_t gi = i0 + i, gk = k0 + E * c;
             uint4 w = make_uint4(0, 0, 0, 0);
             if (gi < p.M && gk < p.K) {
-                float v[8];
-                gen8_any(p.gen, p.r0 + gi, p.c0 + gk, v);
+                float v[E];
 #pragma unroll
-                for (int e = 0; e < 8; ++e)
+                for (int h = 0; h < E / 8; ++h) gen8_any(p.gen, p.r0 + gi, p.c0 + gk + 8 * h, v + 8 * h);
+#pragma unroll
+                for (int e = 0; e < E; ++e)
                     if (gk + e >= p.K) v[e] = 0.f;
-                w = make_uint4(pack_bf16(v[0], v[1]), pack_bf16(v[2], v[3]),
-                               pack_bf16(v[4], v[5]), pack_bf16(v[6], v[7]));
+                w = pack_chunk<kFp8>(v);
             }
-            *reinterpret_cast<uint4 *>(tile + sw_offset(i, 8 * c)) = w;
+            *reinterpret_cast<uint4 *>(tile + sw_byte(i, 16 * c)) = w;
         }
     } else {
-        for (int u = gt; u < BK * (rows / 8); u += nth) {
+        for (int u = gt; u < BKE * (rows / 8); u += nth) {
             const int kk = u / (rows / 8), q = u % (rows / 8);
             const int64_t gk = k0 + kk, gi = i0 + row_lo + 8 * q;
             float v[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
@@ -187,9 +240,13 @@ __device__ __forceinline__ void produce_s_generic(uint8_t *tile, const LowpParam
                     if (gi + e >= p.M) v[e] = 0.f;
             }
 #pragma unroll
-            for (int e = 0; e < 8; ++e)
-                *reinterpret_cast<__nv_bfloat16 *>(tile + sw_offset(row_lo + 8 * q + e, kk)) =
-                    __float2bfloat16_rn(v[e]);
+            for (int e = 0; e < 8; ++e) {
+                uint8_t *dst = tile + sw_byte(row_lo + 8 * q + e, kk * Elem<kFp8>::BYTES);
+                if (kFp8)
+                    *dst = (uint8_t)(pack_e4m3x4(v[e], 0.f, 0.f, 0.f) & 0xFFu);
+                else
+                    *reinterpret_cast<__nv_bfloat16 *>(dst) = __float2bfloat16_rn(v[e]);
+            }
         }
     }
 }
@@ -200,10 +257,13 @@ __device__ __forceinline__ void produce_s_generic(uint8_t *tile, const LowpParam
 // into its peers with a bulk shared-memory copy -- and the CM CTAs of a column group hold the
 // same A tile, which each loads a 1 / CM share of with a TMA multicast to all of them.
 // kFast: natural row follows i and the operator's column offset is a multiple of 4, so every
-// 8-wide k chunk starts on a counter block.
-template <int CN, int CM, bool kFast>
+// k chunk starts on a counter block.  kFp8: e4m3 operands (kind::f8f6f4, 64 k per stage) and
+// the epilogue multiplies each column by its K slice's scale; else BF16 (kind::f16, 32 k).
+template <int CN, int CM, bool kFast, bool kFp8>
 __global__ void __launch_bounds__(NUM_THREADS, 1)
-    sketch_bf16_kernel(const __grid_constant__ CUtensorMap tmap_a, LowpParams p) {
+    sketch_tc_kernel(const __grid_constant__ CUtensorMap tmap_a, LowpParams p) {
+    constexpr int BKE = Elem<kFp8>::BK;
+    constexpr int PER_CHUNK = Elem<kFp8>::PER_CHUNK;
     constexpr int CS = CN * CM;
     constexpr int ROWS = BM / CN;                        // S rows this CTA produces per stage
     constexpr uint32_t PART_BYTES = ROWS * ROW_BYTES;    // their bytes in a stage
@@ -291,7 +351,8 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
     } else if (warp == 1) {
         // ---------------- MMA issuer
         if (lane == 0) {
-            constexpr uint32_t idesc = tc::idesc_bf16_f32(BM, BN / 2);
+            constexpr uint32_t idesc =
+                kFp8 ? tc::idesc_e4m3_f32(BM, BN / 2) : tc::idesc_bf16_f32(BM, BN / 2);
             int64_t it = 0, uc = 0;
             for (int64_t u = cluster_id; u < p.units; u += num_clusters, ++uc) {
                 int64_t m0, n0, ks0, ks1;
@@ -310,11 +371,18 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
                     const uint64_t bdesc1 = tc::kmajor_desc(
                         tc::smem_addr(a_tiles + s * A_STAGE_BYTES + A_STAGE_BYTES / 2), ROW_BYTES);
 #pragma unroll
-                    for (int kk = 0; kk < BK / 16; ++kk) {
+                    for (int kk = 0; kk < ROW_BYTES / 32; ++kk) {
                         const uint32_t acc = (ks > ks0 || kk > 0) ? 1u : 0u;
-                        // advancing 16 BF16 along k = 32 bytes = 2 in the encoded address
-                        tc::mma_f16(tmem, adesc + 2 * kk, bdesc0 + 2 * kk, idesc, acc);
-                        tc::mma_f16(tmem + BN / 2, adesc + 2 * kk, bdesc1 + 2 * kk, idesc, acc);
+                        // one MMA takes 32 bytes of k (16 BF16 or 32 e4m3) = 2 in the encoded
+                        // address
+                        if (kFp8) {
+                            tc::mma_f8(tmem, adesc + 2 * kk, bdesc0 + 2 * kk, idesc, acc);
+                            tc::mma_f8(tmem + BN / 2, adesc + 2 * kk, bdesc1 + 2 * kk, idesc, acc);
+                        } else {
+                            tc::mma_f16(tmem, adesc + 2 * kk, bdesc0 + 2 * kk, idesc, acc);
+                            tc::mma_f16(tmem + BN / 2, adesc + 2 * kk, bdesc1 + 2 * kk, idesc,
+                                        acc);
+                        }
                     }
                     // stage s of every CTA in the cluster may be rewritten by any of them, so
                     // each CTA's MMA completion is signalled to all of them
@@ -352,6 +420,13 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
                 tc::tmem_ld32(tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(c * 32), r);
                 tc::tmem_ld_wait();
                 const int64_t col = n0 + c * 32;
+                if (kFp8) {
+                    // undo the (K slice, column) scales of A (powers of two: exact)
+                    const uint32_t *am = p.amax + g * p.npad + col;
+#pragma unroll
+                    for (int v = 0; v < 32; ++v)
+                        r[v] = __float_as_uint(__uint_as_float(r[v]) * e4m3_scale(am[v]));
+                }
                 if (row < p.M && col < p.N) {
                     if (col + 32 <= p.N && (p.N & 3) == 0) {
 #pragma unroll
@@ -400,7 +475,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
                 for (int t = 0; t < FAST_ROWS; ++t) {
                     const int64_t gi_row = m0 + row_lo + tg / CHUNKS + t * ROW_SLOTS;
                     row_ok[t] = gi_row < p.M;
-                    base[t] = (p.r0 + gi_row) * p.gen.stride + p.c0 / 4 + 2 * fc;
+                    base[t] = (p.r0 + gi_row) * p.gen.stride + p.c0 / 4 + (PER_CHUNK / 4) * fc;
                 }
             }
             for (int64_t ks = ks0; ks < ks1; ++ks, ++it) {
@@ -409,18 +484,20 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
                 const uint32_t ph = (uint32_t)((it / STAGES) & 1);
                 if (!tc::mbar_wait(&empty[s], ph ^ 1, p.err)) goto done;
                 uint8_t *tile = s_tiles + s * S_STAGE_BYTES;
-                const int64_t gk = ks * BK + 8 * fc;
-                if (kFast && gk + 8 <= p.K) {
+                const int64_t gk = ks * BKE + PER_CHUNK * fc;
+                if (kFast && gk + PER_CHUNK <= p.K) {
 #pragma unroll
                     for (int t = 0; t < FAST_ROWS; ++t) {
                         const int i = row_lo + tg / CHUNKS + t * ROW_SLOTS;
-                        const uint4 c = ctr_add(p.gen.ctr, (uint64_t)(base[t] + ks * (BK / 4)));
-                        const uint4 w = row_ok[t] ? gen8_aligned(p.gen.family, c, p.gen.key)
-                                                  : make_uint4(0, 0, 0, 0);
-                        *reinterpret_cast<uint4 *>(tile + sw_offset(i, 8 * fc)) = w;
+                        const uint4 c = ctr_add(p.gen.ctr, (uint64_t)(base[t] + ks * (BKE / 4)));
+                        const uint4 w = row_ok[t]
+                                            ? gen_chunk_aligned<kFp8>(p.gen.family, c, p.gen.key)
+                                            : make_uint4(0, 0, 0, 0);
+                        *reinterpret_cast<uint4 *>(tile + sw_byte(i, 16 * fc)) = w;
                     }
                 } else {
-                    produce_s_generic(tile, p, m0, ks * BK, row_lo, ROWS, tg, GROUP_THREADS);
+                    produce_s_generic<kFp8>(tile, p, m0, ks * BKE, row_lo, ROWS, tg,
+                                            GROUP_THREADS);
                 }
                 tc::fence_proxy_async_smem();
                 tc::named_barrier(1 + gi, GROUP_THREADS);
@@ -450,13 +527,14 @@ done:
     }
 }
 
-// op(A)(k, j) -> At in BF16, k-blocked: element (k, j) at ((k / BK) * npad + j) * BK + k % BK,
-// so the TMA box of a stage (BK consecutive k of 256 consecutive j) is one contiguous block.
-// Rows j in [N, npad) and k in [K, kpad) are written as zeros.  When j has unit stride the
-// kernel transposes a 64 (k) x 128 (j) tile through shared memory (float4 reads along j,
-// 16-byte writes along k); when k has unit stride it converts in order.
-__device__ __forceinline__ int64_t blocked_index(int64_t k, int64_t j, int64_t npad) {
-    return ((k / BK) * npad + j) * BK + (k % BK);
+// op(A)(k, j) -> At, k-blocked with BKE values of k per block: element (k, j) at
+// ((k / BKE) * npad + j) * BKE + k % BKE, so the TMA box of a stage (BKE consecutive k of 256
+// consecutive j, 64 bytes each) is one contiguous block.  Rows j in [N, npad) and k in
+// [K, kpad) are written as zeros.  When j has unit stride the kernels transpose a 64 (k) x 128
+// (j) tile through shared memory (vector reads along j, 16-byte writes along k); when k has
+// unit stride they convert in order.
+__device__ __forceinline__ int64_t blocked_index(int64_t k, int64_t j, int64_t npad, int bke) {
+    return ((k / bke) * npad + j) * bke + (k % bke);
 }
 
 // Loads of A in its storage type (FP32 or BF16), widened to float.
@@ -499,7 +577,7 @@ __global__ void __launch_bounds__(256) convert_a_kernel(const TA *__restrict__ A
             uint2 w;
             w.x = pack_bf16(v[0], v[1]);
             w.y = pack_bf16(v[2], v[3]);
-            *reinterpret_cast<uint2 *>(At + blocked_index(k, j, npad)) = w;
+            *reinterpret_cast<uint2 *>(At + blocked_index(k, j, npad, Elem<false>::BK)) = w;
         }
         return;
     }
@@ -538,7 +616,107 @@ __global__ void __launch_bounds__(256) convert_a_kernel(const TA *__restrict__ A
             q.y = pack_bf16(tile[8 * c + 2][jj], tile[8 * c + 3][jj]);
             q.z = pack_bf16(tile[8 * c + 4][jj], tile[8 * c + 5][jj]);
             q.w = pack_bf16(tile[8 * c + 6][jj], tile[8 * c + 7][jj]);
-            *reinterpret_cast<uint4 *>(At + blocked_index(k, j0 + jj, npad)) = q;
+            *reinterpret_cast<uint4 *>(At + blocked_index(k, j0 + jj, npad, Elem<false>::BK)) = q;
+        }
+        __syncthreads();
+    }
+}
+
+// FP8 path, pass 0: amax[g * npad + j] = max |op(A)(k, j)| over k in K slice g (float bits,
+// atomicMax; the array starts zeroed).  grid.x: blocks of 256 columns (j unit stride) or of 8
+// columns (otherwise, one warp per column); grid.y: chunks of at most 2048 k inside one slice.
+template <typename TA>
+__global__ void __launch_bounds__(256) amax_kernel(const TA *__restrict__ A, int64_t sk,
+                                                   int64_t sj, int64_t K, int64_t N,
+                                                   int64_t k_per_group, int64_t chunks_per_group,
+                                                   uint32_t *__restrict__ amax, int64_t npad) {
+    constexpr int64_t CH = 2048;
+    const int64_t g = blockIdx.y / chunks_per_group;
+    const int64_t kb = g * k_per_group + (blockIdx.y % chunks_per_group) * CH;
+    const int64_t ke = min(min(kb + CH, (g + 1) * k_per_group), K);
+    if (sj == 1) {
+        const int64_t j = blockIdx.x * 256 + threadIdx.x;
+        if (j >= N) return;
+        float m = 0.f;
+        for (int64_t k = kb; k < ke; ++k) m = fmaxf(m, fabsf(load_a(A + k * sk + j)));
+        if (m > 0.f) atomicMax(amax + g * npad + j, __float_as_uint(m));
+    } else {
+        const int64_t j = blockIdx.x * 8 + (threadIdx.x >> 5);
+        if (j >= N) return;
+        const int lane = threadIdx.x & 31;
+        float m = 0.f;
+        for (int64_t k = kb + lane; k < ke; k += 32) m = fmaxf(m, fabsf(load_a(A + k * sk + j * sj)));
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xFFFFFFFFu, m, o));
+        if (lane == 0 && m > 0.f) atomicMax(amax + g * npad + j, __float_as_uint(m));
+    }
+}
+
+// FP8 path, pass 1: op(A)(k, j) / scale(g, j) -> e4m3, k-blocked with 64 k per block.
+template <typename TA>
+__global__ void __launch_bounds__(256) convert_a_fp8_kernel(const TA *__restrict__ A, int64_t sk,
+                                                            int64_t sj, int64_t K, int64_t N,
+                                                            int64_t kpad, int64_t npad,
+                                                            int64_t k_per_group,
+                                                            const uint32_t *__restrict__ amax,
+                                                            uint8_t *__restrict__ At) {
+    constexpr int BKE = Elem<true>::BK;
+    constexpr uintptr_t VEC_ALIGN = 4 * sizeof(TA) - 1;
+    __shared__ float tile[64][129];
+    if (sk == 1 && sj != 1) {
+        // direct: 16 consecutive k of one row j per thread
+        const int64_t kq = kpad / 16;
+        for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < kq * npad;
+             t += (int64_t)gridDim.x * blockDim.x) {
+            const int64_t j = t / kq, k = (t % kq) * 16;
+            float v[16];
+#pragma unroll
+            for (int e = 0; e < 16; ++e) v[e] = 0.f;
+            if (j < N) {
+                const float inv = __fdiv_rn(1.0f, e4m3_scale(amax[(k / k_per_group) * npad + j]));
+                const TA *src = A + j * sj + k;
+                for (int e = 0; e < 16; ++e) v[e] = k + e < K ? load_a(src + e) * inv : 0.f;
+            }
+            *reinterpret_cast<uint4 *>(At + blocked_index(k, j, npad, BKE)) = pack_chunk<true>(v);
+        }
+        return;
+    }
+    const int64_t tk = kpad / 64, tj = (npad + 127) / 128;
+    const bool vec = sj == 1 && (N % 4) == 0 && (sk % 4) == 0 &&
+                     (reinterpret_cast<uintptr_t>(A) & VEC_ALIGN) == 0;
+    for (int64_t t = blockIdx.x; t < tk * tj; t += gridDim.x) {
+        const int64_t k0 = (t % tk) * 64, j0 = (t / tk) * 128;
+        if (vec) {
+            for (int w = threadIdx.x; w < 64 * 32; w += 256) {
+                const int kk = w / 32, jq = (w % 32) * 4;
+                float4 f = make_float4(0.f, 0.f, 0.f, 0.f);
+                if (k0 + kk < K && j0 + jq < N) f = load_a4(A + (k0 + kk) * sk + j0 + jq);
+                tile[kk][jq] = f.x;
+                tile[kk][jq + 1] = f.y;
+                tile[kk][jq + 2] = f.z;
+                tile[kk][jq + 3] = f.w;
+            }
+        } else {
+            for (int w = threadIdx.x; w < 64 * 128; w += 256) {
+                const int kk = w / 128, jj = w % 128;
+                tile[kk][jj] = (k0 + kk < K && j0 + jj < N)
+                                   ? load_a(A + (k0 + kk) * sk + (j0 + jj) * sj)
+                                   : 0.f;
+            }
+        }
+        __syncthreads();
+        // 128 rows j x 4 chunks of 16 k: one 16-byte store each (one K slice per tile, since
+        // slices are whole multiples of 64 k)
+        const int64_t g = k0 / k_per_group;
+        for (int w = threadIdx.x; w < 128 * 4; w += 256) {
+            const int jj = w / 4, c = w % 4;
+            if (j0 + jj >= npad) continue;
+            const float inv = __fdiv_rn(1.0f, e4m3_scale(amax[g * npad + j0 + jj]));
+            float v[16];
+#pragma unroll
+            for (int e = 0; e < 16; ++e) v[e] = tile[16 * c + e][jj] * inv;
+            *reinterpret_cast<uint4 *>(At + blocked_index(k0 + 16 * c, j0 + jj, npad, BKE)) =
+                pack_chunk<true>(v);
         }
         __syncthreads();
     }
@@ -564,17 +742,21 @@ __global__ void lowp_reduce_kernel(int64_t M, int64_t N, int64_t groups, const f
 __device__ int g_lowp_error = 0;
 
 struct Plan {
+    bool fp8;
+    int bke;  // k values per stage
     int64_t k_steps, tiles_m, tiles_n, m_groups, n_groups, groups, ks_per_group, units, kpad,
         npad;
     int cn, cm;
-    size_t at_bytes, partial_bytes, total;
+    size_t at_bytes, amax_bytes, partial_bytes, total;
 };
 
 int resident_clusters(int cs);
 
-Plan make_plan(int64_t M, int64_t N, int64_t K) {
+Plan make_plan(int64_t M, int64_t N, int64_t K, bool fp8) {
     Plan pl{};
-    pl.k_steps = (K + BK - 1) / BK;
+    pl.fp8 = fp8;
+    pl.bke = fp8 ? Elem<true>::BK : Elem<false>::BK;
+    pl.k_steps = (K + pl.bke - 1) / pl.bke;
     pl.tiles_m = (M + BM - 1) / BM;
     pl.tiles_n = (N + BN - 1) / BN;
     pl.cn = pl.tiles_n >= 2 ? 2 : 1;
@@ -582,7 +764,7 @@ Plan make_plan(int64_t M, int64_t N, int64_t K) {
     pl.m_groups = (pl.tiles_m + pl.cm - 1) / pl.cm;
     pl.n_groups = (pl.tiles_n + pl.cn - 1) / pl.cn;
     const int slots = std::max(1, resident_clusters(pl.cn * pl.cm));
-    pl.kpad = pl.k_steps * BK;
+    pl.kpad = pl.k_steps * pl.bke;
     pl.npad = pl.tiles_n * BN;
     // K slices: fill whole waves of resident clusters, keep slices >= 32 k-steps, bound the
     // partial buffer at 1 GiB
@@ -603,17 +785,18 @@ Plan make_plan(int64_t M, int64_t N, int64_t K) {
     pl.ks_per_group = (pl.k_steps + best_g - 1) / best_g;
     pl.groups = (pl.k_steps + pl.ks_per_group - 1) / pl.ks_per_group;
     pl.units = tiles * pl.groups;
-    pl.at_bytes = ((size_t)pl.npad * pl.kpad * 2 + 1023) / 1024 * 1024;
+    pl.at_bytes = ((size_t)pl.npad * pl.kpad * (fp8 ? 1 : 2) + 1023) / 1024 * 1024;
+    pl.amax_bytes = fp8 ? ((size_t)pl.groups * pl.npad * 4 + 1023) / 1024 * 1024 : 0;
     pl.partial_bytes = (size_t)pl.groups * M * N * 4;
-    pl.total = pl.at_bytes + pl.partial_bytes;
+    pl.total = pl.at_bytes + pl.amax_bytes + pl.partial_bytes;
     return pl;
 }
 
-template <int CN, int CM, bool kFast>
+template <int CN, int CM, bool kFast, bool kFp8>
 void set_smem_attr() {
     static bool done = false;
     if (!done) {
-        RBG_CUDA(cudaFuncSetAttribute(sketch_bf16_kernel<CN, CM, kFast>,
+        RBG_CUDA(cudaFuncSetAttribute(sketch_tc_kernel<CN, CM, kFast, kFp8>,
                                       cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
         done = true;
     }
@@ -621,7 +804,7 @@ void set_smem_attr() {
 
 template <int CN, int CM>
 int query_resident_clusters() {
-    set_smem_attr<CN, CM, true>();
+    set_smem_attr<CN, CM, true, false>();
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(CN * CM * 256);
     cfg.blockDim = dim3(NUM_THREADS);
@@ -635,7 +818,7 @@ int query_resident_clusters() {
     cfg.numAttrs = 1;
     int n = 0;
     const cudaError_t e =
-        cudaOccupancyMaxActiveClusters(&n, sketch_bf16_kernel<CN, CM, true>, &cfg);
+        cudaOccupancyMaxActiveClusters(&n, sketch_tc_kernel<CN, CM, true, false>, &cfg);
     if (e != cudaSuccess || n <= 0) {
         cudaGetLastError();
         n = num_sms() / (CN * CM);
@@ -658,9 +841,9 @@ int resident_clusters(int cs) {
     return c;
 }
 
-template <int CN, int CM, bool kFast>
+template <int CN, int CM, bool kFast, bool kFp8>
 void launch_sketch(int clusters, const CUtensorMap &map, const LowpParams &p, cudaStream_t s) {
-    set_smem_attr<CN, CM, kFast>();
+    set_smem_attr<CN, CM, kFast, kFp8>();
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3((unsigned)(clusters * CN * CM));
     cfg.blockDim = dim3(NUM_THREADS);
@@ -673,18 +856,18 @@ void launch_sketch(int clusters, const CUtensorMap &map, const LowpParams &p, cu
     attr[0].val.clusterDim.z = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    RBG_CUDA(cudaLaunchKernelEx(&cfg, sketch_bf16_kernel<CN, CM, kFast>, map, p));
+    RBG_CUDA(cudaLaunchKernelEx(&cfg, sketch_tc_kernel<CN, CM, kFast, kFp8>, map, p));
     RBG_LAUNCHED();
 }
 
-template <bool kFast>
+template <bool kFast, bool kFp8>
 void launch_for(const Plan &pl, const CUtensorMap &map, const LowpParams &p, cudaStream_t s) {
     const int clusters =
         (int)std::min<int64_t>(pl.units, resident_clusters(pl.cn * pl.cm));
-    if (pl.cn == 2 && pl.cm == 2) launch_sketch<2, 2, kFast>(clusters, map, p, s);
-    else if (pl.cn == 2) launch_sketch<2, 1, kFast>(clusters, map, p, s);
-    else if (pl.cm == 2) launch_sketch<1, 2, kFast>(clusters, map, p, s);
-    else launch_sketch<1, 1, kFast>(clusters, map, p, s);
+    if (pl.cn == 2 && pl.cm == 2) launch_sketch<2, 2, kFast, kFp8>(clusters, map, p, s);
+    else if (pl.cn == 2) launch_sketch<2, 1, kFast, kFp8>(clusters, map, p, s);
+    else if (pl.cm == 2) launch_sketch<1, 2, kFast, kFp8>(clusters, map, p, s);
+    else launch_sketch<1, 1, kFast, kFp8>(clusters, map, p, s);
 }
 
 using EncodeFn = CUresult (*)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *,
@@ -707,11 +890,12 @@ EncodeFn encode_fn() {
     return fn;
 }
 
-void lowp_bf16(int64_t M, int64_t N, int64_t K, float alpha, const DenseGen &gen, int64_t r0,
-               int64_t c0, int r_on_i, const Strided &Q, bool a_bf16, float beta, float *out,
-               int64_t os_i, int64_t os_j, void *workspace, size_t ws_bytes, cudaStream_t s) {
+void lowp_run(bool fp8, int64_t M, int64_t N, int64_t K, float alpha, const DenseGen &gen,
+              int64_t r0, int64_t c0, int r_on_i, const Strided &Q, bool a_bf16, float beta,
+              float *out, int64_t os_i, int64_t os_j, void *workspace, size_t ws_bytes,
+              cudaStream_t s) {
     const int sms = num_sms();
-    const Plan pl = make_plan(M, N, K);
+    const Plan pl = make_plan(M, N, K, fp8);
     Scratch own;
     uint8_t *ws = static_cast<uint8_t *>(workspace);
     if (!ws) {
@@ -722,31 +906,58 @@ void lowp_bf16(int64_t M, int64_t N, int64_t K, float alpha, const DenseGen &gen
     } else if ((reinterpret_cast<uintptr_t>(ws) & 1023) != 0) {
         fail(RBG_ERROR_INVALID_ARGUMENT, "workspace must be 1024-byte aligned");
     }
-    __nv_bfloat16 *At = reinterpret_cast<__nv_bfloat16 *>(ws);
-    float *partial = reinterpret_cast<float *>(ws + pl.at_bytes);
+    uint8_t *At = ws;
+    uint32_t *amax = fp8 ? reinterpret_cast<uint32_t *>(ws + pl.at_bytes) : nullptr;
+    float *partial = reinterpret_cast<float *>(ws + pl.at_bytes + pl.amax_bytes);
 
+    if (fp8) {
+        ProfScope prof("lowp_amax", s);
+        RBG_CUDA(cudaMemsetAsync(amax, 0, pl.amax_bytes, s));
+        const int64_t kpg = pl.ks_per_group * pl.bke;
+        const int64_t cpg = (kpg + 2047) / 2048;
+        const dim3 grid((unsigned)(Q.s1 == 1 ? (N + 255) / 256 : (N + 7) / 8),
+                        (unsigned)(pl.groups * cpg));
+        if (grid.y > 65535) fail(RBG_ERROR_UNSUPPORTED, "FP8 path: too many K chunks");
+        if (a_bf16)
+            amax_kernel<<<grid, 256, 0, s>>>(static_cast<const __nv_bfloat16 *>(Q.ptr), Q.s0,
+                                             Q.s1, K, N, kpg, cpg, amax, pl.npad);
+        else
+            amax_kernel<<<grid, 256, 0, s>>>(static_cast<const float *>(Q.ptr), Q.s0, Q.s1, K,
+                                             N, kpg, cpg, amax, pl.npad);
+        RBG_LAUNCHED();
+    }
     {
         ProfScope prof("lowp_convert_a", s);
-        if (a_bf16)
+        const int64_t kpg = pl.ks_per_group * pl.bke;
+        if (fp8 && a_bf16)
+            convert_a_fp8_kernel<<<sms * 8, 256, 0, s>>>(
+                static_cast<const __nv_bfloat16 *>(Q.ptr), Q.s0, Q.s1, K, N, pl.kpad, pl.npad,
+                kpg, amax, At);
+        else if (fp8)
+            convert_a_fp8_kernel<<<sms * 8, 256, 0, s>>>(static_cast<const float *>(Q.ptr), Q.s0,
+                                                         Q.s1, K, N, pl.kpad, pl.npad, kpg, amax,
+                                                         At);
+        else if (a_bf16)
             convert_a_kernel<<<sms * 8, 256, 0, s>>>(static_cast<const __nv_bfloat16 *>(Q.ptr),
-                                                     Q.s0, Q.s1, K, N, pl.kpad, pl.npad, At);
+                                                     Q.s0, Q.s1, K, N, pl.kpad, pl.npad,
+                                                     reinterpret_cast<__nv_bfloat16 *>(At));
         else
             convert_a_kernel<<<sms * 8, 256, 0, s>>>(static_cast<const float *>(Q.ptr), Q.s0,
-                                                     Q.s1, K, N, pl.kpad, pl.npad, At);
+                                                     Q.s1, K, N, pl.kpad, pl.npad,
+                                                     reinterpret_cast<__nv_bfloat16 *>(At));
         RBG_LAUNCHED();
     }
 
     CUtensorMap map;
-    // rows of BK elements: row r = (k / BK) * npad + j
-    const cuuint64_t dims[2] = {(cuuint64_t)BK, (cuuint64_t)pl.npad * pl.k_steps};
-    const cuuint64_t strides[1] = {(cuuint64_t)BK * 2};
-    const cuuint32_t box[2] = {(cuuint32_t)BK, (cuuint32_t)(BN / 2)};
+    // rows of 64 bytes (bke values): row r = (k / bke) * npad + j
+    const cuuint64_t dims[2] = {(cuuint64_t)pl.bke, (cuuint64_t)pl.npad * pl.k_steps};
+    const cuuint64_t strides[1] = {(cuuint64_t)ROW_BYTES};
+    const cuuint32_t box[2] = {(cuuint32_t)pl.bke, (cuuint32_t)(BN / 2)};
     const cuuint32_t estr[2] = {1, 1};
-    const CUresult cr = encode_fn()(&map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, At, dims, strides,
-                                    box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
-                                    CU_TENSOR_MAP_SWIZZLE_64B,
-                                    CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-                                    CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    const CUresult cr = encode_fn()(
+        &map, fp8 ? CU_TENSOR_MAP_DATA_TYPE_UINT8 : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, At, dims,
+        strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B,
+        CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (cr != CUDA_SUCCESS) fail(RBG_ERROR_CUDA, "cuTensorMapEncodeTiled failed");
 
     int *err = nullptr;
@@ -756,12 +967,17 @@ void lowp_bf16(int64_t M, int64_t N, int64_t K, float alpha, const DenseGen &gen
     p.gen = gen; p.r0 = r0; p.c0 = c0; p.r_on_i = r_on_i;
     p.k_steps = pl.k_steps; p.m_groups = pl.m_groups; p.n_groups = pl.n_groups;
     p.ks_per_group = pl.ks_per_group; p.units = pl.units; p.npad = pl.npad;
-    p.partial = partial; p.err = err;
+    p.partial = partial; p.amax = amax; p.err = err;
     const bool fast = r_on_i && (c0 % 4) == 0;
     {
-        ProfScope prof("lowp_sketch_bf16_tc", s);
-        if (fast) launch_for<true>(pl, map, p, s);
-        else launch_for<false>(pl, map, p, s);
+        ProfScope prof(fp8 ? "lowp_sketch_fp8_tc" : "lowp_sketch_bf16_tc", s);
+        if (fp8) {
+            if (fast) launch_for<true, true>(pl, map, p, s);
+            else launch_for<false, true>(pl, map, p, s);
+        } else {
+            if (fast) launch_for<true, false>(pl, map, p, s);
+            else launch_for<false, false>(pl, map, p, s);
+        }
     }
     {
         ProfScope prof("lowp_reduce", s);
@@ -799,10 +1015,10 @@ extern "C" int rbg_lskge3_lowp_workspace(int32_t precision, int64_t d, int64_t n
                                          size_t *bytes) {
     return guarded_lowp([&] {
         if (!bytes) fail(RBG_ERROR_INVALID_ARGUMENT, "bytes must not be NULL");
-        if (precision != RBG_PREC_BF16)
-            fail(RBG_ERROR_UNSUPPORTED, "only RBG_PREC_BF16 is provided");
+        if (precision != RBG_PREC_BF16 && precision != RBG_PREC_FP8_E4M3)
+            fail(RBG_ERROR_INVALID_ARGUMENT, "precision must be RBG_PREC_BF16 or RBG_PREC_FP8_E4M3");
         RBG_REQUIRE("lskge3_lowp", d > 0 && n > 0 && m > 0);
-        *bytes = make_plan(d, n, m).total;
+        *bytes = make_plan(d, n, m, precision == RBG_PREC_FP8_E4M3).total;
     });
 }
 
@@ -823,8 +1039,8 @@ int lowp_entry(int32_t precision, int32_t a_dtype, int32_t layout, int32_t opS, 
                int64_t ro_s, int64_t co_s, const void *A, int64_t lda, float beta, float *B,
                int64_t ldb, void *workspace, size_t workspace_bytes, rbg_stream_t stream) {
     return guarded_lowp([&] {
-        if (precision != RBG_PREC_BF16)
-            fail(RBG_ERROR_UNSUPPORTED, "only RBG_PREC_BF16 is provided");
+        if (precision != RBG_PREC_BF16 && precision != RBG_PREC_FP8_E4M3)
+            fail(RBG_ERROR_INVALID_ARGUMENT, "precision must be RBG_PREC_BF16 or RBG_PREC_FP8_E4M3");
         if (a_dtype != RBG_F32 && a_dtype != RBG_BF16)
             fail(RBG_ERROR_INVALID_ARGUMENT, "a_dtype must be RBG_F32 or RBG_BF16");
         if (layout != RBG_COL_MAJOR && layout != RBG_ROW_MAJOR)
@@ -860,7 +1076,7 @@ int lowp_entry(int32_t precision, int32_t a_dtype, int32_t layout, int32_t opS, 
             return;
         }
         if (!A) fail(RBG_ERROR_INVALID_ARGUMENT, "A must not be NULL");
-        if ((double)((m + BK - 1) / BK) * (double)((n + BN - 1) / BN * BN) > (double)INT32_MAX)
+        if ((double)((m + 31) / 32) * (double)((n + BN - 1) / BN * BN) > (double)INT32_MAX)
             fail(RBG_ERROR_UNSUPPORTED, "dimensions too large for 32-bit TMA coordinates");
         const int64_t ars = layout == RBG_COL_MAJOR ? 1 : lda;
         const int64_t acs = layout == RBG_COL_MAJOR ? lda : 1;
@@ -879,8 +1095,9 @@ int lowp_entry(int32_t precision, int32_t a_dtype, int32_t layout, int32_t opS, 
             r0 = co_s;
             c0 = ro_s;
         }
-        lowp_bf16(d, n, m, alpha, make_dense_gen(S->dist, S->seed_state), r0, c0, r_on_i, Q,
-                  a_dtype == RBG_BF16, beta, B, brs, bcs, workspace, workspace_bytes, s);
+        lowp_run(precision == RBG_PREC_FP8_E4M3, d, n, m, alpha,
+                 make_dense_gen(S->dist, S->seed_state), r0, c0, r_on_i, Q, a_dtype == RBG_BF16,
+                 beta, B, brs, bcs, workspace, workspace_bytes, s);
     });
 }
 }  // namespace

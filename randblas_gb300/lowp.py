@@ -1,7 +1,7 @@
 """Tensor-core precision path (rbg_lskge3_lowp): the left dense sketch with the operator's
-entries generated in-kernel and rounded, together with A, to BF16 (or FP8 e4m3 with per-128
-scales), FP32 accumulation.  No reference counterpart; same argument meaning as
-sketch_general's left form with T = float."""
+entries generated in-kernel and rounded, together with A, to BF16 or FP8 e4m3 (A with one
+power-of-two scale per column and K slice), FP32 accumulation on tcgen05 tensor cores.  No
+reference counterpart; same argument meaning as sketch_general's left form with T = float."""
 from __future__ import annotations
 
 import ctypes as C
