@@ -248,15 +248,23 @@ def main():
     # accuracy of the headline result against an FP64 oracle on sampled row blocks
     headline()
     torch.cuda.synchronize()
-    err_num, err_den = 0.0, 0.0
-    for r0 in (0, 1024, 2048, 4032):
-        Sblk = torch.empty(64 * M_SK, dtype=torch.float64, device=device)
-        rb.fill_dense_unpacked(rb.Layout.RowMajor, S.dist, 64, M_SK, r0, 0, Sblk, S.seed_state)
-        ref = Sblk.view(64, M_SK) @ A.double()
-        err_num += float((B[r0:r0 + 64].double() - ref).norm() ** 2)
-        err_den += float(ref.norm() ** 2)
-        del Sblk, ref
-    rel_err = (err_num / err_den) ** 0.5
+    rel_err = sampled_rel_err(torch, rb, S, A, B, device)
+
+    # the same sketch with FP8 e4m3 operands (a second precision form of this path)
+    fp8 = None
+    if have_lowp:
+        def fused_fp8():
+            lowp.sketch_lowp(rb.Layout.RowMajor, rb.Op.NoTrans, rb.Op.NoTrans, D_SK, N_SK, M_SK,
+                             1.0, S, 0, 0, A, N_SK, 0.0, B, N_SK, precision=lowp.FP8_E4M3)
+        rb.profile.enable(True)
+        ms8 = event_time(torch, fused_fp8, args.steps, args.warmup, stream)
+        prof8 = rb.profile.read()
+        rb.profile.enable(False)
+        fp8 = {"ms_per_step": round(ms8, 4), "TFLOP/s": round(flops / (ms8 * 1e-3) / 1e12, 1),
+               "speedup_vs_fp32_plain": round(ms_plain / ms8, 2),
+               "rel_frobenius_err_vs_fp64": sampled_rel_err(torch, rb, S, A, B, device),
+               "kernels_ms": {k: round(v["ms"] / max(1, v["launches"]), 4)
+                              for k, v in prof8.items()}}
 
     # subspace-embedding distortion of the headline operator on range(A) = range(U):
     # extreme singular values of S U / sqrt(d) (FP64 SVD on the host)
@@ -304,12 +312,8 @@ def main():
                "ms_per_sketch": round(full_s * 1e3, 1)}
 
     # aggregate over ranks
-    ms_max = ms
-    if world > 1:
-        tt = torch.tensor([ms], device=device)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        ms_max = float(tt.item())
-    value = world * flops / (ms_max * 1e-3) / 1e12
+    ms_max = max_time_over_ranks(torch, dist if world > 1 else None, ms, device)
+    value = aggregate_tflops(world, flops, ms_max)
     if rank == 0:
         line = {
             "metric": METRIC, "value": round(value, 2), "unit": "TFLOP/s", "n_gpus": world,
@@ -327,7 +331,7 @@ def main():
                            "TFLOP/s": round(flops / (ms_plain * 1e-3) / 1e12, 2)},
             "speedup_vs_fp32_plain": round(ms_plain / ms_max, 2),
             "rel_frobenius_err_vs_fp64": rel_err,
-            "embedding_distortion": distortion,
+            "embedding_distortion": distortion, "fp8_e4m3": fp8,
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
             "gpu_launches": gpu_launches, "clocks": clk.summary(), "saso": saso,
             "dense_fp64_small": small, "autograd": autograd_row, "batched": batched_row,
@@ -338,18 +342,48 @@ def main():
         dist.destroy_process_group()
 
 
+def max_time_over_ranks(torch, dist, ms, device):
+    """The slowest rank's time per step (every rank calls this; dist None = one process)."""
+    if dist is None:
+        return ms
+    t = torch.tensor([ms], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def aggregate_tflops(world, flops_per_step, ms_max):
+    """Whole-job throughput: every replica sketches one full workload per step (weak scaling)."""
+    return world * flops_per_step / (ms_max * 1e-3) / 1e12
+
+
+def sampled_rel_err(torch, rb, S, A, B, device):
+    """Relative Frobenius error of B = S A on four 64-row blocks against an FP64 product with
+    the FP64 operator rows from fill_dense_unpacked."""
+    err_num, err_den = 0.0, 0.0
+    for r0 in (0, 1024, 2048, 4032):
+        Sblk = torch.empty(64 * M_SK, dtype=torch.float64, device=device)
+        rb.fill_dense_unpacked(rb.Layout.RowMajor, S.dist, 64, M_SK, r0, 0, Sblk, S.seed_state)
+        ref = Sblk.view(64, M_SK) @ A.double()
+        err_num += float((B[r0:r0 + 64].double() - ref).norm() ** 2)
+        err_den += float(ref.norm() ** 2)
+        del Sblk, ref
+    return (err_num / err_den) ** 0.5
+
+
 def embedding_distortion(torch, rb, lowp, have_lowp, S, U, device):
     """max(sigma_max - 1, 1 - sigma_min) of S U / sqrt(d) for the headline path (and the plain
     FP32 path): S is an approximate isometry on range(U) after the 1/sqrt(d) scaling (uniform
     entries have unit variance)."""
     import numpy as np
     out = {}
-    paths = [("plain_fp32", False)] + ([("bf16_tc", True)] if have_lowp else [])
-    for name, fused in paths:
+    paths = [("plain_fp32", None)]
+    if have_lowp:
+        paths += [("bf16_tc", lowp.BF16), ("fp8_e4m3_tc", lowp.FP8_E4M3)]
+    for name, prec in paths:
         SU = torch.empty(D_SK, N_SK, device=device)
-        if fused:
+        if prec is not None:
             lowp.sketch_lowp(rb.Layout.RowMajor, rb.Op.NoTrans, rb.Op.NoTrans, D_SK, N_SK, M_SK,
-                             1.0, S, 0, 0, U, N_SK, 0.0, SU, N_SK)
+                             1.0, S, 0, 0, U, N_SK, 0.0, SU, N_SK, precision=prec)
         else:
             rb.sketch_general(rb.Layout.RowMajor, rb.Op.NoTrans, rb.Op.NoTrans, D_SK, N_SK,
                               M_SK, 1.0, S, U, N_SK, 0.0, SU, N_SK)

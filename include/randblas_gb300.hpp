@@ -1,0 +1,281 @@
+// randblas_gb300.hpp -- C++ front end of the GB300 sketching library, shaped like RandBLAS's own
+// API so a RandBLAS caller can switch its device-memory code paths over by namespace:
+//
+//     #include <randblas_gb300.hpp>
+//     namespace RB = RandBLAS_GB300;   // instead of RandBLAS, for device buffers
+//     RB::DenseDist D(d, m);
+//     RB::DenseSkOp<float> S(D, RB::RNGState(42));
+//     RB::sketch_general(RB::Layout::RowMajor, RB::Op::NoTrans, RB::Op::NoTrans, d, n, m,
+//                        1.0f, S, A_dev, n, 0.0f, B_dev, n);
+//
+// Types and functions mirror RandBLAS (RNGState base.hh:64-164, DenseDist dense_skops.hh:231-350,
+// DenseSkOp 357-478, fill_dense 563-658, SparseDist sparse_skops.hh:131-246, SparseSkOp 289-450,
+// fill_sparse 587-603, sketch_general skge.hh:756-1199, sketch_vector skve.hh:140-246,
+// sketch_sparse sparse_data/sksp.hh:418-539).  Matrix and vector pointers are CUDA device
+// pointers; every call is asynchronous on `stream` (default: the legacy default stream).
+// Failed argument checks throw RandBLAS_GB300::Error carrying the reference's message text;
+// size overflows throw std::overflow_error, as RandBLAS's safe_int_product does.
+#pragma once
+
+#include <cstdint>
+#include <stdexcept>
+#include <string>
+#include <type_traits>
+
+#include "randblas_gb300.h"
+
+namespace RandBLAS_GB300 {
+
+enum class Layout : int32_t { ColMajor = RBG_COL_MAJOR, RowMajor = RBG_ROW_MAJOR };
+enum class Op : int32_t { NoTrans = RBG_NO_TRANS, Trans = RBG_TRANS };
+enum class ScalarDist : int32_t { Gaussian = RBG_GAUSSIAN, Uniform = RBG_UNIFORM };
+enum class Axis : int32_t { Short = RBG_AXIS_SHORT, Long = RBG_AXIS_LONG };
+
+struct Error : std::runtime_error {
+    int code;
+    Error(int c, const std::string &m) : std::runtime_error(m), code(c) {}
+};
+
+namespace detail {
+inline void check(int rc) {
+    if (rc == RBG_SUCCESS) return;
+    const std::string msg = rbg_last_error();
+    if (rc == RBG_ERROR_OVERFLOW) throw std::overflow_error(msg);
+    throw Error(rc, msg);
+}
+template <typename T>
+constexpr int32_t dtype() {
+    static_assert(std::is_same<T, float>::value || std::is_same<T, double>::value,
+                  "T must be float or double");
+    return std::is_same<T, float>::value ? RBG_F32 : RBG_F64;
+}
+template <typename I>
+constexpr int32_t itype() {
+    static_assert(std::is_same<I, int32_t>::value || std::is_same<I, int64_t>::value,
+                  "sint_t must be int32_t or int64_t");
+    return std::is_same<I, int32_t>::value ? RBG_I32 : RBG_I64;
+}
+}  // namespace detail
+
+// RNGState<Philox4x32>: 128-bit counter, 64-bit key; RNGState(k) has counter 0 and key k.
+struct RNGState {
+    rbg_state s{};
+    RNGState() = default;
+    explicit RNGState(uint64_t k) { detail::check(rbg_state_from_key(k, &s)); }
+    explicit RNGState(const rbg_state &raw) : s(raw) {}
+    RNGState incr(uint64_t n) const {
+        rbg_state out;
+        detail::check(rbg_state_incr(&s, n, &out));
+        return RNGState(out);
+    }
+    bool operator==(const RNGState &o) const {
+        for (int i = 0; i < 4; ++i)
+            if (s.counter[i] != o.s.counter[i]) return false;
+        return s.key[0] == o.s.key[0] && s.key[1] == o.s.key[1];
+    }
+    bool operator!=(const RNGState &o) const { return !(*this == o); }
+};
+
+struct DenseDist {
+    rbg_dense_dist d{};
+    int64_t n_rows, n_cols, dim_major, dim_minor;
+    ScalarDist family;
+    Axis major_axis;
+    Layout natural_layout;
+    double isometry_scale;
+    DenseDist(int64_t rows, int64_t cols, ScalarDist fam = ScalarDist::Gaussian,
+              Axis axis = Axis::Long)
+        : n_rows(rows), n_cols(cols), family(fam), major_axis(axis) {
+        d.n_rows = rows;
+        d.n_cols = cols;
+        d.family = static_cast<int32_t>(fam);
+        d.major_axis = static_cast<int32_t>(axis);
+        int32_t nat = 0;
+        detail::check(rbg_dense_dist_properties(&d, &dim_major, &dim_minor, &nat,
+                                                &isometry_scale));
+        natural_layout = static_cast<Layout>(nat);
+    }
+};
+
+// dense::compute_next_state
+inline RNGState compute_next_state(const DenseDist &D, const RNGState &seed) {
+    rbg_state out;
+    detail::check(rbg_dense_next_state(&D.d, &seed.s, &out));
+    return RNGState(out);
+}
+
+template <typename T>
+struct DenseSkOp {
+    DenseDist dist;
+    RNGState seed_state, next_state;
+    int64_t n_rows, n_cols;
+    Layout layout;
+    T *buff = nullptr;  // device buffer once filled (fill_dense); the caller owns it
+    DenseSkOp(const DenseDist &D, const RNGState &seed)
+        : dist(D), seed_state(seed), next_state(compute_next_state(D, seed)),
+          n_rows(D.n_rows), n_cols(D.n_cols), layout(D.natural_layout) {}
+    rbg_dense_skop c() const {
+        rbg_dense_skop s{};
+        s.dist = dist.d;
+        s.seed_state = seed_state.s;
+        s.next_state = next_state.s;
+        s.dtype = detail::dtype<T>();
+        s.layout = static_cast<int32_t>(layout);
+        s.buff = buff;
+        return s;
+    }
+};
+
+struct SparseDist {
+    rbg_sparse_dist d{};
+    int64_t n_rows, n_cols, vec_nnz, dim_major, dim_minor, full_nnz;
+    Axis major_axis;
+    double isometry_scale;
+    SparseDist(int64_t rows, int64_t cols, int64_t nnz_per_vec = 4, Axis axis = Axis::Short)
+        : n_rows(rows), n_cols(cols), vec_nnz(nnz_per_vec), major_axis(axis) {
+        d.n_rows = rows;
+        d.n_cols = cols;
+        d.vec_nnz = nnz_per_vec;
+        d.major_axis = static_cast<int32_t>(axis);
+        detail::check(rbg_sparse_dist_properties(&d, &dim_major, &dim_minor, &full_nnz,
+                                                 &isometry_scale));
+    }
+};
+
+inline RNGState compute_next_state(const SparseDist &D, const RNGState &seed) {
+    rbg_state out;
+    detail::check(rbg_sparse_next_state(&D.d, &seed.s, &out));
+    return RNGState(out);
+}
+
+template <typename T, typename sint_t = int64_t>
+struct SparseSkOp {
+    SparseDist dist;
+    RNGState seed_state, next_state;
+    int64_t n_rows, n_cols;
+    int64_t nnz = -1;  // -1: not sampled (sketching samples in-kernel)
+    T *vals = nullptr;  // device arrays of dist.full_nnz entries for fill_sparse
+    sint_t *rows = nullptr;
+    sint_t *cols = nullptr;
+    SparseSkOp(const SparseDist &D, const RNGState &seed)
+        : dist(D), seed_state(seed), next_state(compute_next_state(D, seed)),
+          n_rows(D.n_rows), n_cols(D.n_cols) {}
+    rbg_sparse_skop c() const {
+        rbg_sparse_skop s{};
+        s.dist = dist.d;
+        s.seed_state = seed_state.s;
+        s.next_state = next_state.s;
+        s.nnz = nnz;
+        s.dtype = detail::dtype<T>();
+        s.itype = detail::itype<sint_t>();
+        s.vals = vals;
+        s.rows = rows;
+        s.cols = cols;
+        return s;
+    }
+};
+
+// ------------------------------------------------------------------ sampling
+template <typename T>
+RNGState fill_dense_unpacked(Layout layout, const DenseDist &D, int64_t n_rows, int64_t n_cols,
+                             int64_t ro_s, int64_t co_s, T *buff, const RNGState &seed,
+                             rbg_stream_t stream = nullptr) {
+    rbg_state next;
+    detail::check(rbg_fill_dense_unpacked(detail::dtype<T>(), static_cast<int32_t>(layout), &D.d,
+                                          n_rows, n_cols, ro_s, co_s, buff, &seed.s, &next,
+                                          stream));
+    return RNGState(next);
+}
+
+template <typename T>
+RNGState fill_dense(const DenseDist &D, T *buff, const RNGState &seed,
+                    rbg_stream_t stream = nullptr) {
+    rbg_state next;
+    detail::check(rbg_fill_dense(detail::dtype<T>(), &D.d, buff, &seed.s, &next, stream));
+    return RNGState(next);
+}
+
+// fill_dense(S): S.buff must point at n_rows * n_cols device entries.
+template <typename T>
+void fill_dense(DenseSkOp<T> &S, rbg_stream_t stream = nullptr) {
+    rbg_dense_skop c = S.c();
+    detail::check(rbg_fill_dense_skop(&c, stream));
+}
+
+// fill_sparse(S): S.vals / rows / cols must point at dist.full_nnz device entries.
+template <typename T, typename I>
+void fill_sparse(SparseSkOp<T, I> &S, rbg_stream_t stream = nullptr) {
+    rbg_sparse_skop c = S.c();
+    detail::check(rbg_fill_sparse(&c, stream));
+    S.nnz = c.nnz;
+}
+
+// ------------------------------------------------------------------ sketch_general
+// Left, submatrix: B = alpha * op(submat(S)) * op(A) + beta * B.
+template <typename T>
+void sketch_general(Layout layout, Op opS, Op opA, int64_t d, int64_t n, int64_t m, T alpha,
+                    const DenseSkOp<T> &S, int64_t ro_s, int64_t co_s, const T *A, int64_t lda,
+                    T beta, T *B, int64_t ldb, rbg_stream_t stream = nullptr) {
+    const rbg_dense_skop c = S.c();
+    detail::check(rbg_lskge3(static_cast<int32_t>(layout), static_cast<int32_t>(opS),
+                             static_cast<int32_t>(opA), d, n, m, alpha, &c, ro_s, co_s, A, lda,
+                             beta, B, ldb, stream));
+}
+// Left, whole operator.
+template <typename T>
+void sketch_general(Layout layout, Op opS, Op opA, int64_t d, int64_t n, int64_t m, T alpha,
+                    const DenseSkOp<T> &S, const T *A, int64_t lda, T beta, T *B, int64_t ldb,
+                    rbg_stream_t stream = nullptr) {
+    const int64_t rows = opS == Op::NoTrans ? d : m, cols = opS == Op::NoTrans ? m : d;
+    if (S.n_rows != rows || S.n_cols != cols)
+        throw Error(RBG_ERROR_INVALID_ARGUMENT,
+                    "(S.n_rows == " + std::to_string(rows) + " && S.n_cols == " +
+                        std::to_string(cols) + ") was required, but did not hold, in function " +
+                        "sketch_general");
+    sketch_general(layout, opS, opA, d, n, m, alpha, S, 0, 0, A, lda, beta, B, ldb, stream);
+}
+// Right, submatrix: B = alpha * op(A) * op(submat(S)) + beta * B.
+template <typename T>
+void sketch_general(Layout layout, Op opA, Op opS, int64_t m, int64_t d, int64_t n, T alpha,
+                    const T *A, int64_t lda, const DenseSkOp<T> &S, int64_t ro_s, int64_t co_s,
+                    T beta, T *B, int64_t ldb, rbg_stream_t stream = nullptr) {
+    const rbg_dense_skop c = S.c();
+    detail::check(rbg_rskge3(static_cast<int32_t>(layout), static_cast<int32_t>(opA),
+                             static_cast<int32_t>(opS), m, d, n, alpha, A, lda, &c, ro_s, co_s,
+                             beta, B, ldb, stream));
+}
+// Left with a sparse operator (sampled in-kernel when S.nnz < 0).
+template <typename T, typename I>
+void sketch_general(Layout layout, Op opS, Op opA, int64_t d, int64_t n, int64_t m, T alpha,
+                    const SparseSkOp<T, I> &S, int64_t ro_s, int64_t co_s, const T *A,
+                    int64_t lda, T beta, T *B, int64_t ldb, rbg_stream_t stream = nullptr) {
+    const rbg_sparse_skop c = S.c();
+    detail::check(rbg_lskges(static_cast<int32_t>(layout), static_cast<int32_t>(opS),
+                             static_cast<int32_t>(opA), d, n, m, alpha, &c, ro_s, co_s, A, lda,
+                             beta, B, ldb, stream));
+}
+// Right with a sparse operator.
+template <typename T, typename I>
+void sketch_general(Layout layout, Op opA, Op opS, int64_t m, int64_t d, int64_t n, T alpha,
+                    const T *A, int64_t lda, const SparseSkOp<T, I> &S, int64_t ro_s,
+                    int64_t co_s, T beta, T *B, int64_t ldb, rbg_stream_t stream = nullptr) {
+    const rbg_sparse_skop c = S.c();
+    detail::check(rbg_rskges(static_cast<int32_t>(layout), static_cast<int32_t>(opA),
+                             static_cast<int32_t>(opS), m, d, n, alpha, A, lda, &c, ro_s, co_s,
+                             beta, B, ldb, stream));
+}
+
+// sketch_vector: y = alpha * op(submat(S)) * x + beta * y.
+template <typename T>
+void sketch_vector(Op opS, int64_t d, int64_t m, T alpha, const DenseSkOp<T> &S, int64_t ro_s,
+                   int64_t co_s, const T *x, int64_t incx, T beta, T *y, int64_t incy,
+                   rbg_stream_t stream = nullptr) {
+    const rbg_dense_skop c = S.c();
+    detail::check(rbg_sketch_vector(static_cast<int32_t>(opS), d, m, alpha, &c, ro_s, co_s, x,
+                                    incx, beta, y, incy, stream));
+}
+
+// Process-wide reproducibility switch (no RandBLAS counterpart).
+inline void set_deterministic(bool on) { detail::check(rbg_set_deterministic(on ? 1 : 0)); }
+
+}  // namespace RandBLAS_GB300

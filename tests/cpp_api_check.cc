@@ -1,0 +1,63 @@
+// A C++ caller of include/randblas_gb300.hpp, built by tests/test_cpp_api.py.  Exercises the
+// host-side parts (states, distributions, next states) and the argument checks, which fail
+// before any device work, so it runs without a GPU.  Prints one line per failed check.
+#include <cstdio>
+#include <string>
+
+#include "randblas_gb300.hpp"
+
+namespace RB = RandBLAS_GB300;
+
+static int failures = 0;
+#define EXPECT(cond)                                                 \
+    do {                                                             \
+        if (!(cond)) {                                               \
+            std::printf("FAILED %s (line %d)\n", #cond, __LINE__);   \
+            ++failures;                                              \
+        }                                                            \
+    } while (0)
+
+int main() {
+    // RNGState(k): counter 0, key k; incr carries across 32-bit limbs
+    const RB::RNGState s(0x100000005ull);
+    EXPECT(s.s.key[0] == 5u && s.s.key[1] == 1u && s.s.counter[0] == 0u);
+    const RB::RNGState t = s.incr(0xFFFFFFFFull).incr(2);
+    EXPECT(t.s.counter[0] == 1u && t.s.counter[1] == 1u);
+
+    // DenseDist(200, 10000): wide, Long axis -> natural RowMajor; next state +200*2500
+    const RB::DenseDist D(200, 10000);
+    EXPECT(D.dim_major == 10000 && D.dim_minor == 200);
+    EXPECT(D.natural_layout == RB::Layout::RowMajor);
+    const RB::DenseSkOp<double> S(D, RB::RNGState(0));
+    EXPECT(S.next_state.s.counter[0] == 500000u);
+
+    // SparseDist(1024, 2^20, 8): SASO, full_nnz = 8 * 2^20, next state + 2^20 * 8
+    const RB::SparseDist SD(1024, 1 << 20, 8);
+    EXPECT(SD.full_nnz == 8ll << 20);
+    const RB::SparseSkOp<float> SS(SD, RB::RNGState(1));
+    EXPECT(SS.next_state.s.counter[0] == (8u << 20));
+
+    // argument checks carry the reference's message text and need no device work
+    const RB::DenseSkOp<float> Sf(RB::DenseDist(64, 1000), RB::RNGState(2));
+    bool threw = false;
+    try {
+        RB::sketch_general(RB::Layout::RowMajor, RB::Op::NoTrans, RB::Op::NoTrans, 64, 8, 999,
+                           1.0f, Sf, static_cast<const float *>(nullptr), 8, 0.0f,
+                           static_cast<float *>(nullptr), 8);
+    } catch (const RB::Error &e) {
+        threw = std::string(e.what()).find("was required, but did not hold") != std::string::npos;
+    }
+    EXPECT(threw);
+    threw = false;
+    try {  // lda < n for row-major op(A)
+        RB::sketch_general(RB::Layout::RowMajor, RB::Op::NoTrans, RB::Op::NoTrans, 64, 8, 1000,
+                           1.0f, Sf, 0, 0, static_cast<const float *>(nullptr), 7, 0.0f,
+                           static_cast<float *>(nullptr), 8);
+    } catch (const RB::Error &e) {
+        threw = e.code == RBG_ERROR_INVALID_ARGUMENT &&
+                std::string(e.what()).find("in function lskge3") != std::string::npos;
+    }
+    EXPECT(threw);
+    std::printf("%s\n", failures ? "FAILED" : "ok");
+    return failures ? 1 : 0;
+}
