@@ -27,6 +27,10 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "S·A sketch time and roofline fraction: BF16-TC fused vs FP32 plain, same GPU"
+# DRAM bytes per launch of the BF16 tensor-core sketch at the headline size, from one ncu capture
+# at m = 2^17 (profiles/sketch_tc_bf16_4096x131072x1024.md: 358.6 MB read, 118.1 MB written)
+# with the reads scaled by 8 to m = 2^20 (they grow with m; the partial-sum writes do not).
+HEADLINE_TRAFFIC_BYTES = 8 * 358.6e6 + 118.1e6
 D_SK, M_SK, N_SK = 4096, 1 << 20, 1024
 SASO_D, SASO_M, SASO_N, SASO_K = 1024, 1 << 20, 256, 8
 
@@ -280,7 +284,9 @@ def main():
         kms, achieved = ms, flops / (ms * 1e-3) / 1e12
     peak = bf16_burst if have_lowp else derived_fp32_peak(torch, clk.summary())
     roofline = {"bound": "tensor", "achieved": round(achieved, 1), "peak": round(peak, 1),
-                "unit": "TFLOP/s", "frac": round(achieved / peak, 4), "traffic": None,
+                "unit": "TFLOP/s", "frac": round(achieved / peak, 4),
+                "traffic": HEADLINE_TRAFFIC_BYTES if have_lowp else None,
+                "traffic_note": "ncu capture at m=2^17 scaled to m=2^20" if have_lowp else None,
                 "kernel": main_kernel, "kernel_ms": round(kms, 4),
                 "peak_source": ("bf16 burst, " + peak_kind) if have_lowp else
                 "FP32 CUDA-core peak derived as SMs x 128 lanes x 2 x median SM clock"}
