@@ -262,6 +262,29 @@ int rbg_sketch_vector_sparse(int32_t opS, int64_t d, int64_t m, double alpha,
                              const void *x, int64_t incx, double beta, void *y, int64_t incy,
                              rbg_stream_t stream);
 
+/* ------------------------------------------------------------------ symmetric data */
+
+/* require_symmetric (RandBLAS/util.hh:128-146): for i < j,
+ * |A(i,j) - A(j,i)| <= (|A(i,j)| + |A(j,i)| + 1) * tol, in precision dtype; no check when
+ * tol < 0.  The first failing pair in the reference's loop order is reported with the
+ * reference's message ("Symmetry check failed. |A(i,j) - A(j,i)| was ..., which exceeds
+ * tolerance of ...").  Synchronises `stream`. */
+int rbg_require_symmetric(int32_t dtype, int32_t layout, const void *A, int64_t n, int64_t lda,
+                          double tol, rbg_stream_t stream);
+/* sketch_symmetric with a dense operator (RandBLAS/sksy.hh:158-529): A is n x n symmetric,
+ * checked with sym_check_tol as above, then
+ *   side 0:  B (d x n) = alpha * submat(S) * A + beta * B   (sksy.hh:293-311, 513-529),
+ *   side 1:  B (n x d) = alpha * A * submat(S) + beta * B   (sksy.hh:158-176, 406-422). */
+int rbg_sketch_symmetric(int32_t side, int32_t layout, int64_t d, int64_t n, double alpha,
+                         const rbg_dense_skop *S, int64_t ro_s, int64_t co_s, const void *A,
+                         int64_t lda, double beta, void *B, int64_t ldb, double sym_check_tol,
+                         rbg_stream_t stream);
+/* The same with a sparse operator. */
+int rbg_sketch_symmetric_sparse(int32_t side, int32_t layout, int64_t d, int64_t n, double alpha,
+                                const rbg_sparse_skop *S, int64_t ro_s, int64_t co_s,
+                                const void *A, int64_t lda, double beta, void *B, int64_t ldb,
+                                double sym_check_tol, rbg_stream_t stream);
+
 /* ------------------------------------------------------------------ sparse data */
 
 /* LSKSP3 / sketch_sparse left (RandBLAS/sparse_data/sksp.hh:132-182, 418-437):

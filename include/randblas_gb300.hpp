@@ -275,6 +275,42 @@ void sketch_vector(Op opS, int64_t d, int64_t m, T alpha, const DenseSkOp<T> &S,
                                     incx, beta, y, incy, stream));
 }
 
+// ------------------------------------------------------------------ sketch_symmetric
+// (sksy.hh:158-529) A is n x n symmetric, checked with sym_check_tol (no check when < 0).
+// Left: B (d x n) = alpha * submat(S) * A + beta * B.
+template <typename T>
+void sketch_symmetric(Layout layout, int64_t d, int64_t n, T alpha, const DenseSkOp<T> &S,
+                      int64_t ro_s, int64_t co_s, const T *A, int64_t lda, T beta, T *B,
+                      int64_t ldb, T sym_check_tol = 0, rbg_stream_t stream = nullptr) {
+    const rbg_dense_skop c = S.c();
+    detail::check(rbg_sketch_symmetric(0, static_cast<int32_t>(layout), d, n, alpha, &c, ro_s,
+                                       co_s, A, lda, beta, B, ldb, sym_check_tol, stream));
+}
+// Right: B (n x d) = alpha * A * submat(S) + beta * B.
+template <typename T>
+void sketch_symmetric(Layout layout, int64_t n, int64_t d, T alpha, const T *A, int64_t lda,
+                      const DenseSkOp<T> &S, int64_t ro_s, int64_t co_s, T beta, T *B,
+                      int64_t ldb, T sym_check_tol = 0, rbg_stream_t stream = nullptr) {
+    const rbg_dense_skop c = S.c();
+    detail::check(rbg_sketch_symmetric(1, static_cast<int32_t>(layout), d, n, alpha, &c, ro_s,
+                                       co_s, A, lda, beta, B, ldb, sym_check_tol, stream));
+}
+// Whole operator, left and right.
+template <typename T>
+void sketch_symmetric(Layout layout, T alpha, const DenseSkOp<T> &S, const T *A, int64_t lda,
+                      T beta, T *B, int64_t ldb, T sym_check_tol = 0,
+                      rbg_stream_t stream = nullptr) {
+    sketch_symmetric(layout, S.n_rows, S.n_cols, alpha, S, 0, 0, A, lda, beta, B, ldb,
+                     sym_check_tol, stream);
+}
+template <typename T>
+void sketch_symmetric(Layout layout, T alpha, const T *A, int64_t lda, const DenseSkOp<T> &S,
+                      T beta, T *B, int64_t ldb, T sym_check_tol = 0,
+                      rbg_stream_t stream = nullptr) {
+    sketch_symmetric(layout, S.n_rows, S.n_cols, alpha, A, lda, S, 0, 0, beta, B, ldb,
+                     sym_check_tol, stream);
+}
+
 // Process-wide reproducibility switch (no RandBLAS counterpart).
 inline void set_deterministic(bool on) { detail::check(rbg_set_deterministic(on ? 1 : 0)); }
 

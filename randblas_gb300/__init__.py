@@ -11,6 +11,6 @@ from .api import (  # noqa: F401
     Axis, COOMatrix, CSCMatrix, CSRMatrix, DenseDist, DenseSkOp, Layout, Op, RNGState,
     ScalarDist, SparseDist, SparseSkOp, deterministic, fill_dense, fill_dense_unpacked, fill_sparse,
     fill_sparse_unpacked_nosub, left_spmm, repeated_fisher_yates, right_spmm, sketch_general,
-    set_deterministic, sketch_sparse, sketch_vector, spmm)
+    require_symmetric, set_deterministic, sketch_sparse, sketch_symmetric, sketch_vector, spmm)
 
 __version__ = "1.1.0"

@@ -138,6 +138,11 @@ SIGNATURES = {
                             C.POINTER(rbg_dense_skop), CI64, CI64, P, CI64, C.c_float, P, CI64, P,
                             C.c_size_t, P], C.c_int),
     "rbg_lowp_status": ([C.POINTER(CI32)], C.c_int),
+    "rbg_require_symmetric": ([CI32, CI32, P, CI64, CI64, CD, P], C.c_int),
+    "rbg_sketch_symmetric": ([CI32, CI32, CI64, CI64, CD, C.POINTER(rbg_dense_skop), CI64, CI64,
+                              P, CI64, CD, P, CI64, CD, P], C.c_int),
+    "rbg_sketch_symmetric_sparse": ([CI32, CI32, CI64, CI64, CD, C.POINTER(rbg_sparse_skop),
+                                     CI64, CI64, P, CI64, CD, P, CI64, CD, P], C.c_int),
     "rbg_lskge3_batched": ([CI32, C.POINTER(rbg_batch_problem), CI64, CI32, P], C.c_int),
     "rbg_batched_tile_configs": ([C.POINTER(CI32)], C.c_int),
     "rbg_batched_tile_shape": ([CI32, C.POINTER(CI32), C.POINTER(CI32)], C.c_int),

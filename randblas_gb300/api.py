@@ -366,6 +366,49 @@ def sketch_general(layout: Layout, op1: Op, op2: Op, a: int, b: int, c: int, alp
          C.byref(S._c()), ro_s, co_s, float(beta), _ptr(B), ldb, st)
 
 
+def require_symmetric(layout: Layout, A: torch.Tensor, n: int, lda: int, tol: float) -> None:
+    """require_symmetric (RandBLAS/util.hh:128-146); raises RandBLASError with the reference's
+    message on the first failing pair; no check when tol < 0.  Synchronises."""
+    call("rbg_require_symmetric", _DT[A.dtype], int(layout), _ptr(A), n, lda, float(tol),
+         _stream())
+
+
+def sketch_symmetric(layout: Layout, *args) -> None:
+    """sketch_symmetric (RandBLAS/sksy.hh:158-529); the side follows the argument order, as in
+    the reference, and A is n x n symmetric (checked with sym_check_tol, default 0):
+
+    * sketch_symmetric(layout, d, n, alpha, S, ro_s, co_s, A, lda, beta, B, ldb[, tol])
+      -> B = alpha * submat(S) * A + beta * B  (d x n)
+    * sketch_symmetric(layout, n, d, alpha, A, lda, S, ro_s, co_s, beta, B, ldb[, tol])
+      -> B = alpha * A * submat(S) + beta * B  (n x d)
+    * sketch_symmetric(layout, alpha, S, A, lda, beta, B, ldb[, tol])  (whole operator, left)
+    * sketch_symmetric(layout, alpha, A, lda, S, beta, B, ldb[, tol])  (whole operator, right)
+    """
+    if len(args) in (11, 12):
+        tol = float(args[11]) if len(args) == 12 else 0.0
+        if _is_skop(args[3]):
+            d, n, alpha, S, ro_s, co_s, A, lda, beta, B, ldb = args[:11]
+            side = 0
+        else:
+            n, d, alpha, A, lda, S, ro_s, co_s, beta, B, ldb = args[:11]
+            side = 1
+    elif len(args) in (7, 8):
+        tol = float(args[7]) if len(args) == 8 else 0.0
+        if _is_skop(args[1]):
+            alpha, S, A, lda, beta, B, ldb = args[:7]
+            side, ro_s, co_s = 0, 0, 0
+            d, n = S.n_rows, S.n_cols
+        else:
+            alpha, A, lda, S, beta, B, ldb = args[:7]
+            side, ro_s, co_s = 1, 0, 0
+            n, d = S.n_rows, S.n_cols
+    else:
+        raise RandBLASError(_lib.ERROR_INVALID_ARGUMENT, "unrecognised sketch_symmetric arguments")
+    fn = "rbg_sketch_symmetric" if isinstance(S, DenseSkOp) else "rbg_sketch_symmetric_sparse"
+    call(fn, side, int(layout), d, n, float(alpha), C.byref(S._c()), ro_s, co_s, _ptr(A), lda,
+         float(beta), _ptr(B), ldb, tol, _stream())
+
+
 def sketch_vector(opS: Op, *args) -> None:
     """sketch_vector (RandBLAS/skve.hh:140-164, 232-246):
     sketch_vector(opS, d, m, alpha, S, ro_s, co_s, x, incx, beta, y, incy) or

@@ -21,7 +21,8 @@ INCLUDE = os.path.join(ROOT, "include")
 BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "librandblas_gb300.so")
 
-SOURCES = ["capi.cu", "fill.cu", "gemm_simt.cu", "spmm.cu", "lowp_tc.cu", "batched.cu"]
+SOURCES = ["capi.cu", "fill.cu", "gemm_simt.cu", "spmm.cu", "lowp_tc.cu", "batched.cu",
+           "symmetric.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

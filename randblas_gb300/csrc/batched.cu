@@ -59,6 +59,20 @@ struct WorkItem {
     int64_t tile;
 };
 
+// W consecutive floats from shared memory at a W * 4-byte aligned address, in one load.
+template <int W>
+__device__ __forceinline__ void load_row(const float *p, float *out) {
+    if constexpr (W == 4) {
+        const float4 v = *reinterpret_cast<const float4 *>(p);
+        out[0] = v.x; out[1] = v.y; out[2] = v.z; out[3] = v.w;
+    } else if constexpr (W == 2) {
+        const float2 v = *reinterpret_cast<const float2 *>(p);
+        out[0] = v.x; out[1] = v.y;
+    } else {
+        out[0] = p[0];
+    }
+}
+
 // One output tile (or one K split of it) of problem `pb`: BMT x BNT, TN columns per thread.
 template <int BMT, int BNT, int TN>
 __device__ __forceinline__ void batched_tile(const ProbDev &pb, int64_t tile, int split,
@@ -88,17 +102,16 @@ __device__ __forceinline__ void batched_tile(const ProbDev &pb, int64_t tile, in
         __syncthreads();
 #pragma unroll
         for (int kk = 0; kk < BK; ++kk) {
+            // explicit vector loads: the tiles are views of flat shared arrays, so the compiler
+            // cannot prove the 16-byte alignment it would need to vectorise on its own (rows are
+            // (width + 4) floats, a multiple of 16 bytes)
             float a[8], b[TN];
-#pragma unroll
-            for (int q = 0; q < 4; ++q) {
-                a[q] = Ps[kk][ty * 4 + q];
-                a[4 + q] = Ps[kk][BMT / 2 + ty * 4 + q];
-            }
-#pragma unroll
-            for (int q = 0; q < TN / 2; ++q) {
-                b[q] = Qs[kk][tx * (TN / 2) + q];
-                b[TN / 2 + q] = Qs[kk][BNT / 2 + tx * (TN / 2) + q];
-            }
+            const float4 a0 = *reinterpret_cast<const float4 *>(&Ps[kk][ty * 4]);
+            const float4 a1 = *reinterpret_cast<const float4 *>(&Ps[kk][BMT / 2 + ty * 4]);
+            a[0] = a0.x; a[1] = a0.y; a[2] = a0.z; a[3] = a0.w;
+            a[4] = a1.x; a[5] = a1.y; a[6] = a1.z; a[7] = a1.w;
+            load_row<TN / 2>(&Qs[kk][tx * (TN / 2)], b);
+            load_row<TN / 2>(&Qs[kk][BNT / 2 + tx * (TN / 2)], b + TN / 2);
 #pragma unroll
             for (int x = 0; x < 8; ++x)
 #pragma unroll
@@ -339,10 +352,13 @@ void build_plan(int32_t layout, const rbg_batch_problem *problems, int64_t count
             pd.counter_off = tile_counters;
             tile_counters += tiles;
         }
-        for (int64_t t = 0; t < tiles; ++t)
-            for (int64_t s = 0; s < splits; ++s) items.push_back(WorkItem{(int32_t)p, (int32_t)s, t});
+        // split-major: the items running at the same time share a K range, so each slab of A
+        // is read from HBM once and reused from L2 by every output tile that needs it
+        for (int64_t sp = 0; sp < splits; ++sp)
+            for (int64_t t = 0; t < tiles; ++t)
+                items.push_back(WorkItem{(int32_t)p, (int32_t)sp, t});
     }
-    // longest processing time first; ties keep problem order
+    // longest processing time first; ties keep problem order (and the split-major order)
     std::stable_sort(items.begin(), items.end(), [&](const WorkItem &a, const WorkItem &b) {
         const ProbDev &pa = descs[a.prob], &pb = descs[b.prob];
         return (double)pa.kt_per_split * pa.bm * pa.bn > (double)pb.kt_per_split * pb.bm * pb.bn;

@@ -55,7 +55,9 @@ __device__ __forceinline__ void gen_p_tile(T (*Ps)[TM + 4], const POperand &P, i
 }
 
 // Strided tile load into a k-major SMEM tile: dst[k][x] = src(k0 + k, x0 + x), x in [0, W).
-// Threads walk the unit-stride dimension when there is one.
+// Threads walk the unit-stride dimension when there is one.  The data matrix is read-only
+// during a sketch, so loads go through the read-only data path (also when the pointer reaches
+// the kernel through memory rather than as a parameter).
 template <typename T, int W>
 __device__ __forceinline__ void load_tile(T (*dst)[W + 4], const T *__restrict__ src,
                                           int64_t sk, int64_t sx, int64_t K, int64_t X,
@@ -63,12 +65,14 @@ __device__ __forceinline__ void load_tile(T (*dst)[W + 4], const T *__restrict__
     if (sx == 1 || sk != 1) {
         for (int w = threadIdx.x; w < BK * W; w += NT) {
             const int k = w / W, x = w % W;
-            dst[k][x] = (k0 + k < K && x0 + x < X) ? src[(k0 + k) * sk + (x0 + x) * sx] : (T)0;
+            dst[k][x] = (k0 + k < K && x0 + x < X) ? __ldg(src + (k0 + k) * sk + (x0 + x) * sx)
+                                                   : (T)0;
         }
     } else {
         for (int w = threadIdx.x; w < BK * W; w += NT) {
             const int x = w / BK, k = w % BK;
-            dst[k][x] = (k0 + k < K && x0 + x < X) ? src[(k0 + k) * sk + (x0 + x) * sx] : (T)0;
+            dst[k][x] = (k0 + k < K && x0 + x < X) ? __ldg(src + (k0 + k) * sk + (x0 + x) * sx)
+                                                   : (T)0;
         }
     }
 }

@@ -58,6 +58,14 @@ int main() {
                 std::string(e.what()).find("in function lskge3") != std::string::npos;
     }
     EXPECT(threw);
+    threw = false;
+    try {  // sketch_symmetric checks A before any device work (here: A missing)
+        RB::sketch_symmetric(RB::Layout::RowMajor, 1.0f, Sf, static_cast<const float *>(nullptr),
+                             1000, 0.0f, static_cast<float *>(nullptr), 1000);
+    } catch (const RB::Error &e) {
+        threw = std::string(e.what()).find("A must not be NULL") != std::string::npos;
+    }
+    EXPECT(threw);
     std::printf("%s\n", failures ? "FAILED" : "ok");
     return failures ? 1 : 0;
 }
