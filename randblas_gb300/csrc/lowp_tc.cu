@@ -353,28 +353,34 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
         if (lane == 0) {
             constexpr uint32_t idesc =
                 kFp8 ? tc::idesc_e4m3_f32(BM, BN / 2) : tc::idesc_bf16_f32(BM, BN / 2);
+            // Stage index and phase advance by increment (no 64-bit division), and the
+            // shared-memory descriptors of stage s are the stage-0 ones plus s stage strides in
+            // their 16-byte address field (addresses stay below 2^18, so the field never
+            // overflows): this thread's instructions are few, which matters because it shares
+            // its sub-partition's issue slots with generator warps.
+            const uint64_t adesc0 = tc::kmajor_desc(tc::smem_addr(s_tiles), ROW_BYTES);
+            const uint64_t bdesc00 = tc::kmajor_desc(tc::smem_addr(a_tiles), ROW_BYTES);
+            const uint64_t bdesc10 =
+                tc::kmajor_desc(tc::smem_addr(a_tiles + A_STAGE_BYTES / 2), ROW_BYTES);
+            int s = 0;
+            uint32_t ph = 0;
             int64_t it = 0, uc = 0;
             for (int64_t u = cluster_id; u < p.units; u += num_clusters, ++uc) {
                 int64_t m0, n0, ks0, ks1;
                 unit_tiles(u, m0, n0, ks0, ks1);
                 if (!tc::mbar_wait(acc_empty, (uint32_t)((uc & 1) ^ 1), p.err, 256)) goto done;
                 tc::tc_fence_after();
+                uint32_t acc = 0;
                 for (int64_t ks = ks0; ks < ks1; ++ks, ++it) {
-                    const int s = (int)(it % STAGES);
-                    const uint32_t ph = (uint32_t)((it / STAGES) & 1);
                     if (!tc::mbar_wait(&full[s], ph, p.err)) goto done;
                     tc::tc_fence_after();
-                    const uint64_t adesc =
-                        tc::kmajor_desc(tc::smem_addr(s_tiles + s * S_STAGE_BYTES), ROW_BYTES);
-                    const uint64_t bdesc0 =
-                        tc::kmajor_desc(tc::smem_addr(a_tiles + s * A_STAGE_BYTES), ROW_BYTES);
-                    const uint64_t bdesc1 = tc::kmajor_desc(
-                        tc::smem_addr(a_tiles + s * A_STAGE_BYTES + A_STAGE_BYTES / 2), ROW_BYTES);
+                    const uint64_t adesc = adesc0 + (uint64_t)(s * (S_STAGE_BYTES >> 4));
+                    const uint64_t bdesc0 = bdesc00 + (uint64_t)(s * (A_STAGE_BYTES >> 4));
+                    const uint64_t bdesc1 = bdesc10 + (uint64_t)(s * (A_STAGE_BYTES >> 4));
 #pragma unroll
                     for (int kk = 0; kk < ROW_BYTES / 32; ++kk) {
-                        const uint32_t acc = (ks > ks0 || kk > 0) ? 1u : 0u;
                         // one MMA takes 32 bytes of k (16 BF16 or 32 e4m3) = 2 in the encoded
-                        // address
+                        // address; the first MMA of a unit overwrites the accumulator
                         if (kFp8) {
                             tc::mma_f8(tmem, adesc + 2 * kk, bdesc0 + 2 * kk, idesc, acc);
                             tc::mma_f8(tmem + BN / 2, adesc + 2 * kk, bdesc1 + 2 * kk, idesc, acc);
@@ -383,6 +389,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
                             tc::mma_f16(tmem + BN / 2, adesc + 2 * kk, bdesc1 + 2 * kk, idesc,
                                         acc);
                         }
+                        acc = 1u;
                     }
                     // stage s of every CTA in the cluster may be rewritten by any of them, so
                     // each CTA's MMA completion is signalled to all of them
@@ -390,6 +397,10 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
                         tc::mma_commit_multicast(&empty[s], (uint16_t)((1u << CS) - 1));
                     else
                         tc::mma_commit(&empty[s]);
+                    if (++s == STAGES) {
+                        s = 0;
+                        ph ^= 1u;
+                    }
                 }
                 tc::mma_commit(acc_full);
             }
