@@ -3,7 +3,7 @@
 Two artefacts:
 
 * ``oracle/liboracle.so`` -- the plain-C restatement in ``oracle/oracle.c``.  Builds
-  anywhere gcc exists (this container and the GPU host alike).
+  anywhere gcc exists (x86-64 and aarch64 alike).
 * ``oracle/_ref/librbref.so`` -- the reference's own RandBLAS headers, compiled directly
   with g++ (no CMake) against the project-written Random123 / BLAS++ stand-ins in
   ``oracle/shim/`` plus ``oracle/ref_driver.cc``.  Built only where the reference source

@@ -1,9 +1,10 @@
 /*
  * oracle.c -- CPU restatement of RandBLAS's sketching hot path.
  *
- * TEST INFRASTRUCTURE ONLY.  This file is the checker for the CUDA library in
- * randblas_gb300/.  Only tests/, __graft_entry__.smoke() and bench.py's CPU
- * baseline leg may load it; the product never links, calls or falls back to it.
+ * TEST INFRASTRUCTURE ONLY.  This file is the oracle the CUDA library in
+ * randblas_gb300/ is tested against.  Only tests/, __graft_entry__.smoke() and
+ * bench.py's CPU baseline leg may load it; the product never links, calls or falls
+ * back to it.
  *
  * Everything here is written from the reference's documented behaviour, one
  * function per reference routine, each citing the reference file:line it

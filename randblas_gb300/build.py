@@ -3,8 +3,7 @@
 Every translation unit is compiled for sm_103a only (``-gencode
 arch=compute_103a,code=sm_103a``), in parallel, then linked into one shared library that
 exports the C ABI of ``include/randblas_gb300.h``.  No CMake; nvcc and a C++ host compiler
-are all it needs, so the same command works in the x86 build container and on the aarch64
-GPU host.
+are all it needs, so the same command works on x86-64 and aarch64 hosts alike.
 """
 from __future__ import annotations
 
