@@ -881,25 +881,6 @@ void launch_for(const Plan &pl, const CUtensorMap &map, const LowpParams &p, cud
     else launch_sketch<1, 1, kFast, kFp8>(clusters, map, p, s);
 }
 
-using EncodeFn = CUresult (*)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *,
-                              const cuuint64_t *, const cuuint64_t *, const cuuint32_t *,
-                              const cuuint32_t *, CUtensorMapInterleave, CUtensorMapSwizzle,
-                              CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
-
-EncodeFn encode_fn() {
-    static EncodeFn fn = nullptr;
-    static std::once_flag once;
-    std::call_once(once, [] {
-        void *p = nullptr;
-        cudaDriverEntryPointQueryResult q;
-        if (cudaGetDriverEntryPoint("cuTensorMapEncodeTiled", &p, cudaEnableDefault, &q) ==
-                cudaSuccess &&
-            q == cudaDriverEntryPointSuccess)
-            fn = reinterpret_cast<EncodeFn>(p);
-    });
-    if (!fn) fail(RBG_ERROR_CUDA, "cuTensorMapEncodeTiled is not available");
-    return fn;
-}
 
 void lowp_run(bool fp8, int64_t M, int64_t N, int64_t K, float alpha, const DenseGen &gen,
               int64_t r0, int64_t c0, int r_on_i, const Strided &Q, bool a_bf16, float beta,
@@ -965,14 +946,13 @@ void lowp_run(bool fp8, int64_t M, int64_t N, int64_t K, float alpha, const Dens
     const cuuint64_t strides[1] = {(cuuint64_t)ROW_BYTES};
     const cuuint32_t box[2] = {(cuuint32_t)pl.bke, (cuuint32_t)(BN / 2)};
     const cuuint32_t estr[2] = {1, 1};
-    const CUresult cr = encode_fn()(
+    const CUresult cr = tc::tensor_map_encoder()(
         &map, fp8 ? CU_TENSOR_MAP_DATA_TYPE_UINT8 : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, At, dims,
         strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B,
         CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (cr != CUDA_SUCCESS) fail(RBG_ERROR_CUDA, "cuTensorMapEncodeTiled failed");
 
-    int *err = nullptr;
-    RBG_CUDA(cudaGetSymbolAddress((void **)&err, g_lowp_error));
+    int *err = tc::wait_error_flag();
     LowpParams p{};
     p.M = M; p.N = N; p.K = K;
     p.gen = gen; p.r0 = r0; p.c0 = c0; p.r_on_i = r_on_i;
@@ -1002,6 +982,29 @@ void lowp_run(bool fp8, int64_t M, int64_t N, int64_t K, float alpha, const Dens
 }
 
 }  // namespace
+
+namespace tc {
+EncodeFn tensor_map_encoder() {
+    static EncodeFn fn = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPoint("cuTensorMapEncodeTiled", &p, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<EncodeFn>(p);
+    });
+    if (!fn) fail(RBG_ERROR_CUDA, "cuTensorMapEncodeTiled is not available");
+    return fn;
+}
+
+int *wait_error_flag() {
+    int *err = nullptr;
+    RBG_CUDA(cudaGetSymbolAddress((void **)&err, g_lowp_error));
+    return err;
+}
+}  // namespace tc
 }  // namespace rbg
 
 using namespace rbg;

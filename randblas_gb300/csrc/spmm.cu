@@ -20,6 +20,7 @@
 #include <algorithm>
 
 #include "rbg_internal.h"
+#include "tc_ptx.cuh"
 
 namespace rbg {
 namespace {
@@ -304,8 +305,44 @@ constexpr int kFusedThreads = RBG_FUSED_THREADS;
 constexpr int kFusedMaxNnz = 16;
 constexpr uint32_t kSignBit = 0x80000000u;
 
-// Column c of submat(S) (minor index co + c): the partial Fisher-Yates shuffle of
-// sparse_skops.hh:51-106 with 32-bit arithmetic (exact: dim_major < 2^32, x0 % span < span).
+// Minor index i of a SASO: the partial Fisher-Yates shuffle of sparse_skops.hh:51-106 with
+// 32-bit arithmetic (exact: dim_major < 2^32, x0 % span < span).  emit(j, major, negative) is
+// called for j = 0 .. vec_nnz - 1 in order; counters run seed + i * vec_nnz + j.
+template <typename F>
+__device__ __forceinline__ void saso_column(const DevState &s, uint64_t i, int vec_nnz,
+                                            uint32_t dim_major, F &&emit) {
+    uint32_t mp[kFusedMaxNnz], mv[kFusedMaxNnz];
+    int msize = 0;
+    const uint64_t off = i * (uint64_t)vec_nnz;
+    for (int j = 0; j < vec_nnz; ++j) {
+        const uint4 r = philox(ctr_add(s.ctr, off + (uint64_t)j), s.key);
+        const uint32_t ell = (uint32_t)j + r.x % (dim_major - (uint32_t)j);
+        uint32_t vj = (uint32_t)j, vl = ell;
+        int sj = -1, sl = -1;
+        for (int q = 0; q < msize; ++q) {
+            if (mp[q] == (uint32_t)j) { vj = mv[q]; sj = q; }
+            if (mp[q] == ell) { vl = mv[q]; sl = q; }
+        }
+        if (ell != (uint32_t)j) {
+            if (sl >= 0) {
+                mv[sl] = vj;
+            } else {
+                mp[msize] = ell;
+                mv[msize] = vj;
+                ++msize;
+            }
+        }
+        if (sj >= 0) {
+            --msize;
+            mp[sj] = mp[msize];
+            mv[sj] = mv[msize];
+        }
+        emit(j, vl, (r.y & 1u) != 0u);
+    }
+}
+
+// Column c of submat(S) (minor index co + c) as kp words (vec_nnz entries, then spare-row
+// padding).
 __global__ void saso_pack_kernel(DevState s, int vec_nnz, int kp, uint32_t dim_major,
                                  int64_t co, int64_t K, int64_t ro, int64_t M,
                                  uint32_t *__restrict__ packed) {
@@ -313,37 +350,14 @@ __global__ void saso_pack_kernel(DevState s, int vec_nnz, int kp, uint32_t dim_m
     const int64_t nthreads = (int64_t)gridDim.x * blockDim.x;
     const uint32_t spare = (uint32_t)M * kFusedRowBytes;
     for (int64_t c = tid; c < K; c += nthreads) {
-        uint32_t mp[kFusedMaxNnz], mv[kFusedMaxNnz], w[kFusedMaxNnz];
-        int msize = 0;
-        const uint64_t off = (uint64_t)(co + c) * (uint64_t)vec_nnz;
-        for (int j = 0; j < vec_nnz; ++j) {
-            const uint4 r = philox(ctr_add(s.ctr, off + (uint64_t)j), s.key);
-            const uint32_t ell = (uint32_t)j + r.x % (dim_major - (uint32_t)j);
-            uint32_t vj = (uint32_t)j, vl = ell;
-            int sj = -1, sl = -1;
-            for (int q = 0; q < msize; ++q) {
-                if (mp[q] == (uint32_t)j) { vj = mv[q]; sj = q; }
-                if (mp[q] == ell) { vl = mv[q]; sl = q; }
-            }
-            if (ell != (uint32_t)j) {
-                if (sl >= 0) {
-                    mv[sl] = vj;
-                } else {
-                    mp[msize] = ell;
-                    mv[msize] = vj;
-                    ++msize;
-                }
-            }
-            if (sj >= 0) {
-                --msize;
-                mp[sj] = mp[msize];
-                mv[sj] = mv[msize];
-            }
-            const int64_t row = (int64_t)vl - ro;
-            w[j] = (row >= 0 && row < M)
-                       ? ((uint32_t)row * kFusedRowBytes) | ((r.y & 1u) ? kSignBit : 0u)
-                       : spare;
-        }
+        uint32_t w[kFusedMaxNnz];
+        saso_column(s, (uint64_t)(co + c), vec_nnz, dim_major,
+                    [&](int j, uint32_t major, bool neg) {
+                        const int64_t row = (int64_t)major - ro;
+                        w[j] = (row >= 0 && row < M)
+                                   ? ((uint32_t)row * kFusedRowBytes) | (neg ? kSignBit : 0u)
+                                   : spare;
+                    });
         for (int j = vec_nnz; j < kp; ++j) w[j] = spare;
         uint4 *dst = reinterpret_cast<uint4 *>(packed + c * kp);
         for (int q = 0; q < kp / 4; ++q)
@@ -494,6 +508,447 @@ void fused_saso(int64_t M, int64_t N, int64_t K, double alpha, const SparseOpera
 }
 
 
+// ------------------------------------------------------------------ row-bucketed SASO
+// The same left sketch as the scatter above (wide SASO, sparse vectors = columns of S, no
+// transpose), with B accumulated in registers instead of shared-memory reductions:
+//  1. saso_bucket_kernel: S's columns are cut into sub-chunks of C columns (C <= 256).  Per
+//     sub-chunk one CTA samples the columns (saso_column), counting sorts the entries by row
+//     of B and writes a record: the entry words (byte offset of the column's row in the staged
+//     A tile, sign in bit 31), in row order and by column within a row, then the u16 row
+//     offsets.  The fixed order makes the sums reproducible.
+//  2. saso_rows_kernel: a CTA owns 512 rows x 64 columns of B and a range of sub-chunks.  Per
+//     sub-chunk one TMA tile load brings the C x 64 block of A and one bulk copy the record
+//     into a 3-stage shared-memory ring.  Each warp owns 16 rows, taken as 8 pairs (r, r + 8):
+//     the two half-warps walk the two rows' entry lists side by side, lane l keeping columns
+//     4 (l & 15) .. 4 (l & 15) + 3 in registers.  There are no atomics: an entry costs one
+//     word load, one 16-byte load per lane and four FMAs with +-1.  The CTAs' ranges are
+//     summed in range order.
+constexpr int kRowsCols = 64;
+constexpr int kRowsRowBytes = kRowsCols * 4;
+constexpr int kRowsPerWarp = 16;
+constexpr int kRowsWarps = 32;
+constexpr int kRowsPerCta = kRowsPerWarp * kRowsWarps;
+constexpr int kRowsStages = 3;
+constexpr int kRowsMaxM = 2048;
+constexpr int kBucketThreads = 256;
+constexpr int kBucketWarps = kBucketThreads / 32;
+constexpr size_t kRowsMaxDynamic = (size_t)226 * 1024;  // leaves room for static shared memory
+
+struct RowsPlan {
+    int C = 0;               // columns of S (rows of A) per sub-chunk
+    uint32_t ent_words = 0;  // vec_nnz * C entry words per record
+    uint32_t rec_bytes = 0;  // entry words + (M + 1) u16 offsets, padded to 16 bytes
+    uint32_t tile_bytes = 0; // C x 64 floats of A
+    uint32_t stage_bytes = 0; // tile, then record (128-byte aligned)
+    size_t smem = 0;         // rows kernel dynamic shared memory
+    size_t bucket_smem = 0;  // bucket kernel dynamic shared memory
+};
+
+// words before the bucket list in shared memory: M + 1 row counters, rounded up to 16 bytes
+__host__ __device__ __forceinline__ uint32_t bucket_head_words(int M) {
+    return (uint32_t)(M + 4) & ~3u;
+}
+
+bool rows_plan(int64_t M, int vec_nnz, RowsPlan &pl) {
+    for (int C = 256; C >= 32; C -= 32) {
+        pl.C = C;
+        pl.ent_words = (uint32_t)(vec_nnz * C);
+        pl.rec_bytes = (uint32_t)((pl.ent_words * 4 + (M + 1) * 2 + 15) & ~(int64_t)15);
+        pl.tile_bytes = (uint32_t)(C * kRowsRowBytes);
+        pl.stage_bytes = (pl.tile_bytes + pl.rec_bytes + 127u) & ~127u;
+        pl.smem = 128 + 128 + (size_t)kRowsStages * pl.stage_bytes;  // barriers, alignment
+        pl.bucket_smem = ((size_t)bucket_head_words((int)M) + pl.ent_words) * 4;
+        if (pl.smem <= kRowsMaxDynamic) return true;
+    }
+    return false;
+}
+
+template <int KP>
+__global__ void __launch_bounds__(kBucketThreads)
+    saso_bucket_kernel(DevState s, int vec_nnz, uint32_t dim_major, int64_t co, int64_t K,
+                       int64_t ro, int M, int C, uint32_t ent_words, uint32_t rec_words,
+                       uint32_t *__restrict__ rec) {
+    extern __shared__ __align__(16) uint32_t bsm[];
+    __shared__ uint32_t wtot[kBucketWarps + 1];
+    const uint32_t head = bucket_head_words(M);
+    uint32_t *start = bsm;        // [M + 1]: counts, then first positions
+    uint32_t *list = bsm + head;  // [ent_words]
+    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    // counts and list start at zero (a list slot that is never written holds offset 0)
+    for (uint32_t i = t; i < head + ent_words; i += kBucketThreads) bsm[i] = 0u;
+    __syncthreads();
+
+    const int64_t sub = blockIdx.x;
+    const int64_t c = sub * C + t;
+    uint32_t row[KP], word[KP], rank[KP];
+#pragma unroll
+    for (int q = 0; q < KP; ++q) row[q] = (uint32_t)M;  // M: no entry
+    if (t < C && c < K)
+        saso_column(s, (uint64_t)(co + c), vec_nnz, dim_major,
+                    [&](int j, uint32_t major, bool neg) {
+                        const int64_t r = (int64_t)major - ro;
+#pragma unroll
+                        for (int q = 0; q < KP; ++q)
+                            if (q == j) {
+                                row[q] = (r >= 0 && r < M) ? (uint32_t)r : (uint32_t)M;
+                                word[q] = ((uint32_t)t * kRowsRowBytes) | (neg ? kSignBit : 0u);
+                            }
+                    });
+#pragma unroll
+    for (int q = 0; q < KP; ++q)
+        if (q < vec_nnz && row[q] < (uint32_t)M) rank[q] = atomicAdd(&start[row[q]], 1u);
+    __syncthreads();
+    // exclusive scan of the row counts, each thread a contiguous run of rows
+    const int per = (M + kBucketThreads - 1) / kBucketThreads;
+    const int r0 = min(M, t * per), r1 = min(M, r0 + per);
+    uint32_t local = 0;
+    for (int r = r0; r < r1; ++r) local += start[r];
+    uint32_t incl = local;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        const uint32_t v = __shfl_up_sync(0xffffffffu, incl, d);
+        if (lane >= d) incl += v;
+    }
+    if (lane == 31) wtot[warp] = incl;
+    __syncthreads();
+    if (t == 0) {
+        uint32_t run = 0;
+        for (int w = 0; w < kBucketWarps; ++w) {
+            const uint32_t v = wtot[w];
+            wtot[w] = run;
+            run += v;
+        }
+        wtot[kBucketWarps] = run;
+        start[M] = run;
+    }
+    __syncthreads();
+    uint32_t run = wtot[warp] + incl - local;
+    for (int r = r0; r < r1; ++r) {
+        const uint32_t v = start[r];
+        start[r] = run;
+        run += v;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int q = 0; q < KP; ++q)
+        if (q < vec_nnz && row[q] < (uint32_t)M) list[start[row[q]] + rank[q]] = word[q];
+    __syncthreads();
+    // the atomics hand out ranks in any order: sort each row's entries by column, which fixes
+    // the order of the sums
+    for (int r = t; r < M; r += kBucketThreads) {
+        const uint32_t b = start[r], e = start[r + 1];
+        for (uint32_t p = b + 1; p < e; ++p) {
+            const uint32_t w = list[p];
+            uint32_t q = p;
+            while (q > b && (list[q - 1] & ~kSignBit) > (w & ~kSignBit)) {
+                list[q] = list[q - 1];
+                --q;
+            }
+            list[q] = w;
+        }
+    }
+    __syncthreads();
+    // record: entry words (zeros past the total), then u16 offsets (the total from row M on)
+    const uint32_t total = start[M];
+    uint32_t *dst = rec + sub * (int64_t)rec_words;
+    for (uint32_t p = t; p < ent_words; p += kBucketThreads) dst[p] = list[p];
+    uint16_t *offs = reinterpret_cast<uint16_t *>(dst + ent_words);
+    for (uint32_t p = t; p < 2 * (rec_words - ent_words); p += kBucketThreads)
+        offs[p] = (uint16_t)(p < (uint32_t)M ? start[p] : total);
+}
+
+struct RowsParams {
+    int M, N, C;
+    int64_t nsub, spc;  // sub-chunks, sub-chunks per CTA range
+    uint32_t ent_words, rec_bytes, tile_bytes, stage_bytes;
+    const unsigned char *rec;
+    float alpha, beta;
+    float *out;
+    int64_t os_i, os_j;
+    float *partial;  // [range][M][N], or nullptr when writing `out` directly
+    int *err;
+};
+
+// One slot of a row's entry list: when i < n, load the entry word at shared address `ea`,
+// then this lane's 4 floats of the A row it names (byte offset in the tile at `tile`), and
+// add them times +-1 into acc.  The word load and the adds are predicated on i < n; a slot
+// past the list reads row 0 of the tile (every temporary stays defined, which keeps register
+// pressure down) and adds nothing.
+__device__ __forceinline__ void saso_slot(float4 &acc, uint32_t ea, uint32_t tile, int i, int n) {
+    asm volatile(
+        "{\n\t"
+        ".reg .pred p;\n\t"
+        ".reg .b32 w, o, sg;\n\t"
+        ".reg .f32 a0, a1, a2, a3;\n\t"
+        "setp.lt.s32 p, %6, %7;\n\t"
+        "mov.b32 w, 0;\n\t"
+        "@p ld.shared.u32 w, [%4];\n\t"
+        "and.b32 o, w, 0x7fffffff;\n\t"
+        "add.u32 o, o, %5;\n\t"
+        "ld.shared.v4.f32 {a0, a1, a2, a3}, [o];\n\t"
+        "and.b32 sg, w, 0x80000000;\n\t"
+        "or.b32 sg, sg, 0x3f800000;\n\t"
+        "@p fma.rn.f32 %0, a0, sg, %0;\n\t"
+        "@p fma.rn.f32 %1, a1, sg, %1;\n\t"
+        "@p fma.rn.f32 %2, a2, sg, %2;\n\t"
+        "@p fma.rn.f32 %3, a3, sg, %3;\n\t"
+        "}"
+        : "+f"(acc.x), "+f"(acc.y), "+f"(acc.z), "+f"(acc.w)
+        : "r"(ea), "r"(tile), "r"(i), "r"(n));
+}
+
+// Refill ring slot `slot` with sub-chunk `sub`: the C x 64 tile of A by TMA, the record by a
+// bulk copy, both completing on the slot's full barrier.
+__device__ __forceinline__ void rows_issue(const CUtensorMap *qmap, const RowsParams &p,
+                                           uint32_t base, int slot, int64_t sub) {
+    const uint32_t st = base + 128u + (uint32_t)slot * p.stage_bytes;
+    const uint32_t bar = base + 8u * (uint32_t)slot;
+    tc::mbar_arrive_expect_tx_at(bar, p.tile_bytes + p.rec_bytes);
+    tc::tma_load_2d_at(st, qmap, bar, (int)blockIdx.x * kRowsCols, (int)(sub * p.C));
+    tc::bulk_load_at(st + p.tile_bytes, p.rec + sub * p.rec_bytes, p.rec_bytes, bar);
+}
+
+// Warp shuffles kept in program order (volatile), so the per-row values of the unrolled row
+// loop are not all computed up front, which would cost registers.
+__device__ __forceinline__ uint32_t shfl_idx_ordered(uint32_t v, int src) {
+    uint32_t r;
+    asm volatile("shfl.sync.idx.b32 %0, %1, %2, 0x1f, 0xffffffff;" : "=r"(r) : "r"(v), "r"(src));
+    return r;
+}
+
+__device__ __forceinline__ int shfl_xor_ordered(int v, int mask) {
+    int r;
+    asm volatile("shfl.sync.bfly.b32 %0, %1, %2, 0x1f, 0xffffffff;" : "=r"(r) : "r"(v), "r"(mask));
+    return r;
+}
+
+// grid (ceil(N / 64), ceil(M / 512), ranges), 1024 threads.  Shared memory: full barriers at
+// base, empty barriers at base + 24, the ring of stages from base + 128.
+__global__ void __launch_bounds__(kRowsWarps * 32, 1)
+    saso_rows_kernel(const __grid_constant__ CUtensorMap qmap, RowsParams p) {
+    extern __shared__ __align__(128) unsigned char rsm_raw[];
+    const uint32_t raw = tc::smem_addr(rsm_raw);
+    const uint32_t base = (raw + 127u) & ~127u;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int wrow = blockIdx.y * kRowsPerCta + warp * kRowsPerWarp;
+    const int nloc = (int)(min(p.nsub, (int64_t)blockIdx.z * p.spc + p.spc) -
+                           (int64_t)blockIdx.z * p.spc);
+    if (threadIdx.x == 0) {
+        uint64_t *bars = reinterpret_cast<uint64_t *>(rsm_raw + (base - raw));
+        for (int q = 0; q < kRowsStages; ++q) {
+            tc::mbar_init(&bars[q], 1);
+            tc::mbar_init(&bars[kRowsStages + q], kRowsWarps);
+        }
+        tc::fence_barrier_init();
+        tc::prefetch_tensormap(&qmap);
+    }
+    __syncthreads();
+    int issued = 0;
+    if (threadIdx.x == 0)
+        for (; issued < min(kRowsStages, nloc); ++issued)
+            rows_issue(&qmap, p, base, issued, (int64_t)blockIdx.z * p.spc + issued);
+
+    // half-warp h works on row r + 8h of the pair (r, r + 8); lane l holds columns
+    // 4 (l & 15) .. 4 (l & 15) + 3 of its rows
+    const int half = lane >> 4;
+    constexpr int kAcc = kRowsPerWarp / 2;
+    float4 acc[kAcc];
+#pragma unroll
+    for (int r = 0; r < kAcc; ++r) acc[r] = make_float4(0.f, 0.f, 0.f, 0.f);
+    // lane l <= 16 reads the offset of row wrow + l (rows past M read the total)
+    const uint32_t off_byte = 2u * (uint32_t)min(wrow + min(lane, kRowsPerWarp), p.M);
+    bool ok = true;
+    int it = 0;
+    for (; it < nloc; ++it) {
+        const int slot = it % kRowsStages;
+        const uint32_t ph = (uint32_t)(it / kRowsStages) & 1u;
+        if (!__all_sync(0xffffffffu, tc::mbar_wait_at(base + 8u * slot, ph, p.err))) {
+            ok = false;
+            break;
+        }
+        const uint32_t st = base + 128u + (uint32_t)slot * p.stage_bytes;
+        const uint32_t tile = st + 16u * (uint32_t)(lane & 15);
+        const uint32_t ents = st + p.tile_bytes;
+        const uint32_t o = tc::lds_u16(ents + 4u * p.ent_words + off_byte);
+        uint32_t b = __shfl_sync(0xffffffffu, o, 8 * half);
+#pragma unroll
+        for (int r = 0; r < kAcc; ++r) {
+            const uint32_t e = min(shfl_idx_ordered(o, r + 1 + 8 * half), p.ent_words);
+            const int n = (int)e - (int)b;  // entries of this half's row
+            const int nmax = max(n, shfl_xor_ordered(n, 16));
+            // both halves run nmax slots (rounded up to even) in step
+            uint32_t ea = ents + 4u * b;
+#pragma unroll 1
+            for (int i = 0; i < nmax; i += 2, ea += 8u) {
+                saso_slot(acc[r], ea, tile, i, n);
+                saso_slot(acc[r], ea + 4u, tile, i + 1, n);
+            }
+            b = e;
+        }
+        __syncwarp();
+        if (lane == 0) tc::mbar_arrive_at(base + 24u + 8u * slot);
+        if (warp == 0 && it + kRowsStages < nloc) {
+            bool freed = true;
+            if (lane == 0) {
+                freed = tc::mbar_wait_at(base + 24u + 8u * slot, ph, p.err);
+                if (freed) {
+                    rows_issue(&qmap, p, base, slot,
+                               (int64_t)blockIdx.z * p.spc + it + kRowsStages);
+                    ++issued;
+                }
+            }
+            if (!__shfl_sync(0xffffffffu, freed, 0)) {
+                ok = false;
+                ++it;  // this sub-chunk was consumed
+                break;
+            }
+        }
+    }
+    if (threadIdx.x == 0) {
+        // after an early exit, wait (bounded, whatever the error word says) for loads still in
+        // flight into the ring
+        __shared__ int drain_err;
+        drain_err = 0;
+        for (int j = it; j < issued; ++j)
+            tc::mbar_wait_at(base + 8u * (j % kRowsStages), (uint32_t)(j / kRowsStages) & 1u,
+                             &drain_err, 200000000ll);
+    }
+    if (!ok) return;
+
+    const int col = (int)blockIdx.x * kRowsCols + 4 * (lane & 15);
+    constexpr int kCols = 4;
+#pragma unroll
+    for (int r = 0; r < kAcc; ++r) {
+        const int row = wrow + r + 8 * half;
+        const float v4[4] = {acc[r].x, acc[r].y, acc[r].z, acc[r].w};
+        if (row >= p.M) break;
+#pragma unroll
+        for (int h = 0; h < kCols; ++h) {
+            const int cc = col + h;
+            if (cc >= p.N) break;
+            if (p.partial) {
+                p.partial[((int64_t)blockIdx.z * p.M + row) * p.N + cc] = v4[h];
+            } else {
+                float &o = p.out[row * p.os_i + cc * p.os_j];
+                o = p.beta == 0.f ? p.alpha * v4[h] : fmaf(p.alpha, v4[h], p.beta * o);
+            }
+        }
+    }
+}
+
+// The row-bucketed path applies: what the scatter needs, plus M <= 2048, row-major op(A) with
+// 16-byte aligned rows (TMA), at least 64 columns and 256 rows.
+bool saso_rows_applies(int dtype, int64_t M, int64_t N, int64_t K, const SparseOperand &Sp,
+                       const Strided &Q) {
+    if (dtype != RBG_F32) return false;
+    if (Sp.kind != SparseOperand::SASO_GEN || !Sp.short_is_row || Sp.trans) return false;
+    if (Sp.vec_nnz < 1 || Sp.vec_nnz > kFusedMaxNnz || Sp.vec_nnz > Sp.dim_major) return false;
+    if (Sp.dim_major >= (int64_t)UINT32_MAX || M > kRowsMaxM || N < kRowsCols || K < 256 ||
+        K > INT32_MAX || N > INT32_MAX)
+        return false;
+    if (Q.s1 != 1 || Q.s0 < N || (Q.s0 * 4) % 16 != 0 ||
+        (reinterpret_cast<uintptr_t>(Q.ptr) & 15) != 0)
+        return false;
+    RowsPlan pl;
+    return rows_plan(M, (int)Sp.vec_nnz, pl);
+}
+
+int64_t gcd64(int64_t a, int64_t b) {
+    while (b) {
+        const int64_t t = a % b;
+        a = b;
+        b = t;
+    }
+    return a;
+}
+
+void saso_rows(int64_t M, int64_t N, int64_t K, double alpha, const SparseOperand &Sp,
+               const Strided &Q, double beta, float *out, int64_t os_i, int64_t os_j,
+               cudaStream_t s) {
+    RowsPlan pl;
+    if (!rows_plan(M, (int)Sp.vec_nnz, pl)) fail(RBG_ERROR_UNSUPPORTED, "SASO row plan");
+    const int64_t nsub = (K + pl.C - 1) / pl.C;
+    Scratch rec((size_t)nsub * pl.rec_bytes, s);
+    {
+        ProfScope prof("saso_bucket", s);
+        static bool attr = false;
+        if (!attr) {
+            RBG_CUDA(cudaFuncSetAttribute(saso_bucket_kernel<8>,
+                                          cudaFuncAttributeMaxDynamicSharedMemorySize, 64 * 1024));
+            RBG_CUDA(cudaFuncSetAttribute(saso_bucket_kernel<16>,
+                                          cudaFuncAttributeMaxDynamicSharedMemorySize, 64 * 1024));
+            attr = true;
+        }
+        if (pl.bucket_smem > 64 * 1024) fail(RBG_ERROR_UNSUPPORTED, "SASO bucket plan");
+        if (Sp.vec_nnz <= 8)
+            saso_bucket_kernel<8><<<(unsigned)nsub, kBucketThreads, pl.bucket_smem, s>>>(
+                Sp.seed, (int)Sp.vec_nnz, (uint32_t)Sp.dim_major, Sp.co, K, Sp.ro, (int)M, pl.C,
+                pl.ent_words, pl.rec_bytes / 4, rec.as<uint32_t>());
+        else
+            saso_bucket_kernel<16><<<(unsigned)nsub, kBucketThreads, pl.bucket_smem, s>>>(
+                Sp.seed, (int)Sp.vec_nnz, (uint32_t)Sp.dim_major, Sp.co, K, Sp.ro, (int)M, pl.C,
+                pl.ent_words, pl.rec_bytes / 4, rec.as<uint32_t>());
+        RBG_LAUNCHED();
+    }
+    const int64_t slices = (N + kRowsCols - 1) / kRowsCols;
+    const int64_t rblocks = (M + kRowsPerCta - 1) / kRowsPerCta;
+    const int64_t base = slices * rblocks;
+    const int64_t sms = num_sms();
+    // K ranges: a whole number of waves over the SMs when that takes few ranges
+    int64_t ranges = sms / gcd64(base, sms);
+    if (ranges > 32) ranges = std::max<int64_t>(1, sms / base);
+    ranges = std::min(ranges, nsub);
+    while (ranges > 1 && (double)ranges * M * N * 4 > (double)(1ll << 30)) --ranges;
+    const int64_t spc = (nsub + ranges - 1) / ranges;
+    ranges = (nsub + spc - 1) / spc;
+    if (slices > INT32_MAX || rblocks > 65535 || ranges > 65535)
+        fail(RBG_ERROR_UNSUPPORTED, "sparse sketch too large");
+    Scratch part;
+    float *partial = nullptr;
+    if (ranges > 1) {
+        part.alloc((size_t)ranges * M * N * sizeof(float), s);
+        partial = part.as<float>();
+    }
+    CUtensorMap map;
+    const cuuint64_t dims[2] = {(cuuint64_t)N, (cuuint64_t)K};
+    const cuuint64_t strides[1] = {(cuuint64_t)Q.s0 * 4};
+    const cuuint32_t box[2] = {(cuuint32_t)kRowsCols, (cuuint32_t)pl.C};
+    const cuuint32_t estr[2] = {1, 1};
+    const CUresult cr = tc::tensor_map_encoder()(
+        &map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<void *>(Q.ptr), dims, strides, box,
+        estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+        CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (cr != CUDA_SUCCESS) fail(RBG_ERROR_CUDA, "cuTensorMapEncodeTiled failed (SASO rows)");
+    RowsParams p{};
+    p.M = (int)M; p.N = (int)N; p.C = pl.C;
+    p.nsub = nsub; p.spc = spc;
+    p.ent_words = pl.ent_words; p.rec_bytes = pl.rec_bytes;
+    p.tile_bytes = pl.tile_bytes; p.stage_bytes = pl.stage_bytes;
+    p.rec = rec.as<unsigned char>();
+    p.alpha = (float)alpha; p.beta = (float)beta;
+    p.out = out; p.os_i = os_i; p.os_j = os_j;
+    p.partial = partial;
+    p.err = tc::wait_error_flag();
+    {
+        ProfScope prof("saso_rows", s);
+        static bool attr = false;
+        if (!attr) {
+            RBG_CUDA(cudaFuncSetAttribute(saso_rows_kernel,
+                                          cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          (int)kRowsMaxDynamic));
+            attr = true;
+        }
+        saso_rows_kernel<<<dim3((unsigned)slices, (unsigned)rblocks, (unsigned)ranges),
+                           kRowsWarps * 32, pl.smem, s>>>(map, p);
+        RBG_LAUNCHED();
+    }
+    if (ranges > 1) {
+        spmm_reduce_kernel<float><<<grid1d(M * N, 256), 256, 0, s>>>(
+            M, N, (int)ranges, partial, (float)alpha, (float)beta, out, os_i, os_j);
+        RBG_LAUNCHED();
+    }
+}
+
 template <typename T>
 void run(int64_t M, int64_t N, int64_t K, double alpha, const SparseOperand &Sp,
          const Strided &Q, double beta, void *out, int64_t os_i, int64_t os_j, cudaStream_t s) {
@@ -640,7 +1095,9 @@ void spmm_sketch(int dtype, int64_t M, int64_t N, int64_t K, double alpha,
         launch_scale(dtype, M, N, os_i, os_j, beta, out, s);
         return;
     }
-    if (fused_saso_applies(dtype, M, K, Sp))
+    if (saso_rows_applies(dtype, M, N, K, Sp, Q))
+        saso_rows(M, N, K, alpha, Sp, Q, beta, static_cast<float *>(out), os_i, os_j, s);
+    else if (fused_saso_applies(dtype, M, K, Sp))
         fused_saso(M, N, K, alpha, Sp, Q, beta, static_cast<float *>(out), os_i, os_j, s);
     else if (dtype == RBG_F32)
         run<float>(M, N, K, alpha, Sp, Q, beta, out, os_i, os_j, s);

@@ -86,6 +86,47 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, int *e
     return true;
 }
 
+// The same operations on mbarriers given by shared-memory address (keeps 64-bit pointers out
+// of register-tight loops).
+__device__ __forceinline__ void mbar_arrive_at(uint32_t bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive_expect_tx_at(uint32_t bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes)
+                 : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait_at(uint32_t bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// mbar_wait for an mbarrier given by address (same budget and error-word rules).
+__device__ __forceinline__ bool mbar_wait_at(uint32_t bar, uint32_t parity, int *err,
+                                             long long budget = 8000000000ll) {
+    if (mbar_try_wait_at(bar, parity)) return true;
+    const long long t0 = clock64();
+    uint32_t spins = 0;
+    while (!mbar_try_wait_at(bar, parity)) {
+        if ((++spins & 63u) == 0) {
+            if (*(volatile int *)err) return false;
+            if (clock64() - t0 > budget) {
+                atomicCAS(err, 0, RBG_ERROR_TIMEOUT);
+                return false;
+            }
+        }
+    }
+    return true;
+}
+
 // ------------------------------------------------------------------ clusters
 __device__ __forceinline__ uint32_t cluster_ctarank() {
     uint32_t r;
@@ -144,6 +185,15 @@ __device__ __forceinline__ void tma_load_2d(void *dst, const CUtensorMap *map, u
         : "memory");
 }
 
+__device__ __forceinline__ void tma_load_2d_at(uint32_t dst, const CUtensorMap *map, uint32_t bar,
+                                               int x, int y) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes"
+        " [%0], [%1, {%3, %4}], [%2];" ::"r"(dst),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(bar), "r"(x), "r"(y)
+        : "memory");
+}
+
 // Tile load delivered to the same shared-memory offset of every CTA in `cta_mask`, each CTA's
 // mbarrier at `bar`'s offset receiving the byte count.
 __device__ __forceinline__ void tma_load_2d_multicast(void *dst, const CUtensorMap *map,
@@ -166,6 +216,23 @@ __device__ __forceinline__ void bulk_copy_to_peer(uint32_t remote_dst, const voi
         " [%0], [%1], %2, [%3];" ::"r"(remote_dst),
         "r"(smem_addr(src)), "r"(bytes), "r"(remote_bar)
         : "memory");
+}
+
+// Copy `bytes` (multiple of 16; both addresses 16-byte aligned) from global memory into this
+// CTA's shared memory at `dst`; the mbarrier at `bar` receives the byte count on completion.
+__device__ __forceinline__ void bulk_load_at(uint32_t dst, const void *src, uint32_t bytes,
+                                             uint32_t bar) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes"
+        " [%0], [%1], %2, [%3];" ::"r"(dst),
+        "l"(reinterpret_cast<uint64_t>(src)), "r"(bytes), "r"(bar)
+        : "memory");
+}
+
+__device__ __forceinline__ uint32_t lds_u16(uint32_t addr) {
+    uint16_t v;
+    asm volatile("ld.shared.u16 %0, [%1];" : "=h"(v) : "r"(addr) : "memory");
+    return v;
 }
 
 // Named barrier over `count` threads (ids 1..15; 0 is __syncthreads).
@@ -291,6 +358,19 @@ __host__ __device__ constexpr uint32_t idesc_bf16_f32(uint32_t M, uint32_t N) {
 __host__ __device__ constexpr uint32_t idesc_e4m3_f32(uint32_t M, uint32_t N) {
     return (1u << 4) | (0u << 7) | (0u << 10) | ((N >> 3) << 17) | ((M >> 4) << 24);
 }
+
+// ------------------------------------------------------------------ host side (lowp_tc.cu)
+using EncodeFn = CUresult (*)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *,
+                              const cuuint64_t *, const cuuint64_t *, const cuuint32_t *,
+                              const cuuint32_t *, CUtensorMapInterleave, CUtensorMapSwizzle,
+                              CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+// cuTensorMapEncodeTiled, looked up once through the runtime's driver entry point.
+EncodeFn tensor_map_encoder();
+
+// Device address of the error word that bounded waits in the pipelined kernels set on a
+// timeout (read and cleared by rbg_lowp_status).
+int *wait_error_flag();
 
 }  // namespace tc
 }  // namespace rbg

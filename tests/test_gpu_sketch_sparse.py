@@ -145,35 +145,110 @@ def test_sketch_sparse_data_golden(rb, oracle):
         check_bound(got, ref, bound, c)
 
 
+def _kernels(rb, fn):
+    """Run fn() with the library's kernel timing on; return (result, names of timed kernels)."""
+    rb.profile.enable(True)
+    try:
+        out = fn()
+        names = set(rb.profile.read())
+    finally:
+        rb.profile.enable(False)
+    return out, names
+
+
 def test_full_size_saso_sketch(rb):
-    """1024 x 2^20 SASO (8 nonzeros per column) times a 2^20 x 256 row-major N(0,1) FP32
-    matrix: relative Frobenius error <= 1e-6 against an FP64 product of the same operator on
-    both paths (fused scatter, deterministic row lists), and bitwise-identical results on a
-    second deterministic run (fixed-order reductions)."""
+    """1024 x 2^20 SASO (8 nonzeros per column) times a 2^20 x 256 N(0,1) FP32 matrix through
+    each of the three SASO paths: row-major A takes the row-bucketed kernels (deterministic, so
+    the default and deterministic modes agree bitwise), column-major A the shared-memory
+    scatter by default and the row lists in deterministic mode.  Each: relative Frobenius error
+    <= 1e-6 against an FP64 product of the same operator; the deterministic paths bitwise
+    reproducible."""
     import torch
     m, d, n = 1 << 20, 1024, 256
     A = torch.empty(m * n, dtype=torch.float32, device="cuda")
     nxt = rb.fill_dense(rb.DenseDist(m, n, rb.ScalarDist.Gaussian, rb.Axis.Short), A,
                         rb.RNGState(0))
     S = rb.SparseSkOp(rb.SparseDist(d, m, 8), nxt)
+    A_cm = A.view(m, n).t().contiguous().view(-1)  # the same matrix, column-major
 
-    def sketch():
-        B = torch.empty(d * n, dtype=torch.float32, device="cuda")
-        rb.sketch_general(rb.Layout.RowMajor, rb.Op.NoTrans, rb.Op.NoTrans, d, n, m, 1.0, S, A,
-                          n, 0.0, B, n)
-        return B
-    B_fast = sketch()
-    rb.set_deterministic(True)
-    try:
-        B_det, B_again = sketch(), sketch()
-    finally:
-        rb.set_deterministic(False)
-    assert torch.equal(B_det, B_again)
+    def sketch(layout, det):
+        def go():
+            B = torch.empty(d * n, dtype=torch.float32, device="cuda")
+            if layout == rb.Layout.RowMajor:
+                rb.sketch_general(layout, rb.Op.NoTrans, rb.Op.NoTrans, d, n, m, 1.0, S, A, n,
+                                  0.0, B, n)
+                return B.view(d, n)
+            rb.sketch_general(layout, rb.Op.NoTrans, rb.Op.NoTrans, d, n, m, 1.0, S, A_cm, m,
+                              0.0, B, d)
+            return B.view(n, d).t()
+        rb.set_deterministic(det)
+        try:
+            return _kernels(rb, go)
+        finally:
+            rb.set_deterministic(False)
+
+    rows_fast, k1 = sketch(rb.Layout.RowMajor, False)
+    rows_det, k2 = sketch(rb.Layout.RowMajor, True)
+    scatter, k3 = sketch(rb.Layout.ColMajor, False)
+    lists, k4 = sketch(rb.Layout.ColMajor, True)
+    lists2, _ = sketch(rb.Layout.ColMajor, True)
+    assert "saso_rows" in k1 and "saso_rows" in k2, (k1, k2)
+    assert "saso_scatter" in k3 and "spmm_rows" in k4, (k3, k4)
+    assert torch.equal(rows_fast, rows_det)
+    assert torch.equal(lists, lists2)
     Sf = rb.SparseSkOp(rb.SparseDist(d, m, 8), nxt)
     rb.fill_sparse(Sf)
     idx = torch.stack([Sf.rows, Sf.cols])
     Ssp = torch.sparse_coo_tensor(idx, Sf.vals.double(), (d, m)).coalesce()
     ref = torch.sparse.mm(Ssp, A.view(m, n).double())
-    for B in (B_fast, B_det):
-        rel = (torch.linalg.norm(B.view(d, n).double() - ref) / torch.linalg.norm(ref)).item()
-        assert rel <= 1e-6, rel
+    for name, B in (("rows", rows_fast), ("scatter", scatter), ("lists", lists)):
+        rel = (torch.linalg.norm(B.double() - ref) / torch.linalg.norm(ref)).item()
+        assert rel <= 1e-6, (name, rel)
+
+
+@pytest.mark.parametrize("M,N,K,k,ro,co,alpha,beta", [
+    (700, 100, 100003, 5, 3, 7, 0.5, 2.0),    # ragged rows, columns and sub-chunks; beta != 0
+    (2048, 64, 4096, 16, 0, 0, 1.0, 0.0),     # largest row count, 16 nonzeros per column
+    (1, 64, 256, 1, 2, 0, -1.5, 0.0),         # one row, one sub-chunk (written directly)
+    (513, 2560, 20000, 8, 0, 300, 1.0, 1.0),  # 40 column slices x 2 row blocks
+])
+def test_saso_row_bucketed(rb, M, N, K, k, ro, co, alpha, beta):
+    """The row-bucketed SASO kernels on ragged shapes and submatrices of a larger operator:
+    the reference's componentwise bound and relative error <= 1e-6 against an FP64 product of
+    the operator from fill_sparse, and bitwise-identical repeated runs."""
+    import torch
+    D = rb.SparseDist(M + ro + 5, K + co + 11, k)
+    st = rb.RNGState(M + 7 * K)
+    lda = (N + 3) // 4 * 4 + 4   # 16-byte aligned rows with padding
+    ldb = N + 1
+    g = torch.Generator(device="cuda").manual_seed(K)
+    A = torch.randn(K * lda, device="cuda", generator=g)
+    B0 = torch.randn(M * ldb, device="cuda", generator=g)
+
+    def go():
+        S = rb.SparseSkOp(D, st)
+        B = B0.clone()
+        rb.sketch_general(rb.Layout.RowMajor, rb.Op.NoTrans, rb.Op.NoTrans, M, N, K, alpha, S,
+                          ro, co, A, lda, beta, B, ldb)
+        return B
+
+    B1, names = _kernels(rb, go)
+    assert "saso_rows" in names and "saso_bucket" in names, names
+    assert torch.equal(B1, go())
+    Sf = rb.SparseSkOp(D, st)
+    rb.fill_sparse(Sf)
+    full = torch.zeros(D.n_rows, D.n_cols, dtype=torch.float64, device="cuda")
+    full.index_put_((Sf.rows.long(), Sf.cols.long()), Sf.vals.double(), accumulate=True)
+    Ssub = full[ro:ro + M, co:co + K]
+    Am = A.view(K, lda)[:, :N].double()
+    Bin = B0.view(M, ldb)[:, :N].double()
+    ref = alpha * (Ssub @ Am) + beta * Bin
+    got = B1.view(M, ldb)[:, :N].double()
+    eps = 2.0**-23
+    bound = abs(alpha) * (2 * K + 16) * eps * (Ssub.abs() @ Am.abs()) + \
+        2 * eps * abs(beta) * Bin.abs() + 1e-300
+    assert bool(((got - ref).abs() <= bound).all())
+    rel = (torch.linalg.norm(got - ref) / torch.linalg.norm(ref)).item()
+    assert rel <= 1e-6, rel
+    # padding columns of B untouched
+    assert torch.equal(B1.view(M, ldb)[:, N:], B0.view(M, ldb)[:, N:])
