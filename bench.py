@@ -184,7 +184,7 @@ def main():
                     help="log2 of m for the dense small cases")
     ap.add_argument("--case", default="full",
                     choices=["full", "lowp-small", "plain-small", "saso", "convert-small",
-                             "batched"],
+                             "batched", "dense-fp64-small"],
                     help="full: the benchmark line; the others run one kernel family on a "
                          "smaller case (for profilers) and print a short JSON line")
     args = ap.parse_args()
@@ -574,6 +574,12 @@ def run_case(args):
         out.update(bench_saso(torch, rb, dev, args, stream, peaks()[0]))
     elif args.case == "batched":
         out.update(bench_batched(torch, rb, dev, args, stream))
+    elif args.case == "dense-fp64-small":
+        rb.profile.enable(True)
+        out.update(bench_small_fp64(torch, rb, dev, stream))
+        out["kernels_ms"] = {k: round(v["ms"] / max(1, v["launches"]), 4)
+                             for k, v in rb.profile.read().items()}
+        rb.profile.enable(False)
     else:
         m = 1 << args.m_log2
         S = rb.DenseSkOp(rb.DenseDist(D_SK, m, rb.ScalarDist.Uniform), rb.RNGState(3))

@@ -25,26 +25,29 @@ using simt::NT;
 using simt::gen_p_tile;
 using simt::load_tile;
 
-template <typename T, bool GEN>
-__global__ void __launch_bounds__(NT, sizeof(T) == 4 ? 2 : 1)
+// TN: output columns per CTA (128, or 64 for narrow problems); each thread owns 8 rows x TN/16
+// columns, in two halves TN/2 apart.
+template <typename T, bool GEN, int TN>
+__global__ void __launch_bounds__(NT, (sizeof(T) == 4 || TN < BN) ? 2 : 1)
     dense_sketch_kernel(int64_t M, int64_t N, int64_t K, POperand P, Strided Q, T alpha, T beta,
                         T *__restrict__ out, int64_t os_i, int64_t os_j, int64_t kt_per_split,
                         T *__restrict__ partial) {
+    constexpr int CPT = TN / 16, CH = CPT / 2;
     __shared__ __align__(16) T Ps[BK][BM + 4];
-    __shared__ __align__(16) T Qs[BK][BN + 4];
+    __shared__ __align__(16) T Qs[BK][TN + 4];
     const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
-    const int64_t tiles_n = (N + BN - 1) / BN;
+    const int64_t tiles_n = (N + TN - 1) / TN;
     const int64_t i0 = (blockIdx.x / tiles_n) * BM;
-    const int64_t j0 = (blockIdx.x % tiles_n) * BN;
+    const int64_t j0 = (blockIdx.x % tiles_n) * TN;
     const int64_t kt_total = (K + BK - 1) / BK;
     const int64_t kt_begin = blockIdx.y * kt_per_split;
     const int64_t kt_end = min(kt_total, kt_begin + kt_per_split);
 
-    T acc[8][8];
+    T acc[8][CPT];
 #pragma unroll
     for (int a = 0; a < 8; ++a)
 #pragma unroll
-        for (int b = 0; b < 8; ++b) acc[a][b] = (T)0;
+        for (int b = 0; b < CPT; ++b) acc[a][b] = (T)0;
 
     const T *Qp = static_cast<const T *>(Q.ptr);
     for (int64_t kt = kt_begin; kt < kt_end; ++kt) {
@@ -56,22 +59,25 @@ __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? 2 : 1)
             load_tile<T, BM>(Ps, static_cast<const T *>(P.buff) + P.base, P.sk, P.si, K, M, k0,
                              i0);
         }
-        load_tile<T, BN>(Qs, Qp, Q.s0, Q.s1, K, N, k0, j0);
+        load_tile<T, TN>(Qs, Qp, Q.s0, Q.s1, K, N, k0, j0);
         __syncthreads();
 #pragma unroll
         for (int kk = 0; kk < BK; ++kk) {
-            T a[8], b[8];
+            T a[8], b[CPT];
 #pragma unroll
             for (int q = 0; q < 4; ++q) {
                 a[q] = Ps[kk][ty * 4 + q];
                 a[4 + q] = Ps[kk][64 + ty * 4 + q];
-                b[q] = Qs[kk][tx * 4 + q];
-                b[4 + q] = Qs[kk][64 + tx * 4 + q];
+            }
+#pragma unroll
+            for (int q = 0; q < CH; ++q) {
+                b[q] = Qs[kk][tx * CH + q];
+                b[CH + q] = Qs[kk][TN / 2 + tx * CH + q];
             }
 #pragma unroll
             for (int x = 0; x < 8; ++x)
 #pragma unroll
-                for (int y = 0; y < 8; ++y) acc[x][y] = fma(a[x], b[y], acc[x][y]);
+                for (int y = 0; y < CPT; ++y) acc[x][y] = fma(a[x], b[y], acc[x][y]);
         }
         __syncthreads();
     }
@@ -81,8 +87,8 @@ __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? 2 : 1)
         const int64_t i = i0 + (x < 4 ? ty * 4 + x : 64 + ty * 4 + (x - 4));
         if (i >= M) continue;
 #pragma unroll
-        for (int y = 0; y < 8; ++y) {
-            const int64_t j = j0 + (y < 4 ? tx * 4 + y : 64 + tx * 4 + (y - 4));
+        for (int y = 0; y < CPT; ++y) {
+            const int64_t j = j0 + (y < CH ? tx * CH + y : TN / 2 + tx * CH + (y - CH));
             if (j >= N) continue;
             if (partial) {
                 partial[((int64_t)blockIdx.y * M + i) * N + j] = acc[x][y];
@@ -111,13 +117,16 @@ __global__ void reduce_splits_kernel(int64_t M, int64_t N, int splits, const T *
     }
 }
 
-// Pick a split of K so that tiles * splits fills whole waves of resident CTAs.
-int choose_splits(int64_t tiles, int64_t kt_total, int64_t out_elems, size_t esz) {
-    const int64_t slots = (int64_t)num_sms() * 2;
+// Pick a split of K so that tiles * splits fills whole waves of `per_sm` resident CTAs per SM
+// (1 for FP64: co-resident FP64 CTAs share the SM's FP64 pipe, so a second CTA on an SM
+// doubles that SM's time).
+int choose_splits(int64_t tiles, int64_t kt_total, int64_t out_elems, size_t esz,
+                  int per_sm = 2) {
+    const int64_t slots = (int64_t)num_sms() * per_sm;
     if (tiles >= 4 * slots || kt_total < 16) return 1;
     int best = 1;
     double best_eff = -1.0;
-    for (int s = 1; s <= 64; ++s) {
+    for (int s = 1; s <= 128; ++s) {
         if (kt_total / s < 8) break;
         if ((double)s * out_elems * esz > (double)(1ll << 30)) break;
         const int64_t ctas = tiles * s;
@@ -131,12 +140,31 @@ int choose_splits(int64_t tiles, int64_t kt_total, int64_t out_elems, size_t esz
     return best;
 }
 
+// Output columns per CTA: 64 when the problem is at most 64 wide (half the wasted columns of
+// a 128-wide tile), else 128.
+int tile_n_for(int64_t N) { return N <= 64 ? 64 : BN; }
+
+template <typename T, bool GEN>
+void launch_dense(int tn, dim3 grid, cudaStream_t s, int64_t M, int64_t N, int64_t K,
+                  const POperand &P, const Strided &Q, double alpha, double beta, void *out,
+                  int64_t os_i, int64_t os_j, int64_t kt_per_split, T *partial) {
+    if (tn == 64)
+        dense_sketch_kernel<T, GEN, 64><<<grid, NT, 0, s>>>(M, N, K, P, Q, (T)alpha, (T)beta,
+                                                            (T *)out, os_i, os_j, kt_per_split,
+                                                            partial);
+    else
+        dense_sketch_kernel<T, GEN, BN><<<grid, NT, 0, s>>>(M, N, K, P, Q, (T)alpha, (T)beta,
+                                                            (T *)out, os_i, os_j, kt_per_split,
+                                                            partial);
+}
+
 template <typename T>
 void run(int64_t M, int64_t N, int64_t K, double alpha, const POperand &P, const Strided &Q,
          double beta, void *out, int64_t os_i, int64_t os_j, cudaStream_t s) {
-    const int64_t tiles = ((M + BM - 1) / BM) * ((N + BN - 1) / BN);
+    const int tn = tile_n_for(N);
+    const int64_t tiles = ((M + BM - 1) / BM) * ((N + tn - 1) / tn);
     const int64_t kt_total = (K + BK - 1) / BK;
-    const int splits = choose_splits(tiles, kt_total, M * N, sizeof(T));
+    const int splits = choose_splits(tiles, kt_total, M * N, sizeof(T), sizeof(T) == 8 ? 1 : 2);
     const int64_t kt_per_split = (kt_total + splits - 1) / splits;
     Scratch ws;
     T *partial = nullptr;
@@ -148,13 +176,11 @@ void run(int64_t M, int64_t N, int64_t K, double alpha, const POperand &P, const
     {
         ProfScope prof(P.buff ? "dense_sketch_simt_loaded" : "dense_sketch_simt_generated", s);
         if (P.buff)
-            dense_sketch_kernel<T, false><<<grid, NT, 0, s>>>(M, N, K, P, Q, (T)alpha, (T)beta,
-                                                              (T *)out, os_i, os_j, kt_per_split,
-                                                              partial);
+            launch_dense<T, false>(tn, grid, s, M, N, K, P, Q, alpha, beta, out, os_i, os_j,
+                                   kt_per_split, partial);
         else
-            dense_sketch_kernel<T, true><<<grid, NT, 0, s>>>(M, N, K, P, Q, (T)alpha, (T)beta,
-                                                             (T *)out, os_i, os_j, kt_per_split,
-                                                             partial);
+            launch_dense<T, true>(tn, grid, s, M, N, K, P, Q, alpha, beta, out, os_i, os_j,
+                                  kt_per_split, partial);
         RBG_LAUNCHED();
     }
     if (splits > 1) {
@@ -223,9 +249,10 @@ void run_noalloc(const DenseLeftProblem &pb, cudaStream_t s) {
              "rbg_lskge3_noalloc: d * n * sizeof(T) = " + std::to_string(slice) +
                  " bytes exceeds its limit of " + std::to_string(kNoallocScratchBytes / 2) +
                  " bytes (half of its fixed 32 MiB scratch); use rbg_lskge3");
-    const int64_t tiles = ((M + BM - 1) / BM) * ((N + BN - 1) / BN);
+    const int tn = tile_n_for(N);
+    const int64_t tiles = ((M + BM - 1) / BM) * ((N + tn - 1) / tn);
     const int64_t kt_total = (K + BK - 1) / BK;
-    int splits = choose_splits(tiles, kt_total, M * N, sizeof(T));
+    int splits = choose_splits(tiles, kt_total, M * N, sizeof(T), sizeof(T) == 8 ? 1 : 2);
     while (splits > 1 && (size_t)splits * slice > kNoallocScratchBytes) --splits;
     const int64_t kt_per_split = (kt_total + splits - 1) / splits;
     T *partial = splits > 1 ? static_cast<T *>(noalloc_scratch_address()) : nullptr;
@@ -233,13 +260,11 @@ void run_noalloc(const DenseLeftProblem &pb, cudaStream_t s) {
     // every partial element is written by exactly one CTA before the reduction reads it, so
     // the scratch needs no clearing between calls
     if (pb.P.buff)
-        dense_sketch_kernel<T, false><<<grid, NT, 0, s>>>(M, N, K, pb.P, pb.Q, (T)pb.alpha,
-                                                          (T)pb.beta, (T *)pb.out, pb.os_i,
-                                                          pb.os_j, kt_per_split, partial);
+        launch_dense<T, false>(tn, grid, s, M, N, K, pb.P, pb.Q, pb.alpha, pb.beta, pb.out,
+                               pb.os_i, pb.os_j, kt_per_split, partial);
     else
-        dense_sketch_kernel<T, true><<<grid, NT, 0, s>>>(M, N, K, pb.P, pb.Q, (T)pb.alpha,
-                                                         (T)pb.beta, (T *)pb.out, pb.os_i,
-                                                         pb.os_j, kt_per_split, partial);
+        launch_dense<T, true>(tn, grid, s, M, N, K, pb.P, pb.Q, pb.alpha, pb.beta, pb.out,
+                              pb.os_i, pb.os_j, kt_per_split, partial);
     RBG_LAUNCHED();
     if (splits > 1) {
         const int64_t work = M * N;
