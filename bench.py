@@ -184,7 +184,7 @@ def main():
                     help="log2 of m for the dense small cases")
     ap.add_argument("--case", default="full",
                     choices=["full", "lowp-small", "plain-small", "saso", "convert-small",
-                             "batched", "dense-fp64-small"],
+                             "batched", "dense-fp64-small", "more-rows"],
                     help="full: the benchmark line; the others run one kernel family on a "
                          "smaller case (for profilers) and print a short JSON line")
     args = ap.parse_args()
@@ -294,6 +294,7 @@ def main():
     # secondary rows: SASO sketch (HBM-bound), the small FP64 dense sketch, the
     # differentiation path and the batching path
     saso = bench_saso(torch, rb, device, args, stream, hbm)
+    more_rows = bench_more_rows(torch, rb, device, stream, hbm)
     small = bench_small_fp64(torch, rb, device, stream)
     autograd_row = bench_autograd(torch, rb, device, stream, bf16_sus)
     batched_row = None if args.no_batched else bench_batched(torch, rb, device, args, stream,
@@ -341,6 +342,7 @@ def main():
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
             "gpu_launches": gpu_launches, "clocks": clk.summary(), "saso": saso,
             "dense_fp64_small": small, "autograd": autograd_row, "batched": batched_row,
+            "more_rows": more_rows,
         }
         print(json.dumps(line))
     if world > 1:
@@ -473,6 +475,77 @@ def bench_saso(torch, rb, device, args, stream, hbm):
     return out
 
 
+def bench_more_rows(torch, rb, device, stream, hbm):
+    """Rows of the hot path outside the five configurations, each timed alone with CUDA events:
+    fill_sparse of the cfg2 SASO operator, the cfg2 sketch with that operator pre-filled (its
+    COO arrays read from HBM), sketch_vector with the 4096 x 2^20 uniform operator, and
+    sketch_sparse of a Gaussian 1024 x 2^17 operator against a 2^17 x 512 CSR matrix with
+    5 nonzeros per row (seeded)."""
+    out = {}
+    m, d, n, k = SASO_M, SASO_D, SASO_N, SASO_K
+    A = torch.empty(m * n, dtype=torch.float32, device=device)
+    nxt = rb.fill_dense(rb.DenseDist(m, n, rb.ScalarDist.Gaussian, rb.Axis.Short), A,
+                        rb.RNGState(0))
+    D = rb.SparseDist(d, m, k)
+    S = rb.SparseSkOp(D, nxt)
+    nnz = D.full_nnz
+    S.rows = torch.empty(nnz, dtype=torch.int64, device=device)
+    S.cols = torch.empty(nnz, dtype=torch.int64, device=device)
+    S.vals = torch.empty(nnz, dtype=torch.float32, device=device)
+    ms = event_time(torch, lambda: rb.fill_sparse(S), 10, 3, stream)
+    written = nnz * (8 + 8 + 4)
+    out["fill_sparse"] = {
+        "workload": "SASO 1024 x 2^20, 8 nnz/col, int64 indices, FP32 values",
+        "ms": round(ms, 4), "G_entries/s": round(nnz / (ms * 1e-3) / 1e9, 1),
+        "GB/s_written": round(written / (ms * 1e-3) / 1e9, 1),
+        "frac_of_hbm": round(written / (ms * 1e-3) / 1e9 / hbm, 4)}
+    B = torch.empty(d * n, dtype=torch.float32, device=device)
+
+    def step():
+        rb.sketch_general(rb.Layout.RowMajor, rb.Op.NoTrans, rb.Op.NoTrans, d, n, m, 1.0, S, A,
+                          n, 0.0, B, n)
+    rb.profile.enable(True)
+    ms = event_time(torch, step, 10, 3, stream)
+    prof = rb.profile.read()
+    rb.profile.enable(False)
+    algo = 4.0 * m * n + 4.0 * d * n + written
+    out["saso_prefilled"] = {
+        "workload": "the cfg2 sketch after fill_sparse: COO operator read from HBM",
+        "ms": round(ms, 4), "GB/s": round(algo / (ms * 1e-3) / 1e9, 1),
+        "frac_of_hbm": round(algo / (ms * 1e-3) / 1e9 / hbm, 4),
+        "kernels_ms": {kk: round(v["ms"] / max(1, v["launches"]), 4) for kk, v in prof.items()}}
+    del A, B, S
+
+    Sv = rb.DenseSkOp(rb.DenseDist(D_SK, M_SK, rb.ScalarDist.Uniform), rb.RNGState(3))
+    g = torch.Generator(device=device).manual_seed(7)
+    x = torch.randn(M_SK, device=device, generator=g)
+    y = torch.empty(D_SK, device=device)
+    ms = event_time(torch, lambda: rb.sketch_vector(rb.Op.NoTrans, D_SK, M_SK, 1.0, Sv, 0, 0, x,
+                                                    1, 0.0, y, 1), 5, 2, stream)
+    entries = D_SK * M_SK
+    out["sketch_vector"] = {
+        "workload": "uniform 4096 x 2^20 operator (RNGState(3)) times a 2^20 FP32 vector",
+        "ms": round(ms, 4), "G_operator_entries/s": round(entries / (ms * 1e-3) / 1e9, 1),
+        "GFLOP/s": round(2.0 * entries / (ms * 1e-3) / 1e9, 1)}
+    del x, y
+
+    ds, ms_, ns, per_row = 1024, 1 << 17, 512, 5
+    rowptr = torch.arange(0, ms_ * per_row + 1, per_row, dtype=torch.int64, device=device)
+    cols = torch.randint(0, ns, (ms_ * per_row,), dtype=torch.int64, device=device, generator=g)
+    vals = torch.randn(ms_ * per_row, device=device, generator=g)
+    Acsr = rb.CSRMatrix(ms_, ns, vals, rowptr, cols)
+    Sg = rb.DenseSkOp(rb.DenseDist(ds, ms_, rb.ScalarDist.Gaussian), rb.RNGState(5))
+    Bs = torch.empty(ds * ns, device=device)
+    ms = event_time(torch, lambda: rb.sketch_sparse(rb.Layout.RowMajor, rb.Op.NoTrans,
+                                                    rb.Op.NoTrans, ds, ns, ms_, 1.0, Sg, 0, 0,
+                                                    Acsr, 0.0, Bs, ns), 5, 2, stream)
+    out["sketch_sparse"] = {
+        "workload": "Gaussian 1024 x 2^17 operator (RNGState(5)) times a 2^17 x 512 CSR matrix, "
+                    "5 nonzeros per row; the operator is materialised as in the reference",
+        "ms": round(ms, 4), "GFLOP/s": round(2.0 * ds * ms_ * per_row / (ms * 1e-3) / 1e9, 1)}
+    return out
+
+
 def batched_workload(torch, rb, device, count=512):
     """512 left sketches: m log-uniform in [2^12, 2^18], n uniform in [16, 512], d = 4n
     (numpy default_rng(0)); A_i N(0,1) FP32 row-major from fill_dense with key 1000 + i;
@@ -574,6 +647,8 @@ def run_case(args):
         out.update(bench_saso(torch, rb, dev, args, stream, peaks()[0]))
     elif args.case == "batched":
         out.update(bench_batched(torch, rb, dev, args, stream))
+    elif args.case == "more-rows":
+        out.update(bench_more_rows(torch, rb, dev, stream, peaks()[0]))
     elif args.case == "dense-fp64-small":
         rb.profile.enable(True)
         out.update(bench_small_fp64(torch, rb, dev, stream))

@@ -424,6 +424,7 @@ SparseOperand sparse_operand_of(const rbg_sparse_skop &S, int trans, int64_t ro,
     op.x_rows = S.dist.n_rows;
     op.x_cols = S.dist.n_cols;
     const SparseInfo info = sparse_info(&S.dist);
+    const int short_is_row = S.dist.n_rows <= S.dist.n_cols;
     if (S.nnz >= 0) {
         op.kind = SparseOperand::COO;
         op.nnz = S.nnz;
@@ -435,9 +436,15 @@ SparseOperand sparse_operand_of(const rbg_sparse_skop &S, int trans, int64_t ro,
             check_nonnull(S.rows, "S.rows");
             check_nonnull(S.cols, "S.cols");
         }
+        if (S.dist.major_axis == RBG_AXIS_SHORT && S.nnz > 0 && S.nnz == info.full_nnz) {
+            op.saso_layout = 1;
+            op.vec_nnz = S.dist.vec_nnz;
+            op.dim_major = info.dim_major;
+            op.dim_minor = info.dim_minor;
+            op.short_is_row = short_is_row;
+        }
         return op;
     }
-    const int short_is_row = S.dist.n_rows <= S.dist.n_cols;
     if (S.dist.major_axis == RBG_AXIS_SHORT && S.dist.vec_nnz <= 64) {
         op.kind = SparseOperand::SASO_GEN;
         op.seed = to_dev(S.seed_state);

@@ -149,6 +149,11 @@ struct SparseOperand {
     // op and submatrix offsets: Sp(i, k) = X(ro + i, co + k) or, when trans, X(ro + k, co + i)
     int trans;
     int64_t ro, co;
+    // COO arrays of a filled SASO operator with all vec_nnz * dim_minor entries: fill_sparse
+    // stores the entries of minor index i at [i * vec_nnz, (i + 1) * vec_nnz) (vec_nnz,
+    // dim_major, dim_minor and short_is_row are then set as for SASO_GEN).  The arrays may
+    // have been changed since; kernels that use this layout check it entry by entry.
+    int saso_layout;
 };
 void spmm_sketch(int dtype, int64_t M, int64_t N, int64_t K, double alpha,
                  const SparseOperand &Sp, const Strided &Q, double beta, void *out,

@@ -535,13 +535,15 @@ constexpr int kBucketWarps = kBucketThreads / 32;
 constexpr size_t kRowsMaxDynamic = (size_t)226 * 1024;  // leaves room for static shared memory
 
 struct RowsPlan {
-    int C = 0;               // columns of S (rows of A) per sub-chunk
-    uint32_t ent_words = 0;  // vec_nnz * C entry words per record
-    uint32_t rec_bytes = 0;  // entry words + (M + 1) u16 offsets, padded to 16 bytes
-    uint32_t tile_bytes = 0; // C x 64 floats of A
+    int C = 0;                // columns of S (rows of A) per sub-chunk
+    int ew = 1;               // words per entry: 1 (offset | sign) or 2 (offset, value)
+    uint32_t ent_cap = 0;     // vec_nnz * C entries per record
+    uint32_t ent_words = 0;   // ent_cap * ew
+    uint32_t rec_bytes = 0;   // entry words + (M + 1) u16 offsets, padded to 16 bytes
+    uint32_t tile_bytes = 0;  // C x 64 floats of A
     uint32_t stage_bytes = 0; // tile, then record (128-byte aligned)
-    size_t smem = 0;         // rows kernel dynamic shared memory
-    size_t bucket_smem = 0;  // bucket kernel dynamic shared memory
+    size_t smem = 0;          // rows kernel dynamic shared memory
+    size_t bucket_smem = 0;   // bucket kernel dynamic shared memory
 };
 
 // words before the bucket list in shared memory: M + 1 row counters, rounded up to 16 bytes
@@ -549,10 +551,12 @@ __host__ __device__ __forceinline__ uint32_t bucket_head_words(int M) {
     return (uint32_t)(M + 4) & ~3u;
 }
 
-bool rows_plan(int64_t M, int vec_nnz, RowsPlan &pl) {
+bool rows_plan(int64_t M, int vec_nnz, int ew, RowsPlan &pl) {
     for (int C = 256; C >= 32; C -= 32) {
         pl.C = C;
-        pl.ent_words = (uint32_t)(vec_nnz * C);
+        pl.ew = ew;
+        pl.ent_cap = (uint32_t)(vec_nnz * C);
+        pl.ent_words = pl.ent_cap * (uint32_t)ew;
         pl.rec_bytes = (uint32_t)((pl.ent_words * 4 + (M + 1) * 2 + 15) & ~(int64_t)15);
         pl.tile_bytes = (uint32_t)(C * kRowsRowBytes);
         pl.stage_bytes = (pl.tile_bytes + pl.rec_bytes + 127u) & ~127u;
@@ -563,37 +567,78 @@ bool rows_plan(int64_t M, int vec_nnz, RowsPlan &pl) {
     return false;
 }
 
-template <int KP>
-__global__ void __launch_bounds__(kBucketThreads)
-    saso_bucket_kernel(DevState s, int vec_nnz, uint32_t dim_major, int64_t co, int64_t K,
-                       int64_t ro, int M, int C, uint32_t ent_words, uint32_t rec_words,
-                       uint32_t *__restrict__ rec) {
+template <typename I>
+struct BucketArgs {
+    DevState seed;  // generated operators
+    int vec_nnz;
+    uint32_t dim_major;
+    int64_t co, K, ro;
+    int M, C;
+    uint32_t ent_words, rec_words;
+    uint32_t *rec;
+    // filled operators: COO arrays in fill_sparse's layout, and the list of entries that are
+    // not where that layout puts them (left to saso_overflow_kernel)
+    const I *rows, *cols;
+    const float *vals;
+    unsigned long long *ovf_count;
+    int64_t *ovf;
+};
+
+// kFilled: read each column's entries from the COO arrays (two words per entry: offset,
+// value); otherwise sample them (one word: offset | sign).
+template <int KP, bool kFilled, typename I>
+__global__ void __launch_bounds__(kBucketThreads) saso_bucket_kernel(BucketArgs<I> a) {
+    constexpr int EW = kFilled ? 2 : 1;
     extern __shared__ __align__(16) uint32_t bsm[];
     __shared__ uint32_t wtot[kBucketWarps + 1];
+    const int M = a.M, vec_nnz = a.vec_nnz;
     const uint32_t head = bucket_head_words(M);
     uint32_t *start = bsm;        // [M + 1]: counts, then first positions
     uint32_t *list = bsm + head;  // [ent_words]
     const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
     // counts and list start at zero (a list slot that is never written holds offset 0)
-    for (uint32_t i = t; i < head + ent_words; i += kBucketThreads) bsm[i] = 0u;
+    for (uint32_t i = t; i < head + a.ent_words; i += kBucketThreads) bsm[i] = 0u;
     __syncthreads();
 
     const int64_t sub = blockIdx.x;
-    const int64_t c = sub * C + t;
-    uint32_t row[KP], word[KP], rank[KP];
+    const int64_t c = sub * a.C + t;
+    uint32_t row[KP], word[KP], val[KP], rank[KP];
 #pragma unroll
     for (int q = 0; q < KP; ++q) row[q] = (uint32_t)M;  // M: no entry
-    if (t < C && c < K)
-        saso_column(s, (uint64_t)(co + c), vec_nnz, dim_major,
-                    [&](int j, uint32_t major, bool neg) {
-                        const int64_t r = (int64_t)major - ro;
+    if (t < a.C && c < a.K) {
+        if constexpr (kFilled) {
+            const int64_t g = a.co + c;  // minor index of this column
 #pragma unroll
-                        for (int q = 0; q < KP; ++q)
-                            if (q == j) {
-                                row[q] = (r >= 0 && r < M) ? (uint32_t)r : (uint32_t)M;
-                                word[q] = ((uint32_t)t * kRowsRowBytes) | (neg ? kSignBit : 0u);
-                            }
-                    });
+            for (int q = 0; q < KP; ++q) {
+                if (q >= vec_nnz) break;
+                const int64_t e = g * vec_nnz + q;
+                const int64_t col = (int64_t)__ldg(a.cols + e);
+                if (col != g) {  // not where fill_sparse puts it
+                    const unsigned long long slot = atomicAdd(a.ovf_count, 1ull);
+                    a.ovf[slot] = e;
+                    continue;
+                }
+                const int64_t r = (int64_t)__ldg(a.rows + e) - a.ro;
+                if (r >= 0 && r < M) {
+                    row[q] = (uint32_t)r;
+                    word[q] = (uint32_t)t * kRowsRowBytes;
+                    val[q] = __float_as_uint(__ldg(a.vals + e));
+                }
+            }
+        } else {
+            saso_column(a.seed, (uint64_t)(a.co + c), vec_nnz, a.dim_major,
+                        [&](int j, uint32_t major, bool neg) {
+                            const int64_t r = (int64_t)major - a.ro;
+#pragma unroll
+                            for (int q = 0; q < KP; ++q)
+                                if (q == j) {
+                                    row[q] = (r >= 0 && r < M) ? (uint32_t)r : (uint32_t)M;
+                                    word[q] = ((uint32_t)t * kRowsRowBytes) |
+                                              (neg ? kSignBit : 0u);
+                                }
+                        });
+        }
+    }
 #pragma unroll
     for (int q = 0; q < KP; ++q)
         if (q < vec_nnz && row[q] < (uint32_t)M) rank[q] = atomicAdd(&start[row[q]], 1u);
@@ -631,36 +676,61 @@ __global__ void __launch_bounds__(kBucketThreads)
     __syncthreads();
 #pragma unroll
     for (int q = 0; q < KP; ++q)
-        if (q < vec_nnz && row[q] < (uint32_t)M) list[start[row[q]] + rank[q]] = word[q];
+        if (q < vec_nnz && row[q] < (uint32_t)M) {
+            const uint32_t pos = (start[row[q]] + rank[q]) * EW;
+            list[pos] = word[q];
+            if constexpr (kFilled) list[pos + 1] = val[q];
+        }
     __syncthreads();
     // the atomics hand out ranks in any order: sort each row's entries by column, which fixes
     // the order of the sums
     for (int r = t; r < M; r += kBucketThreads) {
         const uint32_t b = start[r], e = start[r + 1];
         for (uint32_t p = b + 1; p < e; ++p) {
-            const uint32_t w = list[p];
+            const uint32_t w = list[p * EW];
+            const uint32_t v = kFilled ? list[p * EW + EW - 1] : 0u;
             uint32_t q = p;
-            while (q > b && (list[q - 1] & ~kSignBit) > (w & ~kSignBit)) {
-                list[q] = list[q - 1];
+            while (q > b && (list[(q - 1) * EW] & ~kSignBit) > (w & ~kSignBit)) {
+                list[q * EW] = list[(q - 1) * EW];
+                if constexpr (kFilled) list[q * EW + 1] = list[(q - 1) * EW + 1];
                 --q;
             }
-            list[q] = w;
+            list[q * EW] = w;
+            if constexpr (kFilled) list[q * EW + 1] = v;
         }
     }
     __syncthreads();
     // record: entry words (zeros past the total), then u16 offsets (the total from row M on)
     const uint32_t total = start[M];
-    uint32_t *dst = rec + sub * (int64_t)rec_words;
-    for (uint32_t p = t; p < ent_words; p += kBucketThreads) dst[p] = list[p];
-    uint16_t *offs = reinterpret_cast<uint16_t *>(dst + ent_words);
-    for (uint32_t p = t; p < 2 * (rec_words - ent_words); p += kBucketThreads)
+    uint32_t *dst = a.rec + sub * (int64_t)a.rec_words;
+    for (uint32_t p = t; p < a.ent_words; p += kBucketThreads) dst[p] = list[p];
+    uint16_t *offs = reinterpret_cast<uint16_t *>(dst + a.ent_words);
+    for (uint32_t p = t; p < 2 * (a.rec_words - a.ent_words); p += kBucketThreads)
         offs[p] = (uint16_t)(p < (uint32_t)M ? start[p] : total);
+}
+
+// Entries of a filled operator that are not where fill_sparse puts them: out(r, :) +=
+// alpha * v * Q(k, :) with shared-memory-free atomics, after the main result is written.
+template <typename I>
+__global__ void saso_overflow_kernel(const unsigned long long *count, const int64_t *ovf,
+                                     const I *rows, const I *cols, const float *vals,
+                                     int64_t ro, int64_t co, int64_t M, int64_t K, int64_t N,
+                                     const float *Q, int64_t qs0, float alpha, float *out,
+                                     int64_t os_i, int64_t os_j) {
+    const int64_t n = (int64_t)*count;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n * N;
+         t += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t e = ovf[t / N], j = t % N;
+        const int64_t r = (int64_t)rows[e] - ro, k = (int64_t)cols[e] - co;
+        if (r < 0 || r >= M || k < 0 || k >= K) continue;
+        atomicAdd(out + r * os_i + j * os_j, alpha * vals[e] * Q[k * qs0 + j]);
+    }
 }
 
 struct RowsParams {
     int M, N, C;
     int64_t nsub, spc;  // sub-chunks, sub-chunks per CTA range
-    uint32_t ent_words, rec_bytes, tile_bytes, stage_bytes;
+    uint32_t ent_cap, ent_words, rec_bytes, tile_bytes, stage_bytes;
     const unsigned char *rec;
     float alpha, beta;
     float *out;
@@ -708,6 +778,30 @@ __device__ __forceinline__ void rows_issue(const CUtensorMap *qmap, const RowsPa
     tc::bulk_load_at(st + p.tile_bytes, p.rec + sub * p.rec_bytes, p.rec_bytes, bar);
 }
 
+// The same slot for records with two words per entry (byte offset, FP32 value): `ea` is the
+// entry's address, and the value replaces the +-1.
+__device__ __forceinline__ void saso_slot_valued(float4 &acc, uint32_t ea, uint32_t tile, int i,
+                                                 int n) {
+    asm volatile(
+        "{\n\t"
+        ".reg .pred p;\n\t"
+        ".reg .b32 w, o, v;\n\t"
+        ".reg .f32 a0, a1, a2, a3;\n\t"
+        "setp.lt.s32 p, %6, %7;\n\t"
+        "mov.b32 w, 0;\n\t"
+        "mov.b32 v, 0;\n\t"
+        "@p ld.shared.v2.u32 {w, v}, [%4];\n\t"
+        "add.u32 o, w, %5;\n\t"
+        "ld.shared.v4.f32 {a0, a1, a2, a3}, [o];\n\t"
+        "@p fma.rn.f32 %0, a0, v, %0;\n\t"
+        "@p fma.rn.f32 %1, a1, v, %1;\n\t"
+        "@p fma.rn.f32 %2, a2, v, %2;\n\t"
+        "@p fma.rn.f32 %3, a3, v, %3;\n\t"
+        "}"
+        : "+f"(acc.x), "+f"(acc.y), "+f"(acc.z), "+f"(acc.w)
+        : "r"(ea), "r"(tile), "r"(i), "r"(n));
+}
+
 // Warp shuffles kept in program order (volatile), so the per-row values of the unrolled row
 // loop are not all computed up front, which would cost registers.
 __device__ __forceinline__ uint32_t shfl_idx_ordered(uint32_t v, int src) {
@@ -723,9 +817,12 @@ __device__ __forceinline__ int shfl_xor_ordered(int v, int mask) {
 }
 
 // grid (ceil(N / 64), ceil(M / 512), ranges), 1024 threads.  Shared memory: full barriers at
-// base, empty barriers at base + 24, the ring of stages from base + 128.
+// base, empty barriers at base + 24, the ring of stages from base + 128.  kValued: records
+// with (offset, value) entries.
+template <bool kValued>
 __global__ void __launch_bounds__(kRowsWarps * 32, 1)
     saso_rows_kernel(const __grid_constant__ CUtensorMap qmap, RowsParams p) {
+    constexpr uint32_t kEntryBytes = kValued ? 8u : 4u;
     extern __shared__ __align__(128) unsigned char rsm_raw[];
     const uint32_t raw = tc::smem_addr(rsm_raw);
     const uint32_t base = (raw + 127u) & ~127u;
@@ -773,15 +870,20 @@ __global__ void __launch_bounds__(kRowsWarps * 32, 1)
         uint32_t b = __shfl_sync(0xffffffffu, o, 8 * half);
 #pragma unroll
         for (int r = 0; r < kAcc; ++r) {
-            const uint32_t e = min(shfl_idx_ordered(o, r + 1 + 8 * half), p.ent_words);
+            const uint32_t e = min(shfl_idx_ordered(o, r + 1 + 8 * half), p.ent_cap);
             const int n = (int)e - (int)b;  // entries of this half's row
             const int nmax = max(n, shfl_xor_ordered(n, 16));
             // both halves run nmax slots (rounded up to even) in step
-            uint32_t ea = ents + 4u * b;
+            uint32_t ea = ents + kEntryBytes * b;
 #pragma unroll 1
-            for (int i = 0; i < nmax; i += 2, ea += 8u) {
-                saso_slot(acc[r], ea, tile, i, n);
-                saso_slot(acc[r], ea + 4u, tile, i + 1, n);
+            for (int i = 0; i < nmax; i += 2, ea += 2u * kEntryBytes) {
+                if constexpr (kValued) {
+                    saso_slot_valued(acc[r], ea, tile, i, n);
+                    saso_slot_valued(acc[r], ea + kEntryBytes, tile, i + 1, n);
+                } else {
+                    saso_slot(acc[r], ea, tile, i, n);
+                    saso_slot(acc[r], ea + kEntryBytes, tile, i + 1, n);
+                }
             }
             b = e;
         }
@@ -836,12 +938,18 @@ __global__ void __launch_bounds__(kRowsWarps * 32, 1)
     }
 }
 
-// The row-bucketed path applies: what the scatter needs, plus M <= 2048, row-major op(A) with
-// 16-byte aligned rows (TMA), at least 64 columns and 256 rows.
+// The row-bucketed path applies to the scatter's operators (a sampled wide SASO, no
+// transpose) and to filled SASO operators in fill_sparse's layout (outside deterministic
+// mode: entries moved out of that layout are added with atomics), with M <= 2048, row-major
+// op(A) with 16-byte aligned rows (TMA), at least 64 columns and 256 rows.
 bool saso_rows_applies(int dtype, int64_t M, int64_t N, int64_t K, const SparseOperand &Sp,
                        const Strided &Q) {
     if (dtype != RBG_F32) return false;
-    if (Sp.kind != SparseOperand::SASO_GEN || !Sp.short_is_row || Sp.trans) return false;
+    const bool filled = Sp.kind == SparseOperand::COO && Sp.saso_layout;
+    if (Sp.kind != SparseOperand::SASO_GEN && !filled) return false;
+    if (filled && (deterministic_mode() || (Sp.itype != RBG_I32 && Sp.itype != RBG_I64)))
+        return false;
+    if (!Sp.short_is_row || Sp.trans) return false;
     if (Sp.vec_nnz < 1 || Sp.vec_nnz > kFusedMaxNnz || Sp.vec_nnz > Sp.dim_major) return false;
     if (Sp.dim_major >= (int64_t)UINT32_MAX || M > kRowsMaxM || N < kRowsCols || K < 256 ||
         K > INT32_MAX || N > INT32_MAX)
@@ -850,7 +958,42 @@ bool saso_rows_applies(int dtype, int64_t M, int64_t N, int64_t K, const SparseO
         (reinterpret_cast<uintptr_t>(Q.ptr) & 15) != 0)
         return false;
     RowsPlan pl;
-    return rows_plan(M, (int)Sp.vec_nnz, pl);
+    return rows_plan(M, (int)Sp.vec_nnz, filled ? 2 : 1, pl);
+}
+
+template <bool kFilled, typename I>
+void launch_bucket(const RowsPlan &pl, int64_t nsub, const BucketArgs<I> &a, int vec_nnz,
+                   cudaStream_t s) {
+    static bool attr = false;
+    if (!attr) {
+        RBG_CUDA(cudaFuncSetAttribute(saso_bucket_kernel<8, kFilled, I>,
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize, 64 * 1024));
+        RBG_CUDA(cudaFuncSetAttribute(saso_bucket_kernel<16, kFilled, I>,
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize, 64 * 1024));
+        attr = true;
+    }
+    if (pl.bucket_smem > 64 * 1024) fail(RBG_ERROR_UNSUPPORTED, "SASO bucket plan");
+    if (vec_nnz <= 8)
+        saso_bucket_kernel<8, kFilled, I>
+            <<<(unsigned)nsub, kBucketThreads, pl.bucket_smem, s>>>(a);
+    else
+        saso_bucket_kernel<16, kFilled, I>
+            <<<(unsigned)nsub, kBucketThreads, pl.bucket_smem, s>>>(a);
+    RBG_LAUNCHED();
+}
+
+template <bool kValued>
+void launch_rows(dim3 grid, size_t smem, const CUtensorMap &map, const RowsParams &p,
+                 cudaStream_t s) {
+    static bool attr = false;
+    if (!attr) {
+        RBG_CUDA(cudaFuncSetAttribute(saso_rows_kernel<kValued>,
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)kRowsMaxDynamic));
+        attr = true;
+    }
+    saso_rows_kernel<kValued><<<grid, kRowsWarps * 32, smem, s>>>(map, p);
+    RBG_LAUNCHED();
 }
 
 int64_t gcd64(int64_t a, int64_t b) {
@@ -862,33 +1005,40 @@ int64_t gcd64(int64_t a, int64_t b) {
     return a;
 }
 
+template <typename I>
 void saso_rows(int64_t M, int64_t N, int64_t K, double alpha, const SparseOperand &Sp,
                const Strided &Q, double beta, float *out, int64_t os_i, int64_t os_j,
                cudaStream_t s) {
+    const bool filled = Sp.kind == SparseOperand::COO;
     RowsPlan pl;
-    if (!rows_plan(M, (int)Sp.vec_nnz, pl)) fail(RBG_ERROR_UNSUPPORTED, "SASO row plan");
+    if (!rows_plan(M, (int)Sp.vec_nnz, filled ? 2 : 1, pl))
+        fail(RBG_ERROR_UNSUPPORTED, "SASO row plan");
     const int64_t nsub = (K + pl.C - 1) / pl.C;
     Scratch rec((size_t)nsub * pl.rec_bytes, s);
+    Scratch ovf_count, ovf;
+    BucketArgs<I> a{};
+    a.seed = Sp.seed;
+    a.vec_nnz = (int)Sp.vec_nnz;
+    a.dim_major = (uint32_t)Sp.dim_major;
+    a.co = Sp.co; a.K = K; a.ro = Sp.ro;
+    a.M = (int)M; a.C = pl.C;
+    a.ent_words = pl.ent_words;
+    a.rec_words = pl.rec_bytes / 4;
+    a.rec = rec.as<uint32_t>();
+    if (filled) {
+        ovf_count.alloc(sizeof(unsigned long long), s);
+        ovf.alloc((size_t)Sp.nnz * sizeof(int64_t), s);
+        RBG_CUDA(cudaMemsetAsync(ovf_count.ptr, 0, sizeof(unsigned long long), s));
+        a.rows = static_cast<const I *>(Sp.idx_a);
+        a.cols = static_cast<const I *>(Sp.idx_b);
+        a.vals = static_cast<const float *>(Sp.vals);
+        a.ovf_count = ovf_count.as<unsigned long long>();
+        a.ovf = ovf.as<int64_t>();
+    }
     {
         ProfScope prof("saso_bucket", s);
-        static bool attr = false;
-        if (!attr) {
-            RBG_CUDA(cudaFuncSetAttribute(saso_bucket_kernel<8>,
-                                          cudaFuncAttributeMaxDynamicSharedMemorySize, 64 * 1024));
-            RBG_CUDA(cudaFuncSetAttribute(saso_bucket_kernel<16>,
-                                          cudaFuncAttributeMaxDynamicSharedMemorySize, 64 * 1024));
-            attr = true;
-        }
-        if (pl.bucket_smem > 64 * 1024) fail(RBG_ERROR_UNSUPPORTED, "SASO bucket plan");
-        if (Sp.vec_nnz <= 8)
-            saso_bucket_kernel<8><<<(unsigned)nsub, kBucketThreads, pl.bucket_smem, s>>>(
-                Sp.seed, (int)Sp.vec_nnz, (uint32_t)Sp.dim_major, Sp.co, K, Sp.ro, (int)M, pl.C,
-                pl.ent_words, pl.rec_bytes / 4, rec.as<uint32_t>());
-        else
-            saso_bucket_kernel<16><<<(unsigned)nsub, kBucketThreads, pl.bucket_smem, s>>>(
-                Sp.seed, (int)Sp.vec_nnz, (uint32_t)Sp.dim_major, Sp.co, K, Sp.ro, (int)M, pl.C,
-                pl.ent_words, pl.rec_bytes / 4, rec.as<uint32_t>());
-        RBG_LAUNCHED();
+        if (filled) launch_bucket<true, I>(pl, nsub, a, (int)Sp.vec_nnz, s);
+        else launch_bucket<false, I>(pl, nsub, a, (int)Sp.vec_nnz, s);
     }
     const int64_t slices = (N + kRowsCols - 1) / kRowsCols;
     const int64_t rblocks = (M + kRowsPerCta - 1) / kRowsPerCta;
@@ -922,7 +1072,7 @@ void saso_rows(int64_t M, int64_t N, int64_t K, double alpha, const SparseOperan
     RowsParams p{};
     p.M = (int)M; p.N = (int)N; p.C = pl.C;
     p.nsub = nsub; p.spc = spc;
-    p.ent_words = pl.ent_words; p.rec_bytes = pl.rec_bytes;
+    p.ent_cap = pl.ent_cap; p.ent_words = pl.ent_words; p.rec_bytes = pl.rec_bytes;
     p.tile_bytes = pl.tile_bytes; p.stage_bytes = pl.stage_bytes;
     p.rec = rec.as<unsigned char>();
     p.alpha = (float)alpha; p.beta = (float)beta;
@@ -931,20 +1081,21 @@ void saso_rows(int64_t M, int64_t N, int64_t K, double alpha, const SparseOperan
     p.err = tc::wait_error_flag();
     {
         ProfScope prof("saso_rows", s);
-        static bool attr = false;
-        if (!attr) {
-            RBG_CUDA(cudaFuncSetAttribute(saso_rows_kernel,
-                                          cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                          (int)kRowsMaxDynamic));
-            attr = true;
-        }
-        saso_rows_kernel<<<dim3((unsigned)slices, (unsigned)rblocks, (unsigned)ranges),
-                           kRowsWarps * 32, pl.smem, s>>>(map, p);
-        RBG_LAUNCHED();
+        const dim3 grid((unsigned)slices, (unsigned)rblocks, (unsigned)ranges);
+        if (filled) launch_rows<true>(grid, pl.smem, map, p, s);
+        else launch_rows<false>(grid, pl.smem, map, p, s);
     }
     if (ranges > 1) {
         spmm_reduce_kernel<float><<<grid1d(M * N, 256), 256, 0, s>>>(
             M, N, (int)ranges, partial, (float)alpha, (float)beta, out, os_i, os_j);
+        RBG_LAUNCHED();
+    }
+    if (filled) {
+        // entries moved out of fill_sparse's layout (none for an operator as sampled)
+        saso_overflow_kernel<I><<<(unsigned)num_sms() * 4, 256, 0, s>>>(
+            ovf_count.as<unsigned long long>(), ovf.as<int64_t>(), a.rows, a.cols, a.vals,
+            Sp.ro, Sp.co, M, K, N, static_cast<const float *>(Q.ptr), Q.s0, (float)alpha, out,
+            os_i, os_j);
         RBG_LAUNCHED();
     }
 }
@@ -1095,8 +1246,14 @@ void spmm_sketch(int dtype, int64_t M, int64_t N, int64_t K, double alpha,
         launch_scale(dtype, M, N, os_i, os_j, beta, out, s);
         return;
     }
-    if (saso_rows_applies(dtype, M, N, K, Sp, Q))
-        saso_rows(M, N, K, alpha, Sp, Q, beta, static_cast<float *>(out), os_i, os_j, s);
+    if (saso_rows_applies(dtype, M, N, K, Sp, Q)) {
+        if (Sp.kind == SparseOperand::COO && Sp.itype == RBG_I32)
+            saso_rows<int32_t>(M, N, K, alpha, Sp, Q, beta, static_cast<float *>(out), os_i,
+                               os_j, s);
+        else
+            saso_rows<int64_t>(M, N, K, alpha, Sp, Q, beta, static_cast<float *>(out), os_i,
+                               os_j, s);
+    }
     else if (fused_saso_applies(dtype, M, K, Sp))
         fused_saso(M, N, K, alpha, Sp, Q, beta, static_cast<float *>(out), os_i, os_j, s);
     else if (dtype == RBG_F32)

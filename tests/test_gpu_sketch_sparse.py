@@ -252,3 +252,81 @@ def test_saso_row_bucketed(rb, M, N, K, k, ro, co, alpha, beta):
     assert rel <= 1e-6, rel
     # padding columns of B untouched
     assert torch.equal(B1.view(M, ldb)[:, N:], B0.view(M, ldb)[:, N:])
+
+
+@pytest.mark.parametrize("itype", ["int64", "int32"])
+def test_saso_prefilled_row_bucketed(rb, itype):
+    """A filled SASO operator (fill_sparse's COO arrays) goes through the row-bucketed kernels,
+    which read the values from the arrays (here rescaled) and add entries that are no longer
+    where fill_sparse put them (here 1000 positions shuffled across columns and 50 entries
+    moved to other rows and columns) with atomics.  Checked against an FP64 product of the
+    arrays as they are, on a submatrix; in deterministic mode the row-list path is used and
+    repeats bitwise."""
+    import torch
+    M, N, K, k, ro, co = 700, 96, 50021, 6, 2, 3
+    D = rb.SparseDist(M + 5, K + 9, k)
+    idt = torch.int64 if itype == "int64" else torch.int32
+    S = rb.SparseSkOp(D, rb.RNGState(11), index_dtype=idt)
+    rb.fill_sparse(S)
+    g = torch.Generator(device="cuda").manual_seed(3)
+    S.vals.mul_(0.37)
+    src = torch.randperm(1000, generator=g, device="cuda") + 5000
+    dst = torch.arange(5000, 6000, device="cuda")
+    for arr in (S.rows, S.cols, S.vals):
+        arr[dst] = arr[src].clone()
+    moved = torch.randint(0, D.full_nnz, (50,), generator=g, device="cuda")
+    S.rows[moved] = torch.randint(0, D.n_rows, (50,), generator=g, device="cuda").to(idt)
+    S.cols[moved] = torch.randint(0, D.n_cols, (50,), generator=g, device="cuda").to(idt)
+    A = torch.randn(K * N, device="cuda", generator=g)
+
+    def go():
+        B = torch.zeros(M * N, device="cuda")
+        rb.sketch_general(rb.Layout.RowMajor, rb.Op.NoTrans, rb.Op.NoTrans, M, N, K, 1.0, S, ro,
+                          co, A, N, 0.0, B, N)
+        return B
+
+    B, names = _kernels(rb, go)
+    assert "saso_rows" in names and "saso_bucket" in names, names
+    full = torch.zeros(D.n_rows, D.n_cols, dtype=torch.float64, device="cuda")
+    full.index_put_((S.rows.long(), S.cols.long()), S.vals.double(), accumulate=True)
+    Ssub = full[ro:ro + M, co:co + K]
+    Am = A.view(K, N).double()
+    ref = Ssub @ Am
+    got = B.view(M, N).double()
+    bound = (2 * K + 16) * 2.0**-23 * (Ssub.abs() @ Am.abs()) + 1e-300
+    assert bool(((got - ref).abs() <= bound).all())
+    rel = (torch.linalg.norm(got - ref) / torch.linalg.norm(ref)).item()
+    assert rel <= 1e-6, rel
+    rb.set_deterministic(True)
+    try:
+        (B1, n1), (B2, _) = _kernels(rb, go), _kernels(rb, go)
+    finally:
+        rb.set_deterministic(False)
+    assert "spmm_rows" in n1 and "saso_rows" not in n1, n1
+    assert torch.equal(B1, B2)
+    rel = (torch.linalg.norm(B1.view(M, N).double() - ref) / torch.linalg.norm(ref)).item()
+    assert rel <= 1e-6, rel
+
+
+def test_saso_prefilled_matches_sampled(rb):
+    """The cfg2 shape with the operator filled first: the row-bucketed kernels read the COO
+    arrays and give the sampled path's result to FP32 rounding (<= 1e-6 relative)."""
+    import torch
+    m, d, n = 1 << 18, 1024, 256
+    A = torch.randn(m * n, device="cuda", generator=torch.Generator(device="cuda").manual_seed(1))
+    D = rb.SparseDist(d, m, 8)
+
+    def sketch(S):
+        B = torch.empty(d * n, device="cuda")
+        rb.sketch_general(rb.Layout.RowMajor, rb.Op.NoTrans, rb.Op.NoTrans, d, n, m, 1.0, S, A,
+                          n, 0.0, B, n)
+        return B
+
+    B_gen, n_gen = _kernels(rb, lambda: sketch(rb.SparseSkOp(D, rb.RNGState(9))))
+    Sf = rb.SparseSkOp(D, rb.RNGState(9))
+    rb.fill_sparse(Sf)
+    B_fill, n_fill = _kernels(rb, lambda: sketch(Sf))
+    assert "saso_rows" in n_gen and "saso_rows" in n_fill, (n_gen, n_fill)
+    rel = (torch.linalg.norm(B_fill.double() - B_gen.double()) /
+           torch.linalg.norm(B_gen.double())).item()
+    assert rel <= 1e-6, rel
