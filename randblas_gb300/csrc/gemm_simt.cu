@@ -117,6 +117,92 @@ __global__ void reduce_splits_kernel(int64_t M, int64_t N, int splits, const T *
     }
 }
 
+// ------------------------------------------------------------------ one output column
+// Out(i) = sum_k P(i, k) Q(k) with P generated (sketch_vector, and any sketch with n = 1): no
+// tile padding, so the cost is the generation of P.  partial[split][i] holds each K range's
+// sum, added in split order by reduce_splits_kernel.
+//  * r_on_i (a natural row of S per output i): one warp per output, lanes walking the row's
+//    counter blocks (4 entries each) in turn; the warp's lane sums are combined by a fixed
+//    shuffle tree.
+//  * otherwise (a natural row per k): one thread per counter block along the natural row,
+//    i.e. 4 consecutive outputs, walking k.
+template <typename T>
+__global__ void __launch_bounds__(256) gemv_gen_kernel(int64_t M, int64_t K, POperand P,
+                                                       const T *__restrict__ Q, int64_t qs0,
+                                                       int64_t k_per_split, T *partial) {
+    const DenseGen &g = P.gen;
+    const int64_t kb = (int64_t)blockIdx.y * k_per_split;
+    const int64_t ke = min(K, kb + k_per_split);
+    if (P.r_on_i) {
+        const int64_t i = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+        const int lane = threadIdx.x & 31;
+        if (i >= M) return;
+        const int64_t R = P.r0 + i, cb = P.c0 + kb, ce = P.c0 + ke;  // natural columns
+        T acc = (T)0;
+        for (int64_t b = cb / 4 + lane; 4 * b < ce; b += 32) {
+            float v[4];
+            gen4(g.family, g.counter_of(R, b), g.key, v);
+#pragma unroll
+            for (int l = 0; l < 4; ++l) {
+                const int64_t C = 4 * b + l;
+                if (C >= cb && C < ce)
+                    acc = fma(finish_entry<T>(g.family, v[l]), __ldg(Q + (C - P.c0) * qs0), acc);
+            }
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+        if (lane == 0) partial[(int64_t)blockIdx.y * M + i] = acc;
+    } else {
+        const int64_t b = P.c0 / 4 + blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+        const int64_t i0 = 4 * b - P.c0;  // output of lane 0 of the block (may be negative)
+        if (i0 >= M) return;
+        T acc[4] = {(T)0, (T)0, (T)0, (T)0};
+        for (int64_t k = kb; k < ke; ++k) {
+            float v[4];
+            gen4(g.family, g.counter_of(P.r0 + k, b), g.key, v);
+            const T q = __ldg(Q + k * qs0);
+#pragma unroll
+            for (int l = 0; l < 4; ++l) acc[l] = fma(finish_entry<T>(g.family, v[l]), q, acc[l]);
+        }
+#pragma unroll
+        for (int l = 0; l < 4; ++l)
+            if (i0 + l >= 0 && i0 + l < M) partial[(int64_t)blockIdx.y * M + i0 + l] = acc[l];
+    }
+}
+
+template <typename T>
+void run_gemv(int64_t M, int64_t K, double alpha, const POperand &P, const Strided &Q,
+              double beta, void *out, int64_t os_i, cudaStream_t s) {
+    const int64_t target = (int64_t)num_sms() * 2048 * 2;  // threads in flight
+    int64_t threads, splits;
+    if (P.r_on_i) {
+        threads = M * 32;
+        splits = std::max<int64_t>(1, std::min<int64_t>((target + threads - 1) / threads,
+                                                       (K + 4095) / 4096));
+    } else {
+        threads = (M + 3) / 4 + 1;
+        splits = std::max<int64_t>(1, std::min<int64_t>((target + threads - 1) / threads,
+                                                       (K + 63) / 64));
+    }
+    splits = std::min<int64_t>(splits, 65535);
+    const int64_t k_per_split = (K + splits - 1) / splits;
+    splits = (K + k_per_split - 1) / k_per_split;
+    Scratch ws((size_t)splits * M * sizeof(T), s);
+    const int64_t blocks = (threads + 255) / 256;
+    if (blocks > INT32_MAX) fail(RBG_ERROR_UNSUPPORTED, "sketch with n = 1: too many rows");
+    {
+        ProfScope prof("dense_sketch_gemv_generated", s);
+        gemv_gen_kernel<T><<<dim3((unsigned)blocks, (unsigned)splits), 256, 0, s>>>(
+            M, K, P, static_cast<const T *>(Q.ptr), Q.s0, k_per_split, ws.as<T>());
+        RBG_LAUNCHED();
+    }
+    const int grid_r = (int)std::max<int64_t>(
+        1, std::min<int64_t>((M + 255) / 256, (int64_t)num_sms() * 16));
+    reduce_splits_kernel<T><<<grid_r, 256, 0, s>>>(M, 1, (int)splits, ws.as<T>(), (T)alpha,
+                                                   (T)beta, (T *)out, os_i, 1);
+    RBG_LAUNCHED();
+}
+
 // Pick a split of K so that tiles * splits fills whole waves of `per_sm` resident CTAs per SM
 // (1 for FP64: co-resident FP64 CTAs share the SM's FP64 pipe, so a second CTA on an SM
 // doubles that SM's time).
@@ -161,6 +247,10 @@ void launch_dense(int tn, dim3 grid, cudaStream_t s, int64_t M, int64_t N, int64
 template <typename T>
 void run(int64_t M, int64_t N, int64_t K, double alpha, const POperand &P, const Strided &Q,
          double beta, void *out, int64_t os_i, int64_t os_j, cudaStream_t s) {
+    if (N == 1 && !P.buff) {
+        run_gemv<T>(M, K, alpha, P, Q, beta, out, os_i, s);
+        return;
+    }
     const int tn = tile_n_for(N);
     const int64_t tiles = ((M + BM - 1) / BM) * ((N + tn - 1) / tn);
     const int64_t kt_total = (K + BK - 1) / BK;
