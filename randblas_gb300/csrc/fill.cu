@@ -121,6 +121,33 @@ __global__ void saso_kernel(DevState s, int64_t vec_nnz, int64_t dim_major, int6
         saso_vector(s, vec_nnz, dim_major, i, idx_major, idx_minor, vals, mp, mv);
 }
 
+// dim_major < 2^32 and vec_nnz <= kSasoFastMaxNnz (operators of any practical size): the
+// 32-bit sampler (saso_column), 128 minor indices per block, with the block's entries staged
+// in shared memory so that the stores of all three arrays are contiguous.
+template <typename V, typename I>
+__global__ void __launch_bounds__(128) saso_fast_kernel(DevState s, int vec_nnz,
+                                                        uint32_t dim_major, int64_t dim_minor,
+                                                        I *idx_major, I *idx_minor, V *vals) {
+    __shared__ I smaj[128 * kSasoFastMaxNnz];
+    __shared__ V sval[128 * kSasoFastMaxNnz];
+    for (int64_t base = blockIdx.x * 128ll; base < dim_minor; base += gridDim.x * 128ll) {
+        const int64_t i = base + threadIdx.x;
+        if (i < dim_minor)
+            saso_column(s, (uint64_t)i, vec_nnz, dim_major, [&](int j, uint32_t major, bool neg) {
+                smaj[threadIdx.x * vec_nnz + j] = (I)major;
+                sval[threadIdx.x * vec_nnz + j] = neg ? (V)-1 : (V)1;
+            });
+        __syncthreads();
+        const int64_t n = min((int64_t)128, dim_minor - base) * vec_nnz, off = base * vec_nnz;
+        for (int64_t t = threadIdx.x; t < n; t += 128) {
+            idx_major[off + t] = smaj[t];
+            if (idx_minor) idx_minor[off + t] = (I)(base + t / vec_nnz);
+            if (vals) vals[off + t] = sval[t];
+        }
+        __syncthreads();
+    }
+}
+
 // ------------------------------------------------------------------ LASO
 // One thread per minor index i: vec_nnz iid samples over [0, dim_major) with Rademacher
 // signs (RandBLAS/util.hh:516-546: sample j of the vector uses counter
@@ -266,6 +293,19 @@ void launch_fill_saso(int dtype, int itype, const DevState &seed, int64_t vec_nn
     if (dim_minor <= 0 || vec_nnz <= 0) return;
     const int threads = 128;
     int grid = grid_for(dim_minor, threads);
+    if (dim_major < (int64_t)UINT32_MAX && vec_nnz <= kSasoFastMaxNnz) {
+#define RBG_SASO_FAST(V, I)                                                                  \
+    saso_fast_kernel<V, I><<<grid, 128, 0, s>>>(seed, (int)vec_nnz, (uint32_t)dim_major,     \
+                                                dim_minor, (I *)idx_major, (I *)idx_minor,   \
+                                                (V *)vals)
+        if (dtype == RBG_F32 && itype == RBG_I32) RBG_SASO_FAST(float, int32_t);
+        else if (dtype == RBG_F32) RBG_SASO_FAST(float, int64_t);
+        else if (itype == RBG_I32) RBG_SASO_FAST(double, int32_t);
+        else RBG_SASO_FAST(double, int64_t);
+#undef RBG_SASO_FAST
+        RBG_LAUNCHED();
+        return;
+    }
     int64_t *scratch = nullptr;
     Scratch buf;
     if (vec_nnz > kSasoLocalCap) {

@@ -305,42 +305,6 @@ constexpr int kFusedThreads = RBG_FUSED_THREADS;
 constexpr int kFusedMaxNnz = 16;
 constexpr uint32_t kSignBit = 0x80000000u;
 
-// Minor index i of a SASO: the partial Fisher-Yates shuffle of sparse_skops.hh:51-106 with
-// 32-bit arithmetic (exact: dim_major < 2^32, x0 % span < span).  emit(j, major, negative) is
-// called for j = 0 .. vec_nnz - 1 in order; counters run seed + i * vec_nnz + j.
-template <typename F>
-__device__ __forceinline__ void saso_column(const DevState &s, uint64_t i, int vec_nnz,
-                                            uint32_t dim_major, F &&emit) {
-    uint32_t mp[kFusedMaxNnz], mv[kFusedMaxNnz];
-    int msize = 0;
-    const uint64_t off = i * (uint64_t)vec_nnz;
-    for (int j = 0; j < vec_nnz; ++j) {
-        const uint4 r = philox(ctr_add(s.ctr, off + (uint64_t)j), s.key);
-        const uint32_t ell = (uint32_t)j + r.x % (dim_major - (uint32_t)j);
-        uint32_t vj = (uint32_t)j, vl = ell;
-        int sj = -1, sl = -1;
-        for (int q = 0; q < msize; ++q) {
-            if (mp[q] == (uint32_t)j) { vj = mv[q]; sj = q; }
-            if (mp[q] == ell) { vl = mv[q]; sl = q; }
-        }
-        if (ell != (uint32_t)j) {
-            if (sl >= 0) {
-                mv[sl] = vj;
-            } else {
-                mp[msize] = ell;
-                mv[msize] = vj;
-                ++msize;
-            }
-        }
-        if (sj >= 0) {
-            --msize;
-            mp[sj] = mp[msize];
-            mv[sj] = mv[msize];
-        }
-        emit(j, vl, (r.y & 1u) != 0u);
-    }
-}
-
 // Column c of submat(S) (minor index co + c) as kp words (vec_nnz entries, then spare-row
 // padding).
 __global__ void saso_pack_kernel(DevState s, int vec_nnz, int kp, uint32_t dim_major,
