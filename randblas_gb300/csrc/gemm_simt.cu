@@ -24,6 +24,8 @@ using simt::BK;
 using simt::NT;
 using simt::gen_p_tile;
 using simt::load_tile;
+using simt::load_tile_regs;
+using simt::store_tile_regs;
 
 // TN: output columns per CTA (128, or 64 for narrow problems); each thread owns 8 rows x TN/16
 // columns, in two halves TN/2 apart.
@@ -33,8 +35,11 @@ __global__ void __launch_bounds__(NT, (sizeof(T) == 4 || TN < BN) ? 2 : 1)
                         T *__restrict__ out, int64_t os_i, int64_t os_j, int64_t kt_per_split,
                         T *__restrict__ partial) {
     constexpr int CPT = TN / 16, CH = CPT / 2;
-    __shared__ __align__(16) T Ps[BK][BM + 4];
-    __shared__ __align__(16) T Qs[BK][TN + 4];
+    // two stages for FP32 (the next k step's data tile is loaded into registers while the
+    // current one is computed); one for FP64 (two would exceed 48 KB of static shared memory)
+    constexpr int NBUF = sizeof(T) == 4 ? 2 : 1;
+    __shared__ __align__(16) T Ps[NBUF][BK][BM + 4];
+    __shared__ __align__(16) T Qs[NBUF][BK][TN + 4];
     const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
     const int64_t tiles_n = (N + TN - 1) / TN;
     const int64_t i0 = (blockIdx.x / tiles_n) * BM;
@@ -50,36 +55,41 @@ __global__ void __launch_bounds__(NT, (sizeof(T) == 4 || TN < BN) ? 2 : 1)
         for (int b = 0; b < CPT; ++b) acc[a][b] = (T)0;
 
     const T *Qp = static_cast<const T *>(Q.ptr);
+    T qr[BK * TN / NT];  // this thread's share of the next data tile
+    if (kt_begin < kt_end) load_tile_regs<T, TN>(qr, Qp, Q.s0, Q.s1, K, N, kt_begin * BK, j0);
     for (int64_t kt = kt_begin; kt < kt_end; ++kt) {
         const int64_t k0 = kt * BK;
+        const int buf = NBUF == 2 ? (int)((kt - kt_begin) & 1) : 0;
         if constexpr (GEN) {
-            gen_p_tile<T>(Ps, P, M, K, i0, k0);
+            gen_p_tile<T>(Ps[buf], P, M, K, i0, k0);
         } else {
             // P(i, k) = buff[base + i*si + k*sk]
-            load_tile<T, BM>(Ps, static_cast<const T *>(P.buff) + P.base, P.sk, P.si, K, M, k0,
-                             i0);
+            load_tile<T, BM>(Ps[buf], static_cast<const T *>(P.buff) + P.base, P.sk, P.si, K, M,
+                             k0, i0);
         }
-        load_tile<T, TN>(Qs, Qp, Q.s0, Q.s1, K, N, k0, j0);
+        store_tile_regs<T, TN>(Qs[buf], qr, Q.s0, Q.s1);
+        // with two stages, this barrier also retires the reads of the stage written next
         __syncthreads();
+        if (kt + 1 < kt_end) load_tile_regs<T, TN>(qr, Qp, Q.s0, Q.s1, K, N, k0 + BK, j0);
 #pragma unroll
         for (int kk = 0; kk < BK; ++kk) {
             T a[8], b[CPT];
 #pragma unroll
             for (int q = 0; q < 4; ++q) {
-                a[q] = Ps[kk][ty * 4 + q];
-                a[4 + q] = Ps[kk][64 + ty * 4 + q];
+                a[q] = Ps[buf][kk][ty * 4 + q];
+                a[4 + q] = Ps[buf][kk][64 + ty * 4 + q];
             }
 #pragma unroll
             for (int q = 0; q < CH; ++q) {
-                b[q] = Qs[kk][tx * CH + q];
-                b[CH + q] = Qs[kk][TN / 2 + tx * CH + q];
+                b[q] = Qs[buf][kk][tx * CH + q];
+                b[CH + q] = Qs[buf][kk][TN / 2 + tx * CH + q];
             }
 #pragma unroll
             for (int x = 0; x < 8; ++x)
 #pragma unroll
                 for (int y = 0; y < CPT; ++y) acc[x][y] = fma(a[x], b[y], acc[x][y]);
         }
-        __syncthreads();
+        if (NBUF == 1) __syncthreads();
     }
 
 #pragma unroll

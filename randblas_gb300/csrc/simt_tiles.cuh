@@ -15,6 +15,29 @@ template <typename T, int TM = BM>
 __device__ __forceinline__ void gen_p_tile(T (*Ps)[TM + 4], const POperand &P, int64_t M,
                                            int64_t K, int64_t i0, int64_t k0) {
     const DenseGen &g = P.gen;
+    if (P.r_on_i && ((P.c0 + k0) & 3) == 0 && i0 + TM <= M && k0 + BK <= K) {
+        // interior tile, block-aligned: TM rows x BK / 4 whole counter blocks, no bounds
+        const int64_t b0 = (P.c0 + k0) >> 2;
+        for (int w = threadIdx.x; w < TM * (BK / 4); w += NT) {
+            const int i = w / (BK / 4), b = w % (BK / 4);
+            float v[4];
+            gen4(g.family, g.counter_of(P.r0 + i0 + i, b0 + b), g.key, v);
+#pragma unroll
+            for (int l = 0; l < 4; ++l) Ps[4 * b + l][i] = finish_entry<T>(g.family, v[l]);
+        }
+        return;
+    }
+    if (!P.r_on_i && ((P.c0 + i0) & 3) == 0 && i0 + TM <= M && k0 + BK <= K) {
+        const int64_t b0 = (P.c0 + i0) >> 2;
+        for (int w = threadIdx.x; w < BK * (TM / 4); w += NT) {
+            const int k = w / (TM / 4), b = w % (TM / 4);
+            float v[4];
+            gen4(g.family, g.counter_of(P.r0 + k0 + k, b0 + b), g.key, v);
+#pragma unroll
+            for (int l = 0; l < 4; ++l) Ps[k][4 * b + l] = finish_entry<T>(g.family, v[l]);
+        }
+        return;
+    }
     if (P.r_on_i) {
         // R follows i, C follows k: each of the TM rows needs the counter blocks covering
         // columns [c0 + k0, c0 + k0 + BK).
@@ -74,6 +97,44 @@ __device__ __forceinline__ void load_tile(T (*dst)[W + 4], const T *__restrict__
             dst[k][x] = (k0 + k < K && x0 + x < X) ? __ldg(src + (k0 + k) * sk + (x0 + x) * sx)
                                                    : (T)0;
         }
+    }
+}
+
+// load_tile split in two, so the global loads of the next k step can be in flight while the
+// current one is computed: load_tile_regs reads this thread's BK * W / NT elements (the same
+// elements load_tile would store) into registers; store_tile_regs writes them to the tile.
+template <typename T, int W>
+__device__ __forceinline__ void load_tile_regs(T (&r)[BK * W / NT], const T *__restrict__ src,
+                                               int64_t sk, int64_t sx, int64_t K, int64_t X,
+                                               int64_t k0, int64_t x0) {
+    const bool x_fast = sx == 1 || sk != 1;
+    if (k0 + BK <= K && x0 + W <= X) {  // interior: no bounds
+        const T *base = src + k0 * sk + x0 * sx;
+#pragma unroll
+        for (int e = 0; e < BK * W / NT; ++e) {
+            const int w = threadIdx.x + e * NT;
+            const int k = x_fast ? w / W : w % BK, x = x_fast ? w % W : w / BK;
+            r[e] = __ldg(base + k * sk + x * sx);
+        }
+        return;
+    }
+#pragma unroll
+    for (int e = 0; e < BK * W / NT; ++e) {
+        const int w = threadIdx.x + e * NT;
+        const int k = x_fast ? w / W : w % BK, x = x_fast ? w % W : w / BK;
+        r[e] = (k0 + k < K && x0 + x < X) ? __ldg(src + (k0 + k) * sk + (x0 + x) * sx) : (T)0;
+    }
+}
+
+template <typename T, int W>
+__device__ __forceinline__ void store_tile_regs(T (*dst)[W + 4], const T (&r)[BK * W / NT],
+                                                int64_t sk, int64_t sx) {
+    const bool x_fast = sx == 1 || sk != 1;
+#pragma unroll
+    for (int e = 0; e < BK * W / NT; ++e) {
+        const int w = threadIdx.x + e * NT;
+        const int k = x_fast ? w / W : w % BK, x = x_fast ? w % W : w / BK;
+        dst[k][x] = r[e];
     }
 }
 
