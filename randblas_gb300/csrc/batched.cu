@@ -36,7 +36,9 @@ constexpr int kConfigs = 4;
 constexpr int kTileRows[kConfigs + 1] = {0, 128, 128, 128, 64};
 constexpr int kTileWidth[kConfigs + 1] = {0, 128, 64, 32, 256};
 constexpr int kMaxSplits = 64;
-constexpr int kQsFloats = BK * (256 + 4);
+constexpr int kPsFloats = BK * (BM + 4);   // one operator stage (largest tile)
+constexpr int kQsFloats = BK * (256 + 4);  // one data stage (largest tile)
+constexpr size_t kBatchedSmem = (size_t)2 * (kPsFloats + kQsFloats) * sizeof(float);
 
 struct ProbDev {
     POperand P;       // generated operator
@@ -51,6 +53,7 @@ struct ProbDev {
     int64_t tiles_n;
     int64_t partial_off;  // floats into the partial buffer ([splits][M][N])
     int64_t counter_off;  // ints into the tile counters
+    int32_t paired;       // column tiles taken two at a time by a cluster pair
 };
 
 struct WorkItem {
@@ -74,14 +77,25 @@ __device__ __forceinline__ void load_row(const float *p, float *out) {
 }
 
 // One output tile (or one K split of it) of problem `pb`: BMT x BNT, TN columns per thread.
-template <int BMT, int BNT, int TN>
+// kPair: the two CTAs of a cluster take column tiles `tile` and `tile + 1` (same row block,
+// same split) and share the generated operator tiles, each generating half of every interior
+// tile into both CTAs' stages (remote[q]: CTA q's operator stages), with one cluster barrier
+// per k step.
+template <int BMT, int BNT, int TN, bool kPair>
 __device__ __forceinline__ void batched_tile(const ProbDev &pb, int64_t tile, int split,
                                              float *ps_raw, float *qs_raw, float *partial,
-                                             int *counters, int *s_flag) {
+                                             int *counters, int *s_flag, uint32_t rank,
+                                             const uint32_t (&remote)[2]) {
+    if constexpr (kPair) tile += rank;
     constexpr int TX = BNT / TN;  // thread columns
     static_assert(TX * (BMT / 8) == NT, "one 8 x TN block per thread");
-    float(*Ps)[BMT + 4] = reinterpret_cast<float(*)[BMT + 4]>(ps_raw);
-    float(*Qs)[BNT + 4] = reinterpret_cast<float(*)[BNT + 4]>(qs_raw);
+    // two stages each: stage s of the operator tile at ps_raw + s * kPsStage, of the data tile
+    // at qs_raw + s * kQsStage; the next data tile is loaded into registers while the current
+    // one is computed
+    using PsTile = float[BK][BMT + 4];
+    using QsTile = float[BK][BNT + 4];
+    PsTile *Ps2 = reinterpret_cast<PsTile *>(ps_raw);
+    QsTile *Qs2 = reinterpret_cast<QsTile *>(qs_raw);
     const int tx = threadIdx.x % TX, ty = threadIdx.x / TX;
     const int64_t i0 = (tile / pb.tiles_n) * BMT, j0 = (tile % pb.tiles_n) * BNT;
     const int64_t kt_total = (pb.K + BK - 1) / BK;
@@ -95,11 +109,41 @@ __device__ __forceinline__ void batched_tile(const ProbDev &pb, int64_t tile, in
 #pragma unroll
         for (int b = 0; b < TN; ++b) acc[a][b] = 0.f;
 
+    // register prefetch of the data tile up to 128 columns (the 256-wide tile would spill)
+    constexpr bool kPrefetch = BNT <= 128;
+    float qr[kPrefetch ? BK * BNT / NT : 1];
+    if constexpr (kPrefetch)
+        if (kb < ke)
+            simt::load_tile_regs<float, BNT>(qr, Qp, pb.Q.s0, pb.Q.s1, pb.K, pb.N, kb * BK, j0);
     for (int64_t kt = kb; kt < ke; ++kt) {
         const int64_t k0 = kt * BK;
-        simt::gen_p_tile<float, BMT>(Ps, pb.P, pb.M, pb.K, i0, k0);
-        simt::load_tile<float, BNT>(Qs, Qp, pb.Q.s0, pb.Q.s1, pb.K, pb.N, k0, j0);
-        __syncthreads();
+        const int st = (int)((kt - kb) & 1);
+        float(*Ps)[BMT + 4] = Ps2[st];
+        float(*Qs)[BNT + 4] = Qs2[st];
+        if constexpr (kPair) {
+            // the same decision in both CTAs (same row block, same k)
+            const bool aligned = ((pb.P.r_on_i ? pb.P.c0 + k0 : pb.P.c0 + i0) & 3) == 0;
+            if (aligned && i0 + BMT <= pb.M && k0 + BK <= pb.K)
+                simt::gen_p_tile_shared<BMT, 2>(
+                    remote, (uint32_t)(st * BK * (BMT + 4) * sizeof(float)), pb.P, i0, k0, rank);
+            else
+                simt::gen_p_tile<float, BMT>(Ps, pb.P, pb.M, pb.K, i0, k0);
+        } else {
+            simt::gen_p_tile<float, BMT>(Ps, pb.P, pb.M, pb.K, i0, k0);
+        }
+        if constexpr (kPrefetch)
+            simt::store_tile_regs<float, BNT>(Qs, qr, pb.Q.s0, pb.Q.s1);
+        else
+            simt::load_tile<float, BNT>(Qs, Qp, pb.Q.s0, pb.Q.s1, pb.K, pb.N, k0, j0);
+        // this barrier also retires the reads of the stage written next (in both CTAs of a
+        // pair)
+        if constexpr (kPair) simt::cluster_arrive();
+        else __syncthreads();
+        if constexpr (kPrefetch)
+            if (kt + 1 < ke)
+                simt::load_tile_regs<float, BNT>(qr, Qp, pb.Q.s0, pb.Q.s1, pb.K, pb.N, k0 + BK,
+                                                 j0);
+        if constexpr (kPair) simt::cluster_wait();
 #pragma unroll
         for (int kk = 0; kk < BK; ++kk) {
             // explicit vector loads: the tiles are views of flat shared arrays, so the compiler
@@ -117,8 +161,8 @@ __device__ __forceinline__ void batched_tile(const ProbDev &pb, int64_t tile, in
 #pragma unroll
                 for (int y = 0; y < TN; ++y) acc[x][y] = fmaf(a[x], b[y], acc[x][y]);
         }
-        __syncthreads();
     }
+    __syncthreads();  // the stages are free for the next item
 
     auto row_of = [&](int x) { return i0 + (x < 4 ? ty * 4 + x : BMT / 2 + ty * 4 + (x - 4)); };
     auto col_of = [&](int y) {
@@ -171,19 +215,69 @@ __device__ __forceinline__ void batched_tile(const ProbDev &pb, int64_t tile, in
     }
 }
 
+template <bool kPair>
+__device__ __forceinline__ void batched_dispatch(const ProbDev &pb, const WorkItem &item,
+                                                 float *Ps, float *Qs, float *partial,
+                                                 int *counters, int *s_flag, uint32_t rank,
+                                                 const uint32_t (&remote)[2]) {
+    if (pb.bm == 64)
+        batched_tile<64, 256, 8, kPair>(pb, item.tile, item.split, Ps, Qs, partial, counters,
+                                        s_flag, rank, remote);
+    else if (pb.bn == 128)
+        batched_tile<128, 128, 8, kPair>(pb, item.tile, item.split, Ps, Qs, partial, counters,
+                                         s_flag, rank, remote);
+    else if (pb.bn == 64)
+        batched_tile<128, 64, 4, kPair>(pb, item.tile, item.split, Ps, Qs, partial, counters,
+                                        s_flag, rank, remote);
+    else
+        batched_tile<128, 32, 2, kPair>(pb, item.tile, item.split, Ps, Qs, partial, counters,
+                                        s_flag, rank, remote);
+}
+
+// Launched in clusters of two.  Phase 1: pair items (items[0, n_pairs)), both CTAs of a
+// cluster on the same item -- rank 0 takes it from counter 0 and stores its index into rank
+// 1's shared memory before the cluster barrier.  Phase 2: single items
+// (items[n_pairs, n_items)) from counter 1, each CTA on its own.
 __global__ void __launch_bounds__(NT, 2)
     batched_sketch_kernel(const ProbDev *__restrict__ probs, const WorkItem *__restrict__ items,
-                          int64_t n_items, unsigned long long *work_counter,
+                          int64_t n_pairs, int64_t n_items, unsigned long long *work_counter,
                           float *__restrict__ partial, int *__restrict__ counters) {
-    __shared__ __align__(16) float Ps[BK * (BM + 4)];
-    __shared__ __align__(16) float Qs[kQsFloats];
+    extern __shared__ __align__(16) float bsm_tiles[];  // 2 operator stages, 2 data stages
+    float *Ps = bsm_tiles;
+    float *Qs = bsm_tiles + 2 * kPsFloats;
     __shared__ ProbDev s_pb;
     __shared__ WorkItem s_item;
     __shared__ int s_flag;
     __shared__ unsigned long long s_w;
+    const uint32_t rank = simt::cluster_rank();
+    const uint32_t ps_local = (uint32_t)__cvta_generic_to_shared(Ps);
+    const uint32_t remote[2] = {simt::cluster_map(ps_local, 0), simt::cluster_map(ps_local, 1)};
+    const uint32_t peer_w =
+        simt::cluster_map((uint32_t)__cvta_generic_to_shared(&s_w), rank ^ 1u);
+    simt::cluster_arrive();  // both CTAs run before any store into the other
+    simt::cluster_wait();
+    for (;;) {
+        if (rank == 0 && threadIdx.x == 0) {
+            const unsigned long long w = atomicAdd(work_counter, 1ull);
+            s_w = w;
+            simt::st_cluster(peer_w, w);
+        }
+        simt::cluster_arrive();
+        simt::cluster_wait();
+        if (s_w >= (unsigned long long)n_pairs) break;  // the same in both CTAs
+        if (threadIdx.x == 0) {
+            s_item = items[s_w];
+            s_pb = probs[s_item.prob];
+        }
+        __syncthreads();
+        batched_dispatch<true>(s_pb, s_item, Ps, Qs, partial, counters, &s_flag, rank, remote);
+        // both CTAs are done with this item's stages and with s_w before the next fetch
+        simt::cluster_arrive();
+        simt::cluster_wait();
+    }
     for (;;) {
         if (threadIdx.x == 0) {
-            s_w = atomicAdd(work_counter, 1ull);
+            s_w = (unsigned long long)n_pairs + atomicAdd(work_counter + 1, 1ull);
             if (s_w < (unsigned long long)n_items) {
                 s_item = items[s_w];
                 s_pb = probs[s_item.prob];
@@ -191,23 +285,25 @@ __global__ void __launch_bounds__(NT, 2)
         }
         __syncthreads();
         if (s_w >= (unsigned long long)n_items) break;
-        const int64_t tile = s_item.tile;
-        const int split = s_item.split;
-        if (s_pb.bm == 64)
-            batched_tile<64, 256, 8>(s_pb, tile, split, Ps, Qs, partial, counters, &s_flag);
-        else if (s_pb.bn == 128)
-            batched_tile<128, 128, 8>(s_pb, tile, split, Ps, Qs, partial, counters, &s_flag);
-        else if (s_pb.bn == 64)
-            batched_tile<128, 64, 4>(s_pb, tile, split, Ps, Qs, partial, counters, &s_flag);
-        else
-            batched_tile<128, 32, 2>(s_pb, tile, split, Ps, Qs, partial, counters, &s_flag);
+        batched_dispatch<false>(s_pb, s_item, Ps, Qs, partial, counters, &s_flag, rank, remote);
         __syncthreads();  // s_pb / s_item / s_w are rewritten by the next fetch
     }
 }
 
+void set_batched_smem_attr() {
+    static bool done = false;
+    if (done) return;
+    RBG_CUDA(cudaFuncSetAttribute(batched_sketch_kernel,
+                                  cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)kBatchedSmem));
+    done = true;
+}
+
 int resident_batched_ctas() {
     int per_sm = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batched_sketch_kernel, NT, 0) !=
+    set_batched_smem_attr();
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batched_sketch_kernel, NT,
+                                                      kBatchedSmem) !=
             cudaSuccess ||
         per_sm <= 0) {
         cudaGetLastError();
@@ -218,16 +314,19 @@ int resident_batched_ctas() {
 
 // Tile by a cost model, per k step of 16 and in thread instructions: FMAs over the whole
 // (padded) tile, plus generating its operator rows (Gaussian entries cost about ten times
-// uniform ones), plus staging the data tile.
+// uniform ones; halved when two column tiles share them in a cluster pair), plus staging the
+// data tile.  The 64 x 256 tile runs about 1.3x slower per FMA than the 128-row tiles (two
+// more shared-memory wavefronts per k step for its data rows, no register prefetch).
 int default_config(int64_t m_rows, int64_t n, int family) {
-    const double gen = family == RBG_GAUSSIAN ? 100.0 : 10.0;
     int best = 1;
     double best_cost = 0.0;
     for (int c = 1; c <= kConfigs; ++c) {
         const double bm = kTileRows[c], bn = kTileWidth[c];
-        const double tiles = (double)((m_rows + kTileRows[c] - 1) / kTileRows[c]) *
-                             (double)((n + kTileWidth[c] - 1) / kTileWidth[c]);
-        const double cost = tiles * (bm * bn + bm * gen + 2.0 * bn);
+        const int64_t tiles_n = (n + kTileWidth[c] - 1) / kTileWidth[c];
+        const double gen = family == RBG_GAUSSIAN ? (tiles_n >= 2 ? 50.0 : 100.0) : 10.0;
+        const double tiles = (double)((m_rows + kTileRows[c] - 1) / kTileRows[c]) * tiles_n;
+        const double cost =
+            tiles * (bm * bn * (bm == 64 ? 1.3 : 1.0) + bm * gen + 2.0 * bn);
         if (c == 1 || cost < best_cost * 0.999) {
             best_cost = cost;
             best = c;
@@ -242,12 +341,13 @@ int default_config(int64_t m_rows, int64_t n, int family) {
 // The device memory and launch shape of one batch (the opaque rbg_batched_plan of the C ABI).
 struct rbg_batched_plan_s {
     int64_t n_items = 0;
+    int64_t n_pairs = 0;  // pair items at the front of the item list
     int grid = 0;
     bool stream_ordered = false;  // memory from cudaMallocAsync (freed on a stream)
     void *mem = nullptr;
     rbg::ProbDev *probs = nullptr;
     rbg::WorkItem *items = nullptr;
-    unsigned long long *work_counter = nullptr;  // followed by the tile counters
+    unsigned long long *work_counter = nullptr;  // pair and single counters, then the tile counters
     int *counters = nullptr;
     size_t counter_bytes = 0;  // work counter + tile counters, zeroed before each run
     float *partial = nullptr;
@@ -263,7 +363,7 @@ size_t align256(size_t x) { return (x + 255) / 256 * 256; }
 // Validate the problems and build the descriptors and the sorted work list (host only).
 void build_plan(int32_t layout, const rbg_batch_problem *problems, int64_t count,
                 int32_t tile_config, std::vector<ProbDev> &descs, std::vector<WorkItem> &items,
-                int64_t &partial_floats, int64_t &tile_counters, int &grid) {
+                int64_t &n_pairs, int64_t &partial_floats, int64_t &tile_counters, int &grid) {
     if (layout != RBG_COL_MAJOR && layout != RBG_ROW_MAJOR)
         fail(RBG_ERROR_INVALID_ARGUMENT, "layout must be RBG_COL_MAJOR or RBG_ROW_MAJOR");
     if (count < 0) fail(RBG_ERROR_INVALID_ARGUMENT, "count must be >= 0");
@@ -273,6 +373,8 @@ void build_plan(int32_t layout, const rbg_batch_problem *problems, int64_t count
         fail(RBG_ERROR_INVALID_ARGUMENT, "tile_config must be 0 or a listed configuration");
     descs.clear();
     items.clear();
+    std::vector<WorkItem> pairs;
+    n_pairs = 0;
     partial_floats = 0;
     tile_counters = 0;
     std::vector<int64_t> kt(count, 0);
@@ -334,7 +436,7 @@ void build_plan(int32_t layout, const rbg_batch_problem *problems, int64_t count
     }
     // split long K so that no item costs more than ~1/8 of a CTA's fair share (the device is
     // queried only after every argument has been checked)
-    grid = resident_batched_ctas();
+    grid = std::max(2, resident_batched_ctas() & ~1);  // clusters of two
     const double cap = std::max(total_cost / (8.0 * std::max(grid, 1)), 128.0 * 128.0 * 64.0);
     for (int64_t p = 0; p < count; ++p) {
         ProbDev &pd = descs[p];
@@ -354,33 +456,63 @@ void build_plan(int32_t layout, const rbg_batch_problem *problems, int64_t count
         }
         // split-major: the items running at the same time share a K range, so each slab of A
         // is read from HBM once and reused from L2 by every output tile that needs it
+        // Gaussian operators over two or more column tiles: column tiles (2j, 2j + 1) of a row
+        // block go to a cluster pair that shares the generated operator tiles (a last odd
+        // column tile stays a single item)
+        pd.paired = pd.P.gen.family == RBG_GAUSSIAN && pd.tiles_n >= 2;
+        const int64_t tm = (pd.M + pd.bm - 1) / pd.bm;
         for (int64_t sp = 0; sp < splits; ++sp)
-            for (int64_t t = 0; t < tiles; ++t)
-                items.push_back(WorkItem{(int32_t)p, (int32_t)sp, t});
+            for (int64_t it = 0; it < tm; ++it)
+                for (int64_t jt = 0; jt < pd.tiles_n; ++jt) {
+                    const int64_t t = it * pd.tiles_n + jt;
+                    if (pd.paired && jt + 1 < pd.tiles_n && jt % 2 == 0)
+                        pairs.push_back(WorkItem{(int32_t)p, (int32_t)sp, t});
+                    else if (!pd.paired || jt % 2 == 0)
+                        items.push_back(WorkItem{(int32_t)p, (int32_t)sp, t});
+                }
     }
     // longest processing time first; ties keep problem order (and the split-major order)
-    std::stable_sort(items.begin(), items.end(), [&](const WorkItem &a, const WorkItem &b) {
+    auto lpt = [&](const WorkItem &a, const WorkItem &b) {
         const ProbDev &pa = descs[a.prob], &pb = descs[b.prob];
         return (double)pa.kt_per_split * pa.bm * pa.bn > (double)pb.kt_per_split * pb.bm * pb.bn;
-    });
+    };
+    std::stable_sort(pairs.begin(), pairs.end(), lpt);
+    std::stable_sort(items.begin(), items.end(), lpt);
+    n_pairs = (int64_t)pairs.size();
+    items.insert(items.begin(), pairs.begin(), pairs.end());
 }
 
 void execute_plan(const BatchedPlan &pl, cudaStream_t s) {
     if (pl.n_items == 0) return;
     RBG_CUDA(cudaMemsetAsync(pl.work_counter, 0, pl.counter_bytes, s));
     ProfScope prof("batched_sketch", s);
-    batched_sketch_kernel<<<pl.grid, NT, 0, s>>>(pl.probs, pl.items, pl.n_items,
-                                                 pl.work_counter, pl.partial, pl.counters);
+    set_batched_smem_attr();
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)pl.grid);
+    cfg.blockDim = dim3(NT);
+    cfg.dynamicSmemBytes = kBatchedSmem;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = 2;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    RBG_CUDA(cudaLaunchKernelEx(&cfg, batched_sketch_kernel, (const ProbDev *)pl.probs,
+                                (const WorkItem *)pl.items, pl.n_pairs, pl.n_items,
+                                pl.work_counter, pl.partial, pl.counters));
     RBG_LAUNCHED();
 }
 
 // Lay the plan's device memory out and upload descriptors and items.
 void upload_plan(BatchedPlan &pl, const std::vector<ProbDev> &descs,
-                 const std::vector<WorkItem> &items, int64_t partial_floats,
+                 const std::vector<WorkItem> &items, int64_t n_pairs, int64_t partial_floats,
                  int64_t tile_counters, cudaStream_t s, bool stream_ordered) {
     const size_t probs_b = align256(descs.size() * sizeof(ProbDev));
     const size_t items_b = align256(items.size() * sizeof(WorkItem));
-    const size_t ctr_b = align256(sizeof(unsigned long long) + (size_t)tile_counters * sizeof(int));
+    const size_t ctr_b =
+        align256(2 * sizeof(unsigned long long) + (size_t)tile_counters * sizeof(int));
     const size_t part_b = align256((size_t)partial_floats * sizeof(float));
     pl.bytes = probs_b + items_b + ctr_b + part_b;
     pl.stream_ordered = stream_ordered;
@@ -392,10 +524,11 @@ void upload_plan(BatchedPlan &pl, const std::vector<ProbDev> &descs,
     pl.probs = reinterpret_cast<ProbDev *>(base);
     pl.items = reinterpret_cast<WorkItem *>(base + probs_b);
     pl.work_counter = reinterpret_cast<unsigned long long *>(base + probs_b + items_b);
-    pl.counters = reinterpret_cast<int *>(pl.work_counter + 1);
-    pl.counter_bytes = sizeof(unsigned long long) + (size_t)tile_counters * sizeof(int);
+    pl.counters = reinterpret_cast<int *>(pl.work_counter + 2);
+    pl.counter_bytes = 2 * sizeof(unsigned long long) + (size_t)tile_counters * sizeof(int);
     pl.partial = reinterpret_cast<float *>(base + probs_b + items_b + ctr_b);
     pl.n_items = (int64_t)items.size();
+    pl.n_pairs = n_pairs;
     if (!descs.empty())
         RBG_CUDA(cudaMemcpyAsync(pl.probs, descs.data(), descs.size() * sizeof(ProbDev),
                                  cudaMemcpyHostToDevice, s));
@@ -453,12 +586,14 @@ extern "C" int rbg_batched_plan_create(int32_t layout, const rbg_batch_problem *
         std::vector<WorkItem> items;
         int64_t partial_floats = 0, tile_counters = 0;
         int grid = 0;
-        build_plan(layout, problems, count, tile_config, descs, items, partial_floats,
+        int64_t n_pairs = 0;
+        build_plan(layout, problems, count, tile_config, descs, items, n_pairs, partial_floats,
                    tile_counters, grid);
         auto *pl = new BatchedPlan();
         pl->grid = grid;
         try {
-            upload_plan(*pl, descs, items, partial_floats, tile_counters, nullptr, false);
+            upload_plan(*pl, descs, items, n_pairs, partial_floats, tile_counters, nullptr,
+                        false);
         } catch (...) {
             if (pl->mem) cudaFree(pl->mem);
             delete pl;
@@ -500,12 +635,13 @@ extern "C" int rbg_lskge3_batched(int32_t layout, const rbg_batch_problem *probl
         std::vector<WorkItem> items;
         int64_t partial_floats = 0, tile_counters = 0;
         int grid = 0;
-        build_plan(layout, problems, count, tile_config, descs, items, partial_floats,
+        int64_t n_pairs = 0;
+        build_plan(layout, problems, count, tile_config, descs, items, n_pairs, partial_floats,
                    tile_counters, grid);
         if (items.empty()) return;
         BatchedPlan pl;
         pl.grid = grid;
-        upload_plan(pl, descs, items, partial_floats, tile_counters, s, true);
+        upload_plan(pl, descs, items, n_pairs, partial_floats, tile_counters, s, true);
         execute_plan(pl, s);
         RBG_CUDA(cudaFreeAsync(pl.mem, s));
     });

@@ -28,12 +28,16 @@ using simt::load_tile_regs;
 using simt::store_tile_regs;
 
 // TN: output columns per CTA (128, or 64 for narrow problems); each thread owns 8 rows x TN/16
-// columns, in two halves TN/2 apart.
-template <typename T, bool GEN, int TN>
+// columns, in two halves TN/2 apart.  CL > 1 (FP32, generated operator): the CL CTAs of a
+// thread-block cluster hold CL consecutive column tiles of the same row block and share its
+// operator tiles, each generating 1/CL of every interior tile (one cluster barrier per k step
+// instead of __syncthreads); results are the same bits as with CL = 1.  CL must divide BM / 4.
+template <typename T, bool GEN, int TN, int CL = 1>
 __global__ void __launch_bounds__(NT, (sizeof(T) == 4 || TN < BN) ? 2 : 1)
     dense_sketch_kernel(int64_t M, int64_t N, int64_t K, POperand P, Strided Q, T alpha, T beta,
                         T *__restrict__ out, int64_t os_i, int64_t os_j, int64_t kt_per_split,
                         T *__restrict__ partial) {
+    static_assert(CL == 1 || (GEN && sizeof(T) == 4), "clusters: FP32, generated operator");
     constexpr int CPT = TN / 16, CH = CPT / 2;
     // two stages for FP32 (the next k step's data tile is loaded into registers while the
     // current one is computed); one for FP64 (two would exceed 48 KB of static shared memory)
@@ -57,20 +61,48 @@ __global__ void __launch_bounds__(NT, (sizeof(T) == 4 || TN < BN) ? 2 : 1)
     const T *Qp = static_cast<const T *>(Q.ptr);
     T qr[BK * TN / NT];  // this thread's share of the next data tile
     if (kt_begin < kt_end) load_tile_regs<T, TN>(qr, Qp, Q.s0, Q.s1, K, N, kt_begin * BK, j0);
+    uint32_t remote[CL];  // the operator tiles of the cluster's CTAs
+    uint32_t rank = 0;
+    if constexpr (CL > 1) {
+        rank = simt::cluster_rank();
+        const uint32_t local = (uint32_t)__cvta_generic_to_shared(&Ps[0][0][0]);
+#pragma unroll
+        for (int q = 0; q < CL; ++q) remote[q] = simt::cluster_map(local, (uint32_t)q);
+        simt::cluster_arrive();  // every CTA of the cluster runs before any stores into it
+        simt::cluster_wait();
+    }
     for (int64_t kt = kt_begin; kt < kt_end; ++kt) {
         const int64_t k0 = kt * BK;
         const int buf = NBUF == 2 ? (int)((kt - kt_begin) & 1) : 0;
         if constexpr (GEN) {
-            gen_p_tile<T>(Ps[buf], P, M, K, i0, k0);
+            if constexpr (CL > 1) {
+                // the same decision in every CTA of the cluster (same row block, same k)
+                const bool aligned = ((P.r_on_i ? P.c0 + k0 : P.c0 + i0) & 3) == 0;
+                if (aligned && i0 + BM <= M && k0 + BK <= K)
+                    simt::gen_p_tile_shared<BM, CL>(
+                        remote, (uint32_t)(buf * BK * (BM + 4) * sizeof(float)), P, i0, k0,
+                        rank);
+                else
+                    gen_p_tile<T>(Ps[buf], P, M, K, i0, k0);
+            } else {
+                gen_p_tile<T>(Ps[buf], P, M, K, i0, k0);
+            }
         } else {
             // P(i, k) = buff[base + i*si + k*sk]
             load_tile<T, BM>(Ps[buf], static_cast<const T *>(P.buff) + P.base, P.sk, P.si, K, M,
                              k0, i0);
         }
         store_tile_regs<T, TN>(Qs[buf], qr, Q.s0, Q.s1);
-        // with two stages, this barrier also retires the reads of the stage written next
-        __syncthreads();
-        if (kt + 1 < kt_end) load_tile_regs<T, TN>(qr, Qp, Q.s0, Q.s1, K, N, k0 + BK, j0);
+        // with two stages, this barrier also retires the reads of the stage written next (in
+        // every CTA of the cluster)
+        if constexpr (CL > 1) {
+            simt::cluster_arrive();
+            if (kt + 1 < kt_end) load_tile_regs<T, TN>(qr, Qp, Q.s0, Q.s1, K, N, k0 + BK, j0);
+            simt::cluster_wait();
+        } else {
+            __syncthreads();
+            if (kt + 1 < kt_end) load_tile_regs<T, TN>(qr, Qp, Q.s0, Q.s1, K, N, k0 + BK, j0);
+        }
 #pragma unroll
         for (int kk = 0; kk < BK; ++kk) {
             T a[8], b[CPT];
@@ -244,6 +276,37 @@ template <typename T, bool GEN>
 void launch_dense(int tn, dim3 grid, cudaStream_t s, int64_t M, int64_t N, int64_t K,
                   const POperand &P, const Strided &Q, double alpha, double beta, void *out,
                   int64_t os_i, int64_t os_j, int64_t kt_per_split, T *partial) {
+    if constexpr (GEN && sizeof(T) == 4) {
+        // Gaussian operators: pairs of column tiles of a row block share the generated operator
+        // tiles (measured on GB300: +28-30 % at 2048 x 2^18 x 512 and 1024 x 2^17 x 256).
+        // Larger clusters cost more in cluster barriers than they save, and uniform entries
+        // are too cheap to generate for sharing to pay.
+        const int64_t tiles_n = (N + tn - 1) / tn;
+        const int cl = (P.gen.family == RBG_GAUSSIAN && tiles_n % 2 == 0) ? 2 : 1;
+        if (cl > 1) {
+            cudaLaunchConfig_t cfg = {};
+            cfg.gridDim = grid;
+            cfg.blockDim = dim3(NT);
+            cfg.stream = s;
+            cudaLaunchAttribute attr[1];
+            attr[0].id = cudaLaunchAttributeClusterDimension;
+            attr[0].val.clusterDim.x = (unsigned)cl;
+            attr[0].val.clusterDim.y = 1;
+            attr[0].val.clusterDim.z = 1;
+            cfg.attrs = attr;
+            cfg.numAttrs = 1;
+            const float a = (float)alpha, b = (float)beta;
+            float *o = static_cast<float *>(out);
+            float *pt = reinterpret_cast<float *>(partial);
+#define RBG_DENSE_CLUSTER(TNV, CLV)                                                          \
+    RBG_CUDA(cudaLaunchKernelEx(&cfg, dense_sketch_kernel<float, true, TNV, CLV>, M, N, K, P, \
+                                Q, a, b, o, os_i, os_j, kt_per_split, pt))
+            if (tn == 64) RBG_DENSE_CLUSTER(64, 2);
+            else RBG_DENSE_CLUSTER(BN, 2);
+#undef RBG_DENSE_CLUSTER
+            return;
+        }
+    }
     if (tn == 64)
         dense_sketch_kernel<T, GEN, 64><<<grid, NT, 0, s>>>(M, N, K, P, Q, (T)alpha, (T)beta,
                                                             (T *)out, os_i, os_j, kt_per_split,

@@ -77,6 +77,75 @@ __device__ __forceinline__ void gen_p_tile(T (*Ps)[TM + 4], const POperand &P, i
     }
 }
 
+// ------------------------------------------------------------------ thread-block clusters
+__device__ __forceinline__ uint32_t cluster_rank() {
+    uint32_t r;
+    asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+    return r;
+}
+// the shared::cluster address of the same location in CTA `rank` of the cluster
+__device__ __forceinline__ uint32_t cluster_map(uint32_t local, uint32_t rank) {
+    uint32_t r;
+    asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(local), "r"(rank));
+    return r;
+}
+__device__ __forceinline__ void st_cluster(uint32_t addr, float v) {
+    asm volatile("st.shared::cluster.f32 [%0], %1;" ::"r"(addr), "f"(v) : "memory");
+}
+__device__ __forceinline__ void st_cluster(uint32_t addr, unsigned long long v) {
+    asm volatile("st.shared::cluster.u64 [%0], %1;" ::"r"(addr), "l"(v) : "memory");
+}
+// barrier over all threads of all CTAs of the cluster, split into arrive and wait
+__device__ __forceinline__ void cluster_arrive() {
+    asm volatile("barrier.cluster.arrive.release.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void cluster_wait() {
+    asm volatile("barrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+
+// An interior FP32 operator tile [BK][TM + 4] (whole, block-aligned counter blocks, as in
+// gen_p_tile's fast path) generated by the CL CTAs of a cluster together: CTA `rank`
+// generates 1/CL of it and stores every entry into all CL CTAs' tiles, at remote[q] + off in
+// CTA q.  The caller then runs a cluster barrier before any CTA reads the tile.
+template <int TM, int CL>
+__device__ __forceinline__ void gen_p_tile_shared(const uint32_t (&remote)[CL], uint32_t off0,
+                                                  const POperand &P, int64_t i0, int64_t k0,
+                                                  uint32_t rank) {
+    const DenseGen &g = P.gen;
+    constexpr uint32_t kRowB = (TM + 4) * sizeof(float);
+    if (P.r_on_i) {
+        constexpr int ROWS = TM / CL;  // rows of the tile per CTA
+        const int64_t b0 = (P.c0 + k0) >> 2;
+        for (int w = threadIdx.x; w < ROWS * (BK / 4); w += NT) {
+            const int i = (int)rank * ROWS + w / (BK / 4), b = w % (BK / 4);
+            float v[4];
+            gen4(g.family, g.counter_of(P.r0 + i0 + i, b0 + b), g.key, v);
+#pragma unroll
+            for (int l = 0; l < 4; ++l) {
+                const float e = finish_entry<float>(g.family, v[l]);
+                const uint32_t off = off0 + (4 * b + l) * kRowB + i * 4u;
+#pragma unroll
+                for (int q = 0; q < CL; ++q) st_cluster(remote[q] + off, e);
+            }
+        }
+    } else {
+        constexpr int BLOCKS = TM / 4 / CL;  // counter blocks of a natural row per CTA
+        const int64_t b0 = (P.c0 + i0) >> 2;
+        for (int w = threadIdx.x; w < BK * BLOCKS; w += NT) {
+            const int k = w / BLOCKS, b = (int)rank * BLOCKS + w % BLOCKS;
+            float v[4];
+            gen4(g.family, g.counter_of(P.r0 + k0 + k, b0 + b), g.key, v);
+#pragma unroll
+            for (int l = 0; l < 4; ++l) {
+                const float e = finish_entry<float>(g.family, v[l]);
+                const uint32_t off = off0 + k * kRowB + (4 * b + l) * 4u;
+#pragma unroll
+                for (int q = 0; q < CL; ++q) st_cluster(remote[q] + off, e);
+            }
+        }
+    }
+}
+
 // Strided tile load into a k-major SMEM tile: dst[k][x] = src(k0 + k, x0 + x), x in [0, W).
 // Threads walk the unit-stride dimension when there is one.  The data matrix is read-only
 // during a sketch, so loads go through the read-only data path (also when the pointer reaches
@@ -85,6 +154,16 @@ template <typename T, int W>
 __device__ __forceinline__ void load_tile(T (*dst)[W + 4], const T *__restrict__ src,
                                           int64_t sk, int64_t sx, int64_t K, int64_t X,
                                           int64_t k0, int64_t x0) {
+    if (k0 + BK <= K && x0 + W <= X) {  // interior: no bounds
+        const T *base = src + k0 * sk + x0 * sx;
+        const bool x_fast = sx == 1 || sk != 1;
+#pragma unroll 4
+        for (int w = threadIdx.x; w < BK * W; w += NT) {
+            const int k = x_fast ? w / W : w % BK, x = x_fast ? w % W : w / BK;
+            dst[k][x] = __ldg(base + k * sk + x * sx);
+        }
+        return;
+    }
     if (sx == 1 || sk != 1) {
         for (int w = threadIdx.x; w < BK * W; w += NT) {
             const int k = w / W, x = w % W;

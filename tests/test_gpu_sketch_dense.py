@@ -179,3 +179,27 @@ def test_alpha_zero_and_beta_zero_semantics(rb):
     rb.sketch_general(rb.Layout.RowMajor, rb.Op.NoTrans, rb.Op.NoTrans, 20, 4, 300, 0.0, S, A, 4,
                       3.0, B2, 4)
     assert torch.equal(B2, torch.full_like(B2, 3.0))
+
+
+@pytest.mark.parametrize("family,axis", [("Uniform", "Long"), ("Gaussian", "Long"),
+                                         ("Uniform", "Short"), ("Gaussian", "Short")])
+def test_cluster_shared_operator_tiles_bitwise(rb, family, axis):
+    """Sketches whose data spans several 128-column tiles share each generated operator tile
+    across a thread-block cluster (each CTA generates part of it).  The result must be the same
+    bits as sketching each 128-column block alone (no cluster); K = 240 keeps both unsplit.
+    Both natural layouts of S (rows of S per output row, or per k), and a partial last row
+    block (d = 300)."""
+    import torch
+    d, n, m = 300, 512, 240
+    D = rb.DenseDist(d, m, getattr(rb.ScalarDist, family), getattr(rb.Axis, axis))
+    S = rb.DenseSkOp(D, rb.RNGState(77))
+    A = torch.randn(m, n, device="cuda", generator=torch.Generator(device="cuda").manual_seed(2))
+    B = torch.empty(d, n, device="cuda")
+    rb.sketch_general(rb.Layout.RowMajor, rb.Op.NoTrans, rb.Op.NoTrans, d, n, m, 1.0, S,
+                      A.view(-1), n, 0.0, B.view(-1), n)
+    for c in range(0, n, 128):
+        Ab = A[:, c:c + 128].contiguous()
+        Bb = torch.empty(d, 128, device="cuda")
+        rb.sketch_general(rb.Layout.RowMajor, rb.Op.NoTrans, rb.Op.NoTrans, d, 128, m, 1.0, S,
+                          Ab.view(-1), 128, 0.0, Bb.view(-1), 128)
+        assert torch.equal(B[:, c:c + 128], Bb), c
