@@ -2,8 +2,9 @@
 persistent launch.
 
 1. Every problem of a mixed batch (tails in every dimension, submatrix offsets, Gaussian and
-   uniform operators, alpha / beta, alpha = 0, long K that gets split, every tile width)
-   matches the plain single-problem sketch to FP32 accuracy, and a few match the oracle.
+   uniform operators, alpha / beta, alpha = 0, long K that gets split, every tile width,
+   Gaussian column tiles taken in cluster pairs, with and without a last odd tile) matches the
+   plain single-problem sketch to FP32 accuracy, and a few match the oracle.
 2. Results are bitwise reproducible across runs, and equal between the one-shot call, the
    plan and a replayed CUDA graph of the plan.
 3. The 512-problem batch with the distribution of the batching benchmark (m log-uniform in
@@ -29,6 +30,10 @@ SHAPES = [
     (20, 40, 100, 0, 0, 0, 0.0, 2.0, 0),
     (129, 65, 33, 4, 4, 1, 1.0, -0.5, 2),
     (256, 100, 262144, 0, 0, 0, 1.0, 0.0, 0),
+    # Gaussian over three column tiles of a 4-aligned submatrix: a cluster pair sharing the
+    # operator tiles of interior row blocks, a last odd column tile on its own, a partial row
+    # block
+    (257, 300, 9000, 3, 8, 0, 1.0, 0.0, 1),
 ]
 
 
