@@ -97,6 +97,12 @@ struct LowpParams {
     float *partial;        // [k_groups][M][N]
     const uint32_t *amax;  // FP8: [k_groups][npad] column maxima (float bits); else null
     int *err;
+    // one K slice: the epilogue writes B = alpha * acc + beta * B itself (no partials, no
+    // reduce pass)
+    int direct;
+    float *out;
+    int64_t os_i, os_j;
+    float alpha, beta;
 };
 
 __device__ __forceinline__ float finish_bf16_input(int family, float v) {
@@ -438,7 +444,38 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
                     for (int v = 0; v < 32; ++v)
                         r[v] = __float_as_uint(__uint_as_float(r[v]) * e4m3_scale(am[v]));
                 }
-                if (row < p.M && col < p.N) {
+                if (p.direct) {
+                    if (row < p.M && col < p.N) {
+                        float *o = p.out + row * p.os_i;
+                        if (col + 32 <= p.N && p.os_j == 1 &&
+                            ((reinterpret_cast<uintptr_t>(o + col)) & 15) == 0) {
+#pragma unroll
+                            for (int v = 0; v < 8; ++v) {
+                                float4 *o4 = reinterpret_cast<float4 *>(o + col + 4 * v);
+                                float4 b = make_float4(0.f, 0.f, 0.f, 0.f);
+                                if (p.beta != 0.f) b = *o4;
+                                float4 w;
+                                w.x = p.beta == 0.f ? p.alpha * __uint_as_float(r[4 * v])
+                                                    : fmaf(p.alpha, __uint_as_float(r[4 * v]), p.beta * b.x);
+                                w.y = p.beta == 0.f ? p.alpha * __uint_as_float(r[4 * v + 1])
+                                                    : fmaf(p.alpha, __uint_as_float(r[4 * v + 1]), p.beta * b.y);
+                                w.z = p.beta == 0.f ? p.alpha * __uint_as_float(r[4 * v + 2])
+                                                    : fmaf(p.alpha, __uint_as_float(r[4 * v + 2]), p.beta * b.z);
+                                w.w = p.beta == 0.f ? p.alpha * __uint_as_float(r[4 * v + 3])
+                                                    : fmaf(p.alpha, __uint_as_float(r[4 * v + 3]), p.beta * b.w);
+                                *o4 = w;
+                            }
+                        } else {
+#pragma unroll
+                            for (int v = 0; v < 32; ++v)
+                                if (col + v < p.N) {
+                                    float &x = o[(col + v) * p.os_j];
+                                    const float a = __uint_as_float(r[v]);
+                                    x = p.beta == 0.f ? p.alpha * a : fmaf(p.alpha, a, p.beta * x);
+                                }
+                        }
+                    }
+                } else if (row < p.M && col < p.N) {
                     if (col + 32 <= p.N && (p.N & 3) == 0) {
 #pragma unroll
                         for (int v = 0; v < 8; ++v)
@@ -777,19 +814,22 @@ Plan make_plan(int64_t M, int64_t N, int64_t K, bool fp8) {
     const int slots = std::max(1, resident_clusters(pl.cn * pl.cm));
     pl.kpad = pl.k_steps * pl.bke;
     pl.npad = pl.tiles_n * BN;
-    // K slices: fill whole waves of resident clusters, keep slices >= 32 k-steps, bound the
-    // partial buffer at 1 GiB
+    // K slices: the fewest estimated seconds -- waves of resident clusters times the k-steps of
+    // a slice (about 0.3 us per k-step of a unit on GB300), plus, for more than one slice,
+    // writing the partials and reading them back in the reduce pass at ~6 TB/s -- with slices
+    // of >= 32 k-steps and the partial buffer at most 1 GiB
     const int64_t tiles = pl.m_groups * pl.n_groups;
     int64_t best_g = 1;
-    double best = -1.0;
+    double best = 0.0;
     const int64_t gmax = std::max<int64_t>(1, std::min<int64_t>(pl.k_steps / 32, 64));
     for (int64_t g = 1; g <= gmax; ++g) {
         if ((double)g * M * N * 4 > (double)(1ll << 30)) break;
         const int64_t units = tiles * g;
         const int64_t waves = (units + slots - 1) / slots;
-        const double eff = (double)units / (double)(waves * slots) - 0.001 * (double)g;
-        if (eff > best + 1e-12) {
-            best = eff;
+        const double t = (double)waves * (double)((pl.k_steps + g - 1) / g) * 0.3e-6 +
+                         (g > 1 ? (2.0 * g + 1.0) * (double)M * N * 4.0 / 6.0e12 : 0.0);
+        if (g == 1 || t < best * (1.0 - 1e-9)) {
+            best = t;
             best_g = g;
         }
     }
@@ -798,7 +838,7 @@ Plan make_plan(int64_t M, int64_t N, int64_t K, bool fp8) {
     pl.units = tiles * pl.groups;
     pl.at_bytes = ((size_t)pl.npad * pl.kpad * (fp8 ? 1 : 2) + 1023) / 1024 * 1024;
     pl.amax_bytes = fp8 ? ((size_t)pl.groups * pl.npad * 4 + 1023) / 1024 * 1024 : 0;
-    pl.partial_bytes = (size_t)pl.groups * M * N * 4;
+    pl.partial_bytes = pl.groups == 1 ? 0 : (size_t)pl.groups * M * N * 4;  // 1: written directly
     pl.total = pl.at_bytes + pl.amax_bytes + pl.partial_bytes;
     return pl;
 }
@@ -959,6 +999,9 @@ void lowp_run(bool fp8, int64_t M, int64_t N, int64_t K, float alpha, const Dens
     p.k_steps = pl.k_steps; p.m_groups = pl.m_groups; p.n_groups = pl.n_groups;
     p.ks_per_group = pl.ks_per_group; p.units = pl.units; p.npad = pl.npad;
     p.partial = partial; p.amax = amax; p.err = err;
+    p.direct = pl.groups == 1;
+    p.out = out; p.os_i = os_i; p.os_j = os_j;
+    p.alpha = alpha; p.beta = beta;
     const bool fast = r_on_i && (c0 % 4) == 0;
     {
         ProfScope prof(fp8 ? "lowp_sketch_fp8_tc" : "lowp_sketch_bf16_tc", s);
@@ -970,7 +1013,7 @@ void lowp_run(bool fp8, int64_t M, int64_t N, int64_t K, float alpha, const Dens
             else launch_for<false, false>(pl, map, p, s);
         }
     }
-    {
+    if (!p.direct) {
         ProfScope prof("lowp_reduce", s);
         const int64_t work = M * N;
         const int g = (int)std::max<int64_t>(1, std::min<int64_t>((work + 255) / 256,

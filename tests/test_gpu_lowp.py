@@ -2,7 +2,9 @@
 accumulation.
 
 1. Exactness of the tensor-core mapping: the result equals an FP64 product of the same
-   rounded operands up to FP32 accumulation error (BF16: relative Frobenius <= 2e-5).  For
+   rounded operands up to FP32 accumulation error (BF16: relative Frobenius <= 2e-5; 1e-4
+   for Gaussian operators, whose entries this path computes with the hardware sine, cosine and
+   logarithm, so that a small fraction of them round to the neighbouring BF16 value).  For
    e4m3 the reference rounds each column of A after dividing by one power-of-two scale over the
    whole column, the kernel per K slice; the two differ only for entries in e4m3's subnormal
    range, so the bound is 1e-3 there -- a wrong tile layout or descriptor gives O(1) errors.
@@ -84,7 +86,8 @@ def test_lowp(rb, oracle, case, prec):
     exact = alpha * (opSm.double() @ A64) + beta * B0.double().cpu()
     r1 = float((got - exact_rounded).norm() / exact_rounded.norm())
     r2 = float((got - exact).norm() / exact.norm())
-    assert r1 <= (2e-5 if prec == "bf16" else 1e-3), (case, r1)
+    bound = 1e-3 if prec == "fp8" else (1e-4 if fam == 0 else 2e-5)
+    assert r1 <= bound, (case, r1)
     assert r2 <= (1e-2 if prec == "bf16" else 6e-2), (case, r2)
 
 
