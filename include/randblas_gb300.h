@@ -322,7 +322,11 @@ int rbg_lskge3_lowp_workspace(int32_t precision, int64_t d, int64_t n, int64_t m
  * column and per K slice of the work split, by the power-of-two scale that brings that tile's
  * largest magnitude to <= 448, and the epilogue multiplies the product back (exact).
  * workspace: device buffer of rbg_lskge3_lowp_workspace bytes, or NULL to let the call
- * allocate (stream-ordered) and free it. */
+ * allocate (stream-ordered) and free it.
+ * A and B may be device memory or host memory the GPU can read (pinned/registered memory, or
+ * any host memory where the device reports cudaDevAttrPageableMemoryAccess): the A
+ * conversion pass then reads A over the host link (no separate copy of A) and B is written in
+ * place.  Pageable memory on other systems is rejected with RBG_ERROR_INVALID_ARGUMENT. */
 int rbg_lskge3_lowp(int32_t precision, int32_t layout, int32_t opS, int32_t opA, int64_t d,
                     int64_t n, int64_t m, float alpha, const rbg_dense_skop *S, int64_t ro_s,
                     int64_t co_s, const float *A, int64_t lda, float beta, float *B,

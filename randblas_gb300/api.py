@@ -56,10 +56,22 @@ def _ptr(t: Optional[torch.Tensor]):
     return C.c_void_p(t.data_ptr())
 
 
+def _ptr_device_or_pinned(t: Optional[torch.Tensor]):
+    """A CUDA tensor, or a CPU tensor in pinned memory (for calls that read and write host
+    memory over the host link)."""
+    if t is None:
+        return None
+    if not t.is_cuda and not t.is_pinned():
+        raise RandBLASError(_lib.ERROR_INVALID_ARGUMENT,
+                            "buffers must be CUDA tensors or pinned CPU tensors")
+    return C.c_void_p(t.data_ptr())
+
+
 def set_deterministic(on: bool) -> None:
     """Process-wide reproducibility switch (no reference counterpart): when on, every path
-    adds in a fixed order; when off (default) the fused SASO sketch may vary in its last bits
-    between runs."""
+    adds in a fixed order; when off (default) the SASO shared-memory scatter (column-major data
+    or d > 2048) and entries moved out of fill_sparse's layout in a pre-filled operator may vary
+    in their last bits between runs."""
     call("rbg_set_deterministic", 1 if on else 0)
 
 

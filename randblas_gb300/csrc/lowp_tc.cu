@@ -30,6 +30,7 @@
 
 #include <algorithm>
 #include <mutex>
+#include <string>
 
 #include "rbg_internal.h"
 #include "tc_ptx.cuh"
@@ -912,15 +913,176 @@ void launch_sketch(int clusters, const CUtensorMap &map, const LowpParams &p, cu
 }
 
 template <bool kFast, bool kFp8>
-void launch_for(const Plan &pl, const CUtensorMap &map, const LowpParams &p, cudaStream_t s) {
-    const int clusters =
-        (int)std::min<int64_t>(pl.units, resident_clusters(pl.cn * pl.cm));
+void launch_for(const Plan &pl, const CUtensorMap &map, const LowpParams &p, cudaStream_t s,
+                int spare_clusters = 0) {
+    const int clusters = (int)std::max<int64_t>(
+        1, std::min<int64_t>(pl.units, resident_clusters(pl.cn * pl.cm) - spare_clusters));
     if (pl.cn == 2 && pl.cm == 2) launch_sketch<2, 2, kFast, kFp8>(clusters, map, p, s);
     else if (pl.cn == 2) launch_sketch<2, 1, kFast, kFp8>(clusters, map, p, s);
     else if (pl.cm == 2) launch_sketch<1, 2, kFast, kFp8>(clusters, map, p, s);
     else launch_sketch<1, 1, kFast, kFp8>(clusters, map, p, s);
 }
 
+
+CUtensorMap encode_at_map(const Plan &pl, const void *At) {
+    CUtensorMap map;
+    // rows of 64 bytes (bke values): row r = (k / bke) * npad + j
+    const cuuint64_t dims[2] = {(cuuint64_t)pl.bke, (cuuint64_t)pl.npad * pl.k_steps};
+    const cuuint64_t strides[1] = {(cuuint64_t)ROW_BYTES};
+    const cuuint32_t box[2] = {(cuuint32_t)pl.bke, (cuuint32_t)(BN / 2)};
+    const cuuint32_t estr[2] = {1, 1};
+    const CUresult cr = tc::tensor_map_encoder()(
+        &map, pl.fp8 ? CU_TENSOR_MAP_DATA_TYPE_UINT8 : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2,
+        const_cast<void *>(At), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+        CU_TENSOR_MAP_SWIZZLE_64B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+        CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (cr != CUDA_SUCCESS) fail(RBG_ERROR_CUDA, "cuTensorMapEncodeTiled failed");
+    return map;
+}
+
+// BF16 with A in pinned host memory: K is cut into chunks of kStreamChunk rows of op(A), and
+// three streams overlap: the copy engine brings chunk c + 1 into one of two FP32 staging
+// buffers (cudaMemcpy2DAsync: op(A) row- or column-contiguous) while a small grid converts
+// chunk c to BF16 and the tensor cores sketch chunk c - 1 on a grid that leaves SMs free for
+// the conversion.  Chunk c adds into B (beta for the first chunk, 1 after) with its operator
+// columns (or rows) offset by c * kStreamChunk.  The host link then sets the time, instead
+// of the sum of the transfer and the sketch.
+constexpr int64_t kStreamChunk = 1 << 16;
+constexpr int kStreamConvertCtas = 32;
+constexpr int kStreamSpareClusters = 2;
+
+bool lowp_streams(bool fp8, int64_t K, const void *A, const Strided &Q, const void *workspace) {
+    if (fp8 || workspace || K < 4 * kStreamChunk || (Q.s1 != 1 && Q.s0 != 1)) return false;
+    cudaPointerAttributes pa{};
+    if (cudaPointerGetAttributes(&pa, A) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return pa.type == cudaMemoryTypeHost;  // pinned (the copy engine reads it at full rate)
+}
+
+cudaStream_t stream_once(int which) {
+    static cudaStream_t st[2] = {nullptr, nullptr};
+    static std::once_flag once;
+    std::call_once(once, [] {
+        for (auto &x : st)
+            if (cudaStreamCreateWithFlags(&x, cudaStreamNonBlocking) != cudaSuccess) {
+                cudaGetLastError();
+                x = nullptr;
+            }
+    });
+    if (!st[which]) fail(RBG_ERROR_CUDA, "could not create the streaming streams");
+    return st[which];
+}
+
+void lowp_run_streamed(int64_t M, int64_t N, int64_t K, float alpha, const DenseGen &gen,
+                       int64_t r0, int64_t c0, int r_on_i, const Strided &Q, bool a_bf16,
+                       float beta, float *out, int64_t os_i, int64_t os_j, cudaStream_t s) {
+    const cudaStream_t cps = stream_once(0), cvs = stream_once(1);
+    const int64_t nch = (K + kStreamChunk - 1) / kStreamChunk;
+    const Plan pc = make_plan(M, N, kStreamChunk, false);
+    const Plan pt = make_plan(M, N, K - (nch - 1) * kStreamChunk, false);  // last chunk
+    const size_t esz = a_bf16 ? 2 : 4;
+    const size_t stage_b = ((size_t)kStreamChunk * N * esz + 1023) / 1024 * 1024;
+    const size_t at_b = std::max(pc.at_bytes, pt.at_bytes);
+    const size_t part_b = std::max(pc.partial_bytes, pt.partial_bytes);
+    Scratch buf(2 * stage_b + 2 * at_b + part_b + 1024, s);
+    uint8_t *base = reinterpret_cast<uint8_t *>(
+        (reinterpret_cast<uintptr_t>(buf.ptr) + 1023) & ~uintptr_t(1023));
+    uint8_t *Af[2] = {base, base + stage_b};
+    uint8_t *At[2] = {base + 2 * stage_b, base + 2 * stage_b + at_b};
+    float *partial = reinterpret_cast<float *>(base + 2 * stage_b + 2 * at_b);
+    cudaEvent_t ready, copied[2], converted[2], used[2];
+    RBG_CUDA(cudaEventCreateWithFlags(&ready, cudaEventDisableTiming));
+    for (int q = 0; q < 2; ++q) {
+        RBG_CUDA(cudaEventCreateWithFlags(&copied[q], cudaEventDisableTiming));
+        RBG_CUDA(cudaEventCreateWithFlags(&converted[q], cudaEventDisableTiming));
+        RBG_CUDA(cudaEventCreateWithFlags(&used[q], cudaEventDisableTiming));
+    }
+    RBG_CUDA(cudaEventRecord(ready, s));  // the staging memory and earlier work on s
+    RBG_CUDA(cudaStreamWaitEvent(cps, ready, 0));
+    RBG_CUDA(cudaStreamWaitEvent(cvs, ready, 0));
+    int *err = tc::wait_error_flag();
+    const bool rows = Q.s1 == 1;  // op(A) rows contiguous (else columns)
+    for (int64_t c = 0; c < nch; ++c) {
+        const int b = (int)(c & 1);
+        const Plan &pl = c + 1 < nch ? pc : pt;
+        const int64_t k0 = c * kStreamChunk, kc = std::min(kStreamChunk, K - k0);
+        // 1. copy engine: chunk -> Af[b] (free once chunk c - 2 is converted)
+        if (c >= 2) RBG_CUDA(cudaStreamWaitEvent(cps, converted[b], 0));
+        const uint8_t *src = static_cast<const uint8_t *>(Q.ptr) + (size_t)k0 * Q.s0 * esz;
+        Strided q_dev;
+        q_dev.ptr = Af[b];
+        if (rows) {  // [kc][N], rows of op(A) at pitch s0
+            RBG_CUDA(cudaMemcpy2DAsync(Af[b], (size_t)N * esz, src, (size_t)Q.s0 * esz,
+                                       (size_t)N * esz, (size_t)kc, cudaMemcpyHostToDevice,
+                                       cps));
+            q_dev.s0 = N;
+            q_dev.s1 = 1;
+        } else {     // [N][kc], columns of op(A) at pitch s1
+            RBG_CUDA(cudaMemcpy2DAsync(Af[b], (size_t)kc * esz, src, (size_t)Q.s1 * esz,
+                                       (size_t)kc * esz, (size_t)N, cudaMemcpyHostToDevice,
+                                       cps));
+            q_dev.s0 = 1;
+            q_dev.s1 = kc;
+        }
+        RBG_CUDA(cudaEventRecord(copied[b], cps));
+        // 2. convert Af[b] -> At[b] (free once chunk c - 2 is sketched)
+        RBG_CUDA(cudaStreamWaitEvent(cvs, copied[b], 0));
+        if (c >= 2) RBG_CUDA(cudaStreamWaitEvent(cvs, used[b], 0));
+        {
+            ProfScope prof("lowp_convert_a", cvs);
+            if (a_bf16)
+                convert_a_kernel<<<kStreamConvertCtas, 256, 0, cvs>>>(
+                    static_cast<const __nv_bfloat16 *>(q_dev.ptr), q_dev.s0, q_dev.s1, kc, N,
+                    pl.kpad, pl.npad, reinterpret_cast<__nv_bfloat16 *>(At[b]));
+            else
+                convert_a_kernel<<<kStreamConvertCtas, 256, 0, cvs>>>(
+                    static_cast<const float *>(q_dev.ptr), q_dev.s0, q_dev.s1, kc, N, pl.kpad,
+                    pl.npad, reinterpret_cast<__nv_bfloat16 *>(At[b]));
+            RBG_LAUNCHED();
+        }
+        RBG_CUDA(cudaEventRecord(converted[b], cvs));
+        // 3. sketch the chunk
+        RBG_CUDA(cudaStreamWaitEvent(s, converted[b], 0));
+        const CUtensorMap map = encode_at_map(pl, At[b]);
+        LowpParams p{};
+        p.M = M; p.N = N; p.K = kc;
+        p.gen = gen;
+        p.r0 = r_on_i ? r0 : r0 + k0;
+        p.c0 = r_on_i ? c0 + k0 : c0;
+        p.r_on_i = r_on_i;
+        p.k_steps = pl.k_steps; p.m_groups = pl.m_groups; p.n_groups = pl.n_groups;
+        p.ks_per_group = pl.ks_per_group; p.units = pl.units; p.npad = pl.npad;
+        p.partial = partial; p.amax = nullptr; p.err = err;
+        p.direct = pl.groups == 1;
+        p.out = out; p.os_i = os_i; p.os_j = os_j;
+        p.alpha = alpha; p.beta = c == 0 ? beta : 1.f;
+        {
+            ProfScope prof("lowp_sketch_bf16_tc", s);
+            if (r_on_i && (p.c0 % 4) == 0)
+                launch_for<true, false>(pl, map, p, s, kStreamSpareClusters);
+            else
+                launch_for<false, false>(pl, map, p, s, kStreamSpareClusters);
+        }
+        RBG_CUDA(cudaEventRecord(used[b], s));
+        if (!p.direct) {
+            ProfScope prof("lowp_reduce", s);
+            const int64_t work = M * N;
+            const int g = (int)std::max<int64_t>(
+                1, std::min<int64_t>((work + 255) / 256, (int64_t)num_sms() * 16));
+            lowp_reduce_kernel<<<g, 256, 0, s>>>(M, N, pl.groups, partial, alpha, p.beta, out,
+                                                 os_i, os_j);
+            RBG_LAUNCHED();
+        }
+    }
+    RBG_CUDA(cudaEventDestroy(ready));
+    for (int q = 0; q < 2; ++q) {
+        RBG_CUDA(cudaEventDestroy(copied[q]));
+        RBG_CUDA(cudaEventDestroy(converted[q]));
+        RBG_CUDA(cudaEventDestroy(used[q]));
+    }
+}
 
 void lowp_run(bool fp8, int64_t M, int64_t N, int64_t K, float alpha, const DenseGen &gen,
               int64_t r0, int64_t c0, int r_on_i, const Strided &Q, bool a_bf16, float beta,
@@ -980,17 +1142,7 @@ void lowp_run(bool fp8, int64_t M, int64_t N, int64_t K, float alpha, const Dens
         RBG_LAUNCHED();
     }
 
-    CUtensorMap map;
-    // rows of 64 bytes (bke values): row r = (k / bke) * npad + j
-    const cuuint64_t dims[2] = {(cuuint64_t)pl.bke, (cuuint64_t)pl.npad * pl.k_steps};
-    const cuuint64_t strides[1] = {(cuuint64_t)ROW_BYTES};
-    const cuuint32_t box[2] = {(cuuint32_t)pl.bke, (cuuint32_t)(BN / 2)};
-    const cuuint32_t estr[2] = {1, 1};
-    const CUresult cr = tc::tensor_map_encoder()(
-        &map, fp8 ? CU_TENSOR_MAP_DATA_TYPE_UINT8 : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, At, dims,
-        strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B,
-        CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-    if (cr != CUDA_SUCCESS) fail(RBG_ERROR_CUDA, "cuTensorMapEncodeTiled failed");
+    const CUtensorMap map = encode_at_map(pl, At);
 
     int *err = tc::wait_error_flag();
     LowpParams p{};
@@ -1091,6 +1243,24 @@ extern "C" int rbg_lowp_status(int32_t *code) {
 }
 
 namespace {
+// Device memory, pinned (registered) host memory, or -- on systems where the GPU can access
+// pageable memory (address translation over the host link) -- any host memory.
+void require_gpu_accessible(const void *p, const char *name) {
+    cudaPointerAttributes pa{};
+    if (cudaPointerGetAttributes(&pa, p) != cudaSuccess) {
+        cudaGetLastError();
+        return;
+    }
+    if (pa.type != cudaMemoryTypeUnregistered) return;
+    int dev = 0, pageable = 0;
+    RBG_CUDA(cudaGetDevice(&dev));
+    RBG_CUDA(cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, dev));
+    if (!pageable)
+        fail(RBG_ERROR_INVALID_ARGUMENT,
+             std::string(name) + " is pageable host memory, which this GPU cannot read; pin it "
+                                 "(cudaHostRegister / cudaMallocHost) or pass device memory");
+}
+
 int lowp_entry(int32_t precision, int32_t a_dtype, int32_t layout, int32_t opS, int32_t opA,
                int64_t d, int64_t n, int64_t m, float alpha, const rbg_dense_skop *S,
                int64_t ro_s, int64_t co_s, const void *A, int64_t lda, float beta, float *B,
@@ -1133,6 +1303,10 @@ int lowp_entry(int32_t precision, int32_t a_dtype, int32_t layout, int32_t opS, 
             return;
         }
         if (!A) fail(RBG_ERROR_INVALID_ARGUMENT, "A must not be NULL");
+        // A and B may live in host memory the GPU can read: the A conversion pass then reads
+        // A over the host link, and B is written in place
+        require_gpu_accessible(A, "A");
+        require_gpu_accessible(B, "B");
         if ((double)((m + 31) / 32) * (double)((n + BN - 1) / BN * BN) > (double)INT32_MAX)
             fail(RBG_ERROR_UNSUPPORTED, "dimensions too large for 32-bit TMA coordinates");
         const int64_t ars = layout == RBG_COL_MAJOR ? 1 : lda;
@@ -1152,9 +1326,14 @@ int lowp_entry(int32_t precision, int32_t a_dtype, int32_t layout, int32_t opS, 
             r0 = co_s;
             c0 = ro_s;
         }
-        lowp_run(precision == RBG_PREC_FP8_E4M3, d, n, m, alpha,
-                 make_dense_gen(S->dist, S->seed_state), r0, c0, r_on_i, Q, a_dtype == RBG_BF16,
-                 beta, B, brs, bcs, workspace, workspace_bytes, s);
+        const bool fp8 = precision == RBG_PREC_FP8_E4M3;
+        if (lowp_streams(fp8, m, A, Q, workspace))
+            lowp_run_streamed(d, n, m, alpha, make_dense_gen(S->dist, S->seed_state), r0, c0,
+                              r_on_i, Q, a_dtype == RBG_BF16, beta, B, brs, bcs, s);
+        else
+            lowp_run(fp8, d, n, m, alpha, make_dense_gen(S->dist, S->seed_state), r0, c0,
+                     r_on_i, Q, a_dtype == RBG_BF16, beta, B, brs, bcs, workspace,
+                     workspace_bytes, s);
     });
 }
 }  // namespace

@@ -10,7 +10,7 @@ import torch
 
 from . import _lib
 from ._lib import call
-from .api import DenseSkOp, Layout, Op, _ptr, _stream
+from .api import DenseSkOp, Layout, Op, _ptr, _ptr_device_or_pinned, _stream
 
 BF16 = _lib.PREC_BF16
 FP8_E4M3 = _lib.PREC_FP8_E4M3
@@ -33,7 +33,9 @@ def sketch_lowp(layout: Layout, opS: Op, opA: Op, d: int, n: int, m: int, alpha:
                 B: torch.Tensor, ldb: int, precision: int = BF16,
                 workspace: torch.Tensor | None = None) -> None:
     """B = alpha * op(submat(S)) * op(A) + beta * B on the tensor cores.  A is FP32 or BF16
-    (BF16 data enters the tensor cores unchanged); B is FP32."""
+    (BF16 data enters the tensor cores unchanged); B is FP32.  A and B may be CUDA tensors or
+    pinned CPU tensors (A is then read over the host link by the conversion pass, B written in
+    place)."""
     ws = _ptr(workspace) if workspace is not None else None
     wbytes = workspace.numel() * workspace.element_size() if workspace is not None else 0
     a_dtype = {torch.float32: _lib.F32, torch.bfloat16: _lib.BF16}.get(A.dtype)
@@ -41,7 +43,8 @@ def sketch_lowp(layout: Layout, opS: Op, opA: Op, d: int, n: int, m: int, alpha:
         raise _lib.RandBLASError(_lib.ERROR_INVALID_ARGUMENT,
                                  "the precision path takes FP32 or BF16 A")
     call("rbg_lskge3_lowp_ex", precision, a_dtype, int(layout), int(opS), int(opA), d, n, m,
-         float(alpha), C.byref(S._c()), ro_s, co_s, _ptr(A), lda, float(beta), _ptr(B), ldb, ws,
+         float(alpha), C.byref(S._c()), ro_s, co_s, _ptr_device_or_pinned(A), lda,
+         float(beta), _ptr_device_or_pinned(B), ldb, ws,
          wbytes, _stream())
 
 

@@ -115,3 +115,63 @@ def test_lowp_workspace_and_errors(rb):
         lowp.sketch_lowp(rb.Layout.RowMajor, rb.Op.NoTrans, rb.Op.NoTrans, 256, 64, 4096, 1.0, S,
                          0, 0, A, 64, 0.0, B1, 64, workspace=ws_al[:need - 1024])
     assert lowp.status() == 0
+
+
+@pytest.mark.parametrize("prec", ["bf16", "fp8"])
+def test_lowp_host_buffers(rb, prec):
+    """A and B in pinned host memory, passed to the call itself (the A conversion pass reads A
+    over the host link, B is written in place): the same bits as with device buffers."""
+    import torch
+    from randblas_gb300 import lowp
+    d, n, m = 256, 192, 9000
+    S = rb.DenseSkOp(rb.DenseDist(d, m, rb.ScalarDist.Gaussian), rb.RNGState(12))
+    g = torch.Generator(device="cuda").manual_seed(4)
+    A = torch.randn(m, n, device="cuda", generator=g)
+    B0 = torch.randn(d, n, device="cuda", generator=g)
+    precision = lowp.BF16 if prec == "bf16" else lowp.FP8_E4M3
+    B_dev = B0.clone()
+    lowp.sketch_lowp(rb.Layout.RowMajor, rb.Op.NoTrans, rb.Op.NoTrans, d, n, m, 0.5, S, 0, 0, A,
+                     n, 0.25, B_dev, n, precision=precision)
+    A_host = A.cpu().pin_memory()
+    B_host = B0.cpu().pin_memory()
+    lowp.sketch_lowp(rb.Layout.RowMajor, rb.Op.NoTrans, rb.Op.NoTrans, d, n, m, 0.5, S, 0, 0,
+                     A_host, n, 0.25, B_host, n, precision=precision)
+    torch.cuda.synchronize()
+    assert lowp.status() == 0
+    assert torch.equal(B_host, B_dev.cpu())
+
+
+@pytest.mark.parametrize("axis", ["Long", "Short"])
+def test_lowp_host_a_streamed(rb, axis):
+    """BF16 with A in pinned host memory and K of five 2^16-row chunks (the last one partial):
+    the call converts chunk c on a side stream while it sketches chunk c - 1, adding the
+    chunks into B.  The rounded operands are the same as with device buffers; only the K
+    slices over which the tensor cores accumulate in FP32 differ, so the two results agree
+    within the path's FP32-accumulation bound (2e-5 relative Frobenius, as against an FP64
+    product of the rounded operands).  Both operator orientations (the chunk offset moves the
+    operator's columns or its rows)."""
+    import torch
+    from randblas_gb300 import lowp
+    d, n, m = 200, 96, 300000
+    S = rb.DenseSkOp(rb.DenseDist(d, m, rb.ScalarDist.Gaussian, getattr(rb.Axis, axis)),
+                     rb.RNGState(13))
+    g = torch.Generator(device="cuda").manual_seed(6)
+    A = torch.randn(m, n, device="cuda", generator=g)
+    B0 = torch.randn(d, n, device="cuda", generator=g)
+    B_dev = B0.clone()
+    lowp.sketch_lowp(rb.Layout.RowMajor, rb.Op.NoTrans, rb.Op.NoTrans, d, n, m, 0.5, S, 0, 0, A,
+                     n, 0.25, B_dev, n)
+    A_host = A.cpu().pin_memory()
+    B_str = B0.clone()
+    rb.profile.enable(True)
+    try:
+        lowp.sketch_lowp(rb.Layout.RowMajor, rb.Op.NoTrans, rb.Op.NoTrans, d, n, m, 0.5, S, 0, 0,
+                         A_host, n, 0.25, B_str, n)
+        torch.cuda.synchronize()
+        launches = rb.profile.read()["lowp_sketch_bf16_tc"]["launches"]
+    finally:
+        rb.profile.enable(False)
+    assert lowp.status() == 0
+    assert launches == 5, launches
+    rel = float((B_str.double() - B_dev.double()).norm() / B_dev.double().norm())
+    assert rel <= 2e-5, rel
