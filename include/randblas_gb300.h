@@ -324,9 +324,12 @@ int rbg_lskge3_lowp_workspace(int32_t precision, int64_t d, int64_t n, int64_t m
  * workspace: device buffer of rbg_lskge3_lowp_workspace bytes, or NULL to let the call
  * allocate (stream-ordered) and free it.
  * A and B may be device memory or host memory the GPU can read (pinned/registered memory, or
- * any host memory where the device reports cudaDevAttrPageableMemoryAccess): the A
- * conversion pass then reads A over the host link (no separate copy of A) and B is written in
- * place.  Pageable memory on other systems is rejected with RBG_ERROR_INVALID_ARGUMENT. */
+ * any host memory where the device reports cudaDevAttrPageableMemoryAccess); B is then written
+ * in place.  For BF16 with pinned A, K >= 2^18, op(A) row- or column-contiguous and no
+ * workspace given, the call streams A: 2^16-row chunks are copied by the copy engine, converted
+ * and sketched on three streams, so the transfer and the sketch overlap.  Otherwise the
+ * conversion pass reads A over the host link.  Pageable memory on systems without that access
+ * is rejected with RBG_ERROR_INVALID_ARGUMENT. */
 int rbg_lskge3_lowp(int32_t precision, int32_t layout, int32_t opS, int32_t opA, int64_t d,
                     int64_t n, int64_t m, float alpha, const rbg_dense_skop *S, int64_t ro_s,
                     int64_t co_s, const float *A, int64_t lda, float beta, float *B,
