@@ -913,10 +913,9 @@ void launch_sketch(int clusters, const CUtensorMap &map, const LowpParams &p, cu
 }
 
 template <bool kFast, bool kFp8>
-void launch_for(const Plan &pl, const CUtensorMap &map, const LowpParams &p, cudaStream_t s,
-                int spare_clusters = 0) {
-    const int clusters = (int)std::max<int64_t>(
-        1, std::min<int64_t>(pl.units, resident_clusters(pl.cn * pl.cm) - spare_clusters));
+void launch_for(const Plan &pl, const CUtensorMap &map, const LowpParams &p, cudaStream_t s) {
+    const int clusters =
+        (int)std::min<int64_t>(pl.units, resident_clusters(pl.cn * pl.cm));
     if (pl.cn == 2 && pl.cm == 2) launch_sketch<2, 2, kFast, kFp8>(clusters, map, p, s);
     else if (pl.cn == 2) launch_sketch<2, 1, kFast, kFp8>(clusters, map, p, s);
     else if (pl.cm == 2) launch_sketch<1, 2, kFast, kFp8>(clusters, map, p, s);
@@ -940,16 +939,18 @@ CUtensorMap encode_at_map(const Plan &pl, const void *At) {
     return map;
 }
 
-// BF16 with A in pinned host memory: K is cut into chunks of kStreamChunk rows of op(A), and
-// three streams overlap: the copy engine brings chunk c + 1 into one of two FP32 staging
-// buffers (cudaMemcpy2DAsync: op(A) row- or column-contiguous) while a small grid converts
-// chunk c to BF16 and the tensor cores sketch chunk c - 1 on a grid that leaves SMs free for
-// the conversion.  Chunk c adds into B (beta for the first chunk, 1 after) with its operator
-// columns (or rows) offset by c * kStreamChunk.  The host link then sets the time, instead
-// of the sum of the transfer and the sketch.
-constexpr int64_t kStreamChunk = 1 << 16;
-constexpr int kStreamConvertCtas = 32;
-constexpr int kStreamSpareClusters = 2;
+// BF16 with A in pinned host memory: K is cut into chunks of kStreamChunk rows of op(A).  The
+// copy engine brings chunk c + 1 into one of two FP32 staging buffers (cudaMemcpy2DAsync:
+// op(A) row- or column-contiguous) on its own stream while the main stream converts chunk c to
+// BF16 (full grid, from HBM) and sketches it on the tensor cores (all clusters).  Chunk c adds
+// into B (beta for the first chunk, 1 after) with its operator columns (or rows) offset by
+// c * kStreamChunk.  The host link then sets the time instead of the sum of the transfer and
+// the sketch.  (Converting beside the sketch instead, on a small grid, made the sketch's
+// clusters wait for SMs and the whole step 30-50 % slower and erratic.)
+#ifndef RBG_STREAM_CHUNK_LOG2
+#define RBG_STREAM_CHUNK_LOG2 16
+#endif
+constexpr int64_t kStreamChunk = 1ll << RBG_STREAM_CHUNK_LOG2;
 
 bool lowp_streams(bool fp8, int64_t K, const void *A, const Strided &Q, const void *workspace) {
     if (fp8 || workspace || K < 4 * kStreamChunk || (Q.s1 != 1 && Q.s0 != 1)) return false;
@@ -961,24 +962,24 @@ bool lowp_streams(bool fp8, int64_t K, const void *A, const Strided &Q, const vo
     return pa.type == cudaMemoryTypeHost;  // pinned (the copy engine reads it at full rate)
 }
 
-cudaStream_t stream_once(int which) {
-    static cudaStream_t st[2] = {nullptr, nullptr};
+cudaStream_t copy_stream() {
+    static cudaStream_t st = nullptr;
     static std::once_flag once;
     std::call_once(once, [] {
-        for (auto &x : st)
-            if (cudaStreamCreateWithFlags(&x, cudaStreamNonBlocking) != cudaSuccess) {
-                cudaGetLastError();
-                x = nullptr;
-            }
+        if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess) {
+            cudaGetLastError();
+            st = nullptr;
+        }
     });
-    if (!st[which]) fail(RBG_ERROR_CUDA, "could not create the streaming streams");
-    return st[which];
+    if (!st) fail(RBG_ERROR_CUDA, "could not create the copy stream");
+    return st;
 }
 
 void lowp_run_streamed(int64_t M, int64_t N, int64_t K, float alpha, const DenseGen &gen,
                        int64_t r0, int64_t c0, int r_on_i, const Strided &Q, bool a_bf16,
                        float beta, float *out, int64_t os_i, int64_t os_j, cudaStream_t s) {
-    const cudaStream_t cps = stream_once(0), cvs = stream_once(1);
+    const cudaStream_t cps = copy_stream();
+    const int sms = num_sms();
     const int64_t nch = (K + kStreamChunk - 1) / kStreamChunk;
     const Plan pc = make_plan(M, N, kStreamChunk, false);
     const Plan pt = make_plan(M, N, K - (nch - 1) * kStreamChunk, false);  // last chunk
@@ -986,29 +987,26 @@ void lowp_run_streamed(int64_t M, int64_t N, int64_t K, float alpha, const Dense
     const size_t stage_b = ((size_t)kStreamChunk * N * esz + 1023) / 1024 * 1024;
     const size_t at_b = std::max(pc.at_bytes, pt.at_bytes);
     const size_t part_b = std::max(pc.partial_bytes, pt.partial_bytes);
-    Scratch buf(2 * stage_b + 2 * at_b + part_b + 1024, s);
+    Scratch buf(2 * stage_b + at_b + part_b + 1024, s);
     uint8_t *base = reinterpret_cast<uint8_t *>(
         (reinterpret_cast<uintptr_t>(buf.ptr) + 1023) & ~uintptr_t(1023));
     uint8_t *Af[2] = {base, base + stage_b};
-    uint8_t *At[2] = {base + 2 * stage_b, base + 2 * stage_b + at_b};
-    float *partial = reinterpret_cast<float *>(base + 2 * stage_b + 2 * at_b);
-    cudaEvent_t ready, copied[2], converted[2], used[2];
+    uint8_t *At = base + 2 * stage_b;
+    float *partial = reinterpret_cast<float *>(base + 2 * stage_b + at_b);
+    cudaEvent_t ready, copied[2], converted[2];
     RBG_CUDA(cudaEventCreateWithFlags(&ready, cudaEventDisableTiming));
     for (int q = 0; q < 2; ++q) {
         RBG_CUDA(cudaEventCreateWithFlags(&copied[q], cudaEventDisableTiming));
         RBG_CUDA(cudaEventCreateWithFlags(&converted[q], cudaEventDisableTiming));
-        RBG_CUDA(cudaEventCreateWithFlags(&used[q], cudaEventDisableTiming));
     }
     RBG_CUDA(cudaEventRecord(ready, s));  // the staging memory and earlier work on s
     RBG_CUDA(cudaStreamWaitEvent(cps, ready, 0));
-    RBG_CUDA(cudaStreamWaitEvent(cvs, ready, 0));
     int *err = tc::wait_error_flag();
     const bool rows = Q.s1 == 1;  // op(A) rows contiguous (else columns)
-    for (int64_t c = 0; c < nch; ++c) {
+    auto copy_chunk = [&](int64_t c) -> Strided {
         const int b = (int)(c & 1);
-        const Plan &pl = c + 1 < nch ? pc : pt;
         const int64_t k0 = c * kStreamChunk, kc = std::min(kStreamChunk, K - k0);
-        // 1. copy engine: chunk -> Af[b] (free once chunk c - 2 is converted)
+        // Af[b] is free once chunk c - 2 has been converted
         if (c >= 2) RBG_CUDA(cudaStreamWaitEvent(cps, converted[b], 0));
         const uint8_t *src = static_cast<const uint8_t *>(Q.ptr) + (size_t)k0 * Q.s0 * esz;
         Strided q_dev;
@@ -1027,25 +1025,30 @@ void lowp_run_streamed(int64_t M, int64_t N, int64_t K, float alpha, const Dense
             q_dev.s1 = kc;
         }
         RBG_CUDA(cudaEventRecord(copied[b], cps));
-        // 2. convert Af[b] -> At[b] (free once chunk c - 2 is sketched)
-        RBG_CUDA(cudaStreamWaitEvent(cvs, copied[b], 0));
-        if (c >= 2) RBG_CUDA(cudaStreamWaitEvent(cvs, used[b], 0));
+        return q_dev;
+    };
+    Strided q_next = copy_chunk(0);
+    for (int64_t c = 0; c < nch; ++c) {
+        const int b = (int)(c & 1);
+        const Plan &pl = c + 1 < nch ? pc : pt;
+        const int64_t k0 = c * kStreamChunk, kc = std::min(kStreamChunk, K - k0);
+        const Strided q_dev = q_next;
+        if (c + 1 < nch) q_next = copy_chunk(c + 1);  // in flight during this chunk's work
+        RBG_CUDA(cudaStreamWaitEvent(s, copied[b], 0));
         {
-            ProfScope prof("lowp_convert_a", cvs);
+            ProfScope prof("lowp_convert_a", s);
             if (a_bf16)
-                convert_a_kernel<<<kStreamConvertCtas, 256, 0, cvs>>>(
+                convert_a_kernel<<<sms * 8, 256, 0, s>>>(
                     static_cast<const __nv_bfloat16 *>(q_dev.ptr), q_dev.s0, q_dev.s1, kc, N,
-                    pl.kpad, pl.npad, reinterpret_cast<__nv_bfloat16 *>(At[b]));
+                    pl.kpad, pl.npad, reinterpret_cast<__nv_bfloat16 *>(At));
             else
-                convert_a_kernel<<<kStreamConvertCtas, 256, 0, cvs>>>(
+                convert_a_kernel<<<sms * 8, 256, 0, s>>>(
                     static_cast<const float *>(q_dev.ptr), q_dev.s0, q_dev.s1, kc, N, pl.kpad,
-                    pl.npad, reinterpret_cast<__nv_bfloat16 *>(At[b]));
+                    pl.npad, reinterpret_cast<__nv_bfloat16 *>(At));
             RBG_LAUNCHED();
         }
-        RBG_CUDA(cudaEventRecord(converted[b], cvs));
-        // 3. sketch the chunk
-        RBG_CUDA(cudaStreamWaitEvent(s, converted[b], 0));
-        const CUtensorMap map = encode_at_map(pl, At[b]);
+        RBG_CUDA(cudaEventRecord(converted[b], s));
+        const CUtensorMap map = encode_at_map(pl, At);
         LowpParams p{};
         p.M = M; p.N = N; p.K = kc;
         p.gen = gen;
@@ -1060,17 +1063,14 @@ void lowp_run_streamed(int64_t M, int64_t N, int64_t K, float alpha, const Dense
         p.alpha = alpha; p.beta = c == 0 ? beta : 1.f;
         {
             ProfScope prof("lowp_sketch_bf16_tc", s);
-            if (r_on_i && (p.c0 % 4) == 0)
-                launch_for<true, false>(pl, map, p, s, kStreamSpareClusters);
-            else
-                launch_for<false, false>(pl, map, p, s, kStreamSpareClusters);
+            if (r_on_i && (p.c0 % 4) == 0) launch_for<true, false>(pl, map, p, s);
+            else launch_for<false, false>(pl, map, p, s);
         }
-        RBG_CUDA(cudaEventRecord(used[b], s));
         if (!p.direct) {
             ProfScope prof("lowp_reduce", s);
             const int64_t work = M * N;
             const int g = (int)std::max<int64_t>(
-                1, std::min<int64_t>((work + 255) / 256, (int64_t)num_sms() * 16));
+                1, std::min<int64_t>((work + 255) / 256, (int64_t)sms * 16));
             lowp_reduce_kernel<<<g, 256, 0, s>>>(M, N, pl.groups, partial, alpha, p.beta, out,
                                                  os_i, os_j);
             RBG_LAUNCHED();
@@ -1080,7 +1080,6 @@ void lowp_run_streamed(int64_t M, int64_t N, int64_t K, float alpha, const Dense
     for (int q = 0; q < 2; ++q) {
         RBG_CUDA(cudaEventDestroy(copied[q]));
         RBG_CUDA(cudaEventDestroy(converted[q]));
-        RBG_CUDA(cudaEventDestroy(used[q]));
     }
 }
 
