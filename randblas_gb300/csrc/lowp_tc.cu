@@ -947,10 +947,7 @@ CUtensorMap encode_at_map(const Plan &pl, const void *At) {
 // c * kStreamChunk.  The host link then sets the time instead of the sum of the transfer and
 // the sketch.  (Converting beside the sketch instead, on a small grid, made the sketch's
 // clusters wait for SMs and the whole step 30-50 % slower and erratic.)
-#ifndef RBG_STREAM_CHUNK_LOG2
-#define RBG_STREAM_CHUNK_LOG2 16
-#endif
-constexpr int64_t kStreamChunk = 1ll << RBG_STREAM_CHUNK_LOG2;
+constexpr int64_t kStreamChunk = 1 << 16;
 
 bool lowp_streams(bool fp8, int64_t K, const void *A, const Strided &Q, const void *workspace) {
     if (fp8 || workspace || K < 4 * kStreamChunk || (Q.s1 != 1 && Q.s0 != 1)) return false;
