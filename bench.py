@@ -478,9 +478,9 @@ def bench_saso(torch, rb, device, args, stream, hbm):
 def bench_more_rows(torch, rb, device, stream, hbm):
     """Rows of the hot path outside the five configurations, each timed alone with CUDA events:
     fill_sparse of the cfg2 SASO operator, the cfg2 sketch with that operator pre-filled (its
-    COO arrays read from HBM), sketch_vector with the 4096 x 2^20 uniform operator, and
-    sketch_sparse of a Gaussian 1024 x 2^17 operator against a 2^17 x 512 CSR matrix with
-    5 nonzeros per row (seeded)."""
+    COO arrays read from HBM), sketch_vector with the 4096 x 2^20 uniform operator,
+    random_csr of a 2^17 x 512 matrix with 5 expected nonzeros per row, and sketch_sparse of a
+    Gaussian 1024 x 2^17 operator against that matrix."""
     out = {}
     m, d, n, k = SASO_M, SASO_D, SASO_N, SASO_K
     A = torch.empty(m * n, dtype=torch.float32, device=device)
@@ -530,19 +530,24 @@ def bench_more_rows(torch, rb, device, stream, hbm):
     del x, y
 
     ds, ms_, ns, per_row = 1024, 1 << 17, 512, 5
-    rowptr = torch.arange(0, ms_ * per_row + 1, per_row, dtype=torch.int64, device=device)
-    cols = torch.randint(0, ns, (ms_ * per_row,), dtype=torch.int64, device=device, generator=g)
-    vals = torch.randn(ms_ * per_row, device=device, generator=g)
-    Acsr = rb.CSRMatrix(ms_, ns, vals, rowptr, cols)
+    gen = lambda: rb.random_csr(ms_, ns, per_row / ns, rb.RNGState(11), dtype=torch.float32)
+    ms = event_time(torch, gen, 5, 2, stream)
+    Acsr, _ = gen()
+    nnz_csr = Acsr.vals.numel()
+    out["random_csr"] = {
+        "workload": "random_csr(2^17, 512, density 5/512, RNGState(11)): FP32 values, int64 "
+                    "indices, structure drawn on the GPU, nnz read back, arrays written",
+        "ms": round(ms, 4), "nnz": nnz_csr,
+        "M_nonzeros/s": round(nnz_csr / (ms * 1e-3) / 1e6, 1)}
     Sg = rb.DenseSkOp(rb.DenseDist(ds, ms_, rb.ScalarDist.Gaussian), rb.RNGState(5))
     Bs = torch.empty(ds * ns, device=device)
     ms = event_time(torch, lambda: rb.sketch_sparse(rb.Layout.RowMajor, rb.Op.NoTrans,
                                                     rb.Op.NoTrans, ds, ns, ms_, 1.0, Sg, 0, 0,
                                                     Acsr, 0.0, Bs, ns), 5, 2, stream)
     out["sketch_sparse"] = {
-        "workload": "Gaussian 1024 x 2^17 operator (RNGState(5)) times a 2^17 x 512 CSR matrix, "
-                    "5 nonzeros per row; the operator is materialised as in the reference",
-        "ms": round(ms, 4), "GFLOP/s": round(2.0 * ds * ms_ * per_row / (ms * 1e-3) / 1e9, 1)}
+        "workload": "Gaussian 1024 x 2^17 operator (RNGState(5)) times that 2^17 x 512 CSR "
+                    "matrix; the operator is materialised as in the reference",
+        "ms": round(ms, 4), "GFLOP/s": round(2.0 * ds * nnz_csr / (ms * 1e-3) / 1e9, 1)}
     return out
 
 

@@ -205,6 +205,37 @@ int rbg_fill_sparse(rbg_sparse_skop *S, rbg_stream_t stream);
 int rbg_repeated_fisher_yates(int64_t k, int64_t n, int64_t r, int64_t *samples,
                               const rbg_state *seed, rbg_state *next, rbg_stream_t stream);
 
+/* ------------------------------------------------------------------ random sparse matrices */
+
+/* random_coo / random_csr / random_csc (RandBLAS/sparse_data/random_matrix.hh:135-355): an
+ * m x n sparse matrix whose entries are each present with probability `density`, with
+ * Gaussian values, drawn from the sequential stream at `seed` (random_matrix.hh:63-121).
+ * Positions, order (CSR order for COO), index arrays and the next state are the reference's;
+ * values are its Box-Muller values as rbg_fill_dense computes them.  Two calls, because the
+ * number of nonzeros is random:
+ *   rbg_random_sparse_create  draws the structure on the GPU, writes *nnz and *next
+ *                             (synchronises `stream`); the handle keeps device memory;
+ *   rbg_random_sparse_fill    writes device arrays: COO a = rows[nnz], b = cols[nnz];
+ *                             CSR a = rowptr[m + 1], b = colidxs[nnz];
+ *                             CSC a = colptr[n + 1], b = rowidxs[nnz];
+ *   rbg_random_sparse_destroy frees the handle (synchronous).
+ * density outside [0, 1] fails the reference's check.  Limits of this library: the compressed
+ * formats need fewer than 2^30 stream words (about 5e8 nonzeros) and a minor dimension below
+ * 2^31 - 1; 0 < density < 2^-53 (where log(1 - density) rounds to 0 and the reference's skip
+ * is undefined) returns RBG_ERROR_UNSUPPORTED. */
+typedef struct rbg_random_sparse_s *rbg_random_sparse;
+int rbg_random_sparse_create(int32_t format, int64_t m, int64_t n, double density,
+                             const rbg_state *seed, rbg_random_sparse *out, int64_t *nnz,
+                             rbg_state *next, rbg_stream_t stream);
+int rbg_random_sparse_fill(rbg_random_sparse h, int32_t dtype, int32_t itype, void *vals,
+                           void *a, void *b, rbg_stream_t stream);
+/* near_ties: skips of this matrix whose quotient log(1 - u) / log(1 - density) lay within
+ * 2^-48 (relative) of an integer, where the device logarithm and the host C library's may floor
+ * differently (about 1e-14 per draw; the matrix is the reference's when this is 0);
+ * words_drawn: stream words the reference's loop draws.  Either pointer may be NULL. */
+int rbg_random_sparse_info(rbg_random_sparse h, int64_t *near_ties, int64_t *words_drawn);
+int rbg_random_sparse_destroy(rbg_random_sparse h);
+
 /* ------------------------------------------------------------------ dense operators */
 
 /* LSKGE3 / sketch_general left (RandBLAS/skge.hh:154-202, 756-821, 1073-1097):

@@ -36,6 +36,8 @@
  *                              order, which is implementation-defined, so only the set
  *                              of (index, value) pairs per vector is comparable)
  *   sparse compute_next_state  RandBLAS/sparse_skops.hh:266-283
+ *   PhiloxStream, random_csr/csc/coo
+ *                              RandBLAS/sparse_data/random_matrix.hh:63-121, 135-355
  *
  * Build: gcc -O2 -std=gnu11 -fPIC -shared -ffp-contract=off -fopenmp (oracle/build.py).
  */
@@ -388,4 +390,129 @@ int orc_fill_sparse(int dtype, int itype, int64_t D_rows, int64_t D_cols, int64_
     }
     return orc_fill_laso(dtype, itype, vec_nnz, mx, mn, idxs_long, idxs_short, vals, nnz, seed,
                          next);
+}
+
+/* ------------------------------------------------ random sparse matrices */
+
+/*
+ * PhiloxStream (sparse_data/random_matrix.hh:63-121): 32-bit words dispensed one at a time
+ * from the Philox blocks at counters seed, seed + 1, ...; a Gaussian is the first value of
+ * boxmuller on a fresh word pair, or the cached second value of the previous pair; a
+ * geometric draw is floor(log(1 - u) / log(1 - p)) with u = w * 2^-32 + 2^-33 in double.
+ * The state handed back is the counter after the last block fetched.
+ */
+typedef struct {
+    orc_state s;
+    uint32_t buf[4];
+    int pos;
+    float spare;
+    int has_spare;
+} orc_pstream;
+
+static uint32_t ps_word(orc_pstream *p) {
+    if (p->pos >= 4) {
+        orc_philox4x32_10(p->s.counter, p->s.key, p->buf);
+        orc_ctr_add(p->s.counter, 1);
+        p->pos = 0;
+    }
+    return p->buf[p->pos++];
+}
+
+static float ps_gaussian(orc_pstream *p) {
+    if (p->has_spare) {
+        p->has_spare = 0;
+        return p->spare;
+    }
+    uint32_t a = ps_word(p), b = ps_word(p);
+    float g1, g2;
+    orc_boxmuller(a, b, &g1, &g2);
+    p->spare = g2;
+    p->has_spare = 1;
+    return g1;
+}
+
+static int64_t ps_geometric(orc_pstream *p, double log_1_minus_p) {
+    double u = (double)ps_word(p) * 0x1p-32 + 0x1p-33;
+    return (int64_t)floor(log(1.0 - u) / log_1_minus_p);
+}
+
+/*
+ * random_csr / random_csc / random_coo (sparse_data/random_matrix.hh:135-207, 217-285,
+ * 296-355).  fmt: 0 = COO (a = rows, b = cols, both of length nnz, CSR order), 1 = CSR
+ * (a = rowptr[m + 1], b = colidxs[nnz]), 2 = CSC (a = colptr[n + 1], b = rowidxs[nnz]).
+ * Nonzeros past `cap` are drawn but not stored, so a caller can size the arrays from the
+ * returned nnz and call again.  Returns nnz, or -1 if density is outside [0, 1] (the
+ * reference's randblas_require), or -2 if log(1 - density) rounds to zero (0 < density
+ * < 2^-53, where the reference converts an infinite quotient to int64).
+ */
+int64_t orc_random_sparse(int fmt, int dtype, int itype, int64_t m, int64_t n, double density,
+                          const orc_state *seed, int64_t cap, void *vals, void *a, void *b,
+                          orc_state *next) {
+    if (!(density >= 0.0 && density <= 1.0)) return -1;
+    orc_pstream p;
+    p.s = *seed;
+    p.pos = 4;
+    p.spare = 0.0f;
+    p.has_spare = 0;
+    int64_t k = 0;
+    const int compressed = fmt != 0;
+    const int64_t nmaj = fmt == 2 ? n : m, nmin = fmt == 2 ? m : n;
+    if (density == 0.0 || m == 0 || n == 0) {
+        if (compressed)
+            for (int64_t i = 0; i <= nmaj && nmaj > 0; ++i) put_idx(itype, a, i, 0);
+        *next = p.s;
+        return 0;
+    }
+    if (density >= 1.0) {
+        for (int64_t i = 0; i < nmaj; ++i) {
+            if (compressed) put_idx(itype, a, i, k);
+            for (int64_t j = 0; j < nmin; ++j, ++k) {
+                float v = ps_gaussian(&p);
+                if (k >= cap) continue;
+                put_val(dtype, vals, k, v);
+                if (compressed) {
+                    put_idx(itype, b, k, j);
+                } else {
+                    put_idx(itype, a, k, i);
+                    put_idx(itype, b, k, j);
+                }
+            }
+        }
+        if (compressed) put_idx(itype, a, nmaj, k);
+        *next = p.s;
+        return k;
+    }
+    const double l1mp = log(1.0 - density);
+    if (l1mp == 0.0) return -2;
+    if (compressed) {
+        for (int64_t i = 0; i < nmaj; ++i) {
+            put_idx(itype, a, i, k);
+            int64_t j = ps_geometric(&p, l1mp);
+            while (j < nmin) {
+                float v = ps_gaussian(&p);
+                if (k < cap) {
+                    put_val(dtype, vals, k, v);
+                    put_idx(itype, b, k, j);
+                }
+                ++k;
+                j += 1 + ps_geometric(&p, l1mp);
+            }
+        }
+        put_idx(itype, a, nmaj, k);
+    } else {
+        const int64_t total = m * n;
+        int64_t pos = ps_geometric(&p, l1mp);
+        while (pos < total) {
+            float v = ps_gaussian(&p);
+            if (k < cap) {
+                put_idx(itype, a, k, pos / n);
+                put_idx(itype, b, k, pos % n);
+                put_val(dtype, vals, k, v);
+            }
+            ++k;
+            pos += 1 + ps_geometric(&p, l1mp);
+        }
+    }
+    *next = p.s;
+    return k;
 }

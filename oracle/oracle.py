@@ -85,6 +85,8 @@ class Oracle:
         L.orc_fill_sparse.argtypes = [INT, INT, I64, I64, I64, INT, P, P, P, P, P, P]
         L.orc_fill_sparse.restype = INT
         L.orc_sparse_next_state.argtypes = [INT, I64, I64, I64, P, P]
+        L.orc_random_sparse.argtypes = [INT, INT, INT, I64, I64, C.c_double, P, I64, P, P, P, P]
+        L.orc_random_sparse.restype = I64
 
     # -- RNG ------------------------------------------------------------------------
     def philox(self, counter, key) -> tuple:
@@ -185,12 +187,49 @@ class Oracle:
                                        C.addressof(nxt))
         return nxt
 
+    def random_sparse(self, fmt, dtype, itype, m, n, density, seed: State):
+        """random_coo / random_csr / random_csc (fmt 0 / 1 / 2) -> (vals, a, b, next State).
+
+        COO: a = rows, b = cols; CSR: a = rowptr, b = colidxs; CSC: a = colptr, b = rowidxs.
+        """
+        return _random_sparse(self.lib.orc_random_sparse, fmt, dtype, itype, m, n, density,
+                              seed, lambda rc: ValueError(f"orc_random_sparse failed ({rc})"))
+
     def sparse_dense_matrix(self, dtype, D_rows, D_cols, vec_nnz, major_axis, seed: State):
         vals, rows, cols, _, _ = self.fill_sparse(dtype, 1, D_rows, D_cols, vec_nnz, major_axis,
                                                   seed)
         S = np.zeros((D_rows, D_cols), dtype=np.float64)
         np.add.at(S, (rows, cols), vals.astype(np.float64))
         return S
+
+
+def _random_sparse(fn, fmt, dtype, itype, m, n, density, seed, err, ref=False):
+    it = np.int32 if itype == 0 else np.int64
+    nmaj = n if fmt == 2 else m
+    cap = 0
+    while True:
+        vals = np.zeros(max(cap, 1), _np_dtype(dtype))
+        a = np.zeros(max(nmaj + 1 if fmt else cap, 1), it)
+        b = np.zeros(max(cap, 1), it)
+        nxt = State()
+        if ref:
+            nnz = C.c_int64()
+            rc = fn(fmt, dtype, itype, m, n, density, C.addressof(seed.counter),
+                    C.addressof(seed.key), cap, _ptr(vals), _ptr(a), _ptr(b), C.addressof(nnz),
+                    C.addressof(nxt.counter), C.addressof(nxt.key))
+            if rc:
+                raise err(rc)
+            k = nnz.value
+        else:
+            k = fn(fmt, dtype, itype, m, n, density, C.addressof(seed), cap, _ptr(vals), _ptr(a),
+                   _ptr(b), C.addressof(nxt))
+            if k < 0:
+                raise err(k)
+        if k <= cap:
+            if fmt == 0:
+                return vals[:k], a[:k], b[:k], nxt
+            return vals[:k], a[:nmaj + 1] if nmaj > 0 else a[:0], b[:k], nxt
+        cap = k
 
 
 def find_cblas():
@@ -245,6 +284,8 @@ class RefLib:
                                         I64, I64, INT, P, P, I64, I64, P, I64, C.c_double, P, I64]
         L.rbref_sketch_vector.argtypes = [INT, INT, I64, I64, C.c_double, I64, I64, INT, INT, P,
                                           P, I64, I64, P, I64, C.c_double, P, I64]
+        L.rbref_random_sparse.argtypes = [INT, INT, INT, I64, I64, C.c_double, P, P, I64, P, P,
+                                          P, P, P, P]
         L.rbref_sketch_sparse.argtypes = [INT, INT, INT, INT, INT, I64, I64, I64, C.c_double,
                                           I64, I64, INT, INT, P, P, I64, I64, INT, I64, I64, I64,
                                           P, P, P, C.c_double, P, I64]
@@ -252,6 +293,13 @@ class RefLib:
     def _check(self, rc):
         if rc:
             raise RuntimeError(f"reference error {rc}: {self.lib.rbref_last_error().decode()}")
+
+    def random_sparse(self, fmt, dtype, itype, m, n, density, seed: State):
+        """The reference's random_coo / random_csr / random_csc; same returns as Oracle's."""
+        return _random_sparse(
+            self.lib.rbref_random_sparse, fmt, dtype, itype, m, n, density, seed,
+            lambda rc: RuntimeError(
+                f"reference error {rc}: {self.lib.rbref_last_error().decode()}"), ref=True)
 
     def philox(self, counter, key):
         c, k, o = U32x4(*counter), U32x2(*key), U32x4()

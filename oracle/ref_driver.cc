@@ -16,6 +16,8 @@
 //   rbref_sketch_saso ........... RandBLAS::sketch_general, SparseSkOp (RandBLAS/skge.hh:776,948)
 //   rbref_sketch_vector ......... RandBLAS::sketch_vector         (RandBLAS/skve.hh:140-164)
 //   rbref_sketch_sparse ......... RandBLAS::sketch_sparse         (RandBLAS/sparse_data/sksp.hh:418-539)
+//   rbref_random_sparse ......... random_coo / random_csr / random_csc
+//                                 (RandBLAS/sparse_data/random_matrix.hh:135-355)
 #include <RandBLAS.hh>
 
 #include <cstdint>
@@ -314,6 +316,67 @@ int rbref_sketch_sparse(int dtype, int side, int layout, int opS, int opA, int64
             sketch_sparse_t<double>(side, layout, opS, opA, d, n, m, alpha, D_rows, D_cols,
                                     family, major_axis, ctr, key, ro_s, co_s, fmt, A_rows, A_cols,
                                     nnz, vals, a, b, beta, B, ldb);
+    });
+}
+
+}  // extern "C"
+
+// ------------------------------------------------------------- random sparse matrices
+#include <RandBLAS/sparse_data/random_matrix.hh>
+
+namespace {
+
+// Copies min(nnz, cap) entries (and the nmaj + 1 pointers of a compressed format) out of the
+// reference's own random_coo / random_csr / random_csc; fmt as in rbref_sketch_sparse.
+template <typename T, typename I>
+int64_t random_sparse_t(int fmt, int64_t m, int64_t n, double density, const State &seed,
+                        int64_t cap, void *vals, void *a, void *b, State &next) {
+    using namespace RandBLAS::sparse_data;
+    auto out = [&](const T *v, const I *ia, int64_t na, const I *ib, int64_t nnz) {
+        const int64_t k = nnz < cap ? nnz : cap;
+        if (k > 0) std::memcpy(vals, v, sizeof(T) * k);
+        if (ia && na > 0) std::memcpy(a, ia, sizeof(I) * na);
+        if (ib && k > 0) std::memcpy(b, ib, sizeof(I) * k);
+    };
+    if (fmt == 0) {
+        auto [A, s] = random_coo<T, I>(m, n, density, seed);
+        out(A.vals, A.rows, A.nnz < cap ? A.nnz : cap, A.cols, A.nnz);
+        next = s;
+        return A.nnz;
+    }
+    if (fmt == 1) {
+        auto [A, s] = random_csr<T, I>(m, n, density, seed);
+        out(A.vals, A.rowptr, m + 1, A.colidxs, A.nnz);
+        next = s;
+        return A.nnz;
+    }
+    auto [A, s] = random_csc<T, I>(m, n, density, seed);
+    out(A.vals, A.colptr, n + 1, A.rowidxs, A.nnz);
+    next = s;
+    return A.nnz;
+}
+
+}  // namespace
+
+extern "C" {
+
+// random_coo / random_csr / random_csc (RandBLAS/sparse_data/random_matrix.hh:135-355).
+int rbref_random_sparse(int fmt, int dtype, int itype, int64_t m, int64_t n, double density,
+                        const uint32_t ctr[4], const uint32_t key[2], int64_t cap, void *vals,
+                        void *a, void *b, int64_t *nnz, uint32_t next_ctr[4],
+                        uint32_t next_key[2]) {
+    return guarded([&] {
+        const State seed = make_state(ctr, key);
+        State next;
+        if (dtype == 0 && itype == 0)
+            *nnz = random_sparse_t<float, int32_t>(fmt, m, n, density, seed, cap, vals, a, b, next);
+        else if (dtype == 0)
+            *nnz = random_sparse_t<float, int64_t>(fmt, m, n, density, seed, cap, vals, a, b, next);
+        else if (itype == 0)
+            *nnz = random_sparse_t<double, int32_t>(fmt, m, n, density, seed, cap, vals, a, b, next);
+        else
+            *nnz = random_sparse_t<double, int64_t>(fmt, m, n, density, seed, cap, vals, a, b, next);
+        put_state(next, next_ctr, next_key);
     });
 }
 

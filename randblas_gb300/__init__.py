@@ -10,7 +10,8 @@ from ._lib import RandBLASError, lib  # noqa: F401
 from .api import (  # noqa: F401
     Axis, COOMatrix, CSCMatrix, CSRMatrix, DenseDist, DenseSkOp, Layout, Op, RNGState,
     ScalarDist, SparseDist, SparseSkOp, deterministic, fill_dense, fill_dense_unpacked, fill_sparse,
-    fill_sparse_unpacked_nosub, left_spmm, repeated_fisher_yates, right_spmm, sketch_general,
+    fill_sparse_unpacked_nosub, left_spmm, random_coo, random_csc, random_csr,
+    repeated_fisher_yates, right_spmm, sketch_general,
     require_symmetric, set_deterministic, sketch_sparse, sketch_symmetric, sketch_vector, spmm)
 
 __version__ = "1.1.0"

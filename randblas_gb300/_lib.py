@@ -151,6 +151,11 @@ SIGNATURES = {
     "rbg_batched_plan_execute": ([P, P], C.c_int),
     "rbg_batched_plan_info": ([P, C.POINTER(CI64), C.POINTER(CI64)], C.c_int),
     "rbg_batched_plan_destroy": ([P], C.c_int),
+    "rbg_random_sparse_create": ([CI32, CI64, CI64, CD, PS, C.POINTER(P), C.POINTER(CI64), PS, P],
+                                 C.c_int),
+    "rbg_random_sparse_fill": ([P, CI32, CI32, P, P, P, P], C.c_int),
+    "rbg_random_sparse_info": ([P, C.POINTER(CI64), C.POINTER(CI64)], C.c_int),
+    "rbg_random_sparse_destroy": ([P], C.c_int),
 }
 
 _lock = threading.Lock()

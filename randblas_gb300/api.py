@@ -10,6 +10,7 @@ argument checks raise :class:`RandBLASError` carrying the reference's message
 from __future__ import annotations
 
 import ctypes as C
+import warnings
 from dataclasses import dataclass, field
 from enum import IntEnum
 from typing import Optional
@@ -324,6 +325,59 @@ def _spmat(fmt, n_rows, n_cols, vals, a, b):
     m.idx_a = a.data_ptr() if a.numel() else None
     m.idx_b = b.data_ptr() if b.numel() else None
     return m
+
+
+# ------------------------------------------------------------------ random sparse matrices
+def _random_sparse(fmt, m: int, n: int, density: float, state: RNGState, dtype, itype):
+    if dtype not in _DT or itype not in _IT:
+        raise RandBLASError(_lib.ERROR_INVALID_ARGUMENT,
+                            "dtype must be float32/float64 and itype int32/int64")
+    h = C.c_void_p()
+    nnz = C.c_int64()
+    nxt = _lib.rbg_state()
+    call("rbg_random_sparse_create", fmt, m, n, float(density), C.byref(state._c()),
+         C.byref(h), C.byref(nnz), C.byref(nxt), _stream())
+    try:
+        dev = torch.device("cuda", torch.cuda.current_device())
+        k = nnz.value
+        nmaj = n if fmt == _lib.CSC else m
+        vals = torch.empty(k, dtype=dtype, device=dev)
+        a = torch.empty(k if fmt == _lib.COO else nmaj + 1, dtype=itype, device=dev)
+        b = torch.empty(k, dtype=itype, device=dev)
+        call("rbg_random_sparse_fill", h, _DT[dtype], _IT[itype], _ptr(vals) if k else None,
+             _ptr(a) if a.numel() else None, _ptr(b) if k else None, _stream())
+        ties = C.c_int64()
+        call("rbg_random_sparse_info", h, C.byref(ties), None)
+        if ties.value:
+            warnings.warn(f"{ties.value} geometric skip(s) fell within 2^-48 of an integer; "
+                          "the reference's host logarithm may round them differently")
+    finally:
+        call("rbg_random_sparse_destroy", h)
+    return vals, a, b, RNGState._from_c(nxt)
+
+
+def random_csr(m: int, n: int, density: float, state: RNGState, dtype=torch.float64,
+               itype=torch.int64):
+    """random_csr<T, sint_t>(m, n, density, state) (sparse_data/random_matrix.hh:135-207):
+    returns (CSRMatrix, next_state); each entry is present with probability `density`,
+    values standard Gaussian."""
+    vals, rowptr, colidxs, nxt = _random_sparse(_lib.CSR, m, n, density, state, dtype, itype)
+    return CSRMatrix(m, n, vals, rowptr, colidxs), nxt
+
+
+def random_csc(m: int, n: int, density: float, state: RNGState, dtype=torch.float64,
+               itype=torch.int64):
+    """random_csc<T, sint_t>(m, n, density, state) (sparse_data/random_matrix.hh:217-285)."""
+    vals, colptr, rowidxs, nxt = _random_sparse(_lib.CSC, m, n, density, state, dtype, itype)
+    return CSCMatrix(m, n, vals, rowidxs, colptr), nxt
+
+
+def random_coo(m: int, n: int, density: float, state: RNGState, dtype=torch.float64,
+               itype=torch.int64):
+    """random_coo<T, sint_t>(m, n, density, state) (sparse_data/random_matrix.hh:296-355):
+    entries in CSR order."""
+    vals, rows, cols, nxt = _random_sparse(_lib.COO, m, n, density, state, dtype, itype)
+    return COOMatrix(m, n, vals, rows, cols), nxt
 
 
 # ------------------------------------------------------------------------- sketching

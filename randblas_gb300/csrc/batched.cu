@@ -538,20 +538,6 @@ void upload_plan(BatchedPlan &pl, const std::vector<ProbDev> &descs,
     if (!stream_ordered) RBG_CUDA(cudaStreamSynchronize(s));
 }
 
-template <typename F>
-int guarded_batched(F &&f) {
-    try {
-        f();
-        return RBG_SUCCESS;
-    } catch (const Failure &e) {
-        set_last_error(e.msg);
-        return e.code;
-    } catch (const std::exception &e) {
-        set_last_error(e.what());
-        return RBG_ERROR_ALLOC;
-    }
-}
-
 }  // namespace
 }  // namespace rbg
 
@@ -567,7 +553,7 @@ extern "C" int rbg_batched_tile_configs(int32_t *count) {
 }
 
 extern "C" int rbg_batched_tile_shape(int32_t config, int32_t *rows, int32_t *cols) {
-    return guarded_batched([&] {
+    return guarded([&] {
         if (!rows || !cols) fail(RBG_ERROR_INVALID_ARGUMENT, "rows and cols must not be NULL");
         if (config < 1 || config > kConfigs)
             fail(RBG_ERROR_INVALID_ARGUMENT, "config must be one of the listed configurations");
@@ -579,7 +565,7 @@ extern "C" int rbg_batched_tile_shape(int32_t config, int32_t *rows, int32_t *co
 extern "C" int rbg_batched_plan_create(int32_t layout, const rbg_batch_problem *problems,
                                        int64_t count, int32_t tile_config,
                                        rbg_batched_plan *plan) {
-    return guarded_batched([&] {
+    return guarded([&] {
         if (!plan) fail(RBG_ERROR_INVALID_ARGUMENT, "plan must not be NULL");
         *plan = nullptr;
         std::vector<ProbDev> descs;
@@ -604,7 +590,7 @@ extern "C" int rbg_batched_plan_create(int32_t layout, const rbg_batch_problem *
 }
 
 extern "C" int rbg_batched_plan_execute(rbg_batched_plan plan, rbg_stream_t stream) {
-    return guarded_batched([&] {
+    return guarded([&] {
         if (!plan) fail(RBG_ERROR_INVALID_ARGUMENT, "plan must not be NULL");
         execute_plan(*plan, as_cuda(stream));
     });
@@ -612,7 +598,7 @@ extern "C" int rbg_batched_plan_execute(rbg_batched_plan plan, rbg_stream_t stre
 
 extern "C" int rbg_batched_plan_info(rbg_batched_plan plan, int64_t *work_items,
                                      int64_t *device_bytes) {
-    return guarded_batched([&] {
+    return guarded([&] {
         if (!plan) fail(RBG_ERROR_INVALID_ARGUMENT, "plan must not be NULL");
         if (work_items) *work_items = plan->n_items;
         if (device_bytes) *device_bytes = (int64_t)plan->bytes;
@@ -620,7 +606,7 @@ extern "C" int rbg_batched_plan_info(rbg_batched_plan plan, int64_t *work_items,
 }
 
 extern "C" int rbg_batched_plan_destroy(rbg_batched_plan plan) {
-    return guarded_batched([&] {
+    return guarded([&] {
         if (!plan) return;
         if (plan->mem) RBG_CUDA(cudaFree(plan->mem));
         delete plan;
@@ -629,7 +615,7 @@ extern "C" int rbg_batched_plan_destroy(rbg_batched_plan plan) {
 
 extern "C" int rbg_lskge3_batched(int32_t layout, const rbg_batch_problem *problems,
                                   int64_t count, int32_t tile_config, rbg_stream_t stream) {
-    return guarded_batched([&] {
+    return guarded([&] {
         const cudaStream_t s = as_cuda(stream);
         std::vector<ProbDev> descs;
         std::vector<WorkItem> items;

@@ -158,23 +158,6 @@ using namespace rbg;
 
 namespace {
 
-template <typename F>
-int guarded(F &&f) {
-    try {
-        f();
-        return RBG_SUCCESS;
-    } catch (const Failure &e) {
-        set_last_error(e.msg);
-        return e.code;
-    } catch (const std::bad_alloc &) {
-        set_last_error("host allocation failed");
-        return RBG_ERROR_ALLOC;
-    } catch (const std::exception &e) {
-        set_last_error(e.what());
-        return RBG_ERROR_INVALID_ARGUMENT;
-    }
-}
-
 void check_nonnull(const void *p, const char *what) {
     if (!p) fail(RBG_ERROR_INVALID_ARGUMENT, std::string(what) + " must not be NULL");
 }

@@ -1200,25 +1200,9 @@ int *wait_error_flag() {
 
 using namespace rbg;
 
-namespace {
-template <typename F>
-int guarded_lowp(F &&f) {
-    try {
-        f();
-        return RBG_SUCCESS;
-    } catch (const Failure &e) {
-        set_last_error(e.msg);
-        return e.code;
-    } catch (const std::exception &e) {
-        set_last_error(e.what());
-        return RBG_ERROR_INVALID_ARGUMENT;
-    }
-}
-}  // namespace
-
 extern "C" int rbg_lskge3_lowp_workspace(int32_t precision, int64_t d, int64_t n, int64_t m,
                                          size_t *bytes) {
-    return guarded_lowp([&] {
+    return guarded([&] {
         if (!bytes) fail(RBG_ERROR_INVALID_ARGUMENT, "bytes must not be NULL");
         if (precision != RBG_PREC_BF16 && precision != RBG_PREC_FP8_E4M3)
             fail(RBG_ERROR_INVALID_ARGUMENT, "precision must be RBG_PREC_BF16 or RBG_PREC_FP8_E4M3");
@@ -1228,7 +1212,7 @@ extern "C" int rbg_lskge3_lowp_workspace(int32_t precision, int64_t d, int64_t n
 }
 
 extern "C" int rbg_lowp_status(int32_t *code) {
-    return guarded_lowp([&] {
+    return guarded([&] {
         if (!code) fail(RBG_ERROR_INVALID_ARGUMENT, "code must not be NULL");
         int v = 0;
         RBG_CUDA(cudaMemcpyFromSymbol(&v, g_lowp_error, sizeof v));
@@ -1261,7 +1245,7 @@ int lowp_entry(int32_t precision, int32_t a_dtype, int32_t layout, int32_t opS, 
                int64_t d, int64_t n, int64_t m, float alpha, const rbg_dense_skop *S,
                int64_t ro_s, int64_t co_s, const void *A, int64_t lda, float beta, float *B,
                int64_t ldb, void *workspace, size_t workspace_bytes, rbg_stream_t stream) {
-    return guarded_lowp([&] {
+    return guarded([&] {
         if (precision != RBG_PREC_BF16 && precision != RBG_PREC_FP8_E4M3)
             fail(RBG_ERROR_INVALID_ARGUMENT, "precision must be RBG_PREC_BF16 or RBG_PREC_FP8_E4M3");
         if (a_dtype != RBG_F32 && a_dtype != RBG_BF16)

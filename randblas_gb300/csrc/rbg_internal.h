@@ -5,6 +5,8 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <exception>
+#include <new>
 #include <string>
 
 #include "randblas_gb300.h"
@@ -33,6 +35,25 @@ void set_last_error(const std::string &msg);
 
 void cuda_check(cudaError_t e, const char *what);
 #define RBG_CUDA(call) ::rbg::cuda_check((call), #call)
+
+// Body of every extern "C" entry point: runs f and turns what it throws into a status code
+// plus the thread-local message of rbg_last_error.
+template <typename F>
+int guarded(F &&f) {
+    try {
+        f();
+        return RBG_SUCCESS;
+    } catch (const Failure &e) {
+        set_last_error(e.msg);
+        return e.code;
+    } catch (const std::bad_alloc &) {
+        set_last_error("host allocation failed");
+        return RBG_ERROR_ALLOC;
+    } catch (const std::exception &e) {
+        set_last_error(e.what());
+        return RBG_ERROR_INVALID_ARGUMENT;
+    }
+}
 
 // Call right after each kernel launch of the library: checks the launch and counts it
 // (rbg_kernel_launches).

@@ -74,20 +74,6 @@ void require_symmetric_impl(int32_t dtype, int32_t layout, const void *A, int64_
         check_symmetric<double>(layout, A, n, lda, tol, s);
 }
 
-template <typename F>
-int guarded_sym(F &&f) {
-    try {
-        f();
-        return RBG_SUCCESS;
-    } catch (const Failure &e) {
-        set_last_error(e.msg);
-        return e.code;
-    } catch (const std::exception &e) {
-        set_last_error(e.what());
-        return RBG_ERROR_INVALID_ARGUMENT;
-    }
-}
-
 }  // namespace
 }  // namespace rbg
 
@@ -95,7 +81,7 @@ using namespace rbg;
 
 extern "C" int rbg_require_symmetric(int32_t dtype, int32_t layout, const void *A, int64_t n,
                                      int64_t lda, double tol, rbg_stream_t stream) {
-    return guarded_sym([&] { require_symmetric_impl(dtype, layout, A, n, lda, tol, as_cuda(stream)); });
+    return guarded([&] { require_symmetric_impl(dtype, layout, A, n, lda, tol, as_cuda(stream)); });
 }
 
 extern "C" int rbg_sketch_symmetric(int32_t side, int32_t layout, int64_t d, int64_t n,

@@ -8,12 +8,14 @@ against the project's Random123 / BLAS++ stand-ins -- and records:
   test/test_basic_rng/r123_kat_vectors.txt (parsed from that file);
 * fill_dense.npz, fill_sparse.npz, sketch_*.npz: outputs of the reference's public functions on
   small seeded cases (every layout / op / side / submatrix combination the parity tests use);
+* random_sparse.npz: the reference's random_coo / random_csr / random_csc on small seeded
+  cases (every format, value and index type, densities 0, 1 and in between, empty shapes);
 * full_size.json: SHA-256 digests and next states of the full-size operators of the
   benchmark workloads (the 200 x 10000 Gaussian FP64 operator and its 10000 x 50 uniform data
   matrix; the 1024 x 2^20 SASO with 8 nonzeros per column), so the GPU tests can pin those
   bit for bit without shipping the arrays.
 
-Usage: python tests/golden/make_golden.py
+Usage: python tests/golden/make_golden.py [random_sparse]   (the argument writes only that file)
 """
 from __future__ import annotations
 
@@ -64,8 +66,45 @@ def dense_fill_cases():
     return cases
 
 
+RANDOM_SPARSE_SHAPES = [(100, 200, 0.05), (80, 150, 0.1), (5, 8, 1.0), (7, 9, 1.0),
+                        (10, 20, 0.0), (0, 10, 0.5), (10, 0, 0.5), (1, 1, 0.5), (300, 7, 0.9),
+                        (50, 3000, 1e-4), (2000, 2, 0.3), (13, 17, 0.999999), (64, 64, 0.02)]
+
+# The sketch_sparse benchmark's data matrix: 2^17 x 512 CSR with 5 expected nonzeros per row.
+RANDOM_CSR_FULL = dict(fmt=1, m=1 << 17, n=512, density=5 / 512, ctr=[0, 0, 0, 0], key=[11, 0])
+
+
+def random_sparse_fixtures(ref):
+    arrays, meta = {}, []
+    for i, ((m, n, dens), fmt, dt, it) in enumerate(itertools.product(
+            RANDOM_SPARSE_SHAPES, (0, 1, 2), (0, 1), (0, 1))):
+        c = dict(fmt=fmt, dtype=dt, itype=it, m=m, n=n, density=dens, ctr=[5, 0, 0, 0],
+                 key=[4242, i % 3])
+        vals, a, b, nxt = ref.random_sparse(fmt, dt, it, m, n, dens,
+                                            State.make(c["ctr"], c["key"]))
+        arrays[f"v{i}"], arrays[f"a{i}"], arrays[f"b{i}"] = vals, a, b
+        meta.append(dict(c, nnz=int(vals.size), next=st(nxt)))
+    np.savez_compressed(os.path.join(HERE, "random_sparse.npz"), meta=json.dumps(meta), **arrays)
+    f = RANDOM_CSR_FULL
+    vals, a, b, nxt = ref.random_sparse(f["fmt"], 0, 1, f["m"], f["n"], f["density"],
+                                        State.make(f["ctr"], f["key"]))
+    return dict(f, nnz=int(vals.size), next=st(nxt),
+                rowptr_sha256=hashlib.sha256(a.tobytes()).hexdigest(),
+                colidxs_sha256=hashlib.sha256(b.tobytes()).hexdigest(),
+                vals_sha256=hashlib.sha256(vals.tobytes()).hexdigest())
+
+
 def main():
     ref = RefLib()
+    if sys.argv[1:] == ["random_sparse"]:
+        path = os.path.join(HERE, "full_size.json")
+        with open(path) as f:
+            full = json.load(f)
+        full["random_csr_2^17x512"] = random_sparse_fixtures(ref)
+        with open(path, "w") as f:
+            json.dump(full, f, indent=1)
+        print("random_sparse fixtures written to", HERE)
+        return
     out = {}
 
     kat = kat_rows()
@@ -283,6 +322,7 @@ def main():
                                      rows_sha256=hashlib.sha256(rows.tobytes()).hexdigest(),
                                      cols_sha256=hashlib.sha256(cols.tobytes()).hexdigest(),
                                      vals_sha256=hashlib.sha256(vals.tobytes()).hexdigest())
+    full["random_csr_2^17x512"] = random_sparse_fixtures(ref)
     with open(os.path.join(HERE, "full_size.json"), "w") as f:
         json.dump(full, f, indent=1)
     print("golden fixtures written to", HERE)

@@ -52,3 +52,52 @@ def test_full_size_gaussian_sample(oracle):
                                           State.make(*g["seed"]))
     assert [list(nxt.counter), list(nxt.key)] == g["next"]
     assert np.array_equal(buf[z["idx"]], z["vals"])
+
+
+def test_random_sparse_matches_reference(oracle):
+    """random_coo / random_csr / random_csc (sparse_data/random_matrix.hh:135-355): every
+    array and the next state bit for bit, including densities 0 and 1 and empty shapes."""
+    meta, z = load_golden("random_sparse")
+    for i, c in enumerate(meta):
+        vals, a, b, nxt = oracle.random_sparse(c["fmt"], c["dtype"], c["itype"], c["m"], c["n"],
+                                               c["density"], State.make(c["ctr"], c["key"]))
+        assert vals.size == c["nnz"], c
+        assert [list(nxt.counter), list(nxt.key)] == c["next"], c
+        assert np.array_equal(vals.view(np.uint8), z[f"v{i}"].view(np.uint8)), c
+        assert np.array_equal(a, z[f"a{i}"]) and np.array_equal(b, z[f"b{i}"]), c
+
+
+def test_random_sparse_structure_and_rate(oracle):
+    """The reference's own checks (test/test_datastructures/test_spmats/test_random_matrix.cc):
+    sorted in-range indices, pointers from 0 to nnz, nnz within 4 standard deviations of
+    m * n * density, and a state that advances."""
+    m = n = 1000
+    density = 0.01
+    sd = np.sqrt(m * n * density * (1 - density))
+    for fmt in (0, 1, 2):
+        seed = State.from_key(42)
+        vals, a, b, nxt = oracle.random_sparse(fmt, 1, 1, m, n, density, seed)
+        assert abs(vals.size - m * n * density) < 4 * sd
+        assert nxt.tuple() != seed.tuple()
+        if fmt == 0:
+            key = a * n + b
+            assert np.all(np.diff(key) > 0) and a.min() >= 0 and b.max() < n
+        else:
+            assert a[0] == 0 and a[-1] == vals.size and np.all(np.diff(a) >= 0)
+            for i in range(len(a) - 1):
+                seg = b[a[i]:a[i + 1]]
+                assert np.all(np.diff(seg) > 0) and (seg.size == 0 or (seg[0] >= 0 and
+                                                                       seg[-1] < 1000))
+    with np.testing.assert_raises(ValueError):
+        oracle.random_sparse(1, 1, 1, 4, 4, 1.5, State.from_key(1))
+
+
+def test_full_size_random_csr_digest(oracle):
+    g = golden_json("full_size.json")["random_csr_2^17x512"]
+    vals, a, b, nxt = oracle.random_sparse(g["fmt"], 0, 1, g["m"], g["n"], g["density"],
+                                           State.make(g["ctr"], g["key"]))
+    assert vals.size == g["nnz"]
+    assert [list(nxt.counter), list(nxt.key)] == g["next"]
+    assert hashlib.sha256(a.tobytes()).hexdigest() == g["rowptr_sha256"]
+    assert hashlib.sha256(b.tobytes()).hexdigest() == g["colidxs_sha256"]
+    assert hashlib.sha256(vals.tobytes()).hexdigest() == g["vals_sha256"]
