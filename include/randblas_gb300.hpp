@@ -11,7 +11,8 @@
 // Types and functions mirror RandBLAS (RNGState base.hh:64-164, DenseDist dense_skops.hh:231-350,
 // DenseSkOp 357-478, fill_dense 563-658, SparseDist sparse_skops.hh:131-246, SparseSkOp 289-450,
 // fill_sparse 587-603, sketch_general skge.hh:756-1199, sketch_vector skve.hh:140-246,
-// sketch_sparse sparse_data/sksp.hh:418-539).  Matrix and vector pointers are CUDA device
+// sketch_sparse sparse_data/sksp.hh:418-539, random_coo / random_csr / random_csc
+// sparse_data/random_matrix.hh:135-355).  Matrix and vector pointers are CUDA device
 // pointers; every call is asynchronous on `stream` (default: the legacy default stream).
 // Failed argument checks throw RandBLAS_GB300::Error carrying the reference's message text;
 // size overflows throw std::overflow_error, as RandBLAS's safe_int_product does.
@@ -310,6 +311,50 @@ void sketch_symmetric(Layout layout, T alpha, const T *A, int64_t lda, const Den
     sketch_symmetric(layout, S.n_rows, S.n_cols, alpha, A, lda, S, 0, 0, beta, B, ldb,
                      sym_check_tol, stream);
 }
+
+// ------------------------------------------------------------------ random sparse matrices
+// random_coo / random_csr / random_csc (sparse_data/random_matrix.hh:135-355).  The reference
+// returns an owning host matrix.  Here the number of nonzeros is known only once the structure
+// is drawn, so generation takes two steps:
+// - construct: draws the structure on the GPU and synchronises `stream`;
+// - fill: writes caller-allocated device arrays of nnz() entries, plus the
+//   major dimension + 1 pointers of CSR / CSC.
+enum class SparseFormat : int32_t { COO = RBG_COO, CSR = RBG_CSR, CSC = RBG_CSC };
+
+class RandomSparse {
+  public:
+    RandomSparse(SparseFormat format, int64_t m, int64_t n, double density,
+                 const RNGState &state, rbg_stream_t stream = nullptr) {
+        detail::check(rbg_random_sparse_create(static_cast<int32_t>(format), m, n, density,
+                                               &state.s, &h_, &nnz_, &next_.s, stream));
+    }
+    ~RandomSparse() {
+        if (h_) rbg_random_sparse_destroy(h_);
+    }
+    RandomSparse(const RandomSparse &) = delete;
+    RandomSparse &operator=(const RandomSparse &) = delete;
+    int64_t nnz() const { return nnz_; }
+    // the state random_csr & co. return beside the matrix
+    const RNGState &next_state() const { return next_; }
+    // COO: a = rows, b = cols (CSR order); CSR: a = rowptr, b = colidxs;
+    // CSC: a = colptr, b = rowidxs.
+    template <typename T, typename I>
+    void fill(T *vals, I *a, I *b, rbg_stream_t stream = nullptr) const {
+        detail::check(rbg_random_sparse_fill(h_, detail::dtype<T>(), detail::itype<I>(), vals, a,
+                                             b, stream));
+    }
+    // skips near a rounding tie of the logarithm (0: the matrix is the reference's)
+    int64_t near_ties() const {
+        int64_t t = 0;
+        detail::check(rbg_random_sparse_info(h_, &t, nullptr));
+        return t;
+    }
+
+  private:
+    rbg_random_sparse h_ = nullptr;
+    int64_t nnz_ = 0;
+    RNGState next_;
+};
 
 // Process-wide reproducibility switch (no RandBLAS counterpart).
 inline void set_deterministic(bool on) { detail::check(rbg_set_deterministic(on ? 1 : 0)); }

@@ -66,6 +66,15 @@ int main() {
         threw = std::string(e.what()).find("A must not be NULL") != std::string::npos;
     }
     EXPECT(threw);
+    threw = false;
+    try {  // random_csr's density check (random_matrix.hh:142) fails before any device work
+        RB::RandomSparse R(RB::SparseFormat::CSR, 4, 4, 1.5, RB::RNGState(1));
+    } catch (const RB::Error &e) {
+        threw = std::string(e.what()).find("density >= 0.0 && density <= 1.0") !=
+                    std::string::npos &&
+                std::string(e.what()).find("in function random_csr") != std::string::npos;
+    }
+    EXPECT(threw);
     std::printf("%s\n", failures ? "FAILED" : "ok");
     return failures ? 1 : 0;
 }
