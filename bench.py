@@ -476,11 +476,11 @@ def bench_saso(torch, rb, device, args, stream, hbm):
 
 
 def bench_more_rows(torch, rb, device, stream, hbm):
-    """Rows of the hot path outside the five configurations, each timed alone with CUDA events:
-    fill_sparse of the cfg2 SASO operator, the cfg2 sketch with that operator pre-filled (its
-    COO arrays read from HBM), sketch_vector with the 4096 x 2^20 uniform operator,
-    random_csr of a 2^17 x 512 matrix with 5 expected nonzeros per row, and sketch_sparse of a
-    Gaussian 1024 x 2^17 operator against that matrix."""
+    """Further rows of the hot path, each timed alone with CUDA events: fill_sparse of the
+    1024 x 2^20 SASO operator (8 per column), the SASO sketch of a 2^20 x 256 matrix with that
+    operator pre-filled (its COO arrays read from HBM), sketch_vector with the 4096 x 2^20 uniform
+    operator, random_csr of a 2^17 x 512 matrix with 5 expected nonzeros per row, and
+    sketch_sparse of a Gaussian 1024 x 2^17 operator against that matrix."""
     out = {}
     m, d, n, k = SASO_M, SASO_D, SASO_N, SASO_K
     A = torch.empty(m * n, dtype=torch.float32, device=device)
@@ -510,7 +510,8 @@ def bench_more_rows(torch, rb, device, stream, hbm):
     rb.profile.enable(False)
     algo = 4.0 * m * n + 4.0 * d * n + written
     out["saso_prefilled"] = {
-        "workload": "the cfg2 sketch after fill_sparse: COO operator read from HBM",
+        "workload": "SASO 1024 x 2^20 sketch of a 2^20 x 256 FP32 matrix after fill_sparse: "
+                    "COO operator read from HBM",
         "ms": round(ms, 4), "GB/s": round(algo / (ms * 1e-3) / 1e9, 1),
         "frac_of_hbm": round(algo / (ms * 1e-3) / 1e9 / hbm, 4),
         "kernels_ms": {kk: round(v["ms"] / max(1, v["launches"]), 4) for kk, v in prof.items()}}

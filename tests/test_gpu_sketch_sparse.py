@@ -309,8 +309,9 @@ def test_saso_prefilled_row_bucketed(rb, itype):
 
 
 def test_saso_prefilled_matches_sampled(rb):
-    """The cfg2 shape with the operator filled first: the row-bucketed kernels read the COO
-    arrays and give the sampled path's result to FP32 rounding (<= 1e-6 relative)."""
+    """A 1024 x 2^18 SASO sketch of a 2^18 x 256 matrix with the operator filled first: the
+    row-bucketed kernels read the COO arrays and give the sampled path's result to FP32 rounding
+    (<= 1e-6 relative)."""
     import torch
     m, d, n = 1 << 18, 1024, 256
     A = torch.randn(m * n, device="cuda", generator=torch.Generator(device="cuda").manual_seed(1))
