@@ -693,6 +693,15 @@ void lsksp3_impl(int32_t layout, int32_t opS, int32_t opA, int64_t d, int64_t n,
         launch_scale(S->dtype, d, n, b.rs, b.cs, beta, B, s);
         return;
     }
+    // a generated operator against CSR rows of op(A): generate and apply in one kernel
+    const bool rows_of_opA = (A->format == RBG_CSR && opA == RBG_NO_TRANS) ||
+                             (A->format == RBG_CSC && opA == RBG_TRANS);
+    if (!S->buff && rows_of_opA && gen_spmm_applies(S->dtype, n)) {
+        gen_spmm_sketch(S->dtype, A->itype, d, n, m, alpha,
+                        make_p(*S, opS == RBG_TRANS, ro_s, co_s), A->idx_a, A->idx_b, A->vals,
+                        A->nnz, beta, B, b.rs, b.cs, s);
+        return;
+    }
     Scratch tmp;
     const SubmatView sv = submat_view(*S, sub.rows, sub.cols, ro_s, co_s, tmp, s);
     // Q(k, j) = op(submat(S))(j, k)
@@ -725,6 +734,16 @@ void rsksp3_impl(int32_t layout, int32_t opA, int32_t opS, int64_t m, int64_t d,
     const Strides b = strides_of(layout, ldb);
     if (alpha == 0.0 || n == 0) {
         launch_scale(S->dtype, m, d, b.rs, b.cs, beta, B, s);
+        return;
+    }
+    // B^T = op(S)^T op(A)^T: a generated operator against the rows of op(A)^T (the columns of
+    // op(A)) when they are stored directly
+    const bool cols_of_opA = (A->format == RBG_CSC && opA == RBG_NO_TRANS) ||
+                             (A->format == RBG_CSR && opA == RBG_TRANS);
+    if (!S->buff && cols_of_opA && gen_spmm_applies(S->dtype, m)) {
+        gen_spmm_sketch(S->dtype, A->itype, d, m, n, alpha,
+                        make_p(*S, opS == RBG_NO_TRANS, ro_s, co_s), A->idx_a, A->idx_b, A->vals,
+                        A->nnz, beta, B, b.cs, b.rs, s);
         return;
     }
     Scratch tmp;

@@ -180,4 +180,14 @@ void spmm_sketch(int dtype, int64_t M, int64_t N, int64_t K, double alpha,
                  const SparseOperand &Sp, const Strided &Q, double beta, void *out,
                  int64_t os_i, int64_t os_j, cudaStream_t s);
 
+// Out[M x N] = alpha * P[M x K] * X[K x N] + beta * Out for a generated operator P and sparse X
+// given by its rows: row k's entries are idx[ptr[k] .. ptr[k + 1]) (column j) with values val
+// (ptr, idx in itype; nnz bounds the entry arrays).  Nothing of P is materialised; sums are in
+// a fixed order.  gen_spmm_applies: whether an output of N columns fits the kernel's tile.
+bool gen_spmm_applies(int dtype, int64_t N);
+void gen_spmm_sketch(int dtype, int itype, int64_t M, int64_t N, int64_t K, double alpha,
+                     const POperand &P, const void *ptr, const void *idx, const void *val,
+                     int64_t nnz, double beta, void *out, int64_t os_i, int64_t os_j,
+                     cudaStream_t s);
+
 }  // namespace rbg

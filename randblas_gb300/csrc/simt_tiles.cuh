@@ -11,14 +11,15 @@ namespace simt {
 constexpr int BM = 128, BN = 128, BK = 16, NT = 256;  // tile M, max tile N, k step, threads
 
 // P tile, k-major: Ps[k][i] for i in [0, TM), k in [0, BK).  Entries outside M x K are 0.
-template <typename T, int TM = BM>
-__device__ __forceinline__ void gen_p_tile(T (*Ps)[TM + 4], const POperand &P, int64_t M,
-                                           int64_t K, int64_t i0, int64_t k0) {
+// Generated by THREADS threads of the CTA, this one being number tid.
+template <typename T, int TM, int THREADS>
+__device__ __forceinline__ void gen_p_tile_by(T (*Ps)[TM + 4], const POperand &P, int64_t M,
+                                              int64_t K, int64_t i0, int64_t k0, int tid) {
     const DenseGen &g = P.gen;
     if (P.r_on_i && ((P.c0 + k0) & 3) == 0 && i0 + TM <= M && k0 + BK <= K) {
         // interior tile, block-aligned: TM rows x BK / 4 whole counter blocks, no bounds
         const int64_t b0 = (P.c0 + k0) >> 2;
-        for (int w = threadIdx.x; w < TM * (BK / 4); w += NT) {
+        for (int w = tid; w < TM * (BK / 4); w += THREADS) {
             const int i = w / (BK / 4), b = w % (BK / 4);
             float v[4];
             gen4(g.family, g.counter_of(P.r0 + i0 + i, b0 + b), g.key, v);
@@ -29,7 +30,7 @@ __device__ __forceinline__ void gen_p_tile(T (*Ps)[TM + 4], const POperand &P, i
     }
     if (!P.r_on_i && ((P.c0 + i0) & 3) == 0 && i0 + TM <= M && k0 + BK <= K) {
         const int64_t b0 = (P.c0 + i0) >> 2;
-        for (int w = threadIdx.x; w < BK * (TM / 4); w += NT) {
+        for (int w = tid; w < BK * (TM / 4); w += THREADS) {
             const int k = w / (TM / 4), b = w % (TM / 4);
             float v[4];
             gen4(g.family, g.counter_of(P.r0 + k0 + k, b0 + b), g.key, v);
@@ -44,7 +45,7 @@ __device__ __forceinline__ void gen_p_tile(T (*Ps)[TM + 4], const POperand &P, i
         const int64_t cfirst = P.c0 + k0;
         const int64_t b0 = cfirst / 4;
         const int nb = (int)((cfirst + BK - 1) / 4 - b0 + 1);
-        for (int w = threadIdx.x; w < TM * nb; w += NT) {
+        for (int w = tid; w < TM * nb; w += THREADS) {
             const int i = w / nb, b = w % nb;
             const bool row_ok = i0 + i < M;
             float v[4] = {0.f, 0.f, 0.f, 0.f};
@@ -62,7 +63,7 @@ __device__ __forceinline__ void gen_p_tile(T (*Ps)[TM + 4], const POperand &P, i
         const int64_t cfirst = P.c0 + i0;
         const int64_t b0 = cfirst / 4;
         const int nb = (int)((cfirst + TM - 1) / 4 - b0 + 1);
-        for (int w = threadIdx.x; w < BK * nb; w += NT) {
+        for (int w = tid; w < BK * nb; w += THREADS) {
             const int k = w / nb, b = w % nb;
             const bool k_ok = k0 + k < K;
             float v[4] = {0.f, 0.f, 0.f, 0.f};
@@ -75,6 +76,13 @@ __device__ __forceinline__ void gen_p_tile(T (*Ps)[TM + 4], const POperand &P, i
             }
         }
     }
+}
+
+// gen_p_tile_by with all NT threads of the CTA.
+template <typename T, int TM = BM>
+__device__ __forceinline__ void gen_p_tile(T (*Ps)[TM + 4], const POperand &P, int64_t M,
+                                           int64_t K, int64_t i0, int64_t k0) {
+    gen_p_tile_by<T, TM, NT>(Ps, P, M, K, i0, k0, (int)threadIdx.x);
 }
 
 // ------------------------------------------------------------------ thread-block clusters

@@ -20,6 +20,7 @@
 #include <algorithm>
 
 #include "rbg_internal.h"
+#include "simt_tiles.cuh"
 #include "tc_ptx.cuh"
 
 namespace rbg {
@@ -1200,7 +1201,229 @@ void run(int64_t M, int64_t N, int64_t K, double alpha, const SparseOperand &Sp,
     }
 }
 
+// ------------------------------------------------------------------ generated operator x sparse data
+// LSKSP3 / RSKSP3 (RandBLAS/sparse_data/sksp.hh:132-539) when the dense operator holds no
+// buffer: Out[M x N] = alpha * P[M x K] * X[K x N] + beta * Out with P = op(submat(S)) generated
+// from its counters and X sparse, its rows stored directly (CSR rows, or the CSC columns of a
+// transpose).  The reference fills submat(S) into a temporary and then runs the SpMM; here every
+// operator entry is generated once and used where it is generated.
+//   A CTA owns 32 output rows x all N columns (a shared-memory tile, column stride 33) and a K
+// range, walked 32 k's at a time.  Per iteration:
+//  1. every thread issues the loads of one nonzero of the iteration (and of the next
+//     iteration's row starts), which stay in flight during generation;
+//  2. all 256 threads generate the 32 x 32 operator tile, one Philox block each, with the plain
+//     path's generator (simt::gen_p_tile_by, two 16-wide halves);
+//  3. the nonzeros are staged in shared memory; warp w takes, in entry order, those with
+//     column j = w (mod 8), lane l adding P(l, k) * v to row l of column j.  Iterations with
+//     more than 256 nonzeros read the rest directly.
+// Each output has a single owner that adds in k order, and K ranges are summed in order by
+// spmm_reduce_kernel, so results do not depend on scheduling.
+constexpr int kGenRows = 32;
+constexpr int kGenK = 2 * simt::BK;         // k's per iteration
+constexpr int kGenWarps = simt::NT / 32;
+constexpr int kGenStage = simt::NT;         // nonzeros staged per iteration
+constexpr size_t kGenSpmmMaxSmem = 200 * 1024;
+
+template <typename T>
+size_t gen_spmm_smem(int64_t N) {
+    return sizeof(T) * ((size_t)kGenK * (kGenRows + 4) + (size_t)N * (kGenRows + 1)) +
+           (sizeof(int32_t) + sizeof(T) + 1) * kGenStage + 2 * sizeof(int64_t) * (kGenK + 1) +
+           8;  // alignment of the row starts
+}
+
+// Row (within the iteration) of entry e: the last q in [0, kn) with rs[q] <= e.
+__device__ __forceinline__ int row_in_iteration(const int64_t *rs, int kn, int64_t e) {
+    int lo = 0, hi = kn;  // rs[lo] <= e < rs[hi] for a well-formed row range
+    while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (rs[mid] <= e) lo = mid;
+        else hi = mid;
+    }
+    return lo;
+}
+
+template <typename T, typename I>
+__global__ void __launch_bounds__(simt::NT)
+    gen_spmm_kernel(int64_t M, int64_t N, int64_t K, POperand P, const I *__restrict__ ptr,
+                    const I *__restrict__ idx, const T *__restrict__ val, int64_t nnz,
+                    int64_t k_per_split, T alpha, T beta, T *out, int64_t os_i, int64_t os_j,
+                    T *partial) {
+    extern __shared__ __align__(16) unsigned char gen_smem[];
+    using PsRow = T[kGenRows + 4];
+    PsRow *Ps = reinterpret_cast<PsRow *>(gen_smem);  // kGenK rows
+    T *tile = reinterpret_cast<T *>(gen_smem + sizeof(T) * kGenK * (kGenRows + 4));
+    T *st_v = tile + N * (kGenRows + 1);
+    int32_t *st_j = reinterpret_cast<int32_t *>(st_v + kGenStage);
+    uint8_t *st_k = reinterpret_cast<uint8_t *>(st_j + kGenStage);
+    int64_t *rs_all = reinterpret_cast<int64_t *>(
+        (reinterpret_cast<uintptr_t>(st_k + kGenStage) + 7) & ~uintptr_t(7));  // [2][kGenK + 1]
+    const int64_t i0 = (int64_t)blockIdx.x * kGenRows;
+    const int64_t kb = (int64_t)blockIdx.y * k_per_split;
+    const int64_t ke = min(K, kb + k_per_split);
+    const int64_t iters = (ke - kb + kGenK - 1) / kGenK;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    // row starts, clamped to the entry arrays (a malformed range then holds no entries)
+    auto row_start = [&](int64_t k) {
+        return max((int64_t)0, min((int64_t)ptr[k], nnz));
+    };
+    for (int64_t t = tid; t < N * (kGenRows + 1); t += simt::NT) tile[t] = (T)0;
+    if (tid <= kGenK && kb + tid <= ke) rs_all[tid] = row_start(kb + tid);
+    __syncthreads();
+    for (int64_t it = 0; it < iters; ++it) {
+        const int64_t k0 = kb + it * kGenK;
+        const int kn = (int)min((int64_t)kGenK, ke - k0);
+        const int64_t *rs = rs_all + (it & 1) * (kGenK + 1);
+        int64_t *rs_next = rs_all + ((it + 1) & 1) * (kGenK + 1);
+        const int64_t e_begin = rs[0], e_end = max(rs[kn], e_begin);
+        // 1. loads in flight during generation
+        const int64_t e = e_begin + tid;
+        const bool have = e < e_end;
+        int64_t j = -1;
+        T v = (T)0;
+        if (have) {
+            j = (int64_t)idx[e];
+            v = val[e];
+        }
+        int64_t rn = 0;
+        const bool next_rs = tid <= kGenK && k0 + kGenK + tid <= ke;
+        if (next_rs) rn = row_start(k0 + kGenK + tid);
+        // 2. the 32 x 32 operator tile, one 16-wide half per 128 threads
+        const int half = tid >> 7;
+        simt::gen_p_tile_by<T, kGenRows, simt::NT / 2>(Ps + half * simt::BK, P, M, K, i0,
+                                                       k0 + half * simt::BK, tid & 127);
+        // 3. stage, then apply
+        if (have) {
+            st_j[tid] = (j >= 0 && j < N) ? (int32_t)j : -1;
+            st_v[tid] = v;
+            st_k[tid] = (uint8_t)row_in_iteration(rs, kn, e);
+        }
+        if (next_rs) rs_next[tid] = rn;
+        __syncthreads();
+        const int64_t staged = min(e_end - e_begin, (int64_t)kGenStage);
+        for (int64_t b = 0; b < staged; b += 32) {
+            const int64_t q = b + lane;
+            const int32_t jq = q < staged ? st_j[q] : -1;
+            unsigned mask = __ballot_sync(0xffffffffu, jq >= 0 && (jq & (kGenWarps - 1)) == warp);
+            while (mask) {
+                const int src = __ffs(mask) - 1;
+                mask &= mask - 1;
+                const int64_t slot = b + src;
+                T &o = tile[(int64_t)st_j[slot] * (kGenRows + 1) + lane];
+                o = fma(Ps[st_k[slot]][lane], st_v[slot], o);
+            }
+        }
+        for (int64_t eb = e_begin + kGenStage; eb < e_end; eb += 32) {  // beyond the stage
+            const int64_t eq = eb + lane;
+            const bool in = eq < e_end;
+            const int64_t jq = in ? (int64_t)idx[eq] : -1;
+            const T vq = in ? val[eq] : (T)0;
+            const int kq = in ? row_in_iteration(rs, kn, eq) : 0;
+            unsigned mask = __ballot_sync(
+                0xffffffffu, in && jq >= 0 && jq < N && (int)(jq & (kGenWarps - 1)) == warp);
+            while (mask) {
+                const int src = __ffs(mask) - 1;
+                mask &= mask - 1;
+                const int64_t jj = __shfl_sync(0xffffffffu, jq, src);
+                const T vv = __shfl_sync(0xffffffffu, vq, src);
+                const int kk = __shfl_sync(0xffffffffu, kq, src);
+                T &o = tile[jj * (kGenRows + 1) + lane];
+                o = fma(Ps[kk][lane], vv, o);
+            }
+        }
+        __syncthreads();  // Ps, the stage and rs are rewritten next iteration
+    }
+    const int64_t rows = min((int64_t)kGenRows, M - i0);
+    if (partial) {
+        T *dst = partial + ((int64_t)blockIdx.y * M + i0) * N;
+        for (int64_t t = tid; t < rows * N; t += simt::NT) {
+            const int64_t i = t / N, jc = t % N;
+            dst[i * N + jc] = tile[jc * (kGenRows + 1) + i];
+        }
+        return;
+    }
+    const bool j_fast = os_j <= os_i;
+    for (int64_t t = tid; t < rows * N; t += simt::NT) {
+        const int64_t i = j_fast ? t / N : t % rows;
+        const int64_t jc = j_fast ? t % N : t / rows;
+        T &o = out[(i0 + i) * os_i + jc * os_j];
+        const T acc = tile[jc * (kGenRows + 1) + i];
+        o = (beta == (T)0) ? alpha * acc : fma(alpha, acc, beta * o);
+    }
+}
+
+template <typename T, typename I>
+void gen_spmm_rows(int64_t M, int64_t N, int64_t K, double alpha, const POperand &P,
+                   const void *ptr, const void *idx, const void *val, int64_t nnz, double beta,
+                   void *out, int64_t os_i, int64_t os_j, cudaStream_t s) {
+    const size_t smem = gen_spmm_smem<T>(N);
+    auto kernel = gen_spmm_kernel<T, I>;
+    RBG_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)smem));
+    int per_sm = 0;
+    RBG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, simt::NT, smem));
+    const int64_t tiles = (M + kGenRows - 1) / kGenRows;
+    const int64_t steps = (K + kGenK - 1) / kGenK;
+    const int64_t slots = (int64_t)num_sms() * std::max(1, per_sm);
+    // fill the resident slots, keeping at least 8 iterations per split and the partials
+    // <= 1 GiB
+    int64_t splits = std::max<int64_t>(1, slots / tiles);
+    splits = std::min<int64_t>(splits, std::max<int64_t>(1, steps / 8));
+    splits = std::min<int64_t>(splits, std::max<int64_t>(1, (int64_t(1) << 30) /
+                                                               (M * N * (int64_t)sizeof(T))));
+    const int64_t k_per_split = ((steps + splits - 1) / splits) * kGenK;
+    splits = (K + k_per_split - 1) / k_per_split;
+    Scratch ws;
+    T *partial = nullptr;
+    if (splits > 1) {
+        ws.alloc(sizeof(T) * (size_t)(splits * M * N), s);
+        partial = ws.as<T>();
+    }
+    {
+        ProfScope prof("gen_spmm", s);
+        kernel<<<dim3((unsigned)tiles, (unsigned)splits), simt::NT, smem, s>>>(
+            M, N, K, P, static_cast<const I *>(ptr), static_cast<const I *>(idx),
+            static_cast<const T *>(val), nnz, k_per_split, (T)alpha, (T)beta,
+            static_cast<T *>(out), os_i, os_j, partial);
+        RBG_LAUNCHED();
+    }
+    if (splits > 1) {
+        ProfScope prof("gen_spmm_reduce", s);
+        spmm_reduce_kernel<T><<<grid1d(M * N, 256), 256, 0, s>>>(M, N, (int)splits, partial,
+                                                                (T)alpha, (T)beta,
+                                                                static_cast<T *>(out), os_i, os_j);
+        RBG_LAUNCHED();
+    }
+}
+
 }  // namespace
+
+bool gen_spmm_applies(int dtype, int64_t N) {
+    return N >= 1 && (dtype == RBG_F32 ? gen_spmm_smem<float>(N) : gen_spmm_smem<double>(N)) <=
+                         kGenSpmmMaxSmem;
+}
+
+void gen_spmm_sketch(int dtype, int itype, int64_t M, int64_t N, int64_t K, double alpha,
+                     const POperand &P, const void *ptr, const void *idx, const void *val,
+                     int64_t nnz, double beta, void *out, int64_t os_i, int64_t os_j,
+                     cudaStream_t s) {
+    if (M <= 0 || N <= 0) return;
+    if (K <= 0 || alpha == 0.0) {
+        launch_scale(dtype, M, N, os_i, os_j, beta, out, s);
+        return;
+    }
+    if (dtype == RBG_F32 && itype == RBG_I32)
+        gen_spmm_rows<float, int32_t>(M, N, K, alpha, P, ptr, idx, val, nnz, beta, out, os_i,
+                                      os_j, s);
+    else if (dtype == RBG_F32)
+        gen_spmm_rows<float, int64_t>(M, N, K, alpha, P, ptr, idx, val, nnz, beta, out, os_i,
+                                      os_j, s);
+    else if (itype == RBG_I32)
+        gen_spmm_rows<double, int32_t>(M, N, K, alpha, P, ptr, idx, val, nnz, beta, out, os_i,
+                                       os_j, s);
+    else
+        gen_spmm_rows<double, int64_t>(M, N, K, alpha, P, ptr, idx, val, nnz, beta, out, os_i,
+                                       os_j, s);
+}
 
 void spmm_sketch(int dtype, int64_t M, int64_t N, int64_t K, double alpha,
                  const SparseOperand &Sp, const Strided &Q, double beta, void *out,

@@ -331,3 +331,54 @@ def test_saso_prefilled_matches_sampled(rb):
     rel = (torch.linalg.norm(B_fill.double() - B_gen.double()) /
            torch.linalg.norm(B_gen.double())).item()
     assert rel <= 1e-6, rel
+
+
+def test_sketch_sparse_generated_operator_fused(rb):
+    """sketch_sparse with an unfilled dense operator and CSR data (left) or CSC data (right)
+    generates the operator inside the SpMM (gen_spmm) instead of filling it first: the result
+    matches the materialised operator's path (the operator filled explicitly) to FP32
+    rounding, and repeats bit for bit.  The workload is the benchmark's: a Gaussian 1024 x 2^17
+    operator and the 2^17 x 512 random_csr matrix with 5 nonzeros per row."""
+    import torch
+    d, m, n = 1024, 1 << 17, 512
+    A, _ = rb.random_csr(m, n, 5 / n, rb.RNGState(11), dtype=torch.float32)
+    D = rb.DenseDist(d, m, rb.ScalarDist.Gaussian)
+
+    def left(S):
+        B = torch.empty(d * n, device="cuda")
+        rb.sketch_sparse(rb.Layout.RowMajor, rb.Op.NoTrans, rb.Op.NoTrans, d, n, m, 1.0, S, 0,
+                         0, A, 0.0, B, n)
+        return B
+
+    S = rb.DenseSkOp(D, rb.RNGState(5))
+    got, names = _kernels(rb, lambda: left(S))
+    assert "gen_spmm" in names and "spmm_row_lists" not in names, names
+    again = left(rb.DenseSkOp(D, rb.RNGState(5)))
+    assert torch.equal(got, again)
+    Sf = rb.DenseSkOp(D, rb.RNGState(5))
+    rb.fill_dense(Sf)
+    ref, names_f = _kernels(rb, lambda: left(Sf))
+    assert "gen_spmm" not in names_f
+    rel = float(torch.linalg.vector_norm(got - ref) / torch.linalg.vector_norm(ref))
+    assert rel <= 1e-6, rel
+    print("fused vs materialised operator: rel", rel)
+
+    # right side: B (mr x dr) = A_csc (mr x nr) * S (nr x dr); the fused kernel's output
+    # columns are B's rows, so the right side takes it for moderate mr
+    mr, nr, dr = 300, 1 << 14, 256
+    Ac, _ = rb.random_csc(mr, nr, 0.01, rb.RNGState(12), dtype=torch.float32)
+    Dr = rb.DenseDist(nr, dr, rb.ScalarDist.Uniform)
+
+    def right(S):
+        B = torch.zeros(mr * dr, device="cuda")
+        rb.sketch_sparse(rb.Layout.ColMajor, rb.Op.NoTrans, rb.Op.NoTrans, mr, dr, nr, 1.0, Ac,
+                         S, 0, 0, 0.0, B, mr)
+        return B
+
+    got_r, names_r = _kernels(rb, lambda: right(rb.DenseSkOp(Dr, rb.RNGState(6))))
+    assert "gen_spmm" in names_r, names_r
+    Srf = rb.DenseSkOp(Dr, rb.RNGState(6))
+    rb.fill_dense(Srf)
+    ref_r = right(Srf)
+    rel_r = float(torch.linalg.vector_norm(got_r - ref_r) / torch.linalg.vector_norm(ref_r))
+    assert rel_r <= 1e-6, rel_r
