@@ -547,7 +547,8 @@ def bench_more_rows(torch, rb, device, stream, hbm):
                                                     Acsr, 0.0, Bs, ns), 5, 2, stream)
     out["sketch_sparse"] = {
         "workload": "Gaussian 1024 x 2^17 operator (RNGState(5)) times that 2^17 x 512 CSR "
-                    "matrix; the operator is materialised as in the reference",
+                    "matrix; the operator is generated inside the SpMM (the reference fills it "
+                    "first)",
         "ms": round(ms, 4), "GFLOP/s": round(2.0 * ds * nnz_csr / (ms * 1e-3) / 1e9, 1)}
     return out
 
