@@ -44,6 +44,8 @@ enum { RBG_F32 = 0, RBG_F64 = 1 };
 enum { RBG_BF16 = 2 };
 enum { RBG_I32 = 0, RBG_I64 = 1 };
 enum { RBG_COO = 0, RBG_CSR = 1, RBG_CSC = 2 };
+/* NonzeroSort (RandBLAS/sparse_data/base.hh:108-117), with the reference's character values. */
+enum { RBG_SORT_CSC = 'C', RBG_SORT_CSR = 'R', RBG_SORT_NONE = 'N' };
 enum { RBG_PREC_BF16 = 0, RBG_PREC_FP8_E4M3 = 1 };
 
 enum {
@@ -235,6 +237,38 @@ int rbg_random_sparse_fill(rbg_random_sparse h, int32_t dtype, int32_t itype, vo
  * words_drawn: stream words the reference's loop draws.  Either pointer may be NULL. */
 int rbg_random_sparse_info(rbg_random_sparse h, int64_t *near_ties, int64_t *words_drawn);
 int rbg_random_sparse_destroy(rbg_random_sparse h);
+
+/* ------------------------------------------------------------------ sparse data conversions */
+
+/* The building blocks of RandBLAS's csr_to_coo / csc_to_coo / coo_to_csr / coo_to_csc
+ * (RandBLAS/sparse_data/conversions.hh:49-121), on device arrays.  Each performs the
+ * reference's checks with its messages and synchronises `stream`.  Index arrays are int32 or
+ * int64 (ptr_itype / idx_itype / itype: RBG_I32 or RBG_I64), independently.
+ *
+ * compressed_ptr_to_sorted_idxs (RandBLAS/sparse_data/base.hh:292-302): idxs[0 ..) gets index j
+ * repeated ptr[j + 1] - ptr[j] times, for j < num_comp.  Requires len_idxs >= ptr[num_comp]
+ * and no negative segment. */
+int rbg_compressed_ptr_to_sorted_idxs(int64_t num_comp, int32_t ptr_itype, const void *ptr,
+                                      int64_t len_idxs, int32_t idx_itype, void *idxs,
+                                      rbg_stream_t stream);
+/* sorted_idxs_to_compressed_ptr (RandBLAS/sparse_data/base.hh:278-290): ptr[0] = 0 and
+ * ptr[i + 1] = the number of idxs <= i, for the reference's walk.  A leading negative index
+ * leaves every pointer 0, and indices >= num_comp are not counted.  Requires sorted idxs. */
+int rbg_sorted_idxs_to_compressed_ptr(int64_t len_idxs, int32_t idx_itype, const void *idxs,
+                                      int64_t num_comp, int32_t ptr_itype, void *ptr,
+                                      rbg_stream_t stream);
+/* coo_arrays_determine_sort (RandBLAS/sparse_data/base.hh:142-167): *sort = RBG_SORT_CSC if the
+ * entries are in CSC order (ties allowed), else RBG_SORT_CSR if in CSR order, else
+ * RBG_SORT_NONE. */
+int rbg_coo_determine_sort(int32_t itype, int64_t nnz, const void *rows, const void *cols,
+                           int32_t *sort, rbg_stream_t stream);
+/* coo_arrays_apply_sort / COOMatrix::sort_arrays (RandBLAS/sparse_data/base.hh:169-220,
+ * coo_matrix.hh:222-226): sorts (vals, rows, cols) in place by (row, col) for RBG_SORT_CSR or
+ * (col, row) for RBG_SORT_CSC.  No-op for RBG_SORT_NONE or when the entries are already in that
+ * order.  Entries with equal (row, col) keep their relative order (the reference's std::sort
+ * leaves it unspecified).  dtype: RBG_F32 or RBG_F64. */
+int rbg_coo_apply_sort(int32_t sort, int32_t dtype, int32_t itype, int64_t nnz, void *vals,
+                       void *rows, void *cols, rbg_stream_t stream);
 
 /* ------------------------------------------------------------------ dense operators */
 

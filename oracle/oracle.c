@@ -38,6 +38,8 @@
  *   sparse compute_next_state  RandBLAS/sparse_skops.hh:266-283
  *   PhiloxStream, random_csr/csc/coo
  *                              RandBLAS/sparse_data/random_matrix.hh:63-121, 135-355
+ *   compressed_ptr_to_sorted_idxs, sorted_idxs_to_compressed_ptr, coo_arrays_determine_sort,
+ *   coo_arrays_apply_sort .... RandBLAS/sparse_data/base.hh:119-220, 278-302
  *
  * Build: gcc -O2 -std=gnu11 -fPIC -shared -ffp-contract=off -fopenmp (oracle/build.py).
  */
@@ -515,4 +517,101 @@ int64_t orc_random_sparse(int fmt, int dtype, int itype, int64_t m, int64_t n, d
     }
     *next = p.s;
     return k;
+}
+
+/* ------------------------------------------------------ sparse conversions */
+
+static int64_t get_idx(int itype, const void *p, int64_t i) {
+    return itype == ORC_I32 ? (int64_t)((const int32_t *)p)[i] : ((const int64_t *)p)[i];
+}
+
+/*
+ * compressed_ptr_to_sorted_idxs (sparse_data/base.hh:292-302): index j repeated
+ * ptr[j + 1] - ptr[j] times, from idxs[0].  Returns 1 if len_idxs < ptr[num_comp], 2 at the
+ * first negative segment length (after writing the segments before it), else 0.
+ */
+int orc_compressed_ptr_to_sorted_idxs(int64_t num_comp, int ptr_itype, const void *ptr,
+                                      int64_t len_idxs, int idx_itype, void *idxs) {
+    if (len_idxs < get_idx(ptr_itype, ptr, num_comp)) return 1;
+    int64_t out = 0;
+    for (int64_t j = 0; j < num_comp; ++j) {
+        int64_t cnt = get_idx(ptr_itype, ptr, j + 1) - get_idx(ptr_itype, ptr, j);
+        if (cnt < 0) return 2;
+        for (int64_t t = 0; t < cnt; ++t) put_idx(idx_itype, idxs, out++, j);
+    }
+    return 0;
+}
+
+/*
+ * sorted_idxs_to_compressed_ptr (sparse_data/base.hh:278-290): returns 1 if idxs is not
+ * sorted; else ptr[0] = 0 and ptr[i + 1] = the position after walking past the entries equal
+ * to i, in order.
+ */
+int orc_sorted_idxs_to_compressed_ptr(int64_t len_idxs, int idx_itype, const void *idxs,
+                                      int64_t num_comp, int ptr_itype, void *ptr) {
+    for (int64_t i = 1; i < len_idxs; ++i)
+        if (get_idx(idx_itype, idxs, i - 1) > get_idx(idx_itype, idxs, i)) return 1;
+    put_idx(ptr_itype, ptr, 0, 0);
+    int64_t ell = 0;
+    for (int64_t i = 0; i < num_comp; ++i) {
+        while (ell < len_idxs && get_idx(idx_itype, idxs, ell) == i) ++ell;
+        put_idx(ptr_itype, ptr, i + 1, ell);
+    }
+    return 0;
+}
+
+/* coo_arrays_determine_sort (sparse_data/base.hh:119-167): 'C', 'R' or 'N'. */
+int orc_coo_determine_sort(int itype, int64_t nnz, const void *rows, const void *cols) {
+    int csc = 1, csr = 1;
+    for (int64_t e = 1; e < nnz && (csc || csr); ++e) {
+        int64_t i0 = get_idx(itype, rows, e - 1), j0 = get_idx(itype, cols, e - 1);
+        int64_t i1 = get_idx(itype, rows, e), j1 = get_idx(itype, cols, e);
+        if (csc) csc = j0 < j1 || (j0 == j1 && i0 <= i1);
+        if (csr) csr = i0 < i1 || (i0 == i1 && j0 <= j1);
+    }
+    return csc ? 'C' : csr ? 'R' : 'N';
+}
+
+typedef struct {
+    int64_t major, minor, pos;
+} orc_sort_key;
+
+static int cmp_sort_key(const void *a, const void *b) {
+    const orc_sort_key *x = (const orc_sort_key *)a, *y = (const orc_sort_key *)b;
+    if (x->major != y->major) return x->major < y->major ? -1 : 1;
+    if (x->minor != y->minor) return x->minor < y->minor ? -1 : 1;
+    return x->pos < y->pos ? -1 : x->pos > y->pos;  /* equal keys keep their order */
+}
+
+/*
+ * coo_arrays_apply_sort (sparse_data/base.hh:169-220): sort (vals, rows, cols) by (row, col)
+ * for 'R' or (col, row) for 'C'; no-op for 'N' or when already in that order.  Equal keys keep
+ * their relative order (the reference's std::sort leaves it unspecified).
+ */
+int orc_coo_apply_sort(int sort, int dtype, int itype, int64_t nnz, void *vals, void *rows,
+                       void *cols) {
+    if (sort == 'N' || orc_coo_determine_sort(itype, nnz, rows, cols) == sort) return 0;
+    orc_sort_key *k = (orc_sort_key *)malloc(sizeof(orc_sort_key) * (size_t)(nnz > 0 ? nnz : 1));
+    size_t vsz = dtype == ORC_F32 ? 4 : 8, isz = itype == ORC_I32 ? 4 : 8;
+    char *tv = (char *)malloc(vsz * (size_t)(nnz > 0 ? nnz : 1));
+    char *tr = (char *)malloc(isz * (size_t)(nnz > 0 ? nnz : 1));
+    char *tc = (char *)malloc(isz * (size_t)(nnz > 0 ? nnz : 1));
+    if (!k || !tv || !tr || !tc) { free(k); free(tv); free(tr); free(tc); return 2; }
+    for (int64_t e = 0; e < nnz; ++e) {
+        int64_t r = get_idx(itype, rows, e), c = get_idx(itype, cols, e);
+        k[e].major = sort == 'R' ? r : c;
+        k[e].minor = sort == 'R' ? c : r;
+        k[e].pos = e;
+    }
+    qsort(k, (size_t)nnz, sizeof(orc_sort_key), cmp_sort_key);
+    for (int64_t e = 0; e < nnz; ++e) {
+        memcpy(tv + vsz * e, (char *)vals + vsz * k[e].pos, vsz);
+        memcpy(tr + isz * e, (char *)rows + isz * k[e].pos, isz);
+        memcpy(tc + isz * e, (char *)cols + isz * k[e].pos, isz);
+    }
+    memcpy(vals, tv, vsz * (size_t)nnz);
+    memcpy(rows, tr, isz * (size_t)nnz);
+    memcpy(cols, tc, isz * (size_t)nnz);
+    free(k); free(tv); free(tr); free(tc);
+    return 0;
 }

@@ -57,6 +57,10 @@ def _ptr(a: np.ndarray) -> int:
     return a.ctypes.data
 
 
+def _it(dtype) -> int:
+    return 0 if np.dtype(dtype) == np.int32 else 1
+
+
 class Oracle:
     """The C restatement (oracle/oracle.c)."""
 
@@ -87,6 +91,14 @@ class Oracle:
         L.orc_sparse_next_state.argtypes = [INT, I64, I64, I64, P, P]
         L.orc_random_sparse.argtypes = [INT, INT, INT, I64, I64, C.c_double, P, I64, P, P, P, P]
         L.orc_random_sparse.restype = I64
+        L.orc_compressed_ptr_to_sorted_idxs.argtypes = [I64, INT, P, I64, INT, P]
+        L.orc_compressed_ptr_to_sorted_idxs.restype = INT
+        L.orc_sorted_idxs_to_compressed_ptr.argtypes = [I64, INT, P, I64, INT, P]
+        L.orc_sorted_idxs_to_compressed_ptr.restype = INT
+        L.orc_coo_determine_sort.argtypes = [INT, I64, P, P]
+        L.orc_coo_determine_sort.restype = INT
+        L.orc_coo_apply_sort.argtypes = [INT, INT, INT, I64, P, P, P]
+        L.orc_coo_apply_sort.restype = INT
 
     # -- RNG ------------------------------------------------------------------------
     def philox(self, counter, key) -> tuple:
@@ -195,6 +207,39 @@ class Oracle:
         return _random_sparse(self.lib.orc_random_sparse, fmt, dtype, itype, m, n, density,
                               seed, lambda rc: ValueError(f"orc_random_sparse failed ({rc})"))
 
+    # -- sparse conversions (sparse_data/base.hh:119-220, 278-302) -------------------
+    def compressed_ptr_to_sorted_idxs(self, ptr: np.ndarray, len_idxs: int, idx_dtype):
+        """-> idxs (len_idxs entries, those past ptr[-1] - ptr[0] zero); raises on a failed
+        check (1: len_idxs < ptr[num_comp], 2: negative segment)."""
+        idxs = np.zeros(max(len_idxs, 1), idx_dtype)
+        rc = self.lib.orc_compressed_ptr_to_sorted_idxs(
+            ptr.size - 1, _it(ptr.dtype), _ptr(ptr), len_idxs, _it(idx_dtype), _ptr(idxs))
+        if rc:
+            raise ValueError(f"compressed_ptr_to_sorted_idxs check {rc} failed")
+        return idxs[:len_idxs]
+
+    def sorted_idxs_to_compressed_ptr(self, idxs: np.ndarray, num_comp: int, ptr_dtype):
+        ptr = np.zeros(num_comp + 1, ptr_dtype)
+        rc = self.lib.orc_sorted_idxs_to_compressed_ptr(idxs.size, _it(idxs.dtype), _ptr(idxs),
+                                                        num_comp, _it(ptr_dtype), _ptr(ptr))
+        if rc:
+            raise ValueError("sorted_idxs_to_compressed_ptr: indices not sorted")
+        return ptr
+
+    def coo_determine_sort(self, rows: np.ndarray, cols: np.ndarray) -> str:
+        return chr(self.lib.orc_coo_determine_sort(_it(rows.dtype), rows.size, _ptr(rows),
+                                                   _ptr(cols)))
+
+    def coo_apply_sort(self, sort: str, vals, rows, cols):
+        """Sorts copies; returns (vals, rows, cols)."""
+        vals, rows, cols = vals.copy(), rows.copy(), cols.copy()
+        rc = self.lib.orc_coo_apply_sort(ord(sort), 0 if vals.dtype == np.float32 else 1,
+                                         _it(rows.dtype), vals.size, _ptr(vals), _ptr(rows),
+                                         _ptr(cols))
+        if rc:
+            raise MemoryError("orc_coo_apply_sort")
+        return vals, rows, cols
+
     def sparse_dense_matrix(self, dtype, D_rows, D_cols, vec_nnz, major_axis, seed: State):
         vals, rows, cols, _, _ = self.fill_sparse(dtype, 1, D_rows, D_cols, vec_nnz, major_axis,
                                                   seed)
@@ -284,6 +329,10 @@ class RefLib:
                                         I64, I64, INT, P, P, I64, I64, P, I64, C.c_double, P, I64]
         L.rbref_sketch_vector.argtypes = [INT, INT, I64, I64, C.c_double, I64, I64, INT, INT, P,
                                           P, I64, I64, P, I64, C.c_double, P, I64]
+        L.rbref_compressed_ptr_to_sorted_idxs.argtypes = [I64, INT, P, I64, INT, P]
+        L.rbref_sorted_idxs_to_compressed_ptr.argtypes = [I64, INT, P, I64, INT, P]
+        L.rbref_coo_determine_sort.argtypes = [INT, I64, P, P, P]
+        L.rbref_coo_apply_sort.argtypes = [INT, INT, INT, I64, P, P, P]
         L.rbref_random_sparse.argtypes = [INT, INT, INT, I64, I64, C.c_double, P, P, I64, P, P,
                                           P, P, P, P]
         L.rbref_sketch_sparse.argtypes = [INT, INT, INT, INT, INT, I64, I64, I64, C.c_double,
@@ -293,6 +342,31 @@ class RefLib:
     def _check(self, rc):
         if rc:
             raise RuntimeError(f"reference error {rc}: {self.lib.rbref_last_error().decode()}")
+
+    def compressed_ptr_to_sorted_idxs(self, ptr: np.ndarray, len_idxs: int, idx_dtype):
+        idxs = np.zeros(max(len_idxs, 1), idx_dtype)
+        self._check(self.lib.rbref_compressed_ptr_to_sorted_idxs(
+            ptr.size - 1, _it(ptr.dtype), _ptr(ptr), len_idxs, _it(idx_dtype), _ptr(idxs)))
+        return idxs[:len_idxs]
+
+    def sorted_idxs_to_compressed_ptr(self, idxs: np.ndarray, num_comp: int, ptr_dtype):
+        ptr = np.zeros(num_comp + 1, ptr_dtype)
+        self._check(self.lib.rbref_sorted_idxs_to_compressed_ptr(
+            idxs.size, _it(idxs.dtype), _ptr(idxs), num_comp, _it(ptr_dtype), _ptr(ptr)))
+        return ptr
+
+    def coo_determine_sort(self, rows: np.ndarray, cols: np.ndarray) -> str:
+        out = C.c_int()
+        self._check(self.lib.rbref_coo_determine_sort(_it(rows.dtype), rows.size, _ptr(rows),
+                                                      _ptr(cols), C.addressof(out)))
+        return chr(out.value)
+
+    def coo_apply_sort(self, sort: str, vals, rows, cols):
+        vals, rows, cols = vals.copy(), rows.copy(), cols.copy()
+        self._check(self.lib.rbref_coo_apply_sort(ord(sort), 0 if vals.dtype == np.float32 else 1,
+                                                  _it(rows.dtype), vals.size, _ptr(vals),
+                                                  _ptr(rows), _ptr(cols)))
+        return vals, rows, cols
 
     def random_sparse(self, fmt, dtype, itype, m, n, density, seed: State):
         """The reference's random_coo / random_csr / random_csc; same returns as Oracle's."""

@@ -16,6 +16,9 @@
 //   rbref_sketch_saso ........... RandBLAS::sketch_general, SparseSkOp (RandBLAS/skge.hh:776,948)
 //   rbref_sketch_vector ......... RandBLAS::sketch_vector         (RandBLAS/skve.hh:140-164)
 //   rbref_sketch_sparse ......... RandBLAS::sketch_sparse         (RandBLAS/sparse_data/sksp.hh:418-539)
+//   rbref_compressed_ptr_to_sorted_idxs, rbref_sorted_idxs_to_compressed_ptr,
+//   rbref_coo_determine_sort, rbref_coo_apply_sort
+//                                 (RandBLAS/sparse_data/base.hh:142-220, 278-302)
 //   rbref_random_sparse ......... random_coo / random_csr / random_csc
 //                                 (RandBLAS/sparse_data/random_matrix.hh:135-355)
 #include <RandBLAS.hh>
@@ -377,6 +380,92 @@ int rbref_random_sparse(int fmt, int dtype, int itype, int64_t m, int64_t n, dou
         else
             *nnz = random_sparse_t<double, int64_t>(fmt, m, n, density, seed, cap, vals, a, b, next);
         put_state(next, next_ctr, next_key);
+    });
+}
+
+}  // extern "C"
+
+// ------------------------------------------------------------------ sparse conversions
+namespace {
+
+template <typename F>
+int by_itype2(int it1, int it2, F &&f) {
+    if (it1 == 0 && it2 == 0) f(int32_t{}, int32_t{});
+    else if (it1 == 0) f(int32_t{}, int64_t{});
+    else if (it2 == 0) f(int64_t{}, int32_t{});
+    else f(int64_t{}, int64_t{});
+    return 0;
+}
+
+char sort_char(RandBLAS::sparse_data::NonzeroSort s) {
+    using RandBLAS::sparse_data::NonzeroSort;
+    return s == NonzeroSort::CSC ? 'C' : s == NonzeroSort::CSR ? 'R' : 'N';
+}
+
+RandBLAS::sparse_data::NonzeroSort sort_of(int c) {
+    using RandBLAS::sparse_data::NonzeroSort;
+    return c == 'C' ? NonzeroSort::CSC : c == 'R' ? NonzeroSort::CSR : NonzeroSort::None;
+}
+
+}  // namespace
+
+extern "C" {
+
+// compressed_ptr_to_sorted_idxs (RandBLAS/sparse_data/base.hh:292-302)
+int rbref_compressed_ptr_to_sorted_idxs(int64_t num_comp, int ptr_itype, void *ptr,
+                                        int64_t len_idxs, int idx_itype, void *idxs) {
+    return guarded([&] {
+        by_itype2(ptr_itype, idx_itype, [&](auto p, auto q) {
+            using P = decltype(p);
+            using Q = decltype(q);
+            RandBLAS::sparse_data::compressed_ptr_to_sorted_idxs(num_comp, (P *)ptr, len_idxs,
+                                                                 (Q *)idxs);
+        });
+    });
+}
+
+// sorted_idxs_to_compressed_ptr (RandBLAS/sparse_data/base.hh:278-290)
+int rbref_sorted_idxs_to_compressed_ptr(int64_t len_idxs, int idx_itype, const void *idxs,
+                                        int64_t num_comp, int ptr_itype, void *ptr) {
+    return guarded([&] {
+        by_itype2(idx_itype, ptr_itype, [&](auto p, auto q) {
+            using P = decltype(p);
+            using Q = decltype(q);
+            RandBLAS::sparse_data::sorted_idxs_to_compressed_ptr(len_idxs, (const P *)idxs,
+                                                                 num_comp, (Q *)ptr);
+        });
+    });
+}
+
+// coo_arrays_determine_sort (RandBLAS/sparse_data/base.hh:142-167): 'C', 'R' or 'N'
+int rbref_coo_determine_sort(int itype, int64_t nnz, void *rows, void *cols, int *sort) {
+    return guarded([&] {
+        if (itype == 0)
+            *sort = sort_char(RandBLAS::sparse_data::coo_arrays_determine_sort(
+                nnz, (int32_t *)rows, (int32_t *)cols));
+        else
+            *sort = sort_char(RandBLAS::sparse_data::coo_arrays_determine_sort(
+                nnz, (int64_t *)rows, (int64_t *)cols));
+    });
+}
+
+// coo_arrays_apply_sort (RandBLAS/sparse_data/base.hh:169-220)
+int rbref_coo_apply_sort(int sort, int dtype, int itype, int64_t nnz, void *vals, void *rows,
+                         void *cols) {
+    return guarded([&] {
+        const auto s = sort_of(sort);
+        if (dtype == 0 && itype == 0)
+            RandBLAS::sparse_data::coo_arrays_apply_sort(s, nnz, (float *)vals, (int32_t *)rows,
+                                                         (int32_t *)cols);
+        else if (dtype == 0)
+            RandBLAS::sparse_data::coo_arrays_apply_sort(s, nnz, (float *)vals, (int64_t *)rows,
+                                                         (int64_t *)cols);
+        else if (itype == 0)
+            RandBLAS::sparse_data::coo_arrays_apply_sort(s, nnz, (double *)vals,
+                                                         (int32_t *)rows, (int32_t *)cols);
+        else
+            RandBLAS::sparse_data::coo_arrays_apply_sort(s, nnz, (double *)vals,
+                                                         (int64_t *)rows, (int64_t *)cols);
     });
 }
 

@@ -8,7 +8,9 @@ batching front end (:mod:`randblas_gb300.batched`).
 from . import autograd, lowp, profile  # noqa: F401
 from ._lib import RandBLASError, lib  # noqa: F401
 from .api import (  # noqa: F401
-    Axis, COOMatrix, CSCMatrix, CSRMatrix, DenseDist, DenseSkOp, Layout, Op, RNGState,
+    Axis, COOMatrix, CSCMatrix, CSRMatrix, DenseDist, DenseSkOp, Layout, NonzeroSort, Op, RNGState,
+    compressed_ptr_to_sorted_idxs, coo_arrays_determine_sort, coo_to_csc, coo_to_csr, csc_to_coo,
+    csr_to_coo, sorted_idxs_to_compressed_ptr, transpose_as_coo, transpose_as_csc, transpose_as_csr,
     ScalarDist, SparseDist, SparseSkOp, deterministic, fill_dense, fill_dense_unpacked, fill_sparse,
     fill_sparse_unpacked_nosub, left_spmm, random_coo, random_csc, random_csr,
     repeated_fisher_yates, right_spmm, sketch_general,

@@ -156,6 +156,10 @@ SIGNATURES = {
     "rbg_random_sparse_fill": ([P, CI32, CI32, P, P, P, P], C.c_int),
     "rbg_random_sparse_info": ([P, C.POINTER(CI64), C.POINTER(CI64)], C.c_int),
     "rbg_random_sparse_destroy": ([P], C.c_int),
+    "rbg_compressed_ptr_to_sorted_idxs": ([CI64, CI32, P, CI64, CI32, P, P], C.c_int),
+    "rbg_sorted_idxs_to_compressed_ptr": ([CI64, CI32, P, CI64, CI32, P, P], C.c_int),
+    "rbg_coo_determine_sort": ([CI32, CI64, P, P, C.POINTER(CI32), P], C.c_int),
+    "rbg_coo_apply_sort": ([CI32, CI32, CI32, CI64, P, P, P, P], C.c_int),
 }
 
 _lock = threading.Lock()

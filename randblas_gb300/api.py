@@ -279,6 +279,13 @@ def repeated_fisher_yates(k: int, n: int, r: int, samples: torch.Tensor,
 
 
 # ------------------------------------------------------------------------- sparse data
+class NonzeroSort(IntEnum):
+    """NonzeroSort (sparse_data/base.hh:108-117); NONE stands for the reference's None."""
+    CSC = ord("C")
+    CSR = ord("R")
+    NONE = ord("N")
+
+
 @dataclass
 class COOMatrix:
     n_rows: int
@@ -286,9 +293,24 @@ class COOMatrix:
     vals: torch.Tensor
     rows: torch.Tensor
     cols: torch.Tensor
+    sort: NonzeroSort = NonzeroSort.NONE
 
     def _c(self):
         return _spmat(_lib.COO, self.n_rows, self.n_cols, self.vals, self.rows, self.cols)
+
+    def sort_arrays(self, s: NonzeroSort) -> None:
+        """COOMatrix::sort_arrays (sparse_data/coo_matrix.hh:222-226): sort the entries into
+        CSR or CSC order in place (equal (row, col) entries keep their order)."""
+        k = self.vals.numel()
+        call("rbg_coo_apply_sort", int(s), _DT[self.vals.dtype], _IT[self.rows.dtype], k,
+             _ptr(self.vals) if k else None, _ptr(self.rows) if k else None,
+             _ptr(self.cols) if k else None, _stream())
+        if s != NonzeroSort.NONE:
+            self.sort = NonzeroSort(s)
+
+    def deepcopy(self) -> "COOMatrix":
+        return COOMatrix(self.n_rows, self.n_cols, self.vals.clone(), self.rows.clone(),
+                         self.cols.clone(), self.sort)
 
 
 @dataclass
@@ -325,6 +347,95 @@ def _spmat(fmt, n_rows, n_cols, vals, a, b):
     m.idx_a = a.data_ptr() if a.numel() else None
     m.idx_b = b.data_ptr() if b.numel() else None
     return m
+
+
+# ------------------------------------------------------------------ sparse data conversions
+def coo_arrays_determine_sort(rows: torch.Tensor, cols: torch.Tensor) -> NonzeroSort:
+    """coo_arrays_determine_sort (sparse_data/base.hh:142-167)."""
+    out = C.c_int32()
+    k = rows.numel()
+    call("rbg_coo_determine_sort", _IT[rows.dtype], k, _ptr(rows) if k else None,
+         _ptr(cols) if k else None, C.byref(out), _stream())
+    return NonzeroSort(out.value)
+
+
+def compressed_ptr_to_sorted_idxs(ptr: torch.Tensor, len_idxs: int, dtype=None) -> torch.Tensor:
+    """compressed_ptr_to_sorted_idxs (sparse_data/base.hh:292-302): a new index tensor of
+    len_idxs entries (those past ptr[-1] - ptr[0] are zero)."""
+    dtype = dtype or ptr.dtype
+    idxs = torch.zeros(len_idxs, dtype=dtype, device=ptr.device)
+    call("rbg_compressed_ptr_to_sorted_idxs", ptr.numel() - 1, _IT[ptr.dtype], _ptr(ptr),
+         len_idxs, _IT[dtype], _ptr(idxs) if len_idxs else None, _stream())
+    return idxs
+
+
+def sorted_idxs_to_compressed_ptr(idxs: torch.Tensor, num_comp: int, dtype=None) -> torch.Tensor:
+    """sorted_idxs_to_compressed_ptr (sparse_data/base.hh:278-290): a new pointer tensor of
+    num_comp + 1 entries."""
+    dtype = dtype or idxs.dtype
+    ptr = torch.empty(num_comp + 1, dtype=dtype, device=idxs.device)
+    k = idxs.numel()
+    call("rbg_sorted_idxs_to_compressed_ptr", k, _IT[idxs.dtype], _ptr(idxs) if k else None,
+         num_comp, _IT[dtype], _ptr(ptr), _stream())
+    return ptr
+
+
+def csr_to_coo(A: "CSRMatrix") -> COOMatrix:
+    """csr_to_coo (sparse_data/conversions.hh:63-75): a new COOMatrix in CSR order."""
+    k = A.vals.numel()
+    rows = compressed_ptr_to_sorted_idxs(A.rowptr, k, A.colidxs.dtype)
+    return COOMatrix(A.n_rows, A.n_cols, A.vals.clone(), rows, A.colidxs.clone(),
+                     NonzeroSort.CSR)
+
+
+def csc_to_coo(A: "CSCMatrix") -> COOMatrix:
+    """csc_to_coo (sparse_data/conversions.hh:49-61): a new COOMatrix in CSC order."""
+    k = A.vals.numel()
+    cols = compressed_ptr_to_sorted_idxs(A.colptr, k, A.rowidxs.dtype)
+    return COOMatrix(A.n_rows, A.n_cols, A.vals.clone(), A.rowidxs.clone(), cols,
+                     NonzeroSort.CSC)
+
+
+def coo_to_csr(A: COOMatrix) -> "CSRMatrix":
+    """coo_to_csr (sparse_data/conversions.hh:101-121): a new CSRMatrix.  As in the reference,
+    A.sort == CSR is trusted; otherwise a sorted copy of A is compressed."""
+    B = A if A.sort == NonzeroSort.CSR else A.deepcopy()
+    if B is not A:
+        B.sort_arrays(NonzeroSort.CSR)
+    rowptr = sorted_idxs_to_compressed_ptr(B.rows, A.n_rows)
+    return CSRMatrix(A.n_rows, A.n_cols, B.vals if B is not A else A.vals.clone(), rowptr,
+                     B.cols if B is not A else A.cols.clone())
+
+
+def coo_to_csc(A: COOMatrix) -> "CSCMatrix":
+    """coo_to_csc (sparse_data/conversions.hh:79-99): a new CSCMatrix."""
+    B = A if A.sort == NonzeroSort.CSC else A.deepcopy()
+    if B is not A:
+        B.sort_arrays(NonzeroSort.CSC)
+    colptr = sorted_idxs_to_compressed_ptr(B.cols, A.n_cols)
+    return CSCMatrix(A.n_rows, A.n_cols, B.vals if B is not A else A.vals.clone(),
+                     B.rows if B is not A else A.rows.clone(), colptr)
+
+
+def transpose_as_csr(A: "CSCMatrix", share_memory: bool = True) -> "CSRMatrix":
+    """transpose_as_csr (sparse_data/conversions.hh:128-136): A^T as CSR over A's arrays."""
+    c = (lambda t: t) if share_memory else (lambda t: t.clone())
+    return CSRMatrix(A.n_cols, A.n_rows, c(A.vals), c(A.colptr), c(A.rowidxs))
+
+
+def transpose_as_csc(A: "CSRMatrix", share_memory: bool = True) -> "CSCMatrix":
+    """transpose_as_csc (sparse_data/conversions.hh:138-146): A^T as CSC over A's arrays."""
+    c = (lambda t: t) if share_memory else (lambda t: t.clone())
+    return CSCMatrix(A.n_cols, A.n_rows, c(A.vals), c(A.colidxs), c(A.rowptr))
+
+
+def transpose_as_coo(A: COOMatrix, share_memory: bool = True) -> COOMatrix:
+    """transpose_as_coo (sparse_data/conversions.hh:148-166): rows and cols swapped, the sort
+    flag swapped with them."""
+    c = (lambda t: t) if share_memory else (lambda t: t.clone())
+    flip = {NonzeroSort.CSC: NonzeroSort.CSR, NonzeroSort.CSR: NonzeroSort.CSC}
+    return COOMatrix(A.n_cols, A.n_rows, c(A.vals), c(A.cols), c(A.rows),
+                     flip.get(A.sort, NonzeroSort.NONE))
 
 
 # ------------------------------------------------------------------ random sparse matrices
@@ -377,7 +488,7 @@ def random_coo(m: int, n: int, density: float, state: RNGState, dtype=torch.floa
     """random_coo<T, sint_t>(m, n, density, state) (sparse_data/random_matrix.hh:296-355):
     entries in CSR order."""
     vals, rows, cols, nxt = _random_sparse(_lib.COO, m, n, density, state, dtype, itype)
-    return COOMatrix(m, n, vals, rows, cols), nxt
+    return COOMatrix(m, n, vals, rows, cols, NonzeroSort.CSR), nxt
 
 
 # ------------------------------------------------------------------------- sketching

@@ -21,7 +21,7 @@ BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "librandblas_gb300.so")
 
 SOURCES = ["capi.cu", "fill.cu", "gemm_simt.cu", "spmm.cu", "lowp_tc.cu", "batched.cu",
-           "symmetric.cu", "random_sparse.cu"]
+           "symmetric.cu", "random_sparse.cu", "sparse_convert.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -33,6 +33,14 @@ void set_last_error(const std::string &msg);
                             + (fn));                                                           \
     } while (0)
 
+// RBG_REQUIRE for a condition evaluated elsewhere (on the device, say): the same message with
+// the reference's condition text.
+inline void require_as(bool ok, const char *cond_text, const char *fn) {
+    if (!ok)
+        fail(RBG_ERROR_INVALID_ARGUMENT, std::string("(") + cond_text +
+                                             ") was required, but did not hold, in function " + fn);
+}
+
 void cuda_check(cudaError_t e, const char *what);
 #define RBG_CUDA(call) ::rbg::cuda_check((call), #call)
 

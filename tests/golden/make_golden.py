@@ -8,6 +8,9 @@ against the project's Random123 / BLAS++ stand-ins -- and records:
   test/test_basic_rng/r123_kat_vectors.txt (parsed from that file);
 * fill_dense.npz, fill_sparse.npz, sketch_*.npz: outputs of the reference's public functions on
   small seeded cases (every layout / op / side / submatrix combination the parity tests use);
+* sparse_convert.npz: the reference's coo_arrays_determine_sort / coo_arrays_apply_sort /
+  sorted_idxs_to_compressed_ptr / compressed_ptr_to_sorted_idxs on seeded duplicate-free COO
+  data;
 * random_sparse.npz: the reference's random_coo / random_csr / random_csc on small seeded
   cases (every format, value and index type, densities 0, 1 and in between, empty shapes);
 * full_size.json: SHA-256 digests and next states of the full-size operators of the
@@ -15,7 +18,8 @@ against the project's Random123 / BLAS++ stand-ins -- and records:
   matrix; the 1024 x 2^20 SASO with 8 nonzeros per column), so the GPU tests can pin those
   bit for bit without shipping the arrays.
 
-Usage: python tests/golden/make_golden.py [random_sparse]   (the argument writes only that file)
+Usage: python tests/golden/make_golden.py [random_sparse | sparse_convert]
+(an argument writes only that part)
 """
 from __future__ import annotations
 
@@ -94,8 +98,38 @@ def random_sparse_fixtures(ref):
                 vals_sha256=hashlib.sha256(vals.tobytes()).hexdigest())
 
 
+def sparse_convert_fixtures(ref):
+    rng = np.random.default_rng(2024)
+    arrays, meta = {}, []
+    for i in range(16):
+        m, n = int(rng.integers(1, 200)), int(rng.integers(1, 200))
+        nnz = int(rng.integers(0, min(m * n, 800) + 1))
+        it = np.int32 if i % 2 else np.int64
+        key = rng.choice(m * n, size=nnz, replace=False)  # duplicate-free, random order
+        if i % 6 == 1:
+            key = np.sort(key)  # already in CSR order
+        rows, cols = (key // n).astype(it), (key % n).astype(it)
+        vals = rng.standard_normal(nnz).astype(np.float32 if i % 3 else np.float64)
+        arrays[f"r{i}"], arrays[f"c{i}"], arrays[f"v{i}"] = rows, cols, vals
+        rec = dict(m=m, n=n, nnz=nnz, determine=ref.coo_determine_sort(rows, cols))
+        for s in "RC":
+            sv, sr, sc = ref.coo_apply_sort(s, vals, rows, cols)
+            arrays[f"{s}v{i}"], arrays[f"{s}r{i}"], arrays[f"{s}c{i}"] = sv, sr, sc
+            major, comp = (sr, m) if s == "R" else (sc, n)
+            ptr = ref.sorted_idxs_to_compressed_ptr(major, comp, it)
+            arrays[f"{s}p{i}"] = ptr
+            assert np.array_equal(ref.compressed_ptr_to_sorted_idxs(ptr, nnz, it), major)
+        meta.append(rec)
+    np.savez_compressed(os.path.join(HERE, "sparse_convert.npz"), meta=json.dumps(meta),
+                        **arrays)
+
+
 def main():
     ref = RefLib()
+    if sys.argv[1:] == ["sparse_convert"]:
+        sparse_convert_fixtures(ref)
+        print("sparse_convert fixtures written to", HERE)
+        return
     if sys.argv[1:] == ["random_sparse"]:
         path = os.path.join(HERE, "full_size.json")
         with open(path) as f:
@@ -325,6 +359,7 @@ def main():
     full["random_csr_2^17x512"] = random_sparse_fixtures(ref)
     with open(os.path.join(HERE, "full_size.json"), "w") as f:
         json.dump(full, f, indent=1)
+    sparse_convert_fixtures(ref)
     print("golden fixtures written to", HERE)
 
 

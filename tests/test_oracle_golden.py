@@ -101,3 +101,22 @@ def test_full_size_random_csr_digest(oracle):
     assert hashlib.sha256(a.tobytes()).hexdigest() == g["rowptr_sha256"]
     assert hashlib.sha256(b.tobytes()).hexdigest() == g["colidxs_sha256"]
     assert hashlib.sha256(vals.tobytes()).hexdigest() == g["vals_sha256"]
+
+
+def test_sparse_conversions_match_reference(oracle):
+    """coo_arrays_determine_sort, coo_arrays_apply_sort, sorted_idxs_to_compressed_ptr and
+    compressed_ptr_to_sorted_idxs (sparse_data/base.hh:119-220, 278-302) on duplicate-free
+    COO data, bit for bit."""
+    meta, z = load_golden("sparse_convert")
+    for i, c in enumerate(meta):
+        rows, cols, vals = z[f"r{i}"], z[f"c{i}"], z[f"v{i}"]
+        assert oracle.coo_determine_sort(rows, cols) == c["determine"], c
+        for s in "RC":
+            sv, sr, sc = oracle.coo_apply_sort(s, vals, rows, cols)
+            assert np.array_equal(sv, z[f"{s}v{i}"]) and np.array_equal(sr, z[f"{s}r{i}"])
+            assert np.array_equal(sc, z[f"{s}c{i}"]), (c, s)
+            major, comp = (sr, c["m"]) if s == "R" else (sc, c["n"])
+            ptr = oracle.sorted_idxs_to_compressed_ptr(major, comp, major.dtype)
+            assert np.array_equal(ptr, z[f"{s}p{i}"]), (c, s)
+            assert np.array_equal(oracle.compressed_ptr_to_sorted_idxs(ptr, c["nnz"],
+                                                                       major.dtype), major)
