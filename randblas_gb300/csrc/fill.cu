@@ -265,12 +265,6 @@ __global__ void scale_kernel(int64_t rows, int64_t cols, int64_t rs, int64_t cs,
     }
 }
 
-int grid_for(int64_t work, int threads) {
-    const int64_t want = (work + threads - 1) / threads;
-    const int64_t cap = (int64_t)num_sms() * 16;
-    return (int)std::max<int64_t>(1, std::min(want, cap));
-}
-
 }  // namespace
 
 void launch_fill_dense(int dtype, const DenseGen &g, int64_t R0, int64_t C0, int64_t nr,
@@ -292,7 +286,7 @@ void launch_fill_saso(int dtype, int itype, const DevState &seed, int64_t vec_nn
                       void *vals, cudaStream_t s) {
     if (dim_minor <= 0 || vec_nnz <= 0) return;
     const int threads = 128;
-    int grid = grid_for(dim_minor, threads);
+    int grid = grid_stride_ctas(dim_minor, threads);
     if (dim_major < (int64_t)UINT32_MAX && vec_nnz <= kSasoFastMaxNnz) {
 #define RBG_SASO_FAST(V, I)                                                                  \
     saso_fast_kernel<V, I><<<grid, 128, 0, s>>>(seed, (int)vec_nnz, (uint32_t)dim_major,     \
@@ -338,7 +332,7 @@ int64_t launch_fill_laso(int dtype, int itype, const DevState &seed, int64_t vec
         tmp_cnt((size_t)full * 8, s), counts((size_t)dim_minor * 8, s),
         offsets((size_t)(dim_minor + 1) * 8, s);
     const int threads = 128;
-    const int grid = grid_for(dim_minor, threads);
+    const int grid = grid_stride_ctas(dim_minor, threads);
     if (dtype == RBG_F32)
         laso_sample_kernel<float><<<grid, threads, 0, s>>>(seed, vec_nnz, dim_major, dim_minor,
                                                            tmp_idx.as<int64_t>(),
@@ -376,7 +370,7 @@ int64_t launch_fill_laso(int dtype, int itype, const DevState &seed, int64_t vec
 void launch_scale(int dtype, int64_t rows, int64_t cols, int64_t rs, int64_t cs, double beta,
                   void *X, cudaStream_t s) {
     if (rows <= 0 || cols <= 0 || beta == 1.0) return;
-    const int grid = grid_for(rows * cols, 256);
+    const int grid = grid_stride_ctas(rows * cols, 256);
     if (dtype == RBG_F32)
         scale_kernel<float><<<grid, 256, 0, s>>>(rows, cols, rs, cs, (float)beta, (float *)X);
     else

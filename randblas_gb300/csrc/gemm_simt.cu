@@ -238,8 +238,7 @@ void run_gemv(int64_t M, int64_t K, double alpha, const POperand &P, const Strid
             M, K, P, static_cast<const T *>(Q.ptr), Q.s0, k_per_split, ws.as<T>());
         RBG_LAUNCHED();
     }
-    const int grid_r = (int)std::max<int64_t>(
-        1, std::min<int64_t>((M + 255) / 256, (int64_t)num_sms() * 16));
+    const int grid_r = grid_stride_ctas(M, 256);
     reduce_splits_kernel<T><<<grid_r, 256, 0, s>>>(M, 1, (int)splits, ws.as<T>(), (T)alpha,
                                                    (T)beta, (T *)out, os_i, 1);
     RBG_LAUNCHED();
@@ -348,8 +347,7 @@ void run(int64_t M, int64_t N, int64_t K, double alpha, const POperand &P, const
     }
     if (splits > 1) {
         const int64_t work = M * N;
-        const int grid_r = (int)std::max<int64_t>(
-            1, std::min<int64_t>((work + 255) / 256, (int64_t)num_sms() * 16));
+        const int grid_r = grid_stride_ctas(work, 256);
         reduce_splits_kernel<T><<<grid_r, 256, 0, s>>>(M, N, splits, partial, (T)alpha,
                                                        (T)beta, (T *)out, os_i, os_j);
         RBG_LAUNCHED();
@@ -431,8 +429,7 @@ void run_noalloc(const DenseLeftProblem &pb, cudaStream_t s) {
     RBG_LAUNCHED();
     if (splits > 1) {
         const int64_t work = M * N;
-        const int grid_r = (int)std::max<int64_t>(
-            1, std::min<int64_t>((work + 255) / 256, (int64_t)num_sms() * 16));
+        const int grid_r = grid_stride_ctas(work, 256);
         reduce_splits_kernel<T><<<grid_r, 256, 0, s>>>(M, N, splits, partial, (T)pb.alpha,
                                                        (T)pb.beta, (T *)pb.out, pb.os_i, pb.os_j);
         RBG_LAUNCHED();

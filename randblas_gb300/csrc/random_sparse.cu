@@ -39,6 +39,9 @@ namespace rbg {
 namespace {
 
 constexpr int kThreads = 256;
+
+// CTAs of kThreads for a grid-stride loop over n items
+inline int ctas(int64_t n) { return grid_stride_ctas(n, kThreads); }
 constexpr uint32_t kNearTie = 0x80000000u;  // flag bit of a stored compressed-path skip
 constexpr uint32_t kSkipMask = 0x7fffffffu;
 // relative distance to an integer below which host and device logarithms may floor
@@ -81,11 +84,6 @@ __device__ __forceinline__ int64_t geometric(uint32_t w, double log_1_minus_p, b
     const double f = floor(y);
     near_tie = (y - f) <= kNearIntRel * y || (f + 1.0 - y) <= kNearIntRel * y;
     return (int64_t)f;
-}
-
-inline int grid_for(int64_t n) {
-    return (int)std::max<int64_t>(1, std::min<int64_t>((n + kThreads - 1) / kThreads,
-                                                       (int64_t)num_sms() * 16));
 }
 
 // ----------------------------------------------------------------- compressed (CSR / CSC)
@@ -444,7 +442,7 @@ bool coo_attempt(Handle &h, double l1mp, int64_t K, cudaStream_t s) {
     h.mem = pos;
     RBG_CUDA(cudaMemsetAsync(st.ptr, 0, sizeof(Status), s));
     RBG_CUDA(cudaMemsetAsync(&st.as<Status>()->nnz, 0xFF, sizeof(int64_t), s));
-    coo_skip_kernel<<<grid_for(K), kThreads, 0, s>>>(h.seed, l1mp, total, K, pos,
+    coo_skip_kernel<<<ctas(K), kThreads, 0, s>>>(h.seed, l1mp, total, K, pos,
                                                      tie.as<uint8_t>());
     RBG_LAUNCHED();
     size_t tmp_bytes = 0;
@@ -454,12 +452,12 @@ bool coo_attempt(Handle &h, double l1mp, int64_t K, cudaStream_t s) {
         RBG_CUDA(cub::DeviceScan::InclusiveScan(tmp.ptr, tmp_bytes, pos, pos, SatAdd{total}, K,
                                                 s));
     }
-    coo_count_kernel<<<grid_for(K), kThreads, 0, s>>>(pos, K, total, st.as<Status>());
+    coo_count_kernel<<<ctas(K), kThreads, 0, s>>>(pos, K, total, st.as<Status>());
     RBG_LAUNCHED();
     Status hs{};
     read_status(hs, st.as<Status>(), s);
     if (hs.nnz < 0) return false;  // every candidate still inside the matrix
-    coo_ties_kernel<<<grid_for(hs.nnz + 1), kThreads, 0, s>>>(tie.as<uint8_t>(), st.as<Status>());
+    coo_ties_kernel<<<ctas(hs.nnz + 1), kThreads, 0, s>>>(tie.as<uint8_t>(), st.as<Status>());
     RBG_LAUNCHED();
     read_status(hs, st.as<Status>(), s);
     h.nnz = hs.nnz;
@@ -492,9 +490,9 @@ bool compressed_attempt(Handle &h, double l1mp, int64_t U, cudaStream_t s) {
     int32_t *start = reinterpret_cast<int32_t *>(mem + b_skip + b_csum);
     int64_t *ptr = reinterpret_cast<int64_t *>(mem + b_skip + b_csum + b_start);
 
-    skip_kernel<<<grid_for(U / 4), kThreads, 0, s>>>(c);
+    skip_kernel<<<ctas(U / 4), kThreads, 0, s>>>(c);
     RBG_LAUNCHED();
-    class_terms_kernel<<<grid_for(4 * c.ranks), kThreads, 0, s>>>(c);
+    class_terms_kernel<<<ctas(4 * c.ranks), kThreads, 0, s>>>(c);
     RBG_LAUNCHED();
     size_t tmp_bytes = 0;
     RBG_CUDA(cub::DeviceScan::InclusiveSum(nullptr, tmp_bytes, c.csum, c.csum, 4 * c.ranks, s));
@@ -509,21 +507,21 @@ bool compressed_attempt(Handle &h, double l1mp, int64_t U, cudaStream_t s) {
     RBG_CUDA(cudaMemsetAsync(rid.ptr, 0xFF, sizeof(int32_t) * nodes, s));
     RBG_CUDA(cudaMemsetAsync(rid.ptr, 0, sizeof(int32_t), s));  // node (0, even) is row 0
     RBG_CUDA(cudaMemsetAsync(start, 0xFF, sizeof(int32_t) * h.nmaj, s));
-    successor_kernel<<<grid_for(nodes), kThreads, 0, s>>>(c, Ja.as<int32_t>());
+    successor_kernel<<<ctas(nodes), kThreads, 0, s>>>(c, Ja.as<int32_t>());
     RBG_LAUNCHED();
     int32_t *Jin = Ja.as<int32_t>(), *Jout = Jb.as<int32_t>();
     for (int64_t step = 1; step < h.nmaj; step <<= 1) {
         const int square = 2 * step < h.nmaj;
-        jump_kernel<<<grid_for(nodes), kThreads, 0, s>>>(Jin, Jout, rid.as<int32_t>(), nodes, step,
+        jump_kernel<<<ctas(nodes), kThreads, 0, s>>>(Jin, Jout, rid.as<int32_t>(), nodes, step,
                                                          h.nmaj, square, st.as<Status>());
         RBG_LAUNCHED();
         std::swap(Jin, Jout);
     }
-    collect_kernel<<<grid_for(nodes), kThreads, 0, s>>>(rid.as<int32_t>(), nodes, start);
+    collect_kernel<<<ctas(nodes), kThreads, 0, s>>>(rid.as<int32_t>(), nodes, start);
     RBG_LAUNCHED();
     Scratch cnt(sizeof(int64_t) * (h.nmaj + 1), s);
     RBG_CUDA(cudaMemsetAsync(cnt.as<int64_t>() + h.nmaj, 0, sizeof(int64_t), s));
-    row_count_kernel<<<grid_for(h.nmaj), kThreads, 0, s>>>(c, start, cnt.as<int64_t>(),
+    row_count_kernel<<<ctas(h.nmaj), kThreads, 0, s>>>(c, start, cnt.as<int64_t>(),
                                                            st.as<Status>());
     RBG_LAUNCHED();
     RBG_CUDA(cub::DeviceScan::ExclusiveSum(nullptr, tmp_bytes, cnt.as<int64_t>(), ptr,
@@ -597,7 +595,8 @@ void create(int32_t fmt, int64_t m, int64_t n, double density, const rbg_state *
         }
     }
     if (h.nmin >= (int64_t(1) << 31) - 1)
-        fail(RBG_ERROR_UNSUPPORTED, std::string(fn) + ": the minor dimension must be below 2^31 - 1");
+        fail(RBG_ERROR_UNSUPPORTED,
+             std::string(fn) + ": the minor dimension must be below 2^31 - 1");
     h.kind = Handle::COMPRESSED_GEOM;
     // words: one terminating skip per row, one skip per nonzero and a pair per two nonzeros
     double est = (double)h.nmaj + 2.0 * (mu + 8.0 * sd) + 1024.0;
@@ -617,26 +616,26 @@ void fill_t(const Handle &h, void *vals, void *a, void *b, cudaStream_t s) {
     switch (h.kind) {
     case Handle::EMPTY:
         if (h.fmt != RBG_COO && h.nmaj > 0) {
-            zero_kernel<I><<<grid_for(h.nmaj + 1), kThreads, 0, s>>>(static_cast<I *>(a),
+            zero_kernel<I><<<ctas(h.nmaj + 1), kThreads, 0, s>>>(static_cast<I *>(a),
                                                                     h.nmaj + 1);
             RBG_LAUNCHED();
         }
         return;
     case Handle::FULL:
-        emit_full_kernel<T, I><<<grid_for(std::max(h.nnz, h.nmaj + 1)), kThreads, 0, s>>>(
+        emit_full_kernel<T, I><<<ctas(std::max(h.nnz, h.nmaj + 1)), kThreads, 0, s>>>(
             h.seed, h.fmt, h.nmaj, h.nmin, static_cast<T *>(vals), static_cast<I *>(a),
             static_cast<I *>(b));
         RBG_LAUNCHED();
         return;
     case Handle::COO_GEOM:
         if (h.nnz == 0) return;
-        emit_coo_kernel<T, I><<<grid_for(h.nnz), kThreads, 0, s>>>(
+        emit_coo_kernel<T, I><<<ctas(h.nnz), kThreads, 0, s>>>(
             h.seed, h.coo_pos, h.nnz, h.n, static_cast<T *>(vals), static_cast<I *>(a),
             static_cast<I *>(b));
         RBG_LAUNCHED();
         return;
     case Handle::COMPRESSED_GEOM:
-        emit_compressed_kernel<T, I><<<grid_for(std::max(h.nnz, h.nmaj + 1)), kThreads, 0, s>>>(
+        emit_compressed_kernel<T, I><<<ctas(std::max(h.nnz, h.nmaj + 1)), kThreads, 0, s>>>(
             h.comp, h.start, h.ptr, h.nnz, static_cast<T *>(vals), static_cast<I *>(a),
             static_cast<I *>(b));
         RBG_LAUNCHED();

@@ -4,6 +4,7 @@
 
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstdint>
 #include <exception>
 #include <new>
@@ -84,6 +85,13 @@ int64_t safe_mul(int64_t a, int64_t b);
 inline cudaStream_t as_cuda(rbg_stream_t s) { return reinterpret_cast<cudaStream_t>(s); }
 
 int num_sms();
+
+// CTAs for a grid-stride loop over `work` items, `threads` per CTA: enough to cover the work,
+// at most 16 per SM.
+inline int grid_stride_ctas(int64_t work, int threads) {
+    return (int)std::max<int64_t>(
+        1, std::min<int64_t>((work + threads - 1) / threads, (int64_t)num_sms() * 16));
+}
 
 // Stream-ordered scratch that frees itself (cudaMallocAsync / cudaFreeAsync).
 struct Scratch {

@@ -15,10 +15,8 @@ namespace {
 
 constexpr int kThreads = 256;
 
-inline int grid_for(int64_t n) {
-    return (int)std::max<int64_t>(1, std::min<int64_t>((n + kThreads - 1) / kThreads,
-                                                       (int64_t)num_sms() * 16));
-}
+// CTAs of kThreads for a grid-stride loop over n items
+inline int ctas(int64_t n) { return grid_stride_ctas(n, kThreads); }
 
 // idxs[e] = j for the segment ptr[j] - ptr[0] <= e < ptr[j + 1] - ptr[0] holding e
 template <typename P, typename X>
@@ -144,7 +142,7 @@ int determine_sort(int32_t itype, int64_t nnz, const void *rows, const void *col
     RBG_CUDA(cudaMemsetAsync(flags.ptr, 0, 2 * sizeof(int), s));
     by_itype(itype, [&](auto tag) {
         using I = decltype(tag);
-        sort_state_kernel<I><<<grid_for(nnz), kThreads, 0, s>>>(
+        sort_state_kernel<I><<<ctas(nnz), kThreads, 0, s>>>(
             nnz, static_cast<const I *>(rows), static_cast<const I *>(cols), flags.as<int>());
         RBG_LAUNCHED();
     });
@@ -172,23 +170,23 @@ void apply_sort_t(int32_t sort, int64_t nnz, T *vals, I *rows, I *cols, cudaStre
     const I *minor = sort == RBG_SORT_CSR ? cols : rows;
     Scratch perm_a(sizeof(int64_t) * nnz, s), perm_b(sizeof(int64_t) * nnz, s),
         keys_a(sizeof(I) * nnz, s), keys_b(sizeof(I) * nnz, s);
-    iota_kernel64<<<grid_for(nnz), kThreads, 0, s>>>(nnz, perm_a.as<int64_t>());
+    iota_kernel64<<<ctas(nnz), kThreads, 0, s>>>(nnz, perm_a.as<int64_t>());
     RBG_LAUNCHED();
     sort_pairs<I>(minor, keys_b.as<I>(), perm_a.as<int64_t>(), perm_b.as<int64_t>(), nnz, s);
-    gather_kernel<I><<<grid_for(nnz), kThreads, 0, s>>>(nnz, perm_b.as<int64_t>(), major,
+    gather_kernel<I><<<ctas(nnz), kThreads, 0, s>>>(nnz, perm_b.as<int64_t>(), major,
                                                          keys_a.as<I>());
     RBG_LAUNCHED();
     sort_pairs<I>(keys_a.as<I>(), keys_b.as<I>(), perm_b.as<int64_t>(), perm_a.as<int64_t>(),
                   nnz, s);
     const int64_t *perm = perm_a.as<int64_t>();
     Scratch tv(sizeof(T) * nnz, s), ti(sizeof(I) * nnz, s);
-    gather_kernel<T><<<grid_for(nnz), kThreads, 0, s>>>(nnz, perm, vals, tv.as<T>());
+    gather_kernel<T><<<ctas(nnz), kThreads, 0, s>>>(nnz, perm, vals, tv.as<T>());
     RBG_LAUNCHED();
     RBG_CUDA(cudaMemcpyAsync(vals, tv.ptr, sizeof(T) * nnz, cudaMemcpyDeviceToDevice, s));
-    gather_kernel<I><<<grid_for(nnz), kThreads, 0, s>>>(nnz, perm, rows, ti.as<I>());
+    gather_kernel<I><<<ctas(nnz), kThreads, 0, s>>>(nnz, perm, rows, ti.as<I>());
     RBG_LAUNCHED();
     RBG_CUDA(cudaMemcpyAsync(rows, ti.ptr, sizeof(I) * nnz, cudaMemcpyDeviceToDevice, s));
-    gather_kernel<I><<<grid_for(nnz), kThreads, 0, s>>>(nnz, perm, cols, ti.as<I>());
+    gather_kernel<I><<<ctas(nnz), kThreads, 0, s>>>(nnz, perm, cols, ti.as<I>());
     RBG_LAUNCHED();
     RBG_CUDA(cudaMemcpyAsync(cols, ti.ptr, sizeof(I) * nnz, cudaMemcpyDeviceToDevice, s));
     RBG_CUDA(cudaStreamSynchronize(s));
@@ -220,7 +218,7 @@ extern "C" int rbg_compressed_ptr_to_sorted_idxs(int64_t num_comp, int32_t ptr_i
         RBG_CUDA(cudaMemsetAsync(flag.ptr, 0, sizeof(int), s));
         by_itype(ptr_itype, [&](auto tag) {
             using P = decltype(tag);
-            segments_kernel<P><<<grid_for(num_comp), kThreads, 0, s>>>(
+            segments_kernel<P><<<ctas(num_comp), kThreads, 0, s>>>(
                 num_comp, static_cast<const P *>(ptr), flag.as<int>());
             RBG_LAUNCHED();
         });
@@ -236,7 +234,7 @@ extern "C" int rbg_compressed_ptr_to_sorted_idxs(int64_t num_comp, int32_t ptr_i
             using P = decltype(ptag);
             by_itype(idx_itype, [&](auto xtag) {
                 using X = decltype(xtag);
-                expand_kernel<P, X><<<grid_for(total), kThreads, 0, s>>>(
+                expand_kernel<P, X><<<ctas(total), kThreads, 0, s>>>(
                     num_comp, static_cast<const P *>(ptr), total, static_cast<X *>(idxs));
                 RBG_LAUNCHED();
             });
@@ -261,7 +259,7 @@ extern "C" int rbg_sorted_idxs_to_compressed_ptr(int64_t len_idxs, int32_t idx_i
             RBG_CUDA(cudaMemsetAsync(flag.ptr, 0, sizeof(int), s));
             by_itype(idx_itype, [&](auto tag) {
                 using X = decltype(tag);
-                sorted_kernel<X><<<grid_for(len_idxs), kThreads, 0, s>>>(
+                sorted_kernel<X><<<ctas(len_idxs), kThreads, 0, s>>>(
                     len_idxs, static_cast<const X *>(idxs), flag.as<int>());
                 RBG_LAUNCHED();
             });
@@ -272,7 +270,7 @@ extern "C" int rbg_sorted_idxs_to_compressed_ptr(int64_t len_idxs, int32_t idx_i
             using X = decltype(xtag);
             by_itype(ptr_itype, [&](auto ptag) {
                 using P = decltype(ptag);
-                compress_kernel<X, P><<<grid_for(num_comp + 1), kThreads, 0, s>>>(
+                compress_kernel<X, P><<<ctas(num_comp + 1), kThreads, 0, s>>>(
                     len_idxs, static_cast<const X *>(idxs), num_comp, static_cast<P *>(ptr));
                 RBG_LAUNCHED();
             });

@@ -279,11 +279,6 @@ __global__ void spmm_reduce_kernel(int64_t M, int64_t N, int splits, const T *pa
     }
 }
 
-int grid1d(int64_t work, int threads) {
-    return (int)std::max<int64_t>(
-        1, std::min<int64_t>((work + threads - 1) / threads, (int64_t)num_sms() * 16));
-}
-
 // ------------------------------------------------------------------ fused SASO scatter
 // Left sketch by a SASO operator whose sparse vectors are the columns of S (short axis =
 // columns, no transpose), the shape RandBLAS's LSKGES gives a wide SparseDist
@@ -418,7 +413,7 @@ void fused_saso(int64_t M, int64_t N, int64_t K, double alpha, const SparseOpera
     Scratch packed((size_t)K * kp * sizeof(uint32_t), s);
     {
         ProfScope prof("saso_pack", s);
-        saso_pack_kernel<<<grid1d(K, 128), 128, 0, s>>>(
+        saso_pack_kernel<<<grid_stride_ctas(K, 128), 128, 0, s>>>(
             Sp.seed, (int)Sp.vec_nnz, kp, (uint32_t)Sp.dim_major, Sp.co, K, Sp.ro, M,
             packed.as<uint32_t>());
         RBG_LAUNCHED();
@@ -430,7 +425,8 @@ void fused_saso(int64_t M, int64_t N, int64_t K, double alpha, const SparseOpera
     while (chunks > 1 && (double)chunks * M * N * 4 > (double)(1ll << 30)) --chunks;
     const int64_t k_per_chunk = (K + chunks - 1) / chunks;
     chunks = (K + k_per_chunk - 1) / k_per_chunk;
-    if (slices > INT32_MAX || chunks > 65535) fail(RBG_ERROR_UNSUPPORTED, "sparse sketch too large");
+    if (slices > INT32_MAX || chunks > 65535)
+        fail(RBG_ERROR_UNSUPPORTED, "sparse sketch too large");
     Scratch part;
     float *partial = nullptr;
     if (chunks > 1) {
@@ -466,7 +462,7 @@ void fused_saso(int64_t M, int64_t N, int64_t K, double alpha, const SparseOpera
         RBG_LAUNCHED();
     }
     if (chunks > 1) {
-        spmm_reduce_kernel<float><<<grid1d(M * N, 256), 256, 0, s>>>(
+        spmm_reduce_kernel<float><<<grid_stride_ctas(M * N, 256), 256, 0, s>>>(
             M, N, (int)chunks, partial, (float)alpha, (float)beta, out, os_i, os_j);
         RBG_LAUNCHED();
     }
@@ -1051,7 +1047,7 @@ void saso_rows(int64_t M, int64_t N, int64_t K, double alpha, const SparseOperan
         else launch_rows<false>(grid, pl.smem, map, p, s);
     }
     if (ranges > 1) {
-        spmm_reduce_kernel<float><<<grid1d(M * N, 256), 256, 0, s>>>(
+        spmm_reduce_kernel<float><<<grid_stride_ctas(M * N, 256), 256, 0, s>>>(
             M, N, (int)ranges, partial, (float)alpha, (float)beta, out, os_i, os_j);
         RBG_LAUNCHED();
     }
@@ -1097,34 +1093,34 @@ void run(int64_t M, int64_t N, int64_t K, double alpha, const SparseOperand &Sp,
         if (Sp.kind == SparseOperand::SASO_GEN) {
             if (Sp.vec_nnz > 64)
                 fail(RBG_ERROR_UNSUPPORTED, "in-kernel SASO sampling needs vec_nnz <= 64");
-            saso_entries_kernel<T><<<grid1d(Sp.dim_minor, 128), 128, 0, s>>>(
+            saso_entries_kernel<T><<<grid_stride_ctas(Sp.dim_minor, 128), 128, 0, s>>>(
                 Sp.seed, Sp.vec_nnz, Sp.dim_major, Sp.dim_minor, Sp.short_is_row, ks,
                 keys.as<uint64_t>(), kc.as<int32_t>(), vv.as<T>());
         } else if (Sp.kind == SparseOperand::COO) {
             if (Sp.itype == RBG_I32)
-                coo_entries_kernel<T, int32_t><<<grid1d(slots, th), th, 0, s>>>(
+                coo_entries_kernel<T, int32_t><<<grid_stride_ctas(slots, th), th, 0, s>>>(
                     slots, (const int32_t *)Sp.idx_a, (const int32_t *)Sp.idx_b,
                     (const T *)Sp.vals, ks, keys.as<uint64_t>(), kc.as<int32_t>(), vv.as<T>());
             else
-                coo_entries_kernel<T, int64_t><<<grid1d(slots, th), th, 0, s>>>(
+                coo_entries_kernel<T, int64_t><<<grid_stride_ctas(slots, th), th, 0, s>>>(
                     slots, (const int64_t *)Sp.idx_a, (const int64_t *)Sp.idx_b,
                     (const T *)Sp.vals, ks, keys.as<uint64_t>(), kc.as<int32_t>(), vv.as<T>());
         } else {
             const int by_rows = Sp.kind == SparseOperand::CSR;
             const int64_t lines = by_rows ? Sp.x_rows : Sp.x_cols;
             if (Sp.itype == RBG_I32)
-                compressed_entries_kernel<T, int32_t><<<grid1d(lines, th), th, 0, s>>>(
+                compressed_entries_kernel<T, int32_t><<<grid_stride_ctas(lines, th), th, 0, s>>>(
                     lines, (const int32_t *)Sp.idx_a, (const int32_t *)Sp.idx_b,
                     (const T *)Sp.vals, by_rows, ks, keys.as<uint64_t>(), kc.as<int32_t>(),
                     vv.as<T>());
             else
-                compressed_entries_kernel<T, int64_t><<<grid1d(lines, th), th, 0, s>>>(
+                compressed_entries_kernel<T, int64_t><<<grid_stride_ctas(lines, th), th, 0, s>>>(
                     lines, (const int64_t *)Sp.idx_a, (const int64_t *)Sp.idx_b,
                     (const T *)Sp.vals, by_rows, ks, keys.as<uint64_t>(), kc.as<int32_t>(),
                     vv.as<T>());
         }
         RBG_LAUNCHED();
-        iota_kernel<<<grid1d(slots, th), th, 0, s>>>(slots, perm.as<int32_t>());
+        iota_kernel<<<grid_stride_ctas(slots, th), th, 0, s>>>(slots, perm.as<int32_t>());
         RBG_LAUNCHED();
         // ---- 2. stable sort by key (invalid keys have every bit set and sort last)
         size_t tmp_bytes = 0;
@@ -1138,12 +1134,12 @@ void run(int64_t M, int64_t N, int64_t K, double alpha, const SparseOperand &Sp,
                                                  sperm.as<int32_t>(), (int)slots, 0, end_bit,
                                                  s));
         // sorted entries go back into the `keys` buffer's neighbours: reuse perm/kc storage
-        gather_entries_kernel<T><<<grid1d(slots, th), th, 0, s>>>(
+        gather_entries_kernel<T><<<grid_stride_ctas(slots, th), th, 0, s>>>(
             slots, sperm.as<int32_t>(), kc.as<int32_t>(), vv.as<T>(), perm.as<int32_t>(),
             reinterpret_cast<T *>(keys.ptr));
         RBG_LAUNCHED();
     }
-    rowptr_kernel<<<grid1d(slots + 1, th), th, 0, s>>>(slots, skeys.as<uint64_t>(),
+    rowptr_kernel<<<grid_stride_ctas(slots + 1, th), th, 0, s>>>(slots, skeys.as<uint64_t>(),
                                                         ks.kbits, M, rowptr.as<int64_t>());
     RBG_LAUNCHED();
     prof_lists.finish();
@@ -1194,14 +1190,13 @@ void run(int64_t M, int64_t N, int64_t K, double alpha, const SparseOperand &Sp,
         RBG_LAUNCHED();
     }
     if (splits > 1) {
-        spmm_reduce_kernel<T><<<grid1d(M * N, 256), 256, 0, s>>>(M, N, (int)splits, args.partial,
-                                                                (T)alpha, (T)beta, (T *)out,
-                                                                os_i, os_j);
+        spmm_reduce_kernel<T><<<grid_stride_ctas(M * N, 256), 256, 0, s>>>(
+            M, N, (int)splits, args.partial, (T)alpha, (T)beta, (T *)out, os_i, os_j);
         RBG_LAUNCHED();
     }
 }
 
-// ------------------------------------------------------------------ generated operator x sparse data
+// --------------------------------------------------------- generated operator x sparse data
 // LSKSP3 / RSKSP3 (RandBLAS/sparse_data/sksp.hh:132-539) when the dense operator holds no
 // buffer: Out[M x N] = alpha * P[M x K] * X[K x N] + beta * Out with P = op(submat(S)) generated
 // from its counters and X sparse, its rows stored directly (CSR rows, or the CSC columns of a
@@ -1388,9 +1383,8 @@ void gen_spmm_rows(int64_t M, int64_t N, int64_t K, double alpha, const POperand
     }
     if (splits > 1) {
         ProfScope prof("gen_spmm_reduce", s);
-        spmm_reduce_kernel<T><<<grid1d(M * N, 256), 256, 0, s>>>(M, N, (int)splits, partial,
-                                                                (T)alpha, (T)beta,
-                                                                static_cast<T *>(out), os_i, os_j);
+        spmm_reduce_kernel<T><<<grid_stride_ctas(M * N, 256), 256, 0, s>>>(
+            M, N, (int)splits, partial, (T)alpha, (T)beta, static_cast<T *>(out), os_i, os_j);
         RBG_LAUNCHED();
     }
 }

@@ -38,8 +38,7 @@ void check_symmetric(int32_t layout, const void *Ap, int64_t n, int64_t lda, dou
     Scratch flag(sizeof(unsigned long long), s);
     RBG_CUDA(cudaMemsetAsync(flag.ptr, 0xFF, sizeof(unsigned long long), s));
     const int64_t work = n * n;
-    const int grid = (int)std::max<int64_t>(
-        1, std::min<int64_t>((work + 255) / 256, (int64_t)num_sms() * 16));
+    const int grid = grid_stride_ctas(work, 256);
     symmetry_kernel<T><<<grid, 256, 0, s>>>(A, n, rs, cs, (T)tol_d, flag.as<unsigned long long>());
     RBG_LAUNCHED();
     unsigned long long first = 0;
