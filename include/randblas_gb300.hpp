@@ -12,7 +12,7 @@
 // DenseSkOp 357-478, fill_dense 563-658, SparseDist sparse_skops.hh:131-246, SparseSkOp 289-450,
 // fill_sparse 587-603, sketch_general skge.hh:756-1199, sketch_vector skve.hh:140-246,
 // sketch_sparse sparse_data/sksp.hh:418-539, random_coo / random_csr / random_csc
-// sparse_data/random_matrix.hh:135-355).  Matrix and vector pointers are CUDA device
+// sparse_data/random_matrix.hh:135-355, sparse conversions sparse_data/base.hh:142-302).  Matrix and vector pointers are CUDA device
 // pointers; every call is asynchronous on `stream` (default: the legacy default stream).
 // Failed argument checks throw RandBLAS_GB300::Error carrying the reference's message text;
 // size overflows throw std::overflow_error, as RandBLAS's safe_int_product does.
@@ -310,6 +310,37 @@ void sketch_symmetric(Layout layout, T alpha, const T *A, int64_t lda, const Den
                       rbg_stream_t stream = nullptr) {
     sketch_symmetric(layout, S.n_rows, S.n_cols, alpha, A, lda, S, 0, 0, beta, B, ldb,
                      sym_check_tol, stream);
+}
+
+// ------------------------------------------------------------------ sparse data conversions
+// NonzeroSort (sparse_data/base.hh:108-117) and the conversion building blocks
+// (sparse_data/base.hh:142-220, 278-302) on device arrays; each synchronises `stream`.
+enum class NonzeroSort : int32_t { CSC = RBG_SORT_CSC, CSR = RBG_SORT_CSR, None = RBG_SORT_NONE };
+
+template <typename I1, typename I2>
+void compressed_ptr_to_sorted_idxs(int64_t num_comp, const I1 *ptr, int64_t len_idxs, I2 *idxs,
+                                   rbg_stream_t stream = nullptr) {
+    detail::check(rbg_compressed_ptr_to_sorted_idxs(num_comp, detail::itype<I1>(), ptr, len_idxs,
+                                                    detail::itype<I2>(), idxs, stream));
+}
+template <typename I1, typename I2>
+void sorted_idxs_to_compressed_ptr(int64_t len_idxs, const I1 *idxs, int64_t num_comp, I2 *ptr,
+                                   rbg_stream_t stream = nullptr) {
+    detail::check(rbg_sorted_idxs_to_compressed_ptr(len_idxs, detail::itype<I1>(), idxs,
+                                                    num_comp, detail::itype<I2>(), ptr, stream));
+}
+template <typename I>
+NonzeroSort coo_arrays_determine_sort(int64_t nnz, const I *rows, const I *cols,
+                                      rbg_stream_t stream = nullptr) {
+    int32_t s = RBG_SORT_NONE;
+    detail::check(rbg_coo_determine_sort(detail::itype<I>(), nnz, rows, cols, &s, stream));
+    return static_cast<NonzeroSort>(s);
+}
+template <typename T, typename I>
+void coo_arrays_apply_sort(NonzeroSort s, int64_t nnz, T *vals, I *rows, I *cols,
+                           rbg_stream_t stream = nullptr) {
+    detail::check(rbg_coo_apply_sort(static_cast<int32_t>(s), detail::dtype<T>(),
+                                     detail::itype<I>(), nnz, vals, rows, cols, stream));
 }
 
 // ------------------------------------------------------------------ random sparse matrices

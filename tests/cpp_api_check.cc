@@ -75,6 +75,19 @@ int main() {
                 std::string(e.what()).find("in function random_csr") != std::string::npos;
     }
     EXPECT(threw);
+    // conversions: what needs no device work (an empty sort request, a one-entry sort state,
+    // the reference's size checks) runs on the host
+    EXPECT(RB::coo_arrays_determine_sort<int64_t>(1, nullptr, nullptr) == RB::NonzeroSort::CSC);
+    RB::coo_arrays_apply_sort<float, int64_t>(RB::NonzeroSort::None, 5, nullptr, nullptr,
+                                              nullptr);
+    threw = false;
+    try {
+        RB::sorted_idxs_to_compressed_ptr<int64_t, int64_t>(0, nullptr, -1, nullptr);
+    } catch (const RB::Error &e) {
+        threw = std::string(e.what()).find("in function sorted_idxs_to_compressed_ptr") !=
+                std::string::npos;
+    }
+    EXPECT(threw);
     std::printf("%s\n", failures ? "FAILED" : "ok");
     return failures ? 1 : 0;
 }
