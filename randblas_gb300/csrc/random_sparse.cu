@@ -138,9 +138,9 @@ __global__ void class_terms_kernel(Compressed c) {
     }
 }
 
-// Rank in class b at which the row starting at node (p, pi) ends (its terminating skip), or
-// -1 if that lies beyond the budget.
-__device__ int64_t row_end_rank(const Compressed &c, int64_t p, int pi, int b, int64_t r0) {
+// Rank in class b at which the row starting at word p, whose skips walk class b from rank r0,
+// ends (its terminating skip), or -1 if that lies beyond the budget.
+__device__ int64_t row_end_rank(const Compressed &c, int64_t p, int b, int64_t r0) {
     const int64_t *C = c.csum + b * c.ranks;
     const int64_t g0 = c.skip[p] & kSkipMask;
     if (g0 >= c.nmin) return r0;
@@ -172,7 +172,7 @@ __global__ void successor_kernel(Compressed c, int32_t *J) {
         const int pi = (int)(x & 1);
         const int b = node_class(p, pi);
         const int64_t r0 = class_rank(b, p);
-        const int64_t r = row_end_rank(c, p, pi, b, r0);
+        const int64_t r = row_end_rank(c, p, b, r0);
         int32_t s = -1;
         if (r >= 0) {
             const int64_t q = class_pos(b, r);
@@ -233,7 +233,7 @@ __global__ void row_count_kernel(Compressed c, const int32_t *__restrict__ start
                 continue;
             }
         } else {
-            r = row_end_rank(c, p, pi, b, r0);
+            r = row_end_rank(c, p, b, r0);
             if (r >= 0) st->consumed = class_pos(b, r) + 1;
         }
         if (r < 0) {
