@@ -8,9 +8,11 @@ rounded to BF16, FP32 accumulation) when the library provides it, next to the pl
 path on the same GPU.  Secondary: the 1024 x 2^20 SASO (8 nonzeros per column) sketch of a
 2^20 x 256 N(0,1) matrix, reported in GB/s against the measured HBM copy bandwidth.
 
-python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-Under torchrun (N > 1) every rank runs an independent replica (the path needs no exchange
-between GPUs); the line reports the max time over ranks and the aggregate throughput.
+python bench.py [--gpus 1] [--steps K] [--warmup W] [--impl ours|reference]
+The GPU path is measured on one GPU only: the tensor-core kernel loads A tiles with TMA
+multicast inside a thread-block cluster, which is meant for one GPU's own memory, so
+``--gpus N`` with N > 1 (or a torchrun launch with WORLD_SIZE > 1) is refused with exit status 2.
+The reference arm (``--impl reference``) runs on the host cores of rank 0 only.
 """
 from __future__ import annotations
 
@@ -28,8 +30,8 @@ sys.path.insert(0, ROOT)
 
 METRIC = "S·A sketch time and roofline fraction: BF16-TC fused vs FP32 plain, same GPU"
 # DRAM bytes per launch of the BF16 tensor-core sketch at the headline size, from one ncu capture
-# at m = 2^17 (profiles/sketch_tc_bf16_4096x131072x1024.md: 358.6 MB read, 118.1 MB written)
-# with the reads scaled by 8 to m = 2^20 (they grow with m; the partial-sum writes do not).
+# at m = 2^17 (358.6 MB read, 118.1 MB written) with the reads scaled by 8 to m = 2^20 (they
+# grow with m; the partial-sum writes do not).
 HEADLINE_TRAFFIC_BYTES = 8 * 358.6e6 + 118.1e6
 D_SK, M_SK, N_SK = 4096, 1 << 20, 1024
 SASO_D, SASO_M, SASO_N, SASO_K = 1024, 1 << 20, 256, 8
@@ -195,21 +197,17 @@ def main():
 
     if args.impl == "reference":
         return run_reference(args, rank, world)
+    if world > 1 or args.gpus != 1:
+        return refuse_multi_gpu(args, rank, world)
     if args.case != "full":
         return run_case(args)
 
     import torch
-    import torch.distributed as dist
 
     torch.cuda.set_device(local)
-    if world > 1:
-        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
     device = torch.device("cuda", local)
     from randblas_gb300 import build as rbuild
-    if rank == 0:
-        rbuild.build()
-    if world > 1:
-        dist.barrier()
+    rbuild.build()
     import randblas_gb300 as rb
     from randblas_gb300 import lowp
     stream = torch.cuda.current_stream()
@@ -238,8 +236,6 @@ def main():
     lib = rb.lib()
     rb.profile.enable(True)
     launches0 = lib.rbg_kernel_launches()
-    if world > 1:
-        dist.barrier()
     torch.cuda.synchronize()
     with ClockSampler(local) as clk:
         ms = event_time(torch, headline, args.steps, args.warmup, stream)
@@ -303,65 +299,92 @@ def main():
     # end to end through the C ABI with host buffers
     e2e = None
     A_host = None
-    if not args.no_e2e or (rank == 0 and not args.no_cpu):
+    if not args.no_e2e or not args.no_cpu:
         A_host = A.cpu().pin_memory() if not args.no_e2e else A.cpu()
     if not args.no_e2e:
         e2e = bench_e2e(torch, rb, lowp, have_lowp, S, A_host, args, stream, flops, device)
 
     cpu = None
-    if rank == 0 and not args.no_cpu:
+    if not args.no_cpu:
         t = cpu_precision_sample(args.cpu_rows, A_host.numpy())
         full_s = t * D_SK / args.cpu_rows
         cpu = {"value": round(flops / full_s / 1e12, 5), "unit": "TFLOP/s",
                "cores": os.cpu_count(), "kind": "port",
                "sample": f"operator rows [0,{args.cpu_rows}) of 4096 (oracle OpenMP fill + "
                          f"OpenBLAS SGEMM), {t:.2f} s, scaled by {D_SK // args.cpu_rows}",
-               "ms_per_sketch": round(full_s * 1e3, 1)}
+               "ms_per_sketch": round(full_s * 1e3, 1), "host": host_info()}
 
-    # aggregate over ranks
-    ms_max = max_time_over_ranks(torch, dist if world > 1 else None, ms, device)
-    value = aggregate_tflops(world, flops, ms_max)
+    value = flops / (ms * 1e-3) / 1e12
+    line = {
+        "metric": METRIC, "value": round(value, 2), "unit": "TFLOP/s", "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 4),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "bf16" if have_lowp else "f32", "data": "synthetic",
+        "config": headline_config(),
+        "path": "bf16 tensor-core fused" if have_lowp else "fp32 plain",
+        "a_spectrum": "singular values 1 -> 1e-6 (random orthogonal factors)",
+        "l2": "inputs larger than L2 (A is 4.3 GB)",
+        "fp32_plain": {"ms_per_step": round(ms_plain, 3),
+                       "TFLOP/s": round(flops / (ms_plain * 1e-3) / 1e12, 2)},
+        "speedup_vs_fp32_plain": round(ms_plain / ms, 2),
+        "rel_frobenius_err_vs_fp64": rel_err,
+        "embedding_distortion": distortion, "fp8_e4m3": fp8,
+        "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
+        "gpu_launches": gpu_launches, "clocks": clk.summary(), "saso": saso,
+        "dense_fp64_small": small, "autograd": autograd_row, "batched": batched_row,
+        "more_rows": more_rows,
+    }
+    print(json.dumps(line))
+
+
+def headline_config():
+    """The workload both arms measure (the reference arm's A has another spectrum, which does
+    not change the CPU path's cost)."""
+    return {"workload": "uniform DenseDist 4096 x 2^20 (seed RNGState(3)) left sketch of a "
+                        "2^20 x 1024 FP32 row-major matrix",
+            "d": D_SK, "m": M_SK, "n": N_SK, "parallelism": "one GPU"}
+
+
+def host_info():
+    """CPU model, logical cores and RAM of this host (for the CPU baseline's record)."""
+    model = None
+    try:
+        with open("/proc/cpuinfo") as f:
+            for ln in f:
+                if ln.lower().startswith("model name"):
+                    model = ln.split(":", 1)[1].strip()
+                    break
+    except OSError:
+        pass
+    if model is None:
+        try:
+            out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+            for ln in out.splitlines():
+                if ln.strip().lower().startswith("model name"):
+                    model = ln.split(":", 1)[1].strip()
+                    break
+        except (OSError, subprocess.SubprocessError):
+            pass
+    try:
+        ram = os.sysconf("SC_PAGE_SIZE") * os.sysconf("SC_PHYS_PAGES") / 2 ** 30
+    except (ValueError, OSError):
+        ram = None
+    return {"cpu_model": model, "logical_cores": os.cpu_count(),
+            "ram_gib": round(ram, 1) if ram else None}
+
+
+def refuse_multi_gpu(args, rank, world):
+    """The GPU arm measures one GPU.  Its tensor-core kernel shares A tiles between the CTAs of
+    a thread-block cluster with TMA multicast, which is only meant for one GPU's own memory,
+    so no multi-GPU launch of it is offered: every rank exits with status 2, rank 0 saying
+    why on stderr."""
     if rank == 0:
-        line = {
-            "metric": METRIC, "value": round(value, 2), "unit": "TFLOP/s", "n_gpus": world,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_max, 4),
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "bf16" if have_lowp else "f32", "data": "synthetic",
-            "config": {"workload": "uniform DenseDist 4096 x 2^20 (seed RNGState(3)) left sketch "
-                                   "of a 2^20 x 1024 FP32 row-major matrix, singular values "
-                                   "1 -> 1e-6",
-                       "d": D_SK, "m": M_SK, "n": N_SK,
-                       "path": "bf16 tensor-core fused" if have_lowp else "fp32 plain",
-                       "l2": "inputs larger than L2 (A is 4.3 GB)",
-                       "parallelism": f"replicas x{world}"},
-            "fp32_plain": {"ms_per_step": round(ms_plain, 3),
-                           "TFLOP/s": round(flops / (ms_plain * 1e-3) / 1e12, 2)},
-            "speedup_vs_fp32_plain": round(ms_plain / ms_max, 2),
-            "rel_frobenius_err_vs_fp64": rel_err,
-            "embedding_distortion": distortion, "fp8_e4m3": fp8,
-            "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
-            "gpu_launches": gpu_launches, "clocks": clk.summary(), "saso": saso,
-            "dense_fp64_small": small, "autograd": autograd_row, "batched": batched_row,
-            "more_rows": more_rows,
-        }
-        print(json.dumps(line))
-    if world > 1:
-        dist.barrier()
-        dist.destroy_process_group()
-
-
-def max_time_over_ranks(torch, dist, ms, device):
-    """The slowest rank's time per step (every rank calls this; dist None = one process)."""
-    if dist is None:
-        return ms
-    t = torch.tensor([ms], dtype=torch.float64, device=device)
-    dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    return float(t.item())
-
-
-def aggregate_tflops(world, flops_per_step, ms_max):
-    """Whole-job throughput: every replica sketches one full workload per step (weak scaling)."""
-    return world * flops_per_step / (ms_max * 1e-3) / 1e12
+        sys.stderr.write(json.dumps({
+            "metric": METRIC, "error": "bench.py measures one GPU only",
+            "requested_gpus": max(args.gpus, world),
+            "why": "the tensor-core sketch uses TMA multicast inside a cluster; it runs in "
+                   "single-GPU processes only"}) + "\n")
+    sys.exit(2)
 
 
 def sampled_rel_err(torch, rb, S, A, B, device):
@@ -717,13 +740,13 @@ def run_reference(args, rank, world):
             "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": round(full_s * 1e3, 1), "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": "uniform DenseDist 4096 x 2^20 (seed RNGState(3)) left sketch "
-                                   "of a 2^20 x 1024 FP32 row-major matrix",
-                       "d": D_SK, "m": M_SK, "n": N_SK},
+            "config": headline_config(),
+            "path": "CPU: operator fill + OpenBLAS SGEMM (RandBLAS's materialise-then-gemm)",
+            "a_spectrum": "N(0,1) entries (the cost does not depend on the values)",
             "cpu_baseline": {"value": round(value, 5), "unit": "TFLOP/s",
                              "cores": os.cpu_count(), "kind": "port",
                              "sample": f"operator rows [0,{args.cpu_rows}) per step, scaled by "
-                                       f"{D_SK // args.cpu_rows}"},
+                                       f"{D_SK // args.cpu_rows}", "host": host_info()},
             "e2e": {"value": round(value, 5), "unit": "TFLOP/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
     print(json.dumps(line))

@@ -292,7 +292,8 @@ int rbg_rskge3(int32_t layout, int32_t opA, int32_t opS, int64_t m, int64_t d, i
  * cudaFree), for callers that cannot: code capturing a CUDA graph with a fixed memory plan,
  * or hosts that forbid allocation after start-up.  Its split-K partial sums live in a fixed
  * 32 MiB device array inside the library, which every GPU that loads the library holds until
- * exit; d * n * sizeof(T) may be at most 16 MiB, larger sizes return
+ * exit; d * n * sizeof(T) may be at most 16 MiB -- a limit that holds for every call, also
+ * one whose split plan happens to need no scratch -- and larger sizes return
  * RBG_ERROR_INVALID_ARGUMENT.  The first call on a device looks up that array's address, so
  * make it before any stream capture.  All calls share the array: calls whose kernels can
  * overlap on the GPU race on it. */
@@ -386,8 +387,13 @@ int rbg_lskge3_lowp_workspace(int32_t precision, int64_t d, int64_t n, int64_t m
  * as e4m3 unscaled (|uniform| <= sqrt(3), Gaussians far below e4m3's 448); A is divided, per
  * column and per K slice of the work split, by the power-of-two scale that brings that tile's
  * largest magnitude to <= 448, and the epilogue multiplies the product back (exact).
- * workspace: device buffer of rbg_lskge3_lowp_workspace bytes, or NULL to let the call
- * allocate (stream-ordered) and free it.
+ * workspace: buffer of rbg_lskge3_lowp_workspace bytes in device memory of the current GPU
+ * (cudaMalloc on the device the call runs on; other devices' memory, managed memory and host
+ * memory are rejected with RBG_ERROR_INVALID_ARGUMENT), or NULL to let the call allocate
+ * (stream-ordered) and free it.  The kernel shares A tiles between the CTAs of a thread-block
+ * cluster with TMA multicast, so this path is for single-GPU processes: call it on one GPU,
+ * with its buffers on that GPU (or in host memory as below), never as one rank of a multi-GPU
+ * job.
  * A and B may be device memory or host memory the GPU can read (pinned/registered memory, or
  * any host memory where the device reports cudaDevAttrPageableMemoryAccess); B is then written
  * in place.  For BF16 with pinned A, K >= 2^18, op(A) row- or column-contiguous and no

@@ -405,6 +405,8 @@ template <typename T>
 void run_noalloc(const DenseLeftProblem &pb, cudaStream_t s) {
     const int64_t M = pb.M, N = pb.N, K = pb.K;
     const size_t slice = (size_t)M * (size_t)N * sizeof(T);
+    // the limit holds whether or not this call's split plan needs the scratch, so whether a
+    // size is accepted never depends on the GPU's SM count
     if (slice > kNoallocScratchBytes / 2)
         fail(RBG_ERROR_INVALID_ARGUMENT,
              "rbg_lskge3_noalloc: d * n * sizeof(T) = " + std::to_string(slice) +
@@ -447,26 +449,19 @@ extern "C" int rbg_lskge3_noalloc(int32_t layout, int32_t opS, int32_t opA, int6
                                   int64_t co_s, const void *A, int64_t lda, double beta, void *B,
                                   int64_t ldb, rbg_stream_t stream) {
     using namespace rbg;
-    try {
+    return guarded([&] {
         DenseLeftProblem pb{};
         if (!prepare_dense_left(layout, opS, opA, d, n, m, alpha, S, ro_s, co_s, A, lda, beta, B,
                                 ldb, &pb))
-            return RBG_SUCCESS;
+            return;
         const cudaStream_t s = as_cuda(stream);
         if (pb.K <= 0 || pb.alpha == 0.0) {
             launch_scale(pb.dtype, pb.M, pb.N, pb.os_i, pb.os_j, pb.beta, pb.out, s);
-            return RBG_SUCCESS;
+            return;
         }
         if (pb.dtype == RBG_F32)
             run_noalloc<float>(pb, s);
         else
             run_noalloc<double>(pb, s);
-        return RBG_SUCCESS;
-    } catch (const Failure &e) {
-        set_last_error(e.msg);
-        return e.code;
-    } catch (const std::exception &e) {
-        set_last_error(e.what());
-        return RBG_ERROR_INVALID_ARGUMENT;
-    }
+    });
 }

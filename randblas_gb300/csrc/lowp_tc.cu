@@ -1241,6 +1241,25 @@ void require_gpu_accessible(const void *p, const char *name) {
                                  "(cudaHostRegister / cudaMallocHost) or pass device memory");
 }
 
+// A caller's workspace holds the converted copy of A that the tensor-core kernel loads with
+// TMA, shared between the CTAs of a cluster by multicast: it must be memory of the current GPU
+// itself -- not another GPU's memory, managed memory, or host memory mapped into this GPU.
+void require_current_device_memory(const void *p, const char *name) {
+    cudaPointerAttributes pa{};
+    if (cudaPointerGetAttributes(&pa, p) != cudaSuccess) {
+        cudaGetLastError();
+        fail(RBG_ERROR_INVALID_ARGUMENT,
+             std::string(name) + " must be device memory of the current GPU (its pointer "
+                                 "attributes could not be read)");
+    }
+    int dev = -1;
+    RBG_CUDA(cudaGetDevice(&dev));
+    if (pa.type != cudaMemoryTypeDevice || pa.device != dev)
+        fail(RBG_ERROR_INVALID_ARGUMENT,
+             std::string(name) + " must be device memory of the current GPU (cudaMalloc on "
+                                 "device " + std::to_string(dev) + ")");
+}
+
 int lowp_entry(int32_t precision, int32_t a_dtype, int32_t layout, int32_t opS, int32_t opA,
                int64_t d, int64_t n, int64_t m, float alpha, const rbg_dense_skop *S,
                int64_t ro_s, int64_t co_s, const void *A, int64_t lda, float beta, float *B,
@@ -1275,6 +1294,7 @@ int lowp_entry(int32_t precision, int32_t a_dtype, int32_t layout, int32_t opS, 
         }
         if (d == 0 || n == 0) return;
         if (!B) fail(RBG_ERROR_INVALID_ARGUMENT, "B must not be NULL");
+        if (workspace) require_current_device_memory(workspace, "workspace");
         const cudaStream_t s = as_cuda(stream);
         const int64_t brs = layout == RBG_COL_MAJOR ? 1 : ldb;
         const int64_t bcs = layout == RBG_COL_MAJOR ? ldb : 1;

@@ -90,3 +90,21 @@ def test_argument_checks_use_reference_messages(lib):
     nxt = rb._lib.rbg_state()
     assert lib.rbg_dense_next_state(C.byref(big), C.byref(rb._lib.rbg_state()),
                                     C.byref(nxt)) == 2
+
+
+def test_lowp_rejects_a_host_workspace(lib):
+    """The tensor-core path's workspace must be device memory of the current GPU: host memory
+    is refused before any device work (checked here without a GPU)."""
+    import numpy as np
+
+    import randblas_gb300 as rb
+    S = rb.api.DenseSkOp(rb.DenseDist(256, 1024, rb.ScalarDist.Uniform), rb.RNGState(3))
+    sc = S._c()
+    ws = np.zeros(1 << 20, np.uint8)
+    A = np.zeros((1024, 64), np.float32)
+    B = np.zeros((256, 64), np.float32)
+    rc = lib.rbg_lskge3_lowp(rb._lib.PREC_BF16, 1, 0, 0, 256, 64, 1024, 1.0, C.byref(sc), 0, 0,
+                             A.ctypes.data, 64, 0.0, B.ctypes.data, 64, ws.ctypes.data,
+                             ws.nbytes, None)
+    assert rc == rb._lib.ERROR_INVALID_ARGUMENT
+    assert "workspace must be device memory of the current GPU" in lib.rbg_last_error().decode()

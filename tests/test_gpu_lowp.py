@@ -114,6 +114,24 @@ def test_lowp_workspace_and_errors(rb):
     with pytest.raises(rb.RandBLASError):
         lowp.sketch_lowp(rb.Layout.RowMajor, rb.Op.NoTrans, rb.Op.NoTrans, 256, 64, 4096, 1.0, S,
                          0, 0, A, 64, 0.0, B1, 64, workspace=ws_al[:need - 1024])
+    # the workspace must be memory of this GPU: pinned host memory is refused by the C ABI
+    # (and by the Python front end before it), B is left as it was
+    import ctypes as C
+    host_ws = torch.empty(need + 1024, dtype=torch.uint8, pin_memory=True)
+    hoff = (-host_ws.data_ptr()) % 1024
+    B3 = torch.full((256, 64), 7.0, device="cuda")
+    sc = S._c()
+    rc = rb.lib().rbg_lskge3_lowp(lowp.BF16, 1, 0, 0, 256, 64, 4096, 1.0, C.byref(sc), 0, 0,
+                                  C.c_void_p(A.data_ptr()), 64, 0.0, C.c_void_p(B3.data_ptr()),
+                                  64, C.c_void_p(host_ws.data_ptr() + hoff), need,
+                                  C.c_void_p(torch.cuda.current_stream().cuda_stream))
+    assert rc == rb._lib.ERROR_INVALID_ARGUMENT
+    assert "workspace must be device memory of the current GPU" in \
+        rb.lib().rbg_last_error().decode()
+    with pytest.raises(rb.RandBLASError):
+        lowp.sketch_lowp(rb.Layout.RowMajor, rb.Op.NoTrans, rb.Op.NoTrans, 256, 64, 4096, 1.0, S,
+                         0, 0, A, 64, 0.0, B3, 64, workspace=host_ws[hoff:hoff + need])
+    assert bool((B3 == 7.0).all())
     assert lowp.status() == 0
 
 

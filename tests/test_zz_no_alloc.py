@@ -6,8 +6,10 @@ Some callers cannot allocate device memory while they run -- a CUDA graph captur
 fixed memory plan, or a host that forbids allocation after start-up -- which is why this entry
 point keeps its split-K partial sums in a fixed device array instead."""
 import ctypes as C
+import ctypes.util
+import glob
+import os
 
-import numpy as np
 import pytest
 
 pytestmark = pytest.mark.gpu
@@ -74,3 +76,91 @@ def test_noalloc_rejects_sizes_beyond_its_limit(rb):
     assert rc == 1
     msg = rb.lib().rbg_last_error().decode()
     assert "exceeds its limit" in msg and "rbg_lskge3" in msg
+
+
+# cudaMemPoolAttr values (driver_types.h)
+_RESERVED_CURRENT, _RESERVED_HIGH, _USED_CURRENT, _USED_HIGH = 5, 6, 7, 8
+
+
+def _cudart():
+    """The CUDA runtime, for device-wide memory queries (any copy in the process sees the same
+    device memory pools)."""
+    import torch
+    cands = [ctypes.util.find_library("cudart"), "/usr/local/cuda/lib64/libcudart.so"]
+    tdir = os.path.dirname(torch.__file__)
+    cands += sorted(glob.glob(os.path.join(tdir, "lib", "libcudart*.so*")))
+    cands += sorted(glob.glob(os.path.join(os.path.dirname(tdir), "nvidia", "*", "lib",
+                                           "libcudart.so*")))
+    cands += sorted(glob.glob("/usr/local/cuda/lib64/libcudart.so*"))
+    for c in cands:
+        if c and os.path.exists(c) or (c and "/" not in c):
+            try:
+                return C.CDLL(c)
+            except OSError:
+                continue
+    pytest.fail("no CUDA runtime library found for the memory queries")
+
+
+class _MemProbe:
+    """The default memory pool's used/reserved bytes and high-water marks, plus cudaMemGetInfo."""
+
+    def __init__(self):
+        import torch
+        self.rt = _cudart()
+        self.pool = C.c_void_p()
+        assert self.rt.cudaDeviceGetDefaultMemPool(C.byref(self.pool),
+                                                   torch.cuda.current_device()) == 0
+
+    def attr(self, a):
+        v = C.c_uint64()
+        assert self.rt.cudaMemPoolGetAttribute(self.pool, a, C.byref(v)) == 0
+        return v.value
+
+    def reset_highs(self):
+        zero = C.c_uint64(0)
+        for a in (_USED_HIGH, _RESERVED_HIGH):
+            assert self.rt.cudaMemPoolSetAttribute(self.pool, a, C.byref(zero)) == 0
+
+    def snapshot(self):
+        free, total = C.c_size_t(), C.c_size_t()
+        assert self.rt.cudaMemGetInfo(C.byref(free), C.byref(total)) == 0
+        return {"used": self.attr(_USED_CURRENT), "used_high": self.attr(_USED_HIGH),
+                "reserved": self.attr(_RESERVED_CURRENT),
+                "reserved_high": self.attr(_RESERVED_HIGH), "free": free.value}
+
+
+def test_noalloc_allocates_nothing(rb):
+    """A warmed-up call changes neither the stream-ordered pool's used or reserved bytes (nor
+    their high-water marks) nor the device's free memory.  The same probe around the
+    allocating entry point shows that it does allocate split-K scratch on this case, so the
+    case really uses the fixed array in the allocation-free variant."""
+    import torch
+    dt, lay, fam, d, n, m, ro, co, alpha, beta, tol = CASES[0]
+    dist = rb.DenseDist(d + ro + 1, m + co + 2, rb.ScalarDist(fam))
+    sk = _skop(rb, dist, rb.RNGState(21), torch.float64)
+    g = torch.Generator(device="cuda").manual_seed(21)
+    A = torch.randn(m * n, device="cuda", dtype=torch.float64, generator=g)
+    B = torch.zeros(d * n, device="cuda", dtype=torch.float64)
+    probe = _MemProbe()
+
+    def call(name):
+        assert _run(rb, name, lay, d, n, m, alpha, sk, ro, co, A, m, beta, B, d) == 0, \
+            rb.lib().rbg_last_error()
+        torch.cuda.synchronize()
+
+    call("rbg_lskge3_noalloc")  # warm-up: first call on the device, module loading
+    call("rbg_lskge3")
+    probe.reset_highs()
+    before = probe.snapshot()
+    call("rbg_lskge3_noalloc")
+    call("rbg_lskge3_noalloc")
+    after = probe.snapshot()
+    assert after["used_high"] <= before["used"], (before, after)
+    assert after["reserved_high"] <= before["reserved"], (before, after)
+    assert after["used"] == before["used"] and after["reserved"] == before["reserved"]
+    assert after["free"] == before["free"], (before, after)
+    # positive control: the allocating entry point takes stream-ordered scratch here
+    probe.reset_highs()
+    base = probe.snapshot()
+    call("rbg_lskge3")
+    assert probe.snapshot()["used_high"] > base["used"], "control case needs no scratch"
