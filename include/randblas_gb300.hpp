@@ -387,6 +387,126 @@ class RandomSparse {
     RNGState next_;
 };
 
+// ------------------------------------------------------------------ sparse data and SpMM
+// Non-owning views of device arrays shaped like RandBLAS's expert constructors
+// (sparse_data/coo_matrix.hh:177-193, csr_matrix.hh, csc_matrix.hh:158-167): zero-based
+// indices, int32_t or int64_t.
+namespace sparse_data {
+template <typename T, typename sint_t = int64_t>
+struct COOMatrix {
+    using scalar_t = T;
+    using index_t = sint_t;
+    int64_t n_rows, n_cols, nnz;
+    T *vals;
+    sint_t *rows, *cols;
+    COOMatrix(int64_t n_rows, int64_t n_cols, int64_t nnz, T *vals, sint_t *rows, sint_t *cols)
+        : n_rows(n_rows), n_cols(n_cols), nnz(nnz), vals(vals), rows(rows), cols(cols) {}
+    rbg_spmat c() const {
+        return {RBG_COO, detail::dtype<T>(), detail::itype<sint_t>(), 0, n_rows, n_cols, nnz,
+                vals, rows, cols};
+    }
+};
+template <typename T, typename sint_t = int64_t>
+struct CSRMatrix {
+    using scalar_t = T;
+    using index_t = sint_t;
+    int64_t n_rows, n_cols, nnz;
+    T *vals;
+    sint_t *rowptr, *colidxs;
+    CSRMatrix(int64_t n_rows, int64_t n_cols, int64_t nnz, T *vals, sint_t *rowptr,
+              sint_t *colidxs)
+        : n_rows(n_rows), n_cols(n_cols), nnz(nnz), vals(vals), rowptr(rowptr),
+          colidxs(colidxs) {}
+    rbg_spmat c() const {
+        return {RBG_CSR, detail::dtype<T>(), detail::itype<sint_t>(), 0, n_rows, n_cols, nnz,
+                vals, rowptr, colidxs};
+    }
+};
+template <typename T, typename sint_t = int64_t>
+struct CSCMatrix {
+    using scalar_t = T;
+    using index_t = sint_t;
+    int64_t n_rows, n_cols, nnz;
+    T *vals;
+    sint_t *rowidxs, *colptr;
+    CSCMatrix(int64_t n_rows, int64_t n_cols, int64_t nnz, T *vals, sint_t *rowidxs,
+              sint_t *colptr)
+        : n_rows(n_rows), n_cols(n_cols), nnz(nnz), vals(vals), rowidxs(rowidxs),
+          colptr(colptr) {}
+    rbg_spmat c() const {
+        return {RBG_CSC, detail::dtype<T>(), detail::itype<sint_t>(), 0, n_rows, n_cols, nnz,
+                vals, colptr, rowidxs};
+    }
+};
+
+// left_spmm (sparse_data/spmm_dispatch.hh:52-179):
+//   C (d x n) = alpha * op(submat(A)) * op(B) + beta * C; offsets only for COO data.
+template <typename SpMat, typename T = typename SpMat::scalar_t>
+void left_spmm(Layout layout, Op opA, Op opB, int64_t d, int64_t n, int64_t m, T alpha,
+               const SpMat &A, int64_t ro_a, int64_t co_a, const T *B, int64_t ldb, T beta, T *C,
+               int64_t ldc, rbg_stream_t stream = nullptr) {
+    const rbg_spmat a = A.c();
+    detail::check(rbg_left_spmm(static_cast<int32_t>(layout), static_cast<int32_t>(opA),
+                                static_cast<int32_t>(opB), d, n, m, alpha, &a, ro_a, co_a, B, ldb,
+                                beta, C, ldc, stream));
+}
+// right_spmm (sparse_data/spmm_dispatch.hh:181-219):
+//   C (m x d) = alpha * op(A) * op(submat(B)) + beta * C.
+template <typename SpMat, typename T = typename SpMat::scalar_t>
+void right_spmm(Layout layout, Op opA, Op opB, int64_t m, int64_t d, int64_t n, T alpha,
+                const T *A, int64_t lda, const SpMat &B, int64_t ro_b, int64_t co_b, T beta,
+                T *C, int64_t ldc, rbg_stream_t stream = nullptr) {
+    const rbg_spmat b = B.c();
+    detail::check(rbg_right_spmm(static_cast<int32_t>(layout), static_cast<int32_t>(opA),
+                                 static_cast<int32_t>(opB), m, d, n, alpha, A, lda, &b, ro_b,
+                                 co_b, beta, C, ldc, stream));
+}
+}  // namespace sparse_data
+
+using sparse_data::COOMatrix;
+using sparse_data::CSCMatrix;
+using sparse_data::CSRMatrix;
+
+// spmm (spmm_dispatch.hh:298-302, 376-380): the sparse operand's position picks the side.
+template <typename SpMat, typename T = typename SpMat::scalar_t>
+void spmm(Layout layout, Op opA, Op opB, int64_t m, int64_t n, int64_t k, T alpha,
+          const SpMat &A, const T *B, int64_t ldb, T beta, T *C, int64_t ldc,
+          rbg_stream_t stream = nullptr) {
+    sparse_data::left_spmm(layout, opA, opB, m, n, k, alpha, A, 0, 0, B, ldb, beta, C, ldc,
+                           stream);
+}
+template <typename SpMat, typename T = typename SpMat::scalar_t>
+void spmm(Layout layout, Op opA, Op opB, int64_t m, int64_t n, int64_t k, T alpha, const T *A,
+          int64_t lda, const SpMat &B, T beta, T *C, int64_t ldc,
+          rbg_stream_t stream = nullptr) {
+    sparse_data::right_spmm(layout, opA, opB, m, n, k, alpha, A, lda, B, 0, 0, beta, C, ldc,
+                            stream);
+}
+
+// sketch_sparse (sparse_data/sksp.hh:418-539): dense operator, sparse data.
+// Left: B (d x n) = alpha * op(submat(S)) * op(A) + beta * B.
+template <typename SpMat, typename T>
+void sketch_sparse(Layout layout, Op opS, Op opA, int64_t d, int64_t n, int64_t m, T alpha,
+                   const DenseSkOp<T> &S, int64_t ro_s, int64_t co_s, const SpMat &A, T beta,
+                   T *B, int64_t ldb, rbg_stream_t stream = nullptr) {
+    const rbg_dense_skop s = S.c();
+    const rbg_spmat a = A.c();
+    detail::check(rbg_lsksp3(static_cast<int32_t>(layout), static_cast<int32_t>(opS),
+                             static_cast<int32_t>(opA), d, n, m, alpha, &s, ro_s, co_s, &a, beta,
+                             B, ldb, stream));
+}
+// Right: B (m x d) = alpha * op(A) * op(submat(S)) + beta * B.
+template <typename SpMat, typename T>
+void sketch_sparse(Layout layout, Op opA, Op opS, int64_t m, int64_t d, int64_t n, T alpha,
+                   const SpMat &A, const DenseSkOp<T> &S, int64_t ro_s, int64_t co_s, T beta,
+                   T *B, int64_t ldb, rbg_stream_t stream = nullptr) {
+    const rbg_dense_skop s = S.c();
+    const rbg_spmat a = A.c();
+    detail::check(rbg_rsksp3(static_cast<int32_t>(layout), static_cast<int32_t>(opA),
+                             static_cast<int32_t>(opS), m, d, n, alpha, &a, &s, ro_s, co_s, beta,
+                             B, ldb, stream));
+}
+
 // Process-wide reproducibility switch (no RandBLAS counterpart).
 inline void set_deterministic(bool on) { detail::check(rbg_set_deterministic(on ? 1 : 0)); }
 

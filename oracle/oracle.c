@@ -23,7 +23,9 @@
  *                              RandBLAS/random_gen.hh:60-137 (documented definitions:
  *                              u01(x) = x*2^-32 + 2^-33, uneg11(x) = (int32)x*2^-31 + 2^-32,
  *                              boxmuller = (sin(pi*uneg11(u0))*r, cos(pi*uneg11(u0))*r),
- *                              r = sqrt(-2 log u01(u1))).
+ *                              r = sqrt(-2 log u01(u1))).  sin / cos / log come from the
+ *                              host libm by default (as in the reference), or, in the
+ *                              "shared math" mode (orc_set_math(1)), from shared_math.cc.
  *   fill_dense_submat ........ RandBLAS/dense_skops.hh:96-170
  *   fill_dense_unpacked ...... RandBLAS/dense_skops.hh:563-606
  *   dense compute_next_state . RandBLAS/dense_skops.hh:172-185
@@ -41,7 +43,8 @@
  *   compressed_ptr_to_sorted_idxs, sorted_idxs_to_compressed_ptr, coo_arrays_determine_sort,
  *   coo_arrays_apply_sort .... RandBLAS/sparse_data/base.hh:119-220, 278-302
  *
- * Build: gcc -O2 -std=gnu11 -fPIC -shared -ffp-contract=off -fopenmp (oracle/build.py).
+ * Build: gcc -O2 -std=gnu11 -fPIC -ffp-contract=off -fopenmp, linked with shared_math.cc
+ * (oracle/build.py).
  */
 #define _GNU_SOURCE 1 /* sincosf */
 #include <math.h>
@@ -115,10 +118,27 @@ float orc_uneg11(uint32_t u) { return (float)(int32_t)u * 0x1p-31f + 0x1p-32f; }
 
 float orc_u01(uint32_t u) { return (float)u * 0x1p-32f + 0x1p-33f; }
 
+/* Math functions of the Box-Muller transform: 0 = the host libm (glibc's sincosf / logf, as
+ * the reference calls them), 1 = the shared specification of shared_math.cc (the same
+ * float-float functions the GPU evaluates), for bit-for-bit comparisons. */
+static int g_math_mode = 0;
+void orc_ffm_sincosf(float theta, float *s, float *c);
+float orc_ffm_logf(float x);
+
+void orc_set_math(int mode) { g_math_mode = mode; }
+int orc_get_math(void) { return g_math_mode; }
+
 void orc_boxmuller(uint32_t u0, uint32_t u1, float *first, float *second) {
-    float s, c;
-    sincosf(3.14159265358979323846f * orc_uneg11(u0), &s, &c);
-    float r = sqrtf(-2.0f * logf(orc_u01(u1)));
+    float s, c, l;
+    const float theta = 3.14159265358979323846f * orc_uneg11(u0);
+    if (g_math_mode == 1) {
+        orc_ffm_sincosf(theta, &s, &c);
+        l = orc_ffm_logf(orc_u01(u1));
+    } else {
+        sincosf(theta, &s, &c);
+        l = logf(orc_u01(u1));
+    }
+    float r = sqrtf(-2.0f * l);
     *first = s * r;
     *second = c * r;
 }

@@ -11,6 +11,7 @@ float32, 1 = float64; itype 0 = int32, 1 = int64.  A state is (counter[4], key[2
 """
 from __future__ import annotations
 
+import contextlib
 import ctypes as C
 import glob
 import os
@@ -68,6 +69,8 @@ class Oracle:
         path = path or _build.build_oracle()
         self.lib = C.CDLL(path)
         L = self.lib
+        L.orc_set_math.argtypes = [INT]
+        L.orc_get_math.restype = INT
         L.orc_philox4x32_10.argtypes = [P, P, P]
         L.orc_ctr_add.argtypes = [P, C.c_uint64]
         L.orc_uneg11.argtypes = [C.c_uint32]
@@ -101,6 +104,21 @@ class Oracle:
         L.orc_coo_apply_sort.restype = INT
 
     # -- RNG ------------------------------------------------------------------------
+    def set_math(self, mode: int) -> None:
+        """Box-Muller's sin / cos / log: 0 = host libm (as the reference), 1 = the shared
+        float-float specification the GPU evaluates (bit-for-bit comparisons)."""
+        self.lib.orc_set_math(mode)
+
+    @contextlib.contextmanager
+    def shared_math(self):
+        """Run a block with the shared math functions, then restore the previous mode."""
+        prev = self.lib.orc_get_math()
+        self.lib.orc_set_math(1)
+        try:
+            yield self
+        finally:
+            self.lib.orc_set_math(prev)
+
     def philox(self, counter, key) -> tuple:
         c, k, o = U32x4(*counter), U32x2(*key), U32x4()
         self.lib.orc_philox4x32_10(C.addressof(c), C.addressof(k), C.addressof(o))
@@ -307,6 +325,7 @@ class RefLib:
         self.lib = C.CDLL(path)
         L = self.lib
         L.rbref_last_error.restype = C.c_char_p
+        L.rbref_set_math.argtypes = [INT]
         L.rbref_set_cblas.argtypes = [P, P]
         self._blas = None
         if use_cblas:
@@ -338,6 +357,16 @@ class RefLib:
         L.rbref_sketch_sparse.argtypes = [INT, INT, INT, INT, INT, I64, I64, I64, C.c_double,
                                           I64, I64, INT, INT, P, P, I64, I64, INT, I64, I64, I64,
                                           P, P, P, C.c_double, P, I64]
+        D = C.c_double
+        L.rbref_left_spmm.argtypes = [INT, INT, INT, INT, I64, I64, I64, D, INT, I64, I64, I64,
+                                      P, P, P, I64, I64, P, I64, D, P, I64]
+        L.rbref_right_spmm.argtypes = [INT, INT, INT, INT, I64, I64, I64, D, P, I64, INT, I64,
+                                       I64, I64, P, P, P, I64, I64, D, P, I64]
+
+    def set_math(self, mode: int) -> None:
+        """Box-Muller's sin / cos / log in the reference's own code: 0 = host libm, 1 = the
+        shared float-float specification."""
+        self.lib.rbref_set_math(mode)
 
     def _check(self, rc):
         if rc:
@@ -463,6 +492,23 @@ class RefLib:
                                           _ptr(y), incy)
         self._check(rc)
         return y
+
+    def left_spmm(self, dtype, layout, opA, opB, d, n, m, alpha, fmt, A_rows, A_cols, vals, a,
+                  b, ro_a, co_a, B, ldb, beta, Cm, ldc):
+        """RandBLAS::sparse_data::left_spmm (spmm_dispatch.hh:52-179) on host arrays; Cm is
+        updated in place.  Returns (status, message)."""
+        rc = self.lib.rbref_left_spmm(dtype, layout, opA, opB, d, n, m, alpha, fmt, A_rows,
+                                      A_cols, len(vals), _ptr(vals), _ptr(a), _ptr(b), ro_a,
+                                      co_a, _ptr(B), ldb, beta, _ptr(Cm), ldc)
+        return rc, (self.lib.rbref_last_error().decode() if rc else "")
+
+    def right_spmm(self, dtype, layout, opA, opB, m, d, n, alpha, A, lda, fmt, B_rows, B_cols,
+                   vals, a, b, ro_b, co_b, beta, Cm, ldc):
+        """RandBLAS::sparse_data::right_spmm (spmm_dispatch.hh:181-219) on host arrays."""
+        rc = self.lib.rbref_right_spmm(dtype, layout, opA, opB, m, d, n, alpha, _ptr(A), lda,
+                                       fmt, B_rows, B_cols, len(vals), _ptr(vals), _ptr(a),
+                                       _ptr(b), ro_b, co_b, beta, _ptr(Cm), ldc)
+        return rc, (self.lib.rbref_last_error().decode() if rc else "")
 
     def sketch_sparse(self, dtype, side, layout, opS, opA, d, n, m, alpha, D_rows, D_cols,
                       family, major_axis, seed: State, ro_s, co_s, fmt, A_rows, A_cols, nnz,

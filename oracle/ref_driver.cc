@@ -16,6 +16,9 @@
 //   rbref_sketch_saso ........... RandBLAS::sketch_general, SparseSkOp (RandBLAS/skge.hh:776,948)
 //   rbref_sketch_vector ......... RandBLAS::sketch_vector         (RandBLAS/skve.hh:140-164)
 //   rbref_sketch_sparse ......... RandBLAS::sketch_sparse         (RandBLAS/sparse_data/sksp.hh:418-539)
+//   rbref_left_spmm, rbref_right_spmm
+//                                 RandBLAS::sparse_data::left_spmm / right_spmm
+//                                 (RandBLAS/sparse_data/spmm_dispatch.hh:52-219)
 //   rbref_compressed_ptr_to_sorted_idxs, rbref_sorted_idxs_to_compressed_ptr,
 //   rbref_coo_determine_sort, rbref_coo_apply_sort
 //                                 (RandBLAS/sparse_data/base.hh:142-220, 278-302)
@@ -115,6 +118,9 @@ void sketch_saso_t(int side, int layout, int opS, int opA, int64_t d, int64_t n,
 extern "C" {
 
 const char *rbref_last_error() { return g_err.c_str(); }
+
+// 0: Box-Muller with the host libm (default); 1: with the shared float-float functions.
+void rbref_set_math(int mode) { r123::boxmuller_math_mode() = mode; }
 
 void rbref_set_cblas(void *sgemm, void *dgemm) {
     blas::shim::sgemm_ptr() = (blas::shim::sgemm_fn)sgemm;
@@ -319,6 +325,66 @@ int rbref_sketch_sparse(int dtype, int side, int layout, int opS, int opA, int64
             sketch_sparse_t<double>(side, layout, opS, opA, d, n, m, alpha, D_rows, D_cols,
                                     family, major_axis, ctr, key, ro_s, co_s, fmt, A_rows, A_cols,
                                     nnz, vals, a, b, beta, B, ldb);
+    });
+}
+
+}  // extern "C"
+
+// ------------------------------------------------------------- general sparse x dense
+// Same sparse-matrix convention as sketch_sparse_t (fmt 0 COO, 1 CSR, 2 CSC; int64 indices).
+template <typename T, typename F>
+void with_spmat(int fmt, int64_t n_rows, int64_t n_cols, int64_t nnz, void *vals, int64_t *a,
+                int64_t *b, F &&f) {
+    using namespace RandBLAS::sparse_data;
+    if (fmt == 0) {
+        COOMatrix<T, int64_t> M(n_rows, n_cols, nnz, (T *)vals, a, b);
+        f(M);
+    } else if (fmt == 1) {
+        CSRMatrix<T, int64_t> M(n_rows, n_cols, nnz, (T *)vals, a, b);
+        f(M);
+    } else {
+        CSCMatrix<T, int64_t> M(n_rows, n_cols, nnz, (T *)vals, b, a);
+        f(M);
+    }
+}
+
+extern "C" {
+
+// C = alpha * op(submat(A)) * op(B) + beta * C, A sparse (d x m after op), B dense.
+int rbref_left_spmm(int dtype, int layout, int opA, int opB, int64_t d, int64_t n, int64_t m,
+                    double alpha, int fmt, int64_t A_rows, int64_t A_cols, int64_t nnz,
+                    void *vals, int64_t *a, int64_t *b, int64_t ro_a, int64_t co_a,
+                    const void *B, int64_t ldb, double beta, void *C, int64_t ldc) {
+    return guarded([&] {
+        auto go = [&](auto tag) {
+            using T = decltype(tag);
+            with_spmat<T>(fmt, A_rows, A_cols, nnz, vals, a, b, [&](auto &A) {
+                RandBLAS::sparse_data::left_spmm(lay(layout), op(opA), op(opB), d, n, m, (T)alpha,
+                                                 A, ro_a, co_a, (const T *)B, ldb, (T)beta,
+                                                 (T *)C, ldc);
+            });
+        };
+        if (dtype == 0) go(float{});
+        else go(double{});
+    });
+}
+
+// C = alpha * op(A) * op(submat(B)) + beta * C, A dense (m x n after op), B sparse (n x d).
+int rbref_right_spmm(int dtype, int layout, int opA, int opB, int64_t m, int64_t d, int64_t n,
+                     double alpha, const void *A, int64_t lda, int fmt, int64_t B_rows,
+                     int64_t B_cols, int64_t nnz, void *vals, int64_t *a, int64_t *b,
+                     int64_t ro_b, int64_t co_b, double beta, void *C, int64_t ldc) {
+    return guarded([&] {
+        auto go = [&](auto tag) {
+            using T = decltype(tag);
+            with_spmat<T>(fmt, B_rows, B_cols, nnz, vals, a, b, [&](auto &B) {
+                RandBLAS::sparse_data::right_spmm(lay(layout), op(opA), op(opB), m, d, n,
+                                                  (T)alpha, (const T *)A, lda, B, ro_b, co_b,
+                                                  (T)beta, (T *)C, ldc);
+            });
+        };
+        if (dtype == 0) go(float{});
+        else go(double{});
     });
 }
 

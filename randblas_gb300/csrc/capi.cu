@@ -571,19 +571,42 @@ SparseOperand operand_of_spmat(const rbg_spmat &A, int trans, int64_t ro, int64_
 }
 
 // left_spmm checks on op(A) (d x m at (ro_a, co_a)): COO may be larger, CSR/CSC must match
-// exactly with zero offsets (RandBLAS/sparse_data/spmm_dispatch.hh:99-107).
-void check_left_spmm_dims(const rbg_spmat &A, int32_t opA, int64_t d, int64_t m, int64_t ro_a,
-                          int64_t co_a) {
-    const Dims ax = opA == RBG_NO_TRANS ? Dims{A.n_rows, A.n_cols} : Dims{A.n_cols, A.n_rows};
+// exactly with zero offsets (RandBLAS/sparse_data/spmm_dispatch.hh:99-107).  The reference
+// applies a transposed A by recursing on A.transpose() with the offsets swapped
+// (spmm_dispatch.hh:73-90), so its checks -- and their messages -- name the transposed
+// matrix and offsets; these do the same.
+void check_left_spmm_dims(const rbg_spmat &X, int32_t opA, int64_t d, int64_t m, int64_t ro,
+                          int64_t co) {
+    struct Shape {
+        int64_t n_rows, n_cols;
+    };
+    const bool nt = opA == RBG_NO_TRANS;
+    const Shape A = nt ? Shape{X.n_rows, X.n_cols} : Shape{X.n_cols, X.n_rows};
+    const int64_t ro_a = nt ? ro : co, co_a = nt ? co : ro;
     RBG_REQUIRE("left_spmm", ro_a >= 0 && co_a >= 0);
-    if (A.format == RBG_COO) {
-        RBG_REQUIRE("left_spmm", ax.rows >= d);
-        RBG_REQUIRE("left_spmm", ax.cols >= m);
+    if (X.format == RBG_COO) {
+        RBG_REQUIRE("left_spmm", A.n_rows >= d);
+        RBG_REQUIRE("left_spmm", A.n_cols >= m);
     } else {
-        RBG_REQUIRE("left_spmm", ax.rows == d);
-        RBG_REQUIRE("left_spmm", ax.cols == m);
+        RBG_REQUIRE("left_spmm", A.n_rows == d);
+        RBG_REQUIRE("left_spmm", A.n_cols == m);
         RBG_REQUIRE("left_spmm", ro_a == 0);
         RBG_REQUIRE("left_spmm", co_a == 0);
+    }
+}
+
+// left_spmm's leading-dimension checks (spmm_dispatch.hh:110-135), in its names: the dense
+// operand B (op(B) m x n) and C (d x n), both read in `layout`.
+void check_left_spmm_lds(int32_t layout, int32_t opB, int64_t d, int64_t n, int64_t m,
+                         int64_t ldb, int64_t ldc) {
+    const int64_t rows_B = opB == RBG_NO_TRANS ? m : n;
+    const int64_t cols_B = opB == RBG_NO_TRANS ? n : m;
+    if (layout == RBG_COL_MAJOR) {
+        RBG_REQUIRE("left_spmm", ldb >= rows_B);
+        RBG_REQUIRE("left_spmm", ldc >= d);
+    } else {
+        RBG_REQUIRE("left_spmm", ldc >= n);
+        RBG_REQUIRE("left_spmm", ldb >= cols_B);
     }
 }
 
@@ -596,14 +619,7 @@ void left_spmm_impl(int32_t layout, int32_t opA, int32_t opB, int64_t d, int64_t
     check_nonnull(A, "A");
     validate_spmat(A, A->dtype);
     check_left_spmm_dims(*A, opA, d, m, ro_a, co_a);
-    const Dims b = dims_before_op(m, n, opB);
-    if (layout == RBG_COL_MAJOR) {
-        RBG_REQUIRE("left_spmm", ldb >= b.rows);
-        RBG_REQUIRE("left_spmm", ldc >= d);
-    } else {
-        RBG_REQUIRE("left_spmm", ldc >= n);
-        RBG_REQUIRE("left_spmm", ldb >= b.cols);
-    }
+    check_left_spmm_lds(layout, opB, d, n, m, ldb, ldc);
     if (d == 0 || n == 0) return;
     check_nonnull(C, "C");
     const Strides c = strides_of(layout, ldc);
@@ -624,16 +640,11 @@ void right_spmm_impl(int32_t layout, int32_t opA, int32_t opB, int64_t m, int64_
     check_op(opB);
     check_nonnull(B, "B");
     validate_spmat(B, B->dtype);
-    // C^T = op(submat(B))^T op(A)^T: left_spmm with op flipped on B
+    // C^T = op(submat(B))^T op(A)^T: the reference's reduction to left_spmm with the layout
+    // and B's op flipped (spmm_dispatch.hh:181-219), and its checks in that problem's names
     check_left_spmm_dims(*B, opB == RBG_NO_TRANS ? RBG_TRANS : RBG_NO_TRANS, d, n, ro_b, co_b);
-    const Dims a = dims_before_op(m, n, opA);
-    if (layout == RBG_COL_MAJOR) {
-        RBG_REQUIRE("left_spmm", lda >= a.rows);
-        RBG_REQUIRE("left_spmm", ldc >= m);
-    } else {
-        RBG_REQUIRE("left_spmm", lda >= a.cols);
-        RBG_REQUIRE("left_spmm", ldc >= d);
-    }
+    check_left_spmm_lds(layout == RBG_COL_MAJOR ? RBG_ROW_MAJOR : RBG_COL_MAJOR, opA, d, m, n,
+                        lda, ldc);
     if (d == 0 || m == 0) return;
     check_nonnull(C, "C");
     const Strides c = strides_of(layout, ldc);

@@ -88,6 +88,43 @@ int main() {
                 std::string::npos;
     }
     EXPECT(threw);
+    // sparse data: CSR data with an offset, and a sketch_sparse whose data does not match
+    // op(A)'s size, fail with the reference's messages before any device work
+    {
+        int64_t rowptr[7] = {0, 0, 0, 0, 0, 0, 0};
+        RB::CSRMatrix<double> A(6, 20, 0, nullptr, rowptr, nullptr);
+        threw = false;
+        try {
+            RB::sparse_data::left_spmm(RB::Layout::ColMajor, RB::Op::NoTrans, RB::Op::NoTrans,
+                                       6, 4, 20, 1.0, A, 1, 0, static_cast<const double *>(nullptr),
+                                       20, 0.0, static_cast<double *>(nullptr), 6);
+        } catch (const RB::Error &e) {
+            threw = std::string(e.what()) ==
+                    "(ro_a == 0) was required, but did not hold, in function left_spmm";
+        }
+        EXPECT(threw);
+        threw = false;
+        try {  // spmm's right form: op(B) = A^T must be n x d = 20 x 6, CSR A is 6 x 20 -> ok;
+               // ldc too small for the m x d row-major C
+            RB::spmm(RB::Layout::RowMajor, RB::Op::NoTrans, RB::Op::Trans, 4, 6, 20, 1.0,
+                     static_cast<const double *>(nullptr), 20, A, 0.0,
+                     static_cast<double *>(nullptr), 5);
+        } catch (const RB::Error &e) {
+            threw = std::string(e.what()) ==
+                    "(ldc >= d) was required, but did not hold, in function left_spmm";
+        }
+        EXPECT(threw);
+        RB::DenseSkOp<double> Sd(RB::DenseDist(10, 30), RB::RNGState(2));
+        threw = false;
+        try {
+            RB::sketch_sparse(RB::Layout::RowMajor, RB::Op::NoTrans, RB::Op::NoTrans, 10, 6, 30,
+                              1.0, Sd, 0, 0, A, 0.0, static_cast<double *>(nullptr), 6);
+        } catch (const RB::Error &e) {
+            threw = std::string(e.what()).find("was required, but did not hold") !=
+                    std::string::npos;
+        }
+        EXPECT(threw);
+    }
     std::printf("%s\n", failures ? "FAILED" : "ok");
     return failures ? 1 : 0;
 }

@@ -1,8 +1,9 @@
 """Generate the golden fixtures in tests/golden/ from the reference itself.
 
-Run in a container that has the RandBLAS source tree (default /root/reference, override with
-RANDBLAS_REF_DIR).  It builds oracle/_ref/librbref.so -- the reference's own headers compiled
-against the project's Random123 / BLAS++ stand-ins -- and records:
+Run in a container that has the RandBLAS source tree (RANDBLAS_REF_DIR, else a directory
+named "reference" beside this repository).  It builds oracle/_ref/librbref.so -- the
+reference's own headers compiled against the project's Random123 / BLAS++ stand-ins -- and
+records:
 
 * philox_kat.json: the Philox4x32-10 known-answer rows of the reference's
   test/test_basic_rng/r123_kat_vectors.txt (parsed from that file);
@@ -18,7 +19,15 @@ against the project's Random123 / BLAS++ stand-ins -- and records:
   matrix; the 1024 x 2^20 SASO with 8 nonzeros per column), so the GPU tests can pin those
   bit for bit without shipping the arrays.
 
-Usage: python tests/golden/make_golden.py [random_sparse | sparse_convert]
+* spmm.npz: the reference's left_spmm / right_spmm over COO / CSR / CSC data, every op and
+  layout, FP32 / FP64, COO offsets and duplicates, alpha = 0, beta = 0, empty data, and the
+  argument checks with their messages.
+
+* full_size.json also holds the digests of that 200 x 10000 operator (FP64 and FP32) from
+  the reference's code with Box-Muller's sin / cos / log taken from the shared float-float
+  specification (the "shared math" mode), which the GPU must match bit for bit.
+
+Usage: python tests/golden/make_golden.py [random_sparse | sparse_convert | spmm | shared_math]
 (an argument writes only that part)
 """
 from __future__ import annotations
@@ -124,8 +133,154 @@ def sparse_convert_fixtures(ref):
                         **arrays)
 
 
+def _sparse_arrays(rng, rows, cols, density, fmt, npdt, dup=False):
+    """Seeded sparse data in the reference's convention (fmt 0 COO (a = rows, b = cols) in
+    random order, 1 CSR (a = rowptr, b = colidxs), 2 CSC (a = colptr, b = rowidxs)); int64
+    indices.  dup: COO with some (row, col) pairs repeated."""
+    dense = rng.standard_normal((rows, cols)) * (rng.random((rows, cols)) < density)
+    r_, c_ = np.nonzero(dense)
+    vals = dense[r_, c_]
+    if fmt == 0:
+        if dup and len(vals):
+            k = max(1, len(vals) // 4)
+            pick = rng.integers(0, len(vals), k)
+            r_, c_ = np.concatenate([r_, r_[pick]]), np.concatenate([c_, c_[pick]])
+            vals = np.concatenate([vals, rng.standard_normal(k)])
+        perm = rng.permutation(len(vals))
+        return vals[perm].astype(npdt), r_[perm].astype(np.int64), c_[perm].astype(np.int64)
+    if fmt == 1:
+        a = np.concatenate([[0], np.cumsum(np.bincount(r_, minlength=rows))]).astype(np.int64)
+        return vals.astype(npdt), a, c_.astype(np.int64)
+    order = np.lexsort((r_, c_))
+    a = np.concatenate([[0], np.cumsum(np.bincount(c_, minlength=cols))]).astype(np.int64)
+    return vals[order].astype(npdt), a, r_[order].astype(np.int64)
+
+
+def spmm_fixtures(ref):
+    """left_spmm / right_spmm (RandBLAS/sparse_data/spmm_dispatch.hh:52-219) over COO / CSR /
+    CSC x opA x opB x layout x FP32/FP64, with COO submatrix offsets (coo_spmm_impl.hh:70-92),
+    COO duplicates, alpha = 0, beta = 0 over NaN-filled C, an empty sparse matrix, and the
+    argument checks the reference applies (nonzero offsets or mismatched sizes of CSR / CSC
+    data) with their messages."""
+    rng = np.random.default_rng(2024)
+    arrays, meta = {}, []
+    i = 0
+
+    def record(rec, vals, a, b, dense_in, C0, Cout):
+        nonlocal i
+        arrays[f"v{i}"], arrays[f"a{i}"], arrays[f"b{i}"] = vals, a, b
+        arrays[f"D{i}"], arrays[f"C{i}"], arrays[f"O{i}"] = dense_in, C0, Cout
+        meta.append(rec)
+        i += 1
+
+    def one(side, fmt, lay, opA, opB, dt, d, n, m, alpha, beta, offs=(0, 0), extra=(0, 0),
+            density=0.3, nan_c=False, dup=False, short_ld=None):
+        npdt = np.float32 if dt == 0 else np.float64
+        # the sparse operand, before its op: (sr x sc) = op^-1 of (d x m) on the left,
+        # of (n x d) on the right (right: C (m x d) = op(A) (m x n) op(submat(B)) (n x d))
+        if side == 0:
+            sr, sc = (d, m) if opA == 0 else (m, d)
+        else:
+            sr, sc = (n, d) if opB == 0 else (d, n)
+        ro, co = offs
+        Sr, Sc = sr + ro + extra[0], sc + co + extra[1]
+        vals, a, b = _sparse_arrays(rng, Sr, Sc, density, fmt, npdt, dup)
+        if side == 0:
+            br, bc = (m, n) if opB == 0 else (n, m)
+            cr, cc = d, n
+        else:
+            br, bc = (m, n) if opA == 0 else (n, m)
+            cr, cc = m, d
+        ldd = (br if lay == 0 else bc) + (-1 if short_ld == "dense" else 2)
+        ldc = (cr if lay == 0 else cc) + (-1 if short_ld == "C" else 1)
+        dense_in = rng.standard_normal(ldd * (bc if lay == 0 else br)).astype(npdt)
+        C0 = rng.standard_normal(ldc * (cc if lay == 0 else cr)).astype(npdt)
+        if nan_c:
+            C0[:] = np.nan
+        Cout = C0.copy()
+        if side == 0:
+            rc, msg = ref.left_spmm(dt, lay, opA, opB, d, n, m, alpha, fmt, Sr, Sc, vals, a, b,
+                                    ro, co, dense_in, ldd, beta, Cout, ldc)
+        else:
+            rc, msg = ref.right_spmm(dt, lay, opA, opB, m, d, n, alpha, dense_in, ldd, fmt, Sr,
+                                     Sc, vals, a, b, ro, co, beta, Cout, ldc)
+        record(dict(side=side, fmt=fmt, layout=lay, opA=opA, opB=opB, dtype=dt, d=d, n=n, m=m,
+                    alpha=alpha, beta=beta, ro=ro, co=co, S_rows=Sr, S_cols=Sc, ldd=ldd,
+                    ldc=ldc, dense_rows=br, dense_cols=bc, C_rows=cr, C_cols=cc, rc=rc, msg=msg),
+               vals, a, b, dense_in, C0, Cout)
+
+    for side, fmt, lay, opA, opB, dt in itertools.product((0, 1), (0, 1, 2), (0, 1), (0, 1),
+                                                          (0, 1), (0, 1)):
+        offs = (2, 3) if fmt == 0 else (0, 0)
+        extra = (1, 2) if fmt == 0 else (0, 0)
+        one(side, fmt, lay, opA, opB, dt, 9, 7, 40, 0.75 if i % 3 else -1.5,
+            0.0 if i % 2 else 0.5, offs, extra, nan_c=(i % 4 == 1))
+    # COO with repeated (row, col) pairs, with and without offsets
+    for side, lay, opA, opB in itertools.product((0, 1), (0, 1), (0, 1), (0, 1)):
+        one(side, 0, lay, opA, opB, 1, 11, 5, 33, 1.25, 0.25, (1, 1) if lay else (0, 0),
+            (2, 1) if lay else (0, 0), density=0.4, dup=True)
+    # alpha = 0: C = beta * C, the sparse data is not read
+    for side, fmt in itertools.product((0, 1), (0, 1, 2)):
+        one(side, fmt, 1, 0, 0, 1, 6, 4, 20, 0.0, -2.0)
+        one(side, fmt, 0, 1, 0, 0, 6, 4, 20, 0.0, 0.0, nan_c=True)
+    # no nonzeros at all
+    for side, fmt in itertools.product((0, 1), (0, 1, 2)):
+        one(side, fmt, 0, 0, 1, 1, 8, 3, 17, 1.0, 0.5, density=0.0)
+    # a larger case (multi-block kernels): FP32, every format, both sides
+    for side, fmt in itertools.product((0, 1), (0, 1, 2)):
+        one(side, fmt, 1, 0, 0, 0, 64, 16, 300, 1.0, 0.0, density=0.05)
+    # the reference's argument checks: CSR / CSC data must match the sizes exactly and take no
+    # offsets; COO must be at least the submatrix
+    for side, fmt in itertools.product((0, 1), (1, 2)):
+        one(side, fmt, 0, 0, 0, 1, 6, 4, 20, 1.0, 0.0, offs=(1, 0), extra=(-1, 0))
+        one(side, fmt, 1, 1, 0, 1, 6, 4, 20, 1.0, 0.0, offs=(0, 1), extra=(0, -1))
+        one(side, fmt, 0, 0, 1, 1, 6, 4, 20, 1.0, 0.0, extra=(1, 0))
+    for side in (0, 1):
+        one(side, 0, 0, 0, 0, 1, 6, 4, 20, 1.0, 0.0, offs=(0, 0), extra=(-1, 0))
+    # leading dimensions below the stored sizes
+    for side, lay, opD, which in itertools.product((0, 1), (0, 1), (0, 1), ("dense", "C")):
+        if side == 0:
+            one(side, 1, lay, 0, opD, 0, 6, 4, 20, 1.0, 0.0, short_ld=which)
+        else:
+            one(side, 2, lay, opD, 0, 0, 6, 4, 20, 1.0, 0.0, short_ld=which)
+    np.savez_compressed(os.path.join(HERE, "spmm.npz"), meta=json.dumps(meta), **arrays)
+    return len(meta)
+
+
+def shared_math_fixtures(ref, full):
+    """Digests of the reference's own 200 x 10000 Gaussian FP64 operator (seeded after its data
+    matrix, counter 125000) and of its FP32 form with Box-Muller's sin / cos / log taken from
+    the shared float-float specification (RefLib.set_math(1)): with the same math functions
+    the GPU must reproduce them bit for bit."""
+    ref.set_math(1)
+    try:
+        out = {}
+        for name, dt in (("f64", 1), ("f32", 0)):
+            buf, nxt = ref.fill_dense_unpacked(dt, 1, 200, 10000, 0, 1, 200, 10000, 0, 0,
+                                               State.make([125000, 0, 0, 0], [0, 0]))
+            out[name] = dict(sha256=hashlib.sha256(buf.tobytes()).hexdigest(), next=st(nxt))
+    finally:
+        ref.set_math(0)
+    full["dense_200x10000_shared_math"] = dict(dist=dict(n_rows=200, n_cols=10000, family=0,
+                                                         axis=1),
+                                               seed=[[125000, 0, 0, 0], [0, 0]], layout=1,
+                                               **out)
+
+
 def main():
     ref = RefLib()
+    if sys.argv[1:] == ["shared_math"]:
+        path = os.path.join(HERE, "full_size.json")
+        with open(path) as f:
+            full = json.load(f)
+        shared_math_fixtures(ref, full)
+        with open(path, "w") as f:
+            json.dump(full, f, indent=1)
+        print("shared-math digests written to", path)
+        return
+    if sys.argv[1:] == ["spmm"]:
+        print(spmm_fixtures(ref), "spmm fixtures written to", HERE)
+        return
     if sys.argv[1:] == ["sparse_convert"]:
         sparse_convert_fixtures(ref)
         print("sparse_convert fixtures written to", HERE)
@@ -357,9 +512,11 @@ def main():
                                      cols_sha256=hashlib.sha256(cols.tobytes()).hexdigest(),
                                      vals_sha256=hashlib.sha256(vals.tobytes()).hexdigest())
     full["random_csr_2^17x512"] = random_sparse_fixtures(ref)
+    shared_math_fixtures(ref, full)
     with open(os.path.join(HERE, "full_size.json"), "w") as f:
         json.dump(full, f, indent=1)
     sparse_convert_fixtures(ref)
+    spmm_fixtures(ref)
     print("golden fixtures written to", HERE)
 
 

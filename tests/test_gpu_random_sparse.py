@@ -1,7 +1,8 @@
 """GPU random_coo / random_csr / random_csc (sparse_data/random_matrix.hh:135-355) against the
 reference's outputs (golden fixtures), its full-size digest and the oracle: nonzero counts,
 index arrays, pointers and next states bit for bit; Gaussian values within the Box-Muller
-bound of the dense fills (the same transform on the same words)."""
+bound of the dense fills against the reference's glibc build, and bit for bit against the
+oracle evaluated with the shared math functions (the same transform on the same words)."""
 import hashlib
 import math
 import warnings
@@ -15,7 +16,7 @@ from oracle.oracle import State
 
 pytestmark = pytest.mark.gpu
 
-GAUSS_ULP_MAX = 3  # as for fill_dense's Gaussians: glibc's sincosf / logf vs correctly rounded
+GAUSS_ULP_MAX_GLIBC = 3  # as for fill_dense's Gaussians: glibc's sincosf / logf vs the shared math
 
 
 def _gen(rb, fmt, m, n, density, state, dtype, itype):
@@ -37,13 +38,13 @@ def _check_values(got, ref, what):
     if got.size == 0:
         return 1.0
     u = ulp_distance(got.astype(np.float32), ref.astype(np.float32))
-    assert u.max() <= GAUSS_ULP_MAX, (what, int(u.max()))
+    assert u.max() <= GAUSS_ULP_MAX_GLIBC, (what, int(u.max()))
     # FP64 matrices hold float Box-Muller values promoted to double, as in the reference
     assert np.array_equal(got.astype(np.float32).astype(got.dtype), got), what
     return float(np.mean(u == 0))
 
 
-def test_random_sparse_golden(rb):
+def test_random_sparse_golden(rb, oracle):
     import torch
     meta, z = load_golden("random_sparse")
     exact = []
@@ -60,7 +61,12 @@ def test_random_sparse_golden(rb):
         assert np.array_equal(a, ra), c
         assert np.array_equal(b, z[f"b{i}"]), c
         exact.append(_check_values(vals, z[f"v{i}"], c))
-    print("golden cases:", len(meta), "exact value fraction (min):", min(exact))
+        with oracle.shared_math():
+            ov, oa, ob, _ = oracle.random_sparse(c["fmt"], c["dtype"], c["itype"], c["m"],
+                                                 c["n"], c["density"],
+                                                 State.make(c["ctr"], c["key"]))
+        assert np.array_equal(vals.view(np.uint8), ov.view(np.uint8)), c
+    print("golden cases:", len(meta), "exact value fraction vs glibc (min):", min(exact))
 
 
 def test_random_csr_full_size_digest(rb, oracle):
@@ -77,7 +83,11 @@ def test_random_csr_full_size_digest(rb, oracle):
     ov, _, _, _ = oracle.random_sparse(1, 0, 1, g["m"], g["n"], g["density"], State.make(*seed))
     frac = _check_values(vals, ov, "full size")
     assert frac > 0.95
-    print("2^17 x 512 CSR: nnz", vals.size, "exact values", frac)
+    with oracle.shared_math():
+        ovs, _, _, _ = oracle.random_sparse(1, 0, 1, g["m"], g["n"], g["density"],
+                                            State.make(*seed))
+    assert np.array_equal(vals.view(np.uint32), ovs.view(np.uint32))
+    print("2^17 x 512 CSR: nnz", vals.size, "exact values vs glibc", frac)
 
 
 @pytest.mark.parametrize("fmt,m,n,density", [

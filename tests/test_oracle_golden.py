@@ -120,3 +120,46 @@ def test_sparse_conversions_match_reference(oracle):
             assert np.array_equal(ptr, z[f"{s}p{i}"]), (c, s)
             assert np.array_equal(oracle.compressed_ptr_to_sorted_idxs(ptr, c["nnz"],
                                                                        major.dtype), major)
+
+
+def test_shared_math_oracle_digests(oracle):
+    """The oracle in its shared-math mode reproduces the reference's own 200 x 10000 Gaussian
+    operator computed with the same math functions (digests from tests/golden), FP64 and FP32,
+    and its default mode is left untouched afterwards."""
+    g = golden_json("full_size.json")["dense_200x10000_shared_math"]
+    with oracle.shared_math():
+        for name, dt in (("f64", 1), ("f32", 0)):
+            buf, nxt = oracle.fill_dense_unpacked(dt, 1, 200, 10000, 0, 1, 200, 10000, 0, 0,
+                                                  State.make(*g["seed"]))
+            assert hashlib.sha256(buf.tobytes()).hexdigest() == g[name]["sha256"], name
+            assert [list(nxt.counter), list(nxt.key)] == g[name]["next"]
+    assert oracle.lib.orc_get_math() == 0
+    buf, _ = oracle.fill_dense_unpacked(1, 1, 200, 10000, 0, 1, 200, 10000, 0, 0,
+                                        State.make(*g["seed"]))
+    assert hashlib.sha256(buf.tobytes()).hexdigest() != g["f64"]["sha256"]
+
+
+def test_shared_math_oracle_matches_reference_code(oracle, reflib):
+    """With the shared math functions in both, the restatement and the reference's own headers
+    agree bit for bit on Gaussian fills (every layout, both types, submatrices) and on the
+    values of random sparse matrices; run where the reference tree is present."""
+    reflib.set_math(1)
+    try:
+        with oracle.shared_math():
+            for dt, lay, (R, Cc, nr, nc, ro, co) in [
+                    (0, 1, (300, 7000, 300, 7000, 0, 0)), (1, 0, (300, 7000, 120, 5001, 7, 11)),
+                    (0, 0, (9000, 50, 8000, 33, 5, 3)), (1, 1, (9000, 50, 9000, 50, 0, 0))]:
+                seed = State.make([17, 3, 0, 0], [9, 1])
+                a, an = oracle.fill_dense_unpacked(dt, lay, R, Cc, 0, 1, nr, nc, ro, co, seed)
+                b, bn = reflib.fill_dense_unpacked(dt, lay, R, Cc, 0, 1, nr, nc, ro, co, seed)
+                assert np.array_equal(a.view(np.uint8), b.view(np.uint8))
+                assert list(an.counter) == list(bn.counter)
+            for fmt in (0, 1, 2):
+                ov, oa, ob, _ = oracle.random_sparse(fmt, 0, 1, 3000, 400, 0.01,
+                                                     State.from_key(5))
+                rv, ra, rb_, _ = reflib.random_sparse(fmt, 0, 1, 3000, 400, 0.01,
+                                                      State.from_key(5))
+                assert np.array_equal(ov.view(np.uint32), rv.view(np.uint32))
+                assert np.array_equal(ob, rb_)
+    finally:
+        reflib.set_math(0)
