@@ -9,9 +9,9 @@ path on the same GPU.  Secondary: the 1024 x 2^20 SASO (8 nonzeros per column) s
 2^20 x 256 N(0,1) matrix, reported in GB/s against the measured HBM copy bandwidth.
 
 python bench.py [--gpus 1] [--steps K] [--warmup W] [--impl ours|reference]
-The GPU path is measured on one GPU only: the tensor-core kernel loads A tiles with TMA
-multicast inside a thread-block cluster, which is meant for one GPU's own memory, so
-``--gpus N`` with N > 1 (or a torchrun launch with WORLD_SIZE > 1) is refused with exit status 2.
+The GPU path is measured on one GPU only: the sketch needs no exchange between GPUs and the
+benchmark runs no replicas, so ``--gpus N`` with N > 1 (or a torchrun launch with
+WORLD_SIZE > 1) is refused with exit status 2.
 The reference arm (``--impl reference``) runs on the host cores of rank 0 only.
 """
 from __future__ import annotations
@@ -374,16 +374,13 @@ def host_info():
 
 
 def refuse_multi_gpu(args, rank, world):
-    """The GPU arm measures one GPU.  Its tensor-core kernel shares A tiles between the CTAs of
-    a thread-block cluster with TMA multicast, which is only meant for one GPU's own memory,
-    so no multi-GPU launch of it is offered: every rank exits with status 2, rank 0 saying
-    why on stderr."""
+    """The GPU arm measures one GPU; no multi-GPU launch of it is offered: every rank exits with
+    status 2, rank 0 saying why on stderr."""
     if rank == 0:
         sys.stderr.write(json.dumps({
             "metric": METRIC, "error": "bench.py measures one GPU only",
             "requested_gpus": max(args.gpus, world),
-            "why": "the tensor-core sketch uses TMA multicast inside a cluster; it runs in "
-                   "single-GPU processes only"}) + "\n")
+            "why": "the benchmark measures the single-GPU sketch; it runs no replicas"}) + "\n")
     sys.exit(2)
 
 

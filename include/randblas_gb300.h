@@ -390,10 +390,8 @@ int rbg_lskge3_lowp_workspace(int32_t precision, int64_t d, int64_t n, int64_t m
  * workspace: buffer of rbg_lskge3_lowp_workspace bytes in device memory of the current GPU
  * (cudaMalloc on the device the call runs on; other devices' memory, managed memory and host
  * memory are rejected with RBG_ERROR_INVALID_ARGUMENT), or NULL to let the call allocate
- * (stream-ordered) and free it.  The kernel shares A tiles between the CTAs of a thread-block
- * cluster with TMA multicast, so this path is for single-GPU processes: call it on one GPU,
- * with its buffers on that GPU (or in host memory as below), never as one rank of a multi-GPU
- * job.
+ * (stream-ordered) and free it.  The call runs on one GPU, the current one: its buffers live
+ * on that GPU (or in host memory as below).
  * A and B may be device memory or host memory the GPU can read (pinned/registered memory, or
  * any host memory where the device reports cudaDevAttrPageableMemoryAccess); B is then written
  * in place.  For BF16 with pinned A, K >= 2^18, op(A) row- or column-contiguous and no

@@ -9,9 +9,8 @@
 //  1. convert: op(A) (FP32 or BF16, any layout) -> At, k-blocked ([k / 64 bytes][n][64 bytes]),
 //     so every stage's TMA box is one contiguous block; BF16, or e4m3 after dividing by the
 //     power-of-two scale of its (K slice, column).
-//  2. sketch: persistent clusters of CN x CM CTAs (one per SM), 24 warps with fixed roles --
-//       warp 0      TMA producer: A tiles (512 n-rows x 64 bytes of k) into a 5-stage ring,
-//                   multicast to the CTA's M-peer;
+//  2. sketch: persistent clusters of CN CTAs (one per SM), 24 warps with fixed roles --
+//       warp 0      TMA producer: A tiles (512 n-rows x 64 bytes of k) into a 5-stage ring;
 //       warp 1      MMA issuer (one thread) and tensor-memory owner (512 columns);
 //       warps 4-7   epilogue: tensor memory -> registers -> FP32 partial tile in HBM;
 //       warps 8-23  S producers in 4 groups taking stages in turn: Philox4x32-10 + transform
@@ -90,7 +89,7 @@ struct LowpParams {
     int64_t r0, c0;        // natural coordinates of submat(S)(0, 0)
     int r_on_i;            // 1: natural row follows the output row i
     int64_t k_steps;       // ceil(K / k per stage)
-    int64_t m_groups;      // row groups, each CM tiles of BM rows
+    int64_t m_groups;      // row tiles of BM rows
     int64_t n_groups;      // column groups, each CN tiles of BN columns
     int64_t ks_per_group;  // k-steps per K slice
     int64_t units;         // m_groups * n_groups * k_groups
@@ -258,20 +257,20 @@ __device__ __forceinline__ void produce_s_generic(uint8_t *tile, const LowpParam
     }
 }
 
-// One CTA computes a BM x BN output tile over one K slice per work unit.  The CTAs of a
-// cluster of CN x CM share work: the CN CTAs of a row group hold the same BM rows of S and
-// different BN-column tiles of A -- each produces BM / CN rows of every S stage and copies them
-// into its peers with a bulk shared-memory copy -- and the CM CTAs of a column group hold the
-// same A tile, which each loads a 1 / CM share of with a TMA multicast to all of them.
+// One CTA computes a BM x BN output tile over one K slice per work unit.  The CN CTAs of a
+// cluster hold the same BM rows of S and different BN-column tiles of A: each produces BM / CN
+// rows of every S stage and copies them into its peer with a bulk shared-memory copy.  Each
+// CTA loads its own A tiles (no multicast: clusters of two CTAs tile every SM, and CTAs whose
+// A loads do not wait on each other measured faster than pairs sharing them).
 // kFast: natural row follows i and the operator's column offset is a multiple of 4, so every
 // k chunk starts on a counter block.  kFp8: e4m3 operands (kind::f8f6f4, 64 k per stage) and
 // the epilogue multiplies each column by its K slice's scale; else BF16 (kind::f16, 32 k).
-template <int CN, int CM, bool kFast, bool kFp8>
+template <int CN, bool kFast, bool kFp8>
 __global__ void __launch_bounds__(NUM_THREADS, 1)
     sketch_tc_kernel(const __grid_constant__ CUtensorMap tmap_a, LowpParams p) {
     constexpr int BKE = Elem<kFp8>::BK;
     constexpr int PER_CHUNK = Elem<kFp8>::PER_CHUNK;
-    constexpr int CS = CN * CM;
+    constexpr int CS = CN;
     constexpr int ROWS = BM / CN;                        // S rows this CTA produces per stage
     constexpr uint32_t PART_BYTES = ROWS * ROW_BYTES;    // their bytes in a stage
     constexpr int ROW_SLOTS = GROUP_THREADS / CHUNKS;    // rows a generator group covers at once
@@ -293,7 +292,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const uint32_t rank = CS > 1 ? tc::cluster_ctarank() : 0u;
-    const uint32_t n_idx = rank % CN, m_idx = rank / CN;
+    const uint32_t n_idx = rank;
     const int64_t cluster_id = blockIdx.x / CS;
     const int64_t num_clusters = gridDim.x / CS;
     if (threadIdx.x == 0) {
@@ -320,7 +319,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
         const int64_t mg = u % p.m_groups;
         const int64_t ng = (u / p.m_groups) % p.n_groups;
         const int64_t g = u / (p.m_groups * p.n_groups);
-        m0 = (mg * CM + m_idx) * BM;
+        m0 = mg * BM;
         n0 = (ng * CN + n_idx) * BN;
         ks0 = g * p.ks_per_group;
         ks1 = min(p.k_steps, ks0 + p.ks_per_group);
@@ -341,17 +340,9 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
                     tc::mbar_arrive_expect_tx(&full[s], A_STAGE_BYTES);
                     uint8_t *dst = a_tiles + s * A_STAGE_BYTES;
                     const int64_t row0 = ks * p.npad + n0;  // k-blocked layout
-                    if (CM == 2) {
-                        // this CTA loads half h = m_idx of the tile for itself and its M-peer
-                        const uint16_t mask = (uint16_t)((1u << rank) | (1u << (rank ^ CN)));
-                        tc::tma_load_2d_multicast(dst + m_idx * (A_STAGE_BYTES / 2), &tmap_a,
-                                                  &full[s], 0,
-                                                  (int)(row0 + m_idx * (BN / 2)), mask);
-                    } else {
-                        tc::tma_load_2d(dst, &tmap_a, &full[s], 0, (int)row0);
-                        tc::tma_load_2d(dst + A_STAGE_BYTES / 2, &tmap_a, &full[s], 0,
-                                        (int)(row0 + BN / 2));
-                    }
+                    tc::tma_load_2d(dst, &tmap_a, &full[s], 0, (int)row0);
+                    tc::tma_load_2d(dst + A_STAGE_BYTES / 2, &tmap_a, &full[s], 0,
+                                    (int)(row0 + BN / 2));
                 }
             }
         }
@@ -504,11 +495,12 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
         const int gi = gw / (GEN_WARPS / GEN_GROUPS);
         const int tg = (gw % (GEN_WARPS / GEN_GROUPS)) * 32 + lane;
         const int row_lo = (int)n_idx * ROWS;
-        uint32_t peer_full[STAGES] = {};
-        uint32_t peer_tiles = 0;
+        // the N-peer's copies of the full barriers and S tiles (stage s at + 8 s and
+        // + s * S_STAGE_BYTES): shared::cluster addresses, computed rather than kept in an
+        // array indexed by the stage, which would live in local memory
+        uint32_t peer_full0 = 0, peer_tiles = 0;
         if (CN > 1) {
-            for (int s = 0; s < STAGES; ++s)
-                peer_full[s] = tc::map_to_rank(tc::smem_addr(&full[s]), rank ^ 1u);
+            peer_full0 = tc::map_to_rank(tc::smem_addr(&full[0]), rank ^ 1u);
             peer_tiles = tc::map_to_rank(tc::smem_addr(s_tiles), rank ^ 1u);
         }
         const int fc = tg % CHUNKS;
@@ -556,7 +548,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
                         tc::mbar_arrive_expect_tx(&full[s], PART_BYTES);
                         const uint32_t off = (uint32_t)(s * S_STAGE_BYTES + row_lo * ROW_BYTES);
                         tc::bulk_copy_to_peer(peer_tiles + off, s_tiles + off, PART_BYTES,
-                                              peer_full[s]);
+                                              peer_full0 + 8u * (uint32_t)s);
                     } else {
                         tc::mbar_arrive(&full[s]);
                     }
@@ -795,7 +787,7 @@ struct Plan {
     int bke;  // k values per stage
     int64_t k_steps, tiles_m, tiles_n, m_groups, n_groups, groups, ks_per_group, units, kpad,
         npad;
-    int cn, cm;
+    int cn;
     size_t at_bytes, amax_bytes, partial_bytes, total;
 };
 
@@ -809,10 +801,9 @@ Plan make_plan(int64_t M, int64_t N, int64_t K, bool fp8) {
     pl.tiles_m = (M + BM - 1) / BM;
     pl.tiles_n = (N + BN - 1) / BN;
     pl.cn = pl.tiles_n >= 2 ? 2 : 1;
-    pl.cm = pl.tiles_m >= 2 ? 2 : 1;
-    pl.m_groups = (pl.tiles_m + pl.cm - 1) / pl.cm;
+    pl.m_groups = pl.tiles_m;
     pl.n_groups = (pl.tiles_n + pl.cn - 1) / pl.cn;
-    const int slots = std::max(1, resident_clusters(pl.cn * pl.cm));
+    const int slots = std::max(1, resident_clusters(pl.cn));
     pl.kpad = pl.k_steps * pl.bke;
     pl.npad = pl.tiles_n * BN;
     // K slices: the fewest estimated seconds -- waves of resident clusters times the k-steps of
@@ -844,36 +835,36 @@ Plan make_plan(int64_t M, int64_t N, int64_t K, bool fp8) {
     return pl;
 }
 
-template <int CN, int CM, bool kFast, bool kFp8>
+template <int CN, bool kFast, bool kFp8>
 void set_smem_attr() {
     static bool done = false;
     if (!done) {
-        RBG_CUDA(cudaFuncSetAttribute(sketch_tc_kernel<CN, CM, kFast, kFp8>,
+        RBG_CUDA(cudaFuncSetAttribute(sketch_tc_kernel<CN, kFast, kFp8>,
                                       cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
         done = true;
     }
 }
 
-template <int CN, int CM>
+template <int CN>
 int query_resident_clusters() {
-    set_smem_attr<CN, CM, true, false>();
+    set_smem_attr<CN, true, false>();
     cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3(CN * CM * 256);
+    cfg.gridDim = dim3(CN * 256);
     cfg.blockDim = dim3(NUM_THREADS);
     cfg.dynamicSmemBytes = SMEM_BYTES;
     cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeClusterDimension;
-    attr[0].val.clusterDim.x = CN * CM;
+    attr[0].val.clusterDim.x = CN;
     attr[0].val.clusterDim.y = 1;
     attr[0].val.clusterDim.z = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
     int n = 0;
     const cudaError_t e =
-        cudaOccupancyMaxActiveClusters(&n, sketch_tc_kernel<CN, CM, true, false>, &cfg);
+        cudaOccupancyMaxActiveClusters(&n, sketch_tc_kernel<CN, true, false>, &cfg);
     if (e != cudaSuccess || n <= 0) {
         cudaGetLastError();
-        n = num_sms() / (CN * CM);
+        n = num_sms() / CN;
     }
     return n;
 }
@@ -881,45 +872,40 @@ int query_resident_clusters() {
 // Clusters of `cs` CTAs (one CTA per SM) that fit on the current device at once.
 int resident_clusters(int cs) {
     static std::mutex mu;
-    static int cached[64][5] = {};
+    static int cached[64][3] = {};
     int dev = 0;
     RBG_CUDA(cudaGetDevice(&dev));
     if (dev < 0 || dev >= 64) dev = 0;
     std::lock_guard<std::mutex> g(mu);
     int &c = cached[dev][cs];
-    if (!c) c = cs == 1 ? query_resident_clusters<1, 1>()
-                : cs == 2 ? query_resident_clusters<2, 1>()
-                          : query_resident_clusters<2, 2>();
+    if (!c) c = cs == 1 ? query_resident_clusters<1>() : query_resident_clusters<2>();
     return c;
 }
 
-template <int CN, int CM, bool kFast, bool kFp8>
+template <int CN, bool kFast, bool kFp8>
 void launch_sketch(int clusters, const CUtensorMap &map, const LowpParams &p, cudaStream_t s) {
-    set_smem_attr<CN, CM, kFast, kFp8>();
+    set_smem_attr<CN, kFast, kFp8>();
     cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3((unsigned)(clusters * CN * CM));
+    cfg.gridDim = dim3((unsigned)(clusters * CN));
     cfg.blockDim = dim3(NUM_THREADS);
     cfg.dynamicSmemBytes = SMEM_BYTES;
     cfg.stream = s;
     cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeClusterDimension;
-    attr[0].val.clusterDim.x = CN * CM;
+    attr[0].val.clusterDim.x = CN;
     attr[0].val.clusterDim.y = 1;
     attr[0].val.clusterDim.z = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    RBG_CUDA(cudaLaunchKernelEx(&cfg, sketch_tc_kernel<CN, CM, kFast, kFp8>, map, p));
+    RBG_CUDA(cudaLaunchKernelEx(&cfg, sketch_tc_kernel<CN, kFast, kFp8>, map, p));
     RBG_LAUNCHED();
 }
 
 template <bool kFast, bool kFp8>
 void launch_for(const Plan &pl, const CUtensorMap &map, const LowpParams &p, cudaStream_t s) {
-    const int clusters =
-        (int)std::min<int64_t>(pl.units, resident_clusters(pl.cn * pl.cm));
-    if (pl.cn == 2 && pl.cm == 2) launch_sketch<2, 2, kFast, kFp8>(clusters, map, p, s);
-    else if (pl.cn == 2) launch_sketch<2, 1, kFast, kFp8>(clusters, map, p, s);
-    else if (pl.cm == 2) launch_sketch<1, 2, kFast, kFp8>(clusters, map, p, s);
-    else launch_sketch<1, 1, kFast, kFp8>(clusters, map, p, s);
+    const int clusters = (int)std::min<int64_t>(pl.units, resident_clusters(pl.cn));
+    if (pl.cn == 2) launch_sketch<2, kFast, kFp8>(clusters, map, p, s);
+    else launch_sketch<1, kFast, kFp8>(clusters, map, p, s);
 }
 
 
@@ -1241,9 +1227,9 @@ void require_gpu_accessible(const void *p, const char *name) {
                                  "(cudaHostRegister / cudaMallocHost) or pass device memory");
 }
 
-// A caller's workspace holds the converted copy of A that the tensor-core kernel loads with
-// TMA, shared between the CTAs of a cluster by multicast: it must be memory of the current GPU
-// itself -- not another GPU's memory, managed memory, or host memory mapped into this GPU.
+// A caller's workspace holds the converted copy of A that the tensor-core kernel streams
+// through TMA at HBM rate: it must be memory of the current GPU itself -- not another GPU's
+// memory, managed memory, or host memory mapped into this GPU.
 void require_current_device_memory(const void *p, const char *name) {
     cudaPointerAttributes pa{};
     if (cudaPointerGetAttributes(&pa, p) != cudaSuccess) {

@@ -35,52 +35,57 @@ __device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t *bar, uint32_t by
                  : "memory");
 }
 
-__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
+// try_wait with a suspend-time hint: a thread whose phase is not complete is parked by the
+// hardware until the phase completes or `ns` nanoseconds pass, instead of returning at once,
+// so a waiting warp takes no issue slots from the working ones while it waits.
+constexpr uint32_t kSuspendNs = 20000;
+__device__ __forceinline__ bool mbar_try_wait_hint(uint32_t bar, uint32_t parity, uint32_t ns) {
     uint32_t ok;
     asm volatile(
         "{\n\t.reg .pred p;\n\t"
-        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
         "selp.u32 %0, 1, 0, p;\n\t}"
         : "=r"(ok)
-        : "r"(smem_addr(bar)), "r"(parity)
+        : "r"(bar), "r"(parity), "r"(ns)
         : "memory");
     return ok != 0;
 }
-
-// try_wait with acquire at cluster scope (the phase may have been completed by arrivals
-// from another CTA of the cluster).
-__device__ __forceinline__ bool mbar_try_wait_cluster(uint64_t *bar, uint32_t parity) {
+__device__ __forceinline__ bool mbar_try_wait_cluster_hint(uint32_t bar, uint32_t parity,
+                                                           uint32_t ns) {
     uint32_t ok;
     asm volatile(
         "{\n\t.reg .pred p;\n\t"
-        "mbarrier.try_wait.parity.acquire.cluster.shared::cta.b64 p, [%1], %2;\n\t"
+        "mbarrier.try_wait.parity.acquire.cluster.shared::cta.b64 p, [%1], %2, %3;\n\t"
         "selp.u32 %0, 1, 0, p;\n\t}"
         : "=r"(ok)
-        : "r"(smem_addr(bar)), "r"(parity)
+        : "r"(bar), "r"(parity), "r"(ns)
         : "memory");
     return ok != 0;
 }
 
 // Wait for the phase with the given parity to complete, for at most ~`budget` clock cycles.
 // Returns false (after setting *err) on timeout or if another role already raised *err.
-// `backoff` > 0 sleeps that many nanoseconds between polls once the wait is long, so
-// waiting warps leave issue slots to the working ones.
+// Each try parks the thread for up to kSuspendNs (it is woken when the phase completes);
+// between tries the error word and the budget are checked.  `backoff` > 0 additionally
+// sleeps that many nanoseconds between tries once the wait is long.
 template <bool kCluster = false>
 __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, int *err,
                                           unsigned backoff = 0,
                                           long long budget = 8000000000ll) {
-    if (kCluster ? mbar_try_wait_cluster(bar, parity) : mbar_try_wait(bar, parity)) return true;
+    const uint32_t a = smem_addr(bar);
+    if (kCluster ? mbar_try_wait_cluster_hint(a, parity, kSuspendNs)
+                 : mbar_try_wait_hint(a, parity, kSuspendNs))
+        return true;
     const long long t0 = clock64();
     uint32_t spins = 0;
-    while (!(kCluster ? mbar_try_wait_cluster(bar, parity) : mbar_try_wait(bar, parity))) {
+    while (!(kCluster ? mbar_try_wait_cluster_hint(a, parity, kSuspendNs)
+                      : mbar_try_wait_hint(a, parity, kSuspendNs))) {
         ++spins;
         if (backoff && spins > 8) __nanosleep(backoff);
-        if ((spins & 63u) == 0) {
-            if (*(volatile int *)err) return false;
-            if (clock64() - t0 > budget) {
-                atomicCAS(err, 0, RBG_ERROR_TIMEOUT);
-                return false;
-            }
+        if (*(volatile int *)err) return false;
+        if (clock64() - t0 > budget) {
+            atomicCAS(err, 0, RBG_ERROR_TIMEOUT);
+            return false;
         }
     }
     return true;
@@ -97,31 +102,16 @@ __device__ __forceinline__ void mbar_arrive_expect_tx_at(uint32_t bar, uint32_t 
                  : "memory");
 }
 
-__device__ __forceinline__ bool mbar_try_wait_at(uint32_t bar, uint32_t parity) {
-    uint32_t ok;
-    asm volatile(
-        "{\n\t.reg .pred p;\n\t"
-        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-        "selp.u32 %0, 1, 0, p;\n\t}"
-        : "=r"(ok)
-        : "r"(bar), "r"(parity)
-        : "memory");
-    return ok != 0;
-}
-
-// mbar_wait for an mbarrier given by address (same budget and error-word rules).
+// mbar_wait for an mbarrier given by address (same suspend, budget and error-word rules).
 __device__ __forceinline__ bool mbar_wait_at(uint32_t bar, uint32_t parity, int *err,
                                              long long budget = 8000000000ll) {
-    if (mbar_try_wait_at(bar, parity)) return true;
+    if (mbar_try_wait_hint(bar, parity, kSuspendNs)) return true;
     const long long t0 = clock64();
-    uint32_t spins = 0;
-    while (!mbar_try_wait_at(bar, parity)) {
-        if ((++spins & 63u) == 0) {
-            if (*(volatile int *)err) return false;
-            if (clock64() - t0 > budget) {
-                atomicCAS(err, 0, RBG_ERROR_TIMEOUT);
-                return false;
-            }
+    while (!mbar_try_wait_hint(bar, parity, kSuspendNs)) {
+        if (*(volatile int *)err) return false;
+        if (clock64() - t0 > budget) {
+            atomicCAS(err, 0, RBG_ERROR_TIMEOUT);
+            return false;
         }
     }
     return true;
@@ -191,19 +181,6 @@ __device__ __forceinline__ void tma_load_2d_at(uint32_t dst, const CUtensorMap *
         "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes"
         " [%0], [%1, {%3, %4}], [%2];" ::"r"(dst),
         "l"(reinterpret_cast<uint64_t>(map)), "r"(bar), "r"(x), "r"(y)
-        : "memory");
-}
-
-// Tile load delivered to the same shared-memory offset of every CTA in `cta_mask`, each CTA's
-// mbarrier at `bar`'s offset receiving the byte count.
-__device__ __forceinline__ void tma_load_2d_multicast(void *dst, const CUtensorMap *map,
-                                                      uint64_t *bar, int x, int y,
-                                                      uint16_t cta_mask) {
-    asm volatile(
-        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes"
-        ".multicast::cluster [%0], [%1, {%3, %4}], [%2], %5;" ::"r"(smem_addr(dst)),
-        "l"(reinterpret_cast<uint64_t>(map)), "r"(smem_addr(bar)), "r"(x), "r"(y),
-        "h"(cta_mask)
         : "memory");
 }
 

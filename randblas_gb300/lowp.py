@@ -35,8 +35,7 @@ def sketch_lowp(layout: Layout, opS: Op, opA: Op, d: int, n: int, m: int, alpha:
     """B = alpha * op(submat(S)) * op(A) + beta * B on the tensor cores.  A is FP32 or BF16
     (BF16 data enters the tensor cores unchanged); B is FP32.  A and B may be CUDA tensors or
     pinned CPU tensors (A is then read over the host link by the conversion pass, B written in
-    place).  A workspace, if given, is a CUDA tensor on the current device.  The kernel is for
-    single-GPU processes (A tiles are shared inside a thread-block cluster by TMA multicast)."""
+    place).  A workspace, if given, is a CUDA tensor on the current device."""
     if workspace is not None and (not workspace.is_cuda or
                                   workspace.device.index != torch.cuda.current_device()):
         raise _lib.RandBLASError(_lib.ERROR_INVALID_ARGUMENT,
