@@ -504,25 +504,33 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
             peer_tiles = tc::map_to_rank(tc::smem_addr(s_tiles), rank ^ 1u);
         }
         const int fc = tg % CHUNKS;
-        int64_t it = 0;
+        int64_t it_unit = 0;  // the iteration count (shared by every role) at the unit's start
         for (int64_t u = cluster_id; u < p.units; u += num_clusters) {
             int64_t m0, n0, ks0, ks1;
             unit_tiles(u, m0, n0, ks0, ks1);
-            // fast path: counter offset of each owned row's chunk at k-step 0
-            int64_t base[FAST_ROWS > 0 ? FAST_ROWS : 1];
+            // this group's first k-step of the unit, then every GEN_GROUPS-th; its stage and
+            // phase advance by increment (no division per step)
+            const int64_t skip = ((int64_t)gi - it_unit % GEN_GROUPS + GEN_GROUPS) % GEN_GROUPS;
+            int64_t it = it_unit + skip;
+            int s = (int)(it % STAGES);
+            uint32_t ph = (uint32_t)((it / STAGES) & 1);
+            it_unit += ks1 - ks0;
+            const int64_t ks_first = ks0 + skip;
+            // fast path: the counter of each owned row's chunk at the group's first k-step,
+            // advanced by GEN_GROUPS stages of counters per step
+            uint4 ctr[FAST_ROWS > 0 ? FAST_ROWS : 1];
             bool row_ok[FAST_ROWS > 0 ? FAST_ROWS : 1];
             if (kFast) {
 #pragma unroll
                 for (int t = 0; t < FAST_ROWS; ++t) {
                     const int64_t gi_row = m0 + row_lo + tg / CHUNKS + t * ROW_SLOTS;
                     row_ok[t] = gi_row < p.M;
-                    base[t] = (p.r0 + gi_row) * p.gen.stride + p.c0 / 4 + (PER_CHUNK / 4) * fc;
+                    ctr[t] = ctr_add(p.gen.ctr,
+                                     (uint64_t)((p.r0 + gi_row) * p.gen.stride + p.c0 / 4 +
+                                                (PER_CHUNK / 4) * fc + ks_first * (BKE / 4)));
                 }
             }
-            for (int64_t ks = ks0; ks < ks1; ++ks, ++it) {
-                if ((int)(it % GEN_GROUPS) != gi) continue;
-                const int s = (int)(it % STAGES);
-                const uint32_t ph = (uint32_t)((it / STAGES) & 1);
+            for (int64_t ks = ks_first; ks < ks1; ks += GEN_GROUPS) {
                 if (!tc::mbar_wait(&empty[s], ph ^ 1, p.err)) goto done;
                 uint8_t *tile = s_tiles + s * S_STAGE_BYTES;
                 const int64_t gk = ks * BKE + PER_CHUNK * fc;
@@ -530,9 +538,9 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
 #pragma unroll
                     for (int t = 0; t < FAST_ROWS; ++t) {
                         const int i = row_lo + tg / CHUNKS + t * ROW_SLOTS;
-                        const uint4 c = ctr_add(p.gen.ctr, (uint64_t)(base[t] + ks * (BKE / 4)));
                         const uint4 w = row_ok[t]
-                                            ? gen_chunk_aligned<kFp8>(p.gen.family, c, p.gen.key)
+                                            ? gen_chunk_aligned<kFp8>(p.gen.family, ctr[t],
+                                                                      p.gen.key)
                                             : make_uint4(0, 0, 0, 0);
                         *reinterpret_cast<uint4 *>(tile + sw_byte(i, 16 * fc)) = w;
                     }
@@ -552,6 +560,17 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
                     } else {
                         tc::mbar_arrive(&full[s]);
                     }
+                }
+                if (kFast) {
+#pragma unroll
+                    for (int t = 0; t < FAST_ROWS; ++t)
+                        ctr[t] = ctr_add_u32(ctr[t], (uint32_t)(GEN_GROUPS * (BKE / 4)));
+                }
+                // GEN_GROUPS <= STAGES: at most one wrap of the ring per step
+                s += GEN_GROUPS;
+                if (s >= STAGES) {
+                    s -= STAGES;
+                    ph ^= 1u;
                 }
             }
         }
