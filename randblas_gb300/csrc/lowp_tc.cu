@@ -80,6 +80,8 @@ static_assert(GEN_THREADS % GEN_GROUPS == 0 && GROUP_THREADS % 32 == 0, "generat
 // already complete, so GEN_GROUPS must not exceed STAGES; with more groups a wait can pass a
 // phase early, merging two phases of the stage's barriers.
 static_assert(GEN_GROUPS <= STAGES, "generator groups must not outnumber the stages");
+// group gi synchronises on named barrier 1 + gi; the hardware has barriers 0 .. 15
+static_assert(GEN_GROUPS + 1 <= 16, "one named barrier per generator group");
 constexpr uint32_t TMEM_COLS = 512;
 constexpr int SMEM_BYTES = STAGES * (S_STAGE_BYTES + A_STAGE_BYTES) + 1024 /*align*/ + 256;
 
