@@ -454,7 +454,9 @@ def bench_autograd(torch, rb, device, stream, bf16_peak):
     flops = 2 * 2.0 * d * m * n
     for name, prec, dt in (("fp32_plain", None, torch.float32), ("bf16_tc", "bf16", torch.float32),
                            ("bf16_tc_bf16_input", "bf16", torch.bfloat16)):
-        A = A0.to(dt).requires_grad_(True)
+        # a fresh leaf for every variant (A0.to(float32) would return A0 itself, which would
+        # then require grad and put a cast into the next variant's graph)
+        A = A0.to(dt, copy=True).requires_grad_(True)
 
         def step():
             A.grad = None

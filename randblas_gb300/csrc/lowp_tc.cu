@@ -259,15 +259,83 @@ __device__ __forceinline__ void produce_s_generic(uint8_t *tile, const LowpParam
     }
 }
 
+// Four consecutive natural-column entries at a block-aligned counter, finished as the
+// reduced-precision paths take them (uniform entries scaled by sqrt(3)).
+__device__ __forceinline__ void gen4_finished(int family, uint4 c, uint2 key, float v[4]) {
+    if (family == RBG_UNIFORM) {
+        const uint4 r = philox(c, key);
+        v[0] = __fmul_rn(uneg11_fma(r.x), 1.7320508075688772f);
+        v[1] = __fmul_rn(uneg11_fma(r.y), 1.7320508075688772f);
+        v[2] = __fmul_rn(uneg11_fma(r.z), 1.7320508075688772f);
+        v[3] = __fmul_rn(uneg11_fma(r.w), 1.7320508075688772f);
+    } else {
+        gen4<true>(family, c, key, v);
+    }
+}
+
+// The part of one S stage this CTA produces when the operator enters transposed (natural
+// row = k, natural column = output row i) and the column offset is a multiple of 4: one
+// Philox call gives the entries of 4 consecutive output rows at one k.  A work item is an
+// i-quad by KC consecutive k: KC calls, then one KC-value store into each of the 4 rows of
+// the K-major tile.  The stage must lie inside K (the caller falls back to the generic
+// producer for a last, partial one); rows past M are zero.
+template <bool kFp8, int KC>
+__device__ __forceinline__ void produce_s_transposed(uint8_t *tile, const LowpParams &p,
+                                                     int64_t i0, int64_t k0, int row_lo,
+                                                     int rows, int gt, int nth) {
+    constexpr int BKE = Elem<kFp8>::BK;
+    constexpr int BYTES = Elem<kFp8>::BYTES;
+    static_assert(KC * BYTES == 8 || KC * BYTES == 16, "one 8- or 16-byte store per row");
+    constexpr int KCS = BKE / KC;
+    for (int u = gt; u < (rows / 4) * KCS; u += nth) {
+        const int kc = u % KCS, q4 = u / KCS;
+        const int64_t gi = i0 + row_lo + 4 * q4;  // first of the 4 output rows
+        const int64_t gk = k0 + kc * KC;
+        uint4 c = ctr_add(p.gen.ctr, (uint64_t)((p.r0 + gk) * p.gen.stride + (p.c0 + gi) / 4));
+        float v[KC][4];
+#pragma unroll
+        for (int kk = 0; kk < KC; ++kk) {
+            gen4_finished(p.gen.family, c, p.gen.key, v[kk]);
+            if (kk + 1 < KC) c = ctr_add(c, (uint64_t)p.gen.stride);
+        }
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+            const bool ok = gi + e < p.M;
+            uint8_t *dst = tile + sw_byte(row_lo + 4 * q4 + e, kc * KC * BYTES);
+            if constexpr (KC * BYTES == 16) {
+                uint4 w;
+                if constexpr (kFp8)
+                    w = make_uint4(pack_e4m3x4(v[0][e], v[1][e], v[2][e], v[3][e]),
+                                   pack_e4m3x4(v[4][e], v[5][e], v[6][e], v[7][e]),
+                                   pack_e4m3x4(v[8][e], v[9][e], v[10][e], v[11][e]),
+                                   pack_e4m3x4(v[12][e], v[13][e], v[14][e], v[15][e]));
+                else
+                    w = make_uint4(pack_bf16(v[0][e], v[1][e]), pack_bf16(v[2][e], v[3][e]),
+                                   pack_bf16(v[4][e], v[5][e]), pack_bf16(v[6][e], v[7][e]));
+                *reinterpret_cast<uint4 *>(dst) = ok ? w : make_uint4(0, 0, 0, 0);
+            } else {
+                uint2 w;
+                if constexpr (kFp8)
+                    w = make_uint2(pack_e4m3x4(v[0][e], v[1][e], v[2][e], v[3][e]),
+                                   pack_e4m3x4(v[4][e], v[5][e], v[6][e], v[7][e]));
+                else
+                    w = make_uint2(pack_bf16(v[0][e], v[1][e]), pack_bf16(v[2][e], v[3][e]));
+                *reinterpret_cast<uint2 *>(dst) = ok ? w : make_uint2(0, 0);
+            }
+        }
+    }
+}
+
 // One CTA computes a BM x BN output tile over one K slice per work unit.  The CN CTAs of a
 // cluster hold the same BM rows of S and different BN-column tiles of A: each produces BM / CN
 // rows of every S stage and copies them into its peer with a bulk shared-memory copy.  Each
 // CTA loads its own A tiles (no multicast: clusters of two CTAs tile every SM, and CTAs whose
 // A loads do not wait on each other measured faster than pairs sharing them).
-// kFast: natural row follows i and the operator's column offset is a multiple of 4, so every
-// k chunk starts on a counter block.  kFp8: e4m3 operands (kind::f8f6f4, 64 k per stage) and
+// kMode: 0 the generic producer only; 1 natural row follows i and the operator's column
+// offset is a multiple of 4, so every k chunk starts on a counter block; 2 natural row follows
+// k and the column offset is a multiple of 4, so every i-quad starts on a counter block.  kFp8: e4m3 operands (kind::f8f6f4, 64 k per stage) and
 // the epilogue multiplies each column by its K slice's scale; else BF16 (kind::f16, 32 k).
-template <int CN, bool kFast, bool kFp8>
+template <int CN, int kMode, bool kFp8>
 __global__ void __launch_bounds__(NUM_THREADS, 1)
     sketch_tc_kernel(const __grid_constant__ CUtensorMap tmap_a, LowpParams p) {
     constexpr int BKE = Elem<kFp8>::BK;
@@ -522,7 +590,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
             // advanced by GEN_GROUPS stages of counters per step
             uint4 ctr[FAST_ROWS > 0 ? FAST_ROWS : 1];
             bool row_ok[FAST_ROWS > 0 ? FAST_ROWS : 1];
-            if (kFast) {
+            if (kMode == 1) {
 #pragma unroll
                 for (int t = 0; t < FAST_ROWS; ++t) {
                     const int64_t gi_row = m0 + row_lo + tg / CHUNKS + t * ROW_SLOTS;
@@ -536,7 +604,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
                 if (!tc::mbar_wait(&empty[s], ph ^ 1, p.err)) goto done;
                 uint8_t *tile = s_tiles + s * S_STAGE_BYTES;
                 const int64_t gk = ks * BKE + PER_CHUNK * fc;
-                if (kFast && gk + PER_CHUNK <= p.K) {
+                if (kMode == 1 && gk + PER_CHUNK <= p.K) {
 #pragma unroll
                     for (int t = 0; t < FAST_ROWS; ++t) {
                         const int i = row_lo + tg / CHUNKS + t * ROW_SLOTS;
@@ -546,6 +614,12 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
                                             : make_uint4(0, 0, 0, 0);
                         *reinterpret_cast<uint4 *>(tile + sw_byte(i, 16 * fc)) = w;
                     }
+                } else if (kMode == 2 && (ks + 1) * BKE <= p.K) {
+                    // KC: k values per work item, so that a group's 128 threads get one item
+                    // each (BF16) or two (e4m3: 8 values, one 8-byte store per row)
+                    constexpr int KC = kFp8 ? 8 : (ROWS == 64 ? 4 : 8);
+                    produce_s_transposed<kFp8, KC>(tile, p, m0, ks * BKE, row_lo, ROWS, tg,
+                                                   GROUP_THREADS);
                 } else {
                     produce_s_generic<kFp8>(tile, p, m0, ks * BKE, row_lo, ROWS, tg,
                                             GROUP_THREADS);
@@ -563,7 +637,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
                         tc::mbar_arrive(&full[s]);
                     }
                 }
-                if (kFast) {
+                if (kMode == 1) {
 #pragma unroll
                     for (int t = 0; t < FAST_ROWS; ++t)
                         ctr[t] = ctr_add_u32(ctr[t], (uint32_t)(GEN_GROUPS * (BKE / 4)));
@@ -856,11 +930,11 @@ Plan make_plan(int64_t M, int64_t N, int64_t K, bool fp8) {
     return pl;
 }
 
-template <int CN, bool kFast, bool kFp8>
+template <int CN, int kMode, bool kFp8>
 void set_smem_attr() {
     static bool done = false;
     if (!done) {
-        RBG_CUDA(cudaFuncSetAttribute(sketch_tc_kernel<CN, kFast, kFp8>,
+        RBG_CUDA(cudaFuncSetAttribute(sketch_tc_kernel<CN, kMode, kFp8>,
                                       cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
         done = true;
     }
@@ -868,7 +942,7 @@ void set_smem_attr() {
 
 template <int CN>
 int query_resident_clusters() {
-    set_smem_attr<CN, true, false>();
+    set_smem_attr<CN, 1, false>();
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(CN * 256);
     cfg.blockDim = dim3(NUM_THREADS);
@@ -882,7 +956,7 @@ int query_resident_clusters() {
     cfg.numAttrs = 1;
     int n = 0;
     const cudaError_t e =
-        cudaOccupancyMaxActiveClusters(&n, sketch_tc_kernel<CN, true, false>, &cfg);
+        cudaOccupancyMaxActiveClusters(&n, sketch_tc_kernel<CN, 1, false>, &cfg);
     if (e != cudaSuccess || n <= 0) {
         cudaGetLastError();
         n = num_sms() / CN;
@@ -903,9 +977,9 @@ int resident_clusters(int cs) {
     return c;
 }
 
-template <int CN, bool kFast, bool kFp8>
+template <int CN, int kMode, bool kFp8>
 void launch_sketch(int clusters, const CUtensorMap &map, const LowpParams &p, cudaStream_t s) {
-    set_smem_attr<CN, kFast, kFp8>();
+    set_smem_attr<CN, kMode, kFp8>();
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3((unsigned)(clusters * CN));
     cfg.blockDim = dim3(NUM_THREADS);
@@ -918,15 +992,15 @@ void launch_sketch(int clusters, const CUtensorMap &map, const LowpParams &p, cu
     attr[0].val.clusterDim.z = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    RBG_CUDA(cudaLaunchKernelEx(&cfg, sketch_tc_kernel<CN, kFast, kFp8>, map, p));
+    RBG_CUDA(cudaLaunchKernelEx(&cfg, sketch_tc_kernel<CN, kMode, kFp8>, map, p));
     RBG_LAUNCHED();
 }
 
-template <bool kFast, bool kFp8>
+template <int kMode, bool kFp8>
 void launch_for(const Plan &pl, const CUtensorMap &map, const LowpParams &p, cudaStream_t s) {
     const int clusters = (int)std::min<int64_t>(pl.units, resident_clusters(pl.cn));
-    if (pl.cn == 2) launch_sketch<2, kFast, kFp8>(clusters, map, p, s);
-    else launch_sketch<1, kFast, kFp8>(clusters, map, p, s);
+    if (pl.cn == 2) launch_sketch<2, kMode, kFp8>(clusters, map, p, s);
+    else launch_sketch<1, kMode, kFp8>(clusters, map, p, s);
 }
 
 
@@ -1067,8 +1141,10 @@ void lowp_run_streamed(int64_t M, int64_t N, int64_t K, float alpha, const Dense
         p.alpha = alpha; p.beta = c == 0 ? beta : 1.f;
         {
             ProfScope prof("lowp_sketch_bf16_tc", s);
-            if (r_on_i && (p.c0 % 4) == 0) launch_for<true, false>(pl, map, p, s);
-            else launch_for<false, false>(pl, map, p, s);
+            const int mode = (p.c0 % 4) != 0 ? 0 : r_on_i ? 1 : 2;
+            if (mode == 1) launch_for<1, false>(pl, map, p, s);
+            else if (mode == 2) launch_for<2, false>(pl, map, p, s);
+            else launch_for<0, false>(pl, map, p, s);
         }
         if (!p.direct) {
             ProfScope prof("lowp_reduce", s);
@@ -1157,15 +1233,19 @@ void lowp_run(bool fp8, int64_t M, int64_t N, int64_t K, float alpha, const Dens
     p.direct = pl.groups == 1;
     p.out = out; p.os_i = os_i; p.os_j = os_j;
     p.alpha = alpha; p.beta = beta;
-    const bool fast = r_on_i && (c0 % 4) == 0;
+    // fast producers: the operator's natural column offset is a multiple of 4, so chunks
+    // (natural row follows i: mode 1) or i-quads (it follows k: mode 2) start on counter blocks
+    const int mode = (c0 % 4) != 0 ? 0 : r_on_i ? 1 : 2;
     {
         ProfScope prof(fp8 ? "lowp_sketch_fp8_tc" : "lowp_sketch_bf16_tc", s);
         if (fp8) {
-            if (fast) launch_for<true, true>(pl, map, p, s);
-            else launch_for<false, true>(pl, map, p, s);
+            if (mode == 1) launch_for<1, true>(pl, map, p, s);
+            else if (mode == 2) launch_for<2, true>(pl, map, p, s);
+            else launch_for<0, true>(pl, map, p, s);
         } else {
-            if (fast) launch_for<true, false>(pl, map, p, s);
-            else launch_for<false, false>(pl, map, p, s);
+            if (mode == 1) launch_for<1, false>(pl, map, p, s);
+            else if (mode == 2) launch_for<2, false>(pl, map, p, s);
+            else launch_for<0, false>(pl, map, p, s);
         }
     }
     if (!p.direct) {

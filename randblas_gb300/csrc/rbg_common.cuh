@@ -88,14 +88,28 @@ __device__ __forceinline__ void boxmuller(uint32_t u0, uint32_t u1, float &first
 }
 
 // Box-Muller for the reduced-precision tensor-core paths, whose entries are rounded to BF16 /
-// FP8 afterwards: CUDA's hardware sine, cosine and logarithm intrinsics.  The angle lies in
-// (-pi, pi) and u01 in (0, 1], where their errors (about 1e-6) are far below a BF16 ulp
-// (3.9e-3 relative), so at most a BF16 rounding of the entry changes.
+// FP8 afterwards: the hardware's approximate sine, cosine, base-2 logarithm and square root
+// (one instruction each), with -2 ln(u) taken as log2(u) * (-2 ln 2).  The angle lies in
+// (-pi, pi) and u01 in (0, 1], where their errors (about 1e-6 relative) are far below a BF16
+// ulp (3.9e-3 relative), so at most a BF16 rounding of the entry changes.  The uniform inputs
+// are the exact transforms (each an FMA whose product is exact: one rounding, as above).
+__device__ __forceinline__ float sqrt_approx(float x) {
+    float r;
+    asm("sqrt.approx.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+__device__ __forceinline__ float lg2_approx(float x) {
+    float r;
+    asm("lg2.approx.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
 __device__ __forceinline__ void boxmuller_fast(uint32_t u0, uint32_t u1, float &first,
                                                float &second) {
+    const float v0 = __fmaf_rn(__int2float_rn((int32_t)u0), 0x1p-31f, 0x1p-32f);  // uneg11
+    const float v1 = __fmaf_rn(__uint2float_rn(u1), 0x1p-32f, 0x1p-33f);         // u01
     float s, c;
-    __sincosf(__fmul_rn(3.14159265358979323846f, uneg11(u0)), &s, &c);
-    const float r = __fsqrt_rn(__fmul_rn(-2.0f, __logf(u01(u1))));
+    __sincosf(__fmul_rn(3.14159265358979323846f, v0), &s, &c);
+    const float r = sqrt_approx(__fmul_rn(lg2_approx(v1), -1.3862943611198906f));
     first = __fmul_rn(s, r);
     second = __fmul_rn(c, r);
 }

@@ -66,7 +66,7 @@ __device__ __forceinline__ bool mbar_try_wait_cluster_hint(uint32_t bar, uint32_
 // Wait for the phase with the given parity to complete, for at most ~`budget` clock cycles.
 // Returns false (after setting *err) on timeout or if another role already raised *err.
 // Each try parks the thread for up to kSuspendNs (it is woken when the phase completes);
-// between tries the error word and the budget are checked.  `backoff` > 0 additionally
+// every 16th try also checks the error word and the budget.  `backoff` > 0 additionally
 // sleeps that many nanoseconds between tries once the wait is long.
 template <bool kCluster = false>
 __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, int *err,
@@ -77,18 +77,19 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, int *e
                  : mbar_try_wait_hint(a, parity, kSuspendNs))
         return true;
     const long long t0 = clock64();
-    uint32_t spins = 0;
-    while (!(kCluster ? mbar_try_wait_cluster_hint(a, parity, kSuspendNs)
-                      : mbar_try_wait_hint(a, parity, kSuspendNs))) {
-        ++spins;
+    for (uint32_t spins = 1;; ++spins) {
+        if (kCluster ? mbar_try_wait_cluster_hint(a, parity, kSuspendNs)
+                     : mbar_try_wait_hint(a, parity, kSuspendNs))
+            return true;
         if (backoff && spins > 8) __nanosleep(backoff);
-        if (*(volatile int *)err) return false;
-        if (clock64() - t0 > budget) {
-            atomicCAS(err, 0, RBG_ERROR_TIMEOUT);
-            return false;
+        if ((spins & 15u) == 0) {
+            if (*(volatile int *)err) return false;
+            if (clock64() - t0 > budget) {
+                atomicCAS(err, 0, RBG_ERROR_TIMEOUT);
+                return false;
+            }
         }
     }
-    return true;
 }
 
 // The same operations on mbarriers given by shared-memory address (keeps 64-bit pointers out
@@ -107,14 +108,16 @@ __device__ __forceinline__ bool mbar_wait_at(uint32_t bar, uint32_t parity, int 
                                              long long budget = 8000000000ll) {
     if (mbar_try_wait_hint(bar, parity, kSuspendNs)) return true;
     const long long t0 = clock64();
-    while (!mbar_try_wait_hint(bar, parity, kSuspendNs)) {
-        if (*(volatile int *)err) return false;
-        if (clock64() - t0 > budget) {
-            atomicCAS(err, 0, RBG_ERROR_TIMEOUT);
-            return false;
+    for (uint32_t spins = 1;; ++spins) {
+        if (mbar_try_wait_hint(bar, parity, kSuspendNs)) return true;
+        if ((spins & 15u) == 0) {
+            if (*(volatile int *)err) return false;
+            if (clock64() - t0 > budget) {
+                atomicCAS(err, 0, RBG_ERROR_TIMEOUT);
+                return false;
+            }
         }
     }
-    return true;
 }
 
 // ------------------------------------------------------------------ clusters

@@ -91,6 +91,46 @@ def test_lowp(rb, oracle, case, prec):
     assert r2 <= (1e-2 if prec == "bf16" else 6e-2), (case, r2)
 
 
+@pytest.mark.parametrize("case", [
+    # d, n, m, ro_s, co_s, family, precision: the operator enters transposed (tall, Short
+    # axis: natural row-major, opS = Trans), so its natural rows follow k and, with co_s a
+    # multiple of 4, each generator call covers 4 output rows (the transposed producer);
+    # d = 202 leaves a partial quad, m = 3001 a partial last stage
+    (202, 130, 3001, 5, 8, 1, "bf16"),
+    (256, 520, 4096, 0, 0, 0, "bf16"),
+    (202, 130, 3001, 5, 8, 1, "fp8"),
+    (256, 64, 6000, 3, 4, 0, "fp8"),
+])
+def test_lowp_transposed_operator(rb, oracle, case):
+    import torch
+    from oracle.oracle import State
+    from randblas_gb300 import lowp
+    d, n, m, ro, co, fam, prec = case
+    Dr, Dc = m + ro + 3, d + co + 4          # S is Dr x Dc, op(submat(S)) = submat(S)^T
+    D = rb.DenseDist(Dr, Dc, rb.ScalarDist(fam), rb.Axis.Short)
+    assert D.natural_layout == rb.Layout.RowMajor
+    S = rb.DenseSkOp(D, rb.RNGState(23, counter=(4, 0, 0, 0)))
+    g = torch.Generator(device="cuda").manual_seed(7)
+    A = torch.randn(m, n, device="cuda", generator=g)
+    B = torch.empty(d, n, device="cuda")
+    precision = lowp.BF16 if prec == "bf16" else lowp.FP8_E4M3
+    lowp.sketch_lowp(rb.Layout.RowMajor, rb.Op.Trans, rb.Op.NoTrans, d, n, m, 1.0, S, ro, co, A,
+                     n, 0.0, B, n, precision=precision)
+    assert lowp.status() == 0
+    Ssub = torch.from_numpy(oracle.dense_matrix(0, Dr, Dc, fam, 0, State.make((4, 0, 0, 0),
+                                                (23, 0)), m, d, ro, co))
+    opSm = Ssub.T
+    A64 = A.double().cpu()
+    if prec == "bf16":
+        rounded = _bf16(opSm) @ _bf16(A64)
+    else:
+        rounded = _e4m3(opSm) @ _e4m3_columns(A64)
+    got = B.double().cpu()
+    r1 = float((got - rounded).norm() / rounded.norm())
+    bound = 1e-3 if prec == "fp8" else (1e-4 if fam == 0 else 2e-5)
+    assert r1 <= bound, (case, r1)
+
+
 def test_lowp_workspace_and_errors(rb):
     import torch
     from randblas_gb300 import lowp
