@@ -293,8 +293,7 @@ def main():
     more_rows = bench_more_rows(torch, rb, device, stream, hbm)
     small = bench_small_fp64(torch, rb, device, stream)
     autograd_row = bench_autograd(torch, rb, device, stream, bf16_sus)
-    batched_row = None if args.no_batched else bench_batched(torch, rb, device, args, stream,
-                                                             tune=False)
+    batched_row = None if args.no_batched else bench_batched(torch, rb, device, args, stream)
 
     # end to end through the C ABI with host buffers
     e2e = None
@@ -596,30 +595,46 @@ def batched_workload(torch, rb, device, count=512):
     return probs
 
 
+# n classes of the batching workload for the per-class breakdown (FLOPs grow as n^2 m)
+BATCH_CLASSES = ((16, 64), (65, 128), (129, 256), (257, 512))
+FP32_SIMT_TFLOPS = 152 * 128 * 2 * 2.07e9 / 1e12  # FFMA lanes x 2 FLOP x max SM clock
+
+
 def bench_batched(torch, rb, device, args, stream, tune=True):
+    """The 512-problem batch three ways: 512 separate plain launches, one persistent launch
+    with the library's default tiles, and one with the autotuner's tiles (tuned before the
+    timed region; the tuning time is reported).  Then each n class on its own, batched and
+    as separate launches, with its fraction of the FP32 FFMA peak."""
     import tempfile
+    import time
     from randblas_gb300 import batched
     probs = batched_workload(torch, rb, device)
     flops = sum(2.0 * p.d * p.n * p.m for p in probs)
 
-    def separate():
-        for p in probs:
+    def separate(ps):
+        for p in ps:
             rb.sketch_general(rb.Layout.RowMajor, rb.Op.NoTrans, rb.Op.NoTrans, p.d, p.n, p.m,
                               1.0, p.S, p.A, p.n, 0.0, p.B, p.n)
     steps = max(1, min(args.steps, 3))
-    ms_sep = event_time(torch, separate, steps, 1, stream)
+    ms_sep = event_time(torch, lambda: separate(probs), steps, 1, stream)
     res = {"workload": "512 Gaussian left sketches, m log-uniform [2^12, 2^18], n uniform "
                        "[16, 512], d = 4n, FP32", "gflop": round(flops / 1e9, 1),
            "separate_plain_launches": {"ms": round(ms_sep, 2),
                                        "TFLOP/s": round(flops / ms_sep / 1e9, 2)}}
-    variants = [("default_tiles", None)]
+    tuner = None
     if tune:
-        variants.append(("autotuned", batched.Autotuner(
-            cache_path=os.path.join(tempfile.gettempdir(), "rbg_tiles.json"))))
-    for name, tuner in variants:
+        cache = os.path.join(tempfile.mkdtemp(prefix="rbg_tiles_"), "tiles.json")
+        tuner = batched.Autotuner(cache_path=cache)
+        t0 = time.perf_counter()
+        for p in probs:
+            tuner.choose(p.d, p.n, p.m, int(p.S.dist.family))
+        torch.cuda.synchronize()
+        res["autotune_s"] = round(time.perf_counter() - t0, 1)
+    variants = [("default_tiles", None)] + ([("autotuned", tuner)] if tune else [])
+    for name, tn in variants:
         for p in probs:
             p.tile_config = 0
-        plan = batched.BatchedPlan(probs, tuner=tuner)
+        plan = batched.BatchedPlan(probs, tuner=tn)
         graph = plan.capture()
         ms = event_time(torch, graph.replay, steps, 1, stream)
         res[name] = {"ms": round(ms, 2), "TFLOP/s": round(flops / ms / 1e9, 2),
@@ -632,6 +647,26 @@ def bench_batched(torch, rb, device, args, stream, tune=True):
             shapes[key] = shapes.get(key, 0) + 1
         res[name]["tiles"] = shapes
         plan.close()
+    per_class = {}
+    for lo, hi in BATCH_CLASSES:
+        sub = [p for p in probs if lo <= p.n <= hi]
+        if not sub:
+            continue
+        fl = sum(2.0 * p.d * p.n * p.m for p in sub)
+        for p in sub:
+            p.tile_config = 0
+        plan = batched.BatchedPlan(sub, tuner=tuner)
+        graph = plan.capture()
+        ms_b = event_time(torch, graph.replay, steps, 1, stream)
+        plan.close()
+        ms_s = event_time(torch, lambda: separate(sub), steps, 1, stream)
+        per_class[f"n{lo}-{hi}"] = {
+            "problems": len(sub), "gflop_share": round(fl / flops, 3),
+            "batched_TFLOP/s": round(fl / ms_b / 1e9, 2),
+            "separate_TFLOP/s": round(fl / ms_s / 1e9, 2),
+            "batched_frac_fp32_peak": round(fl / ms_b / 1e9 / FP32_SIMT_TFLOPS, 3)}
+    res["per_class"] = per_class
+    res["fp32_peak_TFLOP/s"] = round(FP32_SIMT_TFLOPS, 1)
     return res
 
 

@@ -9,11 +9,12 @@
 //  1. convert: op(A) (FP32 or BF16, any layout) -> At, k-blocked ([k / 64 bytes][n][64 bytes]),
 //     so every stage's TMA box is one contiguous block; BF16, or e4m3 after dividing by the
 //     power-of-two scale of its (K slice, column).
-//  2. sketch: persistent clusters of CN CTAs (one per SM), 24 warps with fixed roles --
+//  2. sketch: persistent clusters of CN CTAs (one per SM), 16 or 24 warps with fixed roles --
 //       warp 0      TMA producer: A tiles (512 n-rows x 64 bytes of k) into a 5-stage ring;
 //       warp 1      MMA issuer (one thread) and tensor-memory owner (512 columns);
 //       warps 4-7   epilogue: tensor memory -> registers -> FP32 partial tile in HBM;
-//       warps 8-23  S producers in 4 groups taking stages in turn: Philox4x32-10 + transform
+//       warps 8-    S producers (8 or 16 warps) in 4 groups taking stages in turn:
+//                   Philox4x32-10 + transform
 //                   for their half of a 128-row S stage (the N-peer makes the other half and
 //                   copies it over with a bulk shared-memory copy), stored in the 64-byte
 //                   swizzled K-major layout the tensor core reads.
@@ -52,28 +53,22 @@ struct Elem {
     static constexpr int BK = ROW_BYTES / BYTES;  // 32 (BF16) or 64 (e4m3)
     static constexpr int PER_CHUNK = 16 / BYTES;  // 8 or 16
 };
-// Warp roles: 0 TMA, 1 MMA, 4-7 epilogue (one per tensor-memory lane quarter), generator
-// warps from 8 on.  A warp runs on sub-partition id % 4.  With GEN_SKIP_MMA_SP the generators
-// avoid the MMA issuer's sub-partition (id % 4 == 1), whose warps above 8 then stay idle.
-#ifndef RBG_GEN_WARPS
-#define RBG_GEN_WARPS 16
-#endif
-#ifndef RBG_GEN_GROUPS
-#define RBG_GEN_GROUPS 4
-#endif
-#ifndef RBG_GEN_SKIP_MMA_SP
-#define RBG_GEN_SKIP_MMA_SP 0
-#endif
+// Warp roles: 0 TMA, 1 MMA, 4-7 epilogue (one per tensor-memory lane quarter), kGenWarps
+// generator warps from 8 on, in GEN_GROUPS groups of consecutive warps; a warp runs on
+// sub-partition id % 4.  Generator warps share the sub-partitions' issue slots with the MMA
+// and TMA threads: 16 suit launches that generation bounds (e4m3, Gaussian entries, operators
+// not shared by a cluster pair), 8 the uniform BF16 sketch of a cluster pair, whose MMA issue
+// is the tighter limit (measured at 4096 x 2^20 x 1024: 5.77 ms against 5.97 with 16).
 constexpr int EPI_WARP0 = 4;
 constexpr int GEN_WARP0 = 8;
-constexpr int GEN_WARPS = RBG_GEN_WARPS;
-constexpr bool GEN_SKIP_MMA_SP = RBG_GEN_SKIP_MMA_SP != 0;
-constexpr int NUM_THREADS = 32 * (GEN_WARP0 + (GEN_SKIP_MMA_SP ? GEN_WARPS / 3 * 4 : GEN_WARPS));
-constexpr int GEN_THREADS = GEN_WARPS * 32;
-constexpr int GEN_GROUPS = RBG_GEN_GROUPS;           // groups take stages in turn
-constexpr int GROUP_THREADS = GEN_THREADS / GEN_GROUPS;
-static_assert(!GEN_SKIP_MMA_SP || GEN_WARPS % 3 == 0, "generator warp layout");
-static_assert(GEN_THREADS % GEN_GROUPS == 0 && GROUP_THREADS % 32 == 0, "generator groups");
+constexpr int GEN_GROUPS = 4;  // groups take stages in turn
+template <int kGenWarps>
+struct GenLayout {
+    static constexpr int THREADS = 32 * (GEN_WARP0 + kGenWarps);
+    static constexpr int GROUP_WARPS = kGenWarps / GEN_GROUPS;
+    static constexpr int GROUP_THREADS = 32 * GROUP_WARPS;
+    static_assert(kGenWarps % GEN_GROUPS == 0, "generator groups of whole warps");
+};
 // A group's previous stage (it - GEN_GROUPS) guarantees only that the MMAs up to
 // it - GEN_GROUPS - STAGES have completed.  Its parity wait on the empty barrier of stage it
 // is unambiguous only if the phase before the awaited one (the MMAs of it - STAGES) is
@@ -335,14 +330,16 @@ __device__ __forceinline__ void produce_s_transposed(uint8_t *tile, const LowpPa
 // offset is a multiple of 4, so every k chunk starts on a counter block; 2 natural row follows
 // k and the column offset is a multiple of 4, so every i-quad starts on a counter block.  kFp8: e4m3 operands (kind::f8f6f4, 64 k per stage) and
 // the epilogue multiplies each column by its K slice's scale; else BF16 (kind::f16, 32 k).
-template <int CN, int kMode, bool kFp8>
-__global__ void __launch_bounds__(NUM_THREADS, 1)
-    sketch_tc_kernel(const __grid_constant__ CUtensorMap tmap_a, LowpParams p) {
+template <int CN, int kMode, bool kFp8, int kGenWarps>
+__global__ void __launch_bounds__(GenLayout<kGenWarps>::THREADS, 1)
+    sketch_tc_kernel(const __grid_constant__ CUtensorMap tmap_a,
+                     const __grid_constant__ LowpParams p) {
     constexpr int BKE = Elem<kFp8>::BK;
     constexpr int PER_CHUNK = Elem<kFp8>::PER_CHUNK;
     constexpr int CS = CN;
     constexpr int ROWS = BM / CN;                        // S rows this CTA produces per stage
     constexpr uint32_t PART_BYTES = ROWS * ROW_BYTES;    // their bytes in a stage
+    constexpr int GROUP_THREADS = GenLayout<kGenWarps>::GROUP_THREADS;
     constexpr int ROW_SLOTS = GROUP_THREADS / CHUNKS;    // rows a generator group covers at once
     constexpr int FAST_ROWS = ROWS / ROW_SLOTS;          // rows per generator thread per stage
     static_assert(ROWS % ROW_SLOTS == 0, "generator mapping");
@@ -556,14 +553,12 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
             __syncwarp();
             if (lane == 0) tc::mbar_arrive(acc_empty);
         }
-    } else if (warp >= GEN_WARP0 && (!GEN_SKIP_MMA_SP || (warp & 3) != 1)) {
+    } else if (warp >= GEN_WARP0) {
         // ---------------- S producers: GEN_GROUPS groups, group gi takes the stages with
         // it % GEN_GROUPS == gi
-        const int gw = GEN_SKIP_MMA_SP
-                           ? ((warp - GEN_WARP0) >> 2) * 3 + ((warp & 3) == 0 ? 0 : (warp & 3) - 1)
-                           : warp - GEN_WARP0;
-        const int gi = gw / (GEN_WARPS / GEN_GROUPS);
-        const int tg = (gw % (GEN_WARPS / GEN_GROUPS)) * 32 + lane;
+        const int gw = warp - GEN_WARP0;
+        const int gi = gw / GenLayout<kGenWarps>::GROUP_WARPS;
+        const int tg = (gw % GenLayout<kGenWarps>::GROUP_WARPS) * 32 + lane;
         const int row_lo = (int)n_idx * ROWS;
         // the N-peer's copies of the full barriers and S tiles (stage s at + 8 s and
         // + s * S_STAGE_BYTES): shared::cluster addresses, computed rather than kept in an
@@ -930,33 +925,40 @@ Plan make_plan(int64_t M, int64_t N, int64_t K, bool fp8) {
     return pl;
 }
 
-template <int CN, int kMode, bool kFp8>
+template <int CN, int kMode, bool kFp8, int kGenWarps>
 void set_smem_attr() {
     static bool done = false;
     if (!done) {
-        RBG_CUDA(cudaFuncSetAttribute(sketch_tc_kernel<CN, kMode, kFp8>,
+        RBG_CUDA(cudaFuncSetAttribute(sketch_tc_kernel<CN, kMode, kFp8, kGenWarps>,
                                       cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
         done = true;
     }
 }
 
+// One launch configuration of clusters of CN CTAs (one CTA per SM, shared memory decides).
 template <int CN>
-int query_resident_clusters() {
-    set_smem_attr<CN, 1, false>();
+cudaLaunchConfig_t cluster_config(int clusters, int threads, cudaLaunchAttribute *attr) {
     cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3(CN * 256);
-    cfg.blockDim = dim3(NUM_THREADS);
+    cfg.gridDim = dim3((unsigned)(clusters * CN));
+    cfg.blockDim = dim3((unsigned)threads);
     cfg.dynamicSmemBytes = SMEM_BYTES;
-    cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeClusterDimension;
     attr[0].val.clusterDim.x = CN;
     attr[0].val.clusterDim.y = 1;
     attr[0].val.clusterDim.z = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
+    return cfg;
+}
+
+template <int CN>
+int query_resident_clusters() {
+    set_smem_attr<CN, 1, false, 16>();
+    cudaLaunchAttribute attr[1];
+    const cudaLaunchConfig_t cfg = cluster_config<CN>(256, GenLayout<16>::THREADS, attr);
     int n = 0;
     const cudaError_t e =
-        cudaOccupancyMaxActiveClusters(&n, sketch_tc_kernel<CN, 1, false>, &cfg);
+        cudaOccupancyMaxActiveClusters(&n, sketch_tc_kernel<CN, 1, false, 16>, &cfg);
     if (e != cudaSuccess || n <= 0) {
         cudaGetLastError();
         n = num_sms() / CN;
@@ -977,30 +979,29 @@ int resident_clusters(int cs) {
     return c;
 }
 
-template <int CN, int kMode, bool kFp8>
+template <int CN, int kMode, bool kFp8, int kGenWarps>
 void launch_sketch(int clusters, const CUtensorMap &map, const LowpParams &p, cudaStream_t s) {
-    set_smem_attr<CN, kMode, kFp8>();
-    cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3((unsigned)(clusters * CN));
-    cfg.blockDim = dim3(NUM_THREADS);
-    cfg.dynamicSmemBytes = SMEM_BYTES;
-    cfg.stream = s;
+    set_smem_attr<CN, kMode, kFp8, kGenWarps>();
     cudaLaunchAttribute attr[1];
-    attr[0].id = cudaLaunchAttributeClusterDimension;
-    attr[0].val.clusterDim.x = CN;
-    attr[0].val.clusterDim.y = 1;
-    attr[0].val.clusterDim.z = 1;
-    cfg.attrs = attr;
-    cfg.numAttrs = 1;
-    RBG_CUDA(cudaLaunchKernelEx(&cfg, sketch_tc_kernel<CN, kMode, kFp8>, map, p));
+    cudaLaunchConfig_t cfg = cluster_config<CN>(clusters, GenLayout<kGenWarps>::THREADS, attr);
+    cfg.stream = s;
+    RBG_CUDA(cudaLaunchKernelEx(&cfg, sketch_tc_kernel<CN, kMode, kFp8, kGenWarps>, map, p));
     RBG_LAUNCHED();
 }
 
+// Cluster pairs sharing uniform BF16 operator rows that start on counter blocks take the
+// 8-generator-warp form; everything else 16 generator warps.
 template <int kMode, bool kFp8>
 void launch_for(const Plan &pl, const CUtensorMap &map, const LowpParams &p, cudaStream_t s) {
     const int clusters = (int)std::min<int64_t>(pl.units, resident_clusters(pl.cn));
-    if (pl.cn == 2) launch_sketch<2, kMode, kFp8>(clusters, map, p, s);
-    else launch_sketch<1, kMode, kFp8>(clusters, map, p, s);
+    if constexpr (kMode == 1 && !kFp8) {
+        if (pl.cn == 2 && p.gen.family == RBG_UNIFORM) {
+            launch_sketch<2, kMode, kFp8, 8>(clusters, map, p, s);
+            return;
+        }
+    }
+    if (pl.cn == 2) launch_sketch<2, kMode, kFp8, 16>(clusters, map, p, s);
+    else launch_sketch<1, kMode, kFp8, 16>(clusters, map, p, s);
 }
 
 
