@@ -381,6 +381,17 @@ __global__ void __launch_bounds__(GenLayout<kGenWarps>::THREADS, 1)
     if (CS > 1) tc::cluster_sync();  // peers' barriers are initialised before any signal
     tc::tc_fence_after();
     const uint32_t tmem = *tmem_slot;
+    // The TMA and MMA roles run their loops on the whole warp, issuing from one elected lane,
+    // with 16 generator warps (measured 3-5% faster there); with 8, lane 0 alone runs them
+    // (1% faster there).
+    constexpr bool kWarpLoops = kGenWarps == 16;
+    auto role_sync = [] {
+        if constexpr (kWarpLoops) __syncwarp();
+    };
+    auto role_lead = [] {
+        if constexpr (kWarpLoops) return tc::elect_one();
+        else return true;
+    };
 
     auto unit_tiles = [&](int64_t u, int64_t &m0, int64_t &n0, int64_t &ks0, int64_t &ks1) {
         const int64_t mg = u % p.m_groups;
@@ -394,34 +405,44 @@ __global__ void __launch_bounds__(GenLayout<kGenWarps>::THREADS, 1)
     };
 
     if (warp == 0) {
-        // ---------------- TMA producer
-        if (lane == 0) {
-            int64_t it = 0;
+        // ---------------- TMA producer: the whole warp runs the loop and one elected lane
+        // issues the loads (kWarpLoops), or lane 0 alone runs it
+        if (kWarpLoops || lane == 0) {
+            int s = 0;
+            uint32_t ph = 0;
             for (int64_t u = cluster_id; u < p.units; u += num_clusters) {
                 int64_t m0, n0, ks0, ks1;
                 unit_tiles(u, m0, n0, ks0, ks1);
-                for (int64_t ks = ks0; ks < ks1; ++ks, ++it) {
-                    const int s = (int)(it % STAGES);
-                    const uint32_t ph = (uint32_t)((it / STAGES) & 1);
+                for (int64_t ks = ks0; ks < ks1; ++ks) {
                     if (!tc::mbar_wait(&empty[s], ph ^ 1, p.err)) goto done;
-                    tc::mbar_arrive_expect_tx(&full[s], A_STAGE_BYTES);
-                    uint8_t *dst = a_tiles + s * A_STAGE_BYTES;
-                    const int64_t row0 = ks * p.npad + n0;  // k-blocked layout
-                    tc::tma_load_2d(dst, &tmap_a, &full[s], 0, (int)row0);
-                    tc::tma_load_2d(dst + A_STAGE_BYTES / 2, &tmap_a, &full[s], 0,
-                                    (int)(row0 + BN / 2));
+                    role_sync();
+                    if (role_lead()) {
+                        tc::mbar_arrive_expect_tx(&full[s], A_STAGE_BYTES);
+                        uint8_t *dst = a_tiles + s * A_STAGE_BYTES;
+                        const int64_t row0 = ks * p.npad + n0;  // k-blocked layout
+                        tc::tma_load_2d(dst, &tmap_a, &full[s], 0, (int)row0);
+                        tc::tma_load_2d(dst + A_STAGE_BYTES / 2, &tmap_a, &full[s], 0,
+                                        (int)(row0 + BN / 2));
+                    }
+                    role_sync();
+                    if (++s == STAGES) {
+                        s = 0;
+                        ph ^= 1u;
+                    }
                 }
             }
         }
     } else if (warp == 1) {
-        // ---------------- MMA issuer
-        if (lane == 0) {
+        // ---------------- MMA issuer: the whole warp runs the loop (its counters and
+        // descriptors stay warp-uniform) and one elected lane issues the MMAs and commits
+        // (kWarpLoops), or lane 0 alone runs it
+        if (kWarpLoops || lane == 0) {
             constexpr uint32_t idesc =
                 kFp8 ? tc::idesc_e4m3_f32(BM, BN / 2) : tc::idesc_bf16_f32(BM, BN / 2);
             // Stage index and phase advance by increment (no 64-bit division), and the
             // shared-memory descriptors of stage s are the stage-0 ones plus s stage strides in
             // their 16-byte address field (addresses stay below 2^18, so the field never
-            // overflows): this thread's instructions are few, which matters because it shares
+            // overflows): this warp's instructions are few, which matters because it shares
             // its sub-partition's issue slots with generator warps.
             const uint64_t adesc0 = tc::kmajor_desc(tc::smem_addr(s_tiles), ROW_BYTES);
             const uint64_t bdesc00 = tc::kmajor_desc(tc::smem_addr(a_tiles), ROW_BYTES);
@@ -434,40 +455,49 @@ __global__ void __launch_bounds__(GenLayout<kGenWarps>::THREADS, 1)
                 int64_t m0, n0, ks0, ks1;
                 unit_tiles(u, m0, n0, ks0, ks1);
                 if (!tc::mbar_wait(acc_empty, (uint32_t)((uc & 1) ^ 1), p.err, 256)) goto done;
+                role_sync();
                 tc::tc_fence_after();
                 uint32_t acc = 0;
                 for (int64_t ks = ks0; ks < ks1; ++ks, ++it) {
                     if (!tc::mbar_wait(&full[s], ph, p.err)) goto done;
+                    role_sync();
                     tc::tc_fence_after();
                     const uint64_t adesc = adesc0 + (uint64_t)(s * (S_STAGE_BYTES >> 4));
                     const uint64_t bdesc0 = bdesc00 + (uint64_t)(s * (A_STAGE_BYTES >> 4));
                     const uint64_t bdesc1 = bdesc10 + (uint64_t)(s * (A_STAGE_BYTES >> 4));
+                    if (role_lead()) {
 #pragma unroll
-                    for (int kk = 0; kk < ROW_BYTES / 32; ++kk) {
-                        // one MMA takes 32 bytes of k (16 BF16 or 32 e4m3) = 2 in the encoded
-                        // address; the first MMA of a unit overwrites the accumulator
-                        if (kFp8) {
-                            tc::mma_f8(tmem, adesc + 2 * kk, bdesc0 + 2 * kk, idesc, acc);
-                            tc::mma_f8(tmem + BN / 2, adesc + 2 * kk, bdesc1 + 2 * kk, idesc, acc);
-                        } else {
-                            tc::mma_f16(tmem, adesc + 2 * kk, bdesc0 + 2 * kk, idesc, acc);
-                            tc::mma_f16(tmem + BN / 2, adesc + 2 * kk, bdesc1 + 2 * kk, idesc,
-                                        acc);
+                        for (int kk = 0; kk < ROW_BYTES / 32; ++kk) {
+                            // one MMA takes 32 bytes of k (16 BF16 or 32 e4m3) = 2 in the
+                            // encoded address; the first MMA of a unit overwrites the
+                            // accumulator
+                            const uint32_t accum = kk == 0 ? acc : 1u;
+                            if (kFp8) {
+                                tc::mma_f8(tmem, adesc + 2 * kk, bdesc0 + 2 * kk, idesc, accum);
+                                tc::mma_f8(tmem + BN / 2, adesc + 2 * kk, bdesc1 + 2 * kk, idesc,
+                                           accum);
+                            } else {
+                                tc::mma_f16(tmem, adesc + 2 * kk, bdesc0 + 2 * kk, idesc, accum);
+                                tc::mma_f16(tmem + BN / 2, adesc + 2 * kk, bdesc1 + 2 * kk,
+                                            idesc, accum);
+                            }
                         }
-                        acc = 1u;
+                        // stage s of every CTA in the cluster may be rewritten by any of them,
+                        // so each CTA's MMA completion is signalled to all of them
+                        if (CS > 1)
+                            tc::mma_commit_multicast(&empty[s], (uint16_t)((1u << CS) - 1));
+                        else
+                            tc::mma_commit(&empty[s]);
                     }
-                    // stage s of every CTA in the cluster may be rewritten by any of them, so
-                    // each CTA's MMA completion is signalled to all of them
-                    if (CS > 1)
-                        tc::mma_commit_multicast(&empty[s], (uint16_t)((1u << CS) - 1));
-                    else
-                        tc::mma_commit(&empty[s]);
+                    role_sync();
+                    acc = 1u;
                     if (++s == STAGES) {
                         s = 0;
                         ph ^= 1u;
                     }
                 }
-                tc::mma_commit(acc_full);
+                if (role_lead()) tc::mma_commit(acc_full);
+                role_sync();
             }
             // wait until the last arrivals on this CTA's stage barriers -- including the
             // peers' -- have landed, so nothing targets this CTA after it exits

@@ -120,6 +120,21 @@ __device__ __forceinline__ bool mbar_wait_at(uint32_t bar, uint32_t parity, int 
     }
 }
 
+// True in exactly one lane of the (converged, full) warp.  A warp that runs a loop on all
+// lanes and issues its single-thread instructions under elect_one() keeps the loop's counters
+// and descriptors warp-uniform.
+__device__ __forceinline__ bool elect_one() {
+    uint32_t pred;
+    asm volatile(
+        "{\n\t"
+        ".reg .pred p;\n\t"
+        "elect.sync _|p, 0xffffffff;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t"
+        "}"
+        : "=r"(pred));
+    return pred != 0;
+}
+
 // ------------------------------------------------------------------ clusters
 __device__ __forceinline__ uint32_t cluster_ctarank() {
     uint32_t r;
