@@ -83,6 +83,7 @@ constexpr int SMEM_BYTES = STAGES * (S_STAGE_BYTES + A_STAGE_BYTES) + 1024 /*ali
 struct LowpParams {
     int64_t M, N, K;       // d, n, m
     DenseGen gen;          // operator entries
+    RoundKeys rk;          // gen.key's round keys (the fast producers' Philox)
     int64_t r0, c0;        // natural coordinates of submat(S)(0, 0)
     int r_on_i;            // 1: natural row follows the output row i
     int64_t k_steps;       // ceil(K / k per stage)
@@ -162,7 +163,7 @@ __device__ __forceinline__ uint4 pack_chunk(const float *v) {
 // PER_CHUNK consecutive natural-column entries starting at a block-aligned counter `c`
 // (PER_CHUNK / 4 Philox calls), finished (uniform entries scaled) and packed.
 template <bool kFp8>
-__device__ __forceinline__ uint4 gen_chunk_aligned(int family, uint4 c, uint2 key) {
+__device__ __forceinline__ uint4 gen_chunk_aligned(int family, uint4 c, const RoundKeys &key) {
     constexpr int E = Elem<kFp8>::PER_CHUNK;
     float v[E];
     if (family == RBG_UNIFORM) {
@@ -256,7 +257,8 @@ __device__ __forceinline__ void produce_s_generic(uint8_t *tile, const LowpParam
 
 // Four consecutive natural-column entries at a block-aligned counter, finished as the
 // reduced-precision paths take them (uniform entries scaled by sqrt(3)).
-__device__ __forceinline__ void gen4_finished(int family, uint4 c, uint2 key, float v[4]) {
+__device__ __forceinline__ void gen4_finished(int family, uint4 c, const RoundKeys &key,
+                                              float v[4]) {
     if (family == RBG_UNIFORM) {
         const uint4 r = philox(c, key);
         v[0] = __fmul_rn(uneg11_fma(r.x), 1.7320508075688772f);
@@ -290,7 +292,7 @@ __device__ __forceinline__ void produce_s_transposed(uint8_t *tile, const LowpPa
         float v[KC][4];
 #pragma unroll
         for (int kk = 0; kk < KC; ++kk) {
-            gen4_finished(p.gen.family, c, p.gen.key, v[kk]);
+            gen4_finished(p.gen.family, c, p.rk, v[kk]);
             if (kk + 1 < KC) c = ctr_add(c, (uint64_t)p.gen.stride);
         }
 #pragma unroll
@@ -635,7 +637,7 @@ __global__ void __launch_bounds__(GenLayout<kGenWarps>::THREADS, 1)
                         const int i = row_lo + tg / CHUNKS + t * ROW_SLOTS;
                         const uint4 w = row_ok[t]
                                             ? gen_chunk_aligned<kFp8>(p.gen.family, ctr[t],
-                                                                      p.gen.key)
+                                                                      p.rk)
                                             : make_uint4(0, 0, 0, 0);
                         *reinterpret_cast<uint4 *>(tile + sw_byte(i, 16 * fc)) = w;
                     }
@@ -1161,6 +1163,7 @@ void lowp_run_streamed(int64_t M, int64_t N, int64_t K, float alpha, const Dense
         LowpParams p{};
         p.M = M; p.N = N; p.K = kc;
         p.gen = gen;
+        p.rk = round_keys(gen.key);
         p.r0 = r_on_i ? r0 : r0 + k0;
         p.c0 = r_on_i ? c0 + k0 : c0;
         p.r_on_i = r_on_i;
@@ -1257,7 +1260,7 @@ void lowp_run(bool fp8, int64_t M, int64_t N, int64_t K, float alpha, const Dens
     int *err = tc::wait_error_flag();
     LowpParams p{};
     p.M = M; p.N = N; p.K = K;
-    p.gen = gen; p.r0 = r0; p.c0 = c0; p.r_on_i = r_on_i;
+    p.gen = gen; p.rk = round_keys(gen.key); p.r0 = r0; p.c0 = c0; p.r_on_i = r_on_i;
     p.k_steps = pl.k_steps; p.m_groups = pl.m_groups; p.n_groups = pl.n_groups;
     p.ks_per_group = pl.ks_per_group; p.units = pl.units; p.npad = pl.npad;
     p.partial = partial; p.amax = amax; p.err = err;

@@ -34,6 +34,28 @@ __device__ __forceinline__ uint4 philox(uint4 c, uint2 k) {
     return c;
 }
 
+// The ten round keys of one key (key + r * Weyl, r = 0 .. 9), computed once on the host and
+// passed in kernel parameters: the rounds then read them as constant operands instead of
+// advancing the key in registers on every call.
+struct RoundKeys {
+    uint2 k[10];
+};
+__host__ __device__ inline RoundKeys round_keys(uint2 key) {
+    RoundKeys rk;
+    for (int r = 0; r < 10; ++r)
+        rk.k[r] = make_uint2(key.x + (uint32_t)r * kWeylA, key.y + (uint32_t)r * kWeylB);
+    return rk;
+}
+__device__ __forceinline__ uint4 philox(uint4 c, const RoundKeys &rk) {
+#pragma unroll
+    for (int round = 0; round < 10; ++round) {
+        const uint32_t hi_a = __umulhi(kMulA, c.x), lo_a = kMulA * c.x;
+        const uint32_t hi_b = __umulhi(kMulB, c.z), lo_b = kMulB * c.z;
+        c = make_uint4(hi_b ^ c.y ^ rk.k[round].x, lo_b, hi_a ^ c.w ^ rk.k[round].y, lo_a);
+    }
+    return c;
+}
+
 // counter + n, the counter read as a little-endian 128-bit integer
 // (Random123's r123array4x32::incr, asserted by test/test_basic_rng/test_r123.cc:705-797).
 __host__ __device__ __forceinline__ uint4 ctr_add(uint4 c, uint64_t n) {
@@ -116,8 +138,8 @@ __device__ __forceinline__ void boxmuller_fast(uint32_t u0, uint32_t u1, float &
 
 // Four operator entries from one Philox call: Gaussian pairs (lanes 0,1) and (2,3), or
 // four uniforms on (-1, 1).  Uniform entries are NOT scaled here (see scale_uniform).
-template <bool kFast = false>
-__device__ __forceinline__ void gen4(int family, uint4 ctr, uint2 key, float v[4]) {
+template <bool kFast = false, typename Key = uint2>
+__device__ __forceinline__ void gen4(int family, uint4 ctr, const Key &key, float v[4]) {
     const uint4 r = philox(ctr, key);
     if (family == RBG_GAUSSIAN) {
         if (kFast) {
