@@ -234,16 +234,19 @@ def main():
     ms_plain = event_time(torch, plain, plain_steps, 1, stream)
 
     lib = rb.lib()
-    rb.profile.enable(True)
     launches0 = lib.rbg_kernel_launches()
     torch.cuda.synchronize()
     with ClockSampler(local) as clk:
         ms = event_time(torch, headline, args.steps, args.warmup, stream)
     launches = (lib.rbg_kernel_launches() - launches0)
-    prof = rb.profile.read()
-    rb.profile.enable(False)
     per_step_launches = launches / (args.steps + args.warmup)
     gpu_launches = int(round(per_step_launches * args.steps))
+    # per-kernel times from a second pass with the library's event profiling on (its events
+    # are kept out of the timed steps above)
+    rb.profile.enable(True)
+    event_time(torch, headline, args.steps, 1, stream)
+    prof = rb.profile.read()
+    rb.profile.enable(False)
 
     # accuracy of the headline result against an FP64 oracle on sampled row blocks
     headline()
@@ -321,6 +324,7 @@ def main():
         "dtype": "bf16" if have_lowp else "f32", "data": "synthetic",
         "config": headline_config(),
         "path": "bf16 tensor-core fused" if have_lowp else "fp32 plain",
+        "kernels_ms": {k: round(v["ms"] / max(1, v["launches"]), 4) for k, v in prof.items()},
         "a_spectrum": "singular values 1 -> 1e-6 (random orthogonal factors)",
         "l2": "inputs larger than L2 (A is 4.3 GB)",
         "fp32_plain": {"ms_per_step": round(ms_plain, 3),
@@ -463,7 +467,36 @@ def bench_autograd(torch, rb, device, stream, bf16_peak):
             loss.backward()
         ms = event_time(torch, step, 3, 1, stream)
         out[name] = {"ms_fwd_bwd": round(ms, 3), "TFLOP/s": round(flops / (ms * 1e-3) / 1e12, 1)}
+        if prec is not None and dt == torch.float32:
+            out[name + "_graphed"] = autograd_graphed(torch, autograd, S, A, Bt, flops, stream)
     return out
+
+
+def autograd_graphed(torch, autograd, S, A, Bt, flops, stream):
+    """The same forward + backward captured once in a CUDA graph and replayed: the device time
+    of the step without host time between launches (A.grad is the graph's static output)."""
+    try:
+        side = torch.cuda.Stream()
+        side.wait_stream(torch.cuda.current_stream())
+        with torch.cuda.stream(side):
+            for _ in range(3):
+                A.grad = None
+                ((autograd.sketch(S, A, precision="bf16") - Bt) ** 2).sum().backward()
+        torch.cuda.current_stream().wait_stream(side)
+        graph = torch.cuda.CUDAGraph()
+        A.grad = None
+        with torch.cuda.graph(graph, capture_error_mode="relaxed"):
+            ((autograd.sketch(S, A, precision="bf16") - Bt) ** 2).sum().backward()
+        static_grad = A.grad
+        ms = event_time(torch, graph.replay, 5, 2, stream)
+        A.grad = None
+        ((autograd.sketch(S, A, precision="bf16") - Bt) ** 2).sum().backward()
+        same = bool(torch.equal(static_grad, A.grad))
+        return {"ms_fwd_bwd": round(ms, 3), "TFLOP/s": round(flops / (ms * 1e-3) / 1e12, 1),
+                "grad_equals_eager": same}
+    except Exception as e:  # capture is a measurement aid, not part of the product path
+        torch.cuda.synchronize()
+        return {"error": str(e).splitlines()[0][:160]}
 
 
 def derived_fp32_peak(torch, clocks):
