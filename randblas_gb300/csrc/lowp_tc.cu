@@ -1302,8 +1302,9 @@ EncodeFn tensor_map_encoder() {
     std::call_once(once, [] {
         void *p = nullptr;
         cudaDriverEntryPointQueryResult q;
-        if (cudaGetDriverEntryPoint("cuTensorMapEncodeTiled", &p, cudaEnableDefault, &q) ==
-                cudaSuccess &&
+        // cuTensorMapEncodeTiled as introduced in CUDA 12.0 (the version its ABI dates from)
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000,
+                                             cudaEnableDefault, &q) == cudaSuccess &&
             q == cudaDriverEntryPointSuccess)
             fn = reinterpret_cast<EncodeFn>(p);
     });
