@@ -220,7 +220,9 @@ int rbg_repeated_fisher_yates(int64_t k, int64_t n, int64_t r, int64_t *samples,
  *   rbg_random_sparse_fill    writes device arrays: COO a = rows[nnz], b = cols[nnz];
  *                             CSR a = rowptr[m + 1], b = colidxs[nnz];
  *                             CSC a = colptr[n + 1], b = rowidxs[nnz];
- *   rbg_random_sparse_destroy frees the handle (synchronous).
+ *   rbg_random_sparse_destroy frees the handle; its device memory is released in stream
+ *                             order on the stream of the last create or fill call (which
+ *                             must still exist), after the work queued there.
  * density outside [0, 1] fails the reference's check.  Limits of this library: the compressed
  * formats need fewer than 2^30 stream words (about 5e8 nonzeros) and a minor dimension below
  * 2^31 - 1; 0 < density < 2^-53 (where log(1 - density) rounds to 0 and the reference's skip

@@ -408,6 +408,7 @@ struct rbg_random_sparse_s {
     // device memory kept for the fill: COO positions, or the compressed path's skips, class
     // sums, row starts and pointers
     void *mem = nullptr;
+    cudaStream_t stream = nullptr;  // of the last create / fill call: mem is freed on it
     int64_t *coo_pos = nullptr;
     int32_t *start = nullptr;
     int64_t *ptr = nullptr;
@@ -419,12 +420,13 @@ using Handle = rbg_random_sparse_s;
 
 size_t align_up(size_t x) { return (x + 255) & ~size_t(255); }
 
-void *device_alloc(size_t bytes) {
+// Stream-ordered device memory that outlives the call (the handle's), freed by release().
+void *device_alloc(size_t bytes, cudaStream_t s) {
     void *p = nullptr;
-    const cudaError_t e = cudaMalloc(&p, std::max<size_t>(bytes, 256));
+    const cudaError_t e = cudaMallocAsync(&p, std::max<size_t>(bytes, 256), s);
     if (e != cudaSuccess) {
         cudaGetLastError();
-        fail(RBG_ERROR_ALLOC, "cudaMalloc of " + std::to_string(bytes) + " bytes failed");
+        fail(RBG_ERROR_ALLOC, "cudaMallocAsync of " + std::to_string(bytes) + " bytes failed");
     }
     return p;
 }
@@ -438,7 +440,7 @@ void read_status(Status &host, const Status *dev, cudaStream_t s) {
 bool coo_attempt(Handle &h, double l1mp, int64_t K, cudaStream_t s) {
     const int64_t total = h.m * h.n;
     Scratch st(sizeof(Status), s), tie(K, s);
-    int64_t *pos = static_cast<int64_t *>(device_alloc(sizeof(int64_t) * K));
+    int64_t *pos = static_cast<int64_t *>(device_alloc(sizeof(int64_t) * K, s));
     h.mem = pos;
     RBG_CUDA(cudaMemsetAsync(st.ptr, 0, sizeof(Status), s));
     RBG_CUDA(cudaMemsetAsync(&st.as<Status>()->nnz, 0xFF, sizeof(int64_t), s));
@@ -483,7 +485,7 @@ bool compressed_attempt(Handle &h, double l1mp, int64_t U, cudaStream_t s) {
     const size_t b_csum = align_up(sizeof(int64_t) * 4 * c.ranks);
     const size_t b_start = align_up(sizeof(int32_t) * h.nmaj);
     const size_t b_ptr = align_up(sizeof(int64_t) * (h.nmaj + 1));
-    char *mem = static_cast<char *>(device_alloc(b_skip + b_csum + b_start + b_ptr));
+    char *mem = static_cast<char *>(device_alloc(b_skip + b_csum + b_start + b_ptr, s));
     h.mem = mem;
     c.skip = reinterpret_cast<uint32_t *>(mem);
     c.csum = reinterpret_cast<int64_t *>(mem + b_skip);
@@ -531,12 +533,14 @@ bool compressed_attempt(Handle &h, double l1mp, int64_t U, cudaStream_t s) {
         RBG_CUDA(cub::DeviceScan::ExclusiveSum(tmp.ptr, tmp_bytes, cnt.as<int64_t>(), ptr,
                                                h.nmaj + 1, s));
     }
+    // the pointer array's last entry (nnz) travels back with the status: one read, one sync
+    RBG_CUDA(cudaMemcpyAsync(&st.as<Status>()->nnz, ptr + h.nmaj, sizeof(int64_t),
+                             cudaMemcpyDeviceToDevice, s));
     Status hs{};
     read_status(hs, st.as<Status>(), s);
     if (hs.broken) fail(RBG_ERROR_CUDA, "random sparse generator: inconsistent row chain");
     if (hs.overflow) return false;
-    RBG_CUDA(cudaMemcpyAsync(&h.nnz, ptr + h.nmaj, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
-    RBG_CUDA(cudaStreamSynchronize(s));
+    h.nnz = hs.nnz;
     h.consumed = hs.consumed;
     h.ambiguous = hs.ambiguous;
     h.comp = c;
@@ -545,8 +549,10 @@ bool compressed_attempt(Handle &h, double l1mp, int64_t U, cudaStream_t s) {
     return true;
 }
 
+// Frees the handle's memory in stream order on the stream of its last create / fill call, so
+// no sync is needed and work already queued there finishes first.
 void release(Handle &h) {
-    if (h.mem) cudaFree(h.mem);
+    if (h.mem) cudaFreeAsync(h.mem, h.stream);
     h.mem = nullptr;
 }
 
@@ -558,6 +564,7 @@ void create(int32_t fmt, int64_t m, int64_t n, double density, const rbg_state *
     const char *fn = fn_name(fmt);
     RBG_REQUIRE(fn, density >= 0.0 && density <= 1.0);  // random_matrix.hh:142, 224, 303
     RBG_REQUIRE(fn, m >= 0 && n >= 0);
+    h.stream = s;
     h.fmt = fmt;
     h.m = m;
     h.n = n;
@@ -687,6 +694,7 @@ extern "C" int rbg_random_sparse_fill(rbg_random_sparse h, int32_t dtype, int32_
         if (itype == RBG_I32 && (h->nnz > INT32_MAX || h->m > INT32_MAX || h->n > INT32_MAX))
             fail(RBG_ERROR_OVERFLOW, "nnz or a dimension does not fit 32-bit indices");
         const cudaStream_t s = as_cuda(stream);
+        h->stream = s;
         if (dtype == RBG_F32 && itype == RBG_I32) fill_t<float, int32_t>(*h, vals, a, b, s);
         else if (dtype == RBG_F32) fill_t<float, int64_t>(*h, vals, a, b, s);
         else if (itype == RBG_I32) fill_t<double, int32_t>(*h, vals, a, b, s);
@@ -706,7 +714,7 @@ extern "C" int rbg_random_sparse_info(rbg_random_sparse h, int64_t *near_ties,
 extern "C" int rbg_random_sparse_destroy(rbg_random_sparse h) {
     return guarded([&] {
         if (!h) return;
-        if (h->mem) RBG_CUDA(cudaFree(h->mem));
+        if (h->mem) RBG_CUDA(cudaFreeAsync(h->mem, h->stream));
         h->mem = nullptr;
         delete h;
     });
