@@ -133,3 +133,41 @@ def test_bf16_path_full_size(rb, adtype):
     ry = float((Y.detach().double() - Yref).norm() / Yref.norm())
     rg = float((A.grad.double() - Gref).norm() / Gref.norm())
     assert ry < 1e-2 and rg < 1e-2, (ry, rg)
+
+
+def test_bf16_step_replays_from_cuda_graph(rb):
+    """Forward + backward on the tensor-core path captured once in a CUDA graph: replays give
+    the eager gradient bit for bit (the kernels launch stream-ordered work only, and every sum
+    has a fixed order), including after the data changes in place."""
+    import torch
+    from randblas_gb300 import autograd
+    d, m, n = 256, 8192, 96
+    S = rb.DenseSkOp(rb.DenseDist(d, m, rb.ScalarDist.Gaussian), rb.RNGState(8))
+    g = torch.Generator(device="cuda").manual_seed(8)
+    A = torch.randn(m, n, device="cuda", generator=g).requires_grad_(True)
+    B = torch.randn(d, n, device="cuda", generator=g)
+
+    def step():
+        ((autograd.sketch(S, A, precision="bf16") - B) ** 2).sum().backward()
+    side = torch.cuda.Stream()
+    side.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(side):
+        for _ in range(2):
+            A.grad = None
+            step()
+    torch.cuda.current_stream().wait_stream(side)
+    graph = torch.cuda.CUDAGraph()
+    A.grad = None
+    with torch.cuda.graph(graph, capture_error_mode="relaxed"):
+        step()
+    static_grad = A.grad
+    for _ in range(2):
+        graph.replay()
+        with torch.no_grad():
+            A.mul_(1.5)  # new data in the captured input
+        graph.replay()
+        torch.cuda.synchronize()
+        replayed = static_grad.clone()
+        A.grad = None
+        step()
+        assert torch.equal(replayed, A.grad)
