@@ -675,7 +675,8 @@ def bench_batched(torch, rb, device, args, stream, tune=True):
                      "work_items": plan.info()["work_items"]}
         shapes = {}
         for p in probs:
-            key = "x".join(map(str, batched.tile_shape(p.tile_config))) if p.tile_config \
+            key = "x".join(str(x) if x else "all" for x in batched.tile_shape(p.tile_config)) \
+                if p.tile_config \
                 else "library"
             shapes[key] = shapes.get(key, 0) + 1
         res[name]["tiles"] = shapes

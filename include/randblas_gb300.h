@@ -446,7 +446,9 @@ int rbg_lskge3_batched(int32_t layout, const rbg_batch_problem *problems, int64_
                        int32_t tile_config, rbg_stream_t stream);
 /* Number of tile configurations the batched kernel offers (ids 1..count). */
 int rbg_batched_tile_configs(int32_t *count);
-/* Output tile shape (rows x columns) of configuration `config`. */
+/* Output tile shape (rows x columns) of configuration `config`; columns 0 means a row block
+ * over every column of the problem (its operator rows generated once per chunk of k and used
+ * by each 128-column pass). */
 int rbg_batched_tile_shape(int32_t config, int32_t *rows, int32_t *cols);
 
 /* A reusable batch: validates the problems and uploads the work list once (synchronous);

@@ -10,9 +10,9 @@ RNGState), data A_i and output B_i, all row-major or all column-major CUDA tenso
 * :func:`sketch_batched` -- one stream-ordered call.
 * :class:`BatchedPlan` -- validate and upload once, then :meth:`BatchedPlan.execute` (a memset
   and one kernel launch, capturable) or :meth:`BatchedPlan.capture` into a CUDA graph.
-* :class:`Autotuner` -- picks each problem's output tile (128 x 128, 128 x 64, 128 x 32 or
-  64 x 256) per shape class by timing every candidate on the same synthetic batch on the
-  device, and caches the choices as JSON.
+* :class:`Autotuner` -- picks each problem's output tile (128 x 128, 128 x 64, 128 x 32,
+  64 x 256, or 128-row blocks over all columns) per shape class by timing every candidate on
+  the same synthetic batch on the device, and caches the choices as JSON.
 """
 from __future__ import annotations
 
@@ -56,7 +56,9 @@ def tile_configs() -> List[int]:
 
 
 def tile_shape(config: int):
-    """(rows, columns) of the output tile of a configuration."""
+    """(rows, columns) of the output tile of a configuration; columns 0 is a row block over
+    every column of the problem (operator rows generated once, used by every 128-column
+    pass)."""
     r, c = C.c_int32(), C.c_int32()
     call("rbg_batched_tile_shape", int(config), C.byref(r), C.byref(c))
     return r.value, c.value

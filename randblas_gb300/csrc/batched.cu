@@ -11,8 +11,11 @@
 // FP32 accumulators per thread).  Problems with long K are split so no item dominates the
 // tail; the CTA that finishes a tile's last split (an atomic per tile, no waiting) sums the
 // splits' partial tiles in split order, so results do not depend on scheduling.
-// The tile width BN (128, 64 or 32) is chosen per problem -- by the caller (an autotuner),
-// or by a waste-based rule here.
+// The tile is chosen per problem -- by the caller (an autotuner), or here: Gaussian problems
+// take row blocks (128 rows over all columns, the operator rows generated once per chunk of
+// 128 k's and used by every 128-column pass, the pass accumulators parked in a per-CTA scratch
+// area between chunks), so each operator entry is generated once per problem; uniform ones
+// take a 128 x (128, 64 or 32) or 64 x 256 tile by a cost model.
 #include <algorithm>
 #include <cstring>
 #include <numeric>
@@ -28,17 +31,24 @@ using simt::BK;
 using simt::BM;
 using simt::NT;
 
-constexpr int kConfigs = 4;
+constexpr int kConfigs = 5;
 // config id -> output tile (rows x columns); every configuration is 256 threads with 8 x TN
 // accumulators each.  The operator tile (rows x 16 per k step) is generated once per output
 // tile, so wider tiles spend less on generation per FLOP and narrower ones waste less on
-// padding columns.
-constexpr int kTileRows[kConfigs + 1] = {0, 128, 128, 128, 64};
-constexpr int kTileWidth[kConfigs + 1] = {0, 128, 64, 32, 256};
+// padding columns.  Configuration 5 (kRowBlock) is a row block of 128 rows over ALL of the
+// problem's columns: its operator rows are generated once per chunk of kChunkK k's into shared
+// memory and used by every 128-column pass, whose accumulators wait between chunks in a
+// per-CTA scratch area (L2-resident), so each generated entry serves all n columns.
+constexpr int kRowBlock = 5;
+constexpr int kTileRows[kConfigs + 1] = {0, 128, 128, 128, 64, 128};
+constexpr int kTileWidth[kConfigs + 1] = {0, 128, 64, 32, 256, 128};  // 5: width of one pass
 constexpr int kMaxSplits = 64;
+constexpr int kChunkK = 8 * BK;            // row-block configuration: k's per generated chunk
 constexpr int kPsFloats = BK * (BM + 4);   // one operator stage (largest tile)
 constexpr int kQsFloats = BK * (256 + 4);  // one data stage (largest tile)
-constexpr size_t kBatchedSmem = (size_t)2 * (kPsFloats + kQsFloats) * sizeof(float);
+constexpr size_t kBatchedSmem =
+    sizeof(float) * (size_t)std::max(2 * (kPsFloats + kQsFloats),
+                                     kChunkK * (BM + 4) + 2 * BK * (BM + 4));
 
 struct ProbDev {
     POperand P;       // generated operator
@@ -54,6 +64,7 @@ struct ProbDev {
     int64_t partial_off;  // floats into the partial buffer ([splits][M][N])
     int64_t counter_off;  // ints into the tile counters
     int32_t paired;       // column tiles taken two at a time by a cluster pair
+    int32_t passes;       // row-block configuration: 128-column passes (else 0)
 };
 
 struct WorkItem {
@@ -215,12 +226,169 @@ __device__ __forceinline__ void batched_tile(const ProbDev &pb, int64_t tile, in
     }
 }
 
+// Configuration kRowBlock: one item is a row block (128 rows) of problem `pb` over one K split
+// and all of its columns, in pb.passes passes of 128 columns.  Per chunk of kChunkK k's the
+// operator rows are generated once into shared memory (chunk[k][i]); each pass then loads its
+// accumulators (8 x 8 per thread) from this CTA's scratch area -- zeros in the first chunk --,
+// runs the chunk's k steps against staged 16 x 128 data tiles (the next tile's loads in flight
+// in registers) and stores the accumulators back, or in the last chunk writes them out as the
+// other configurations do (the output directly with one split, else its split slot, the last
+// split summing the slots in split order).
+__device__ __forceinline__ void batched_rowblock(const ProbDev &pb, int64_t tile, int split,
+                                                 float *smem, float *partial, int *counters,
+                                                 int *s_flag, float *scratch) {
+    constexpr int BMT = 128, BNT = 128, TN = 8, TX = BNT / TN;
+    static_assert(TX * (BMT / 8) == NT, "one 8 x TN block per thread");
+    using ChunkRow = float[BMT + 4];
+    using QsTile = float[BK][BNT + 4];
+    ChunkRow *chunk = reinterpret_cast<ChunkRow *>(smem);                    // [kChunkK]
+    QsTile *Qs2 = reinterpret_cast<QsTile *>(smem + kChunkK * (BMT + 4));     // [2]
+    const int tx = threadIdx.x % TX, ty = threadIdx.x / TX;
+    const int64_t i0 = tile * BMT;
+    const int64_t kt_total = (pb.K + BK - 1) / BK;
+    const int64_t kb = (int64_t)split * pb.kt_per_split;
+    const int64_t ke = min(kt_total, kb + pb.kt_per_split);
+    const float *Qp = static_cast<const float *>(pb.Q.ptr);
+    constexpr int QR = BK * BNT / NT;
+    float qr[QR];
+    // the data tiles in (chunk, pass, k step) order; prefetch the first
+    if (kb < ke) simt::load_tile_regs<float, BNT>(qr, Qp, pb.Q.s0, pb.Q.s1, pb.K, pb.N, kb * BK, 0);
+    int stage = 0;
+    auto row_of = [&](int x) { return i0 + (x < 4 ? ty * 4 + x : BMT / 2 + ty * 4 + (x - 4)); };
+    if (kb >= ke) {
+        // nothing to multiply (alpha == 0 or m == 0; one split): B = beta * B
+        for (int w = threadIdx.x; w < BMT * pb.passes * BNT; w += NT) {
+            const int64_t i = i0 + w / (pb.passes * BNT), j = w % (pb.passes * BNT);
+            if (i >= pb.M || j >= pb.N) continue;
+            float &o = pb.out[i * pb.os_i + j * pb.os_j];
+            o = pb.beta == 0.f ? 0.f : pb.beta * o;
+        }
+        __syncthreads();
+        return;
+    }
+    for (int64_t c0 = kb; c0 < ke; c0 += kChunkK / BK) {
+        const int steps = (int)min((int64_t)(kChunkK / BK), ke - c0);
+        const bool first = c0 == kb, last = c0 + steps == ke;
+        for (int q = 0; q < steps; ++q)
+            simt::gen_p_tile<float, BMT>(chunk + q * BK, pb.P, pb.M, pb.K, i0, (c0 + q) * BK);
+        // (the chunk is published by the first k step's barrier below)
+        for (int pass = 0; pass < pb.passes; ++pass) {
+            const int64_t j0 = (int64_t)pass * BNT;
+            float acc[8][TN];
+            float *sc = scratch + (int64_t)pass * 64 * NT + threadIdx.x;
+#pragma unroll
+            for (int a = 0; a < 8; ++a)
+#pragma unroll
+                for (int b = 0; b < TN; ++b) acc[a][b] = first ? 0.f : sc[(a * TN + b) * NT];
+            for (int q = 0; q < steps; ++q) {
+                float(*Qs)[BNT + 4] = Qs2[stage];
+                simt::store_tile_regs<float, BNT>(Qs, qr, pb.Q.s0, pb.Q.s1);
+                __syncthreads();  // the chunk (first step) and this data tile are complete
+                // the next data tile in (chunk, pass, step) order
+                int64_t nk = c0 + q + 1, nj = j0;
+                if (q + 1 == steps) {
+                    nk = c0;
+                    nj = j0 + BNT;
+                    if (pass + 1 == pb.passes) {
+                        nk = c0 + steps;
+                        nj = 0;
+                    }
+                }
+                if (nk < ke)
+                    simt::load_tile_regs<float, BNT>(qr, Qp, pb.Q.s0, pb.Q.s1, pb.K, pb.N,
+                                                     nk * BK, nj);
+                const float(*Ps)[BMT + 4] = chunk + q * BK;
+#pragma unroll
+                for (int kk = 0; kk < BK; ++kk) {
+                    float a[8], b[TN];
+                    const float4 a0 = *reinterpret_cast<const float4 *>(&Ps[kk][ty * 4]);
+                    const float4 a1 = *reinterpret_cast<const float4 *>(&Ps[kk][BMT / 2 + ty * 4]);
+                    a[0] = a0.x; a[1] = a0.y; a[2] = a0.z; a[3] = a0.w;
+                    a[4] = a1.x; a[5] = a1.y; a[6] = a1.z; a[7] = a1.w;
+                    const float4 b0 = *reinterpret_cast<const float4 *>(&Qs[kk][tx * 4]);
+                    const float4 b1 = *reinterpret_cast<const float4 *>(&Qs[kk][BNT / 2 + tx * 4]);
+                    b[0] = b0.x; b[1] = b0.y; b[2] = b0.z; b[3] = b0.w;
+                    b[4] = b1.x; b[5] = b1.y; b[6] = b1.z; b[7] = b1.w;
+#pragma unroll
+                    for (int x = 0; x < 8; ++x)
+#pragma unroll
+                        for (int y = 0; y < TN; ++y) acc[x][y] = fmaf(a[x], b[y], acc[x][y]);
+                }
+                stage ^= 1;
+            }
+            if (!last) {
+#pragma unroll
+                for (int a = 0; a < 8; ++a)
+#pragma unroll
+                    for (int b = 0; b < TN; ++b) sc[(a * TN + b) * NT] = acc[a][b];
+                continue;
+            }
+            auto col_of = [&](int y) {
+                return j0 + (y < TN / 2 ? tx * (TN / 2) + y : BNT / 2 + tx * (TN / 2) + (y - TN / 2));
+            };
+            if (pb.splits == 1) {
+#pragma unroll
+                for (int x = 0; x < 8; ++x) {
+                    const int64_t i = row_of(x);
+                    if (i >= pb.M) continue;
+#pragma unroll
+                    for (int y = 0; y < TN; ++y) {
+                        const int64_t j = col_of(y);
+                        if (j >= pb.N) continue;
+                        float &o = pb.out[i * pb.os_i + j * pb.os_j];
+                        o = pb.beta == 0.f ? pb.alpha * acc[x][y]
+                                           : fmaf(pb.alpha, acc[x][y], pb.beta * o);
+                    }
+                }
+                continue;
+            }
+            float *mine = partial + pb.partial_off + (int64_t)split * pb.M * pb.N;
+#pragma unroll
+            for (int x = 0; x < 8; ++x) {
+                const int64_t i = row_of(x);
+                if (i >= pb.M) continue;
+#pragma unroll
+                for (int y = 0; y < TN; ++y) {
+                    const int64_t j = col_of(y);
+                    if (j < pb.N) mine[i * pb.N + j] = acc[x][y];
+                }
+            }
+            __threadfence();
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                const int done =
+                    atomicAdd(counters + pb.counter_off + tile * pb.passes + pass, 1);
+                *s_flag = done == pb.splits - 1;
+            }
+            __syncthreads();
+            if (*s_flag) {
+                __threadfence();
+                const float *base = partial + pb.partial_off;
+                for (int w = threadIdx.x; w < BMT * BNT; w += NT) {
+                    const int64_t i = i0 + w / BNT, j = j0 + w % BNT;
+                    if (i >= pb.M || j >= pb.N) continue;
+                    float sum = 0.f;
+                    for (int sp = 0; sp < pb.splits; ++sp)
+                        sum += __ldcg(base + ((int64_t)sp * pb.M + i) * pb.N + j);
+                    float &o = pb.out[i * pb.os_i + j * pb.os_j];
+                    o = pb.beta == 0.f ? pb.alpha * sum : fmaf(pb.alpha, sum, pb.beta * o);
+                }
+            }
+            __syncthreads();  // s_flag is rewritten by the next pass
+        }
+        __syncthreads();  // every pass is done with the chunk before it is regenerated
+    }
+    __syncthreads();  // the stages are free for the next item
+}
+
 template <bool kPair>
 __device__ __forceinline__ void batched_dispatch(const ProbDev &pb, const WorkItem &item,
                                                  float *Ps, float *Qs, float *partial,
                                                  int *counters, int *s_flag, uint32_t rank,
-                                                 const uint32_t (&remote)[2]) {
-    if (pb.bm == 64)
+                                                 const uint32_t (&remote)[2], float *scratch) {
+    if (!kPair && pb.passes > 0)
+        batched_rowblock(pb, item.tile, item.split, Ps, partial, counters, s_flag, scratch);
+    else if (pb.bm == 64)
         batched_tile<64, 256, 8, kPair>(pb, item.tile, item.split, Ps, Qs, partial, counters,
                                         s_flag, rank, remote);
     else if (pb.bn == 128)
@@ -241,7 +409,8 @@ __device__ __forceinline__ void batched_dispatch(const ProbDev &pb, const WorkIt
 __global__ void __launch_bounds__(NT, 2)
     batched_sketch_kernel(const ProbDev *__restrict__ probs, const WorkItem *__restrict__ items,
                           int64_t n_pairs, int64_t n_items, unsigned long long *work_counter,
-                          float *__restrict__ partial, int *__restrict__ counters) {
+                          float *__restrict__ partial, int *__restrict__ counters,
+                          float *__restrict__ scratch, int64_t scratch_stride) {
     extern __shared__ __align__(16) float bsm_tiles[];  // 2 operator stages, 2 data stages
     float *Ps = bsm_tiles;
     float *Qs = bsm_tiles + 2 * kPsFloats;
@@ -270,7 +439,8 @@ __global__ void __launch_bounds__(NT, 2)
             s_pb = probs[s_item.prob];
         }
         __syncthreads();
-        batched_dispatch<true>(s_pb, s_item, Ps, Qs, partial, counters, &s_flag, rank, remote);
+        batched_dispatch<true>(s_pb, s_item, Ps, Qs, partial, counters, &s_flag, rank, remote,
+                               nullptr);
         // both CTAs are done with this item's stages and with s_w before the next fetch
         simt::cluster_arrive();
         simt::cluster_wait();
@@ -285,7 +455,8 @@ __global__ void __launch_bounds__(NT, 2)
         }
         __syncthreads();
         if (s_w >= (unsigned long long)n_items) break;
-        batched_dispatch<false>(s_pb, s_item, Ps, Qs, partial, counters, &s_flag, rank, remote);
+        batched_dispatch<false>(s_pb, s_item, Ps, Qs, partial, counters, &s_flag, rank, remote,
+                                scratch + (int64_t)blockIdx.x * scratch_stride);
         __syncthreads();  // s_pb / s_item / s_w are rewritten by the next fetch
     }
 }
@@ -312,21 +483,25 @@ int resident_batched_ctas() {
     return per_sm * num_sms();
 }
 
-// Tile by a cost model, per k step of 16 and in thread instructions: FMAs over the whole
-// (padded) tile, plus generating its operator rows (Gaussian entries cost about ten times
-// uniform ones; halved when two column tiles share them in a cluster pair), plus staging the
-// data tile.  The 64 x 256 tile runs about 1.3x slower per FMA than the 128-row tiles (two
-// more shared-memory wavefronts per k step for its data rows, no register prefetch).
+// Tile for a problem the caller left to the library.  Gaussian operators take row blocks.
+// Uniform ones take the cheapest tile by a cost model, per k step of 16 and in thread
+// instructions: FMAs over the whole (padded) tile, plus generating its operator rows, plus
+// staging the data tile.  The 64 x 256 tile runs about 1.3x slower per FMA than the 128-row
+// tiles (two more shared-memory wavefronts per k step for its data rows, no register
+// prefetch).
 int default_config(int64_t m_rows, int64_t n, int family) {
+    // Gaussian operators: row blocks, whose entries are generated once for all columns
+    // (measured faster than every other configuration in each n class of 16..512, up to 1.25x
+    // for n > 256)
+    if (family == RBG_GAUSSIAN) return kRowBlock;
     int best = 1;
     double best_cost = 0.0;
-    for (int c = 1; c <= kConfigs; ++c) {
+    for (int c = 1; c < kRowBlock; ++c) {
         const double bm = kTileRows[c], bn = kTileWidth[c];
         const int64_t tiles_n = (n + kTileWidth[c] - 1) / kTileWidth[c];
-        const double gen = family == RBG_GAUSSIAN ? (tiles_n >= 2 ? 50.0 : 100.0) : 10.0;
+        const double gen = 10.0;  // uniform entries
         const double tiles = (double)((m_rows + kTileRows[c] - 1) / kTileRows[c]) * tiles_n;
-        const double cost =
-            tiles * (bm * bn * (bm == 64 ? 1.3 : 1.0) + bm * gen + 2.0 * bn);
+        const double cost = tiles * (bm * bn * (bm == 64 ? 1.3 : 1.0) + bm * gen + 2.0 * bn);
         if (c == 1 || cost < best_cost * 0.999) {
             best_cost = cost;
             best = c;
@@ -343,6 +518,7 @@ struct rbg_batched_plan_s {
     int64_t n_items = 0;
     int64_t n_pairs = 0;  // pair items at the front of the item list
     int grid = 0;
+    int64_t scratch_stride = 0;  // floats of row-block accumulator scratch per CTA
     bool stream_ordered = false;  // memory from cudaMallocAsync (freed on a stream)
     void *mem = nullptr;
     rbg::ProbDev *probs = nullptr;
@@ -351,6 +527,7 @@ struct rbg_batched_plan_s {
     int *counters = nullptr;
     size_t counter_bytes = 0;  // work counter + tile counters, zeroed before each run
     float *partial = nullptr;
+    float *scratch = nullptr;  // grid x scratch_stride floats
     size_t bytes = 0;
 };
 
@@ -361,9 +538,13 @@ using BatchedPlan = rbg_batched_plan_s;
 size_t align256(size_t x) { return (x + 255) / 256 * 256; }
 
 // Validate the problems and build the descriptors and the sorted work list (host only).
+// Columns an item of problem `pd` covers: its tile width, or every pass of a row block.
+int64_t item_width(const ProbDev &pd) { return pd.passes ? (int64_t)pd.passes * pd.bn : pd.bn; }
+
 void build_plan(int32_t layout, const rbg_batch_problem *problems, int64_t count,
                 int32_t tile_config, std::vector<ProbDev> &descs, std::vector<WorkItem> &items,
-                int64_t &n_pairs, int64_t &partial_floats, int64_t &tile_counters, int &grid) {
+                int64_t &n_pairs, int64_t &partial_floats, int64_t &tile_counters, int &grid,
+                int64_t &scratch_stride) {
     if (layout != RBG_COL_MAJOR && layout != RBG_ROW_MAJOR)
         fail(RBG_ERROR_INVALID_ARGUMENT, "layout must be RBG_COL_MAJOR or RBG_ROW_MAJOR");
     if (count < 0) fail(RBG_ERROR_INVALID_ARGUMENT, "count must be >= 0");
@@ -377,6 +558,7 @@ void build_plan(int32_t layout, const rbg_batch_problem *problems, int64_t count
     n_pairs = 0;
     partial_floats = 0;
     tile_counters = 0;
+    scratch_stride = 0;
     std::vector<int64_t> kt(count, 0);
     double total_cost = 0.0;
     descs.resize(count);
@@ -430,9 +612,16 @@ void build_plan(int32_t layout, const rbg_batch_problem *problems, int64_t count
         pd.bm = kTileRows[c];
         pd.bn = kTileWidth[c];
         pd.tiles_n = (pd.N + pd.bn - 1) / pd.bn;
+        if (c == kRowBlock) {
+            // one item per row block, covering every column in passes
+            pd.passes = (int32_t)pd.tiles_n;
+            pd.tiles_n = 1;
+            scratch_stride = std::max<int64_t>(scratch_stride, (int64_t)pd.passes * 64 * NT);
+        }
         kt[p] = (pd.K + BK - 1) / BK;
         const int64_t tiles = ((pd.M + pd.bm - 1) / pd.bm) * pd.tiles_n;
-        total_cost += (double)tiles * (double)std::max<int64_t>(kt[p], 1) * pd.bm * pd.bn;
+        total_cost += (double)tiles * (double)std::max<int64_t>(kt[p], 1) * pd.bm *
+                      (double)item_width(pd);
     }
     // split long K so that no item costs more than ~1/8 of a CTA's fair share (the device is
     // queried only after every argument has been checked)
@@ -442,7 +631,8 @@ void build_plan(int32_t layout, const rbg_batch_problem *problems, int64_t count
         ProbDev &pd = descs[p];
         if (pd.M == 0 || pd.N == 0) continue;
         const int64_t tiles = ((pd.M + pd.bm - 1) / pd.bm) * pd.tiles_n;
-        const int64_t cap_kt = std::max<int64_t>(32, (int64_t)(cap / ((double)pd.bm * pd.bn)));
+        const int64_t cap_kt =
+            std::max<int64_t>(32, (int64_t)(cap / ((double)pd.bm * (double)item_width(pd))));
         int64_t splits = kt[p] > 0 ? (kt[p] + cap_kt - 1) / cap_kt : 1;
         splits = std::min<int64_t>(splits, kMaxSplits);
         pd.kt_per_split = kt[p] > 0 ? (kt[p] + splits - 1) / splits : 0;
@@ -452,14 +642,14 @@ void build_plan(int32_t layout, const rbg_batch_problem *problems, int64_t count
             pd.partial_off = partial_floats;
             partial_floats += splits * pd.M * pd.N;
             pd.counter_off = tile_counters;
-            tile_counters += tiles;
+            tile_counters += tiles * std::max<int64_t>(1, pd.passes);
         }
         // split-major: the items running at the same time share a K range, so each slab of A
         // is read from HBM once and reused from L2 by every output tile that needs it
         // Gaussian operators over two or more column tiles: column tiles (2j, 2j + 1) of a row
         // block go to a cluster pair that shares the generated operator tiles (a last odd
         // column tile stays a single item)
-        pd.paired = pd.P.gen.family == RBG_GAUSSIAN && pd.tiles_n >= 2;
+        pd.paired = pd.P.gen.family == RBG_GAUSSIAN && pd.tiles_n >= 2 && pd.passes == 0;
         const int64_t tm = (pd.M + pd.bm - 1) / pd.bm;
         for (int64_t sp = 0; sp < splits; ++sp)
             for (int64_t it = 0; it < tm; ++it)
@@ -474,7 +664,8 @@ void build_plan(int32_t layout, const rbg_batch_problem *problems, int64_t count
     // longest processing time first; ties keep problem order (and the split-major order)
     auto lpt = [&](const WorkItem &a, const WorkItem &b) {
         const ProbDev &pa = descs[a.prob], &pb = descs[b.prob];
-        return (double)pa.kt_per_split * pa.bm * pa.bn > (double)pb.kt_per_split * pb.bm * pb.bn;
+        return (double)pa.kt_per_split * pa.bm * (double)item_width(pa) >
+               (double)pb.kt_per_split * pb.bm * (double)item_width(pb);
     };
     std::stable_sort(pairs.begin(), pairs.end(), lpt);
     std::stable_sort(items.begin(), items.end(), lpt);
@@ -501,7 +692,8 @@ void execute_plan(const BatchedPlan &pl, cudaStream_t s) {
     cfg.numAttrs = 1;
     RBG_CUDA(cudaLaunchKernelEx(&cfg, batched_sketch_kernel, (const ProbDev *)pl.probs,
                                 (const WorkItem *)pl.items, pl.n_pairs, pl.n_items,
-                                pl.work_counter, pl.partial, pl.counters));
+                                pl.work_counter, pl.partial, pl.counters, pl.scratch,
+                                pl.scratch_stride));
     RBG_LAUNCHED();
 }
 
@@ -514,7 +706,8 @@ void upload_plan(BatchedPlan &pl, const std::vector<ProbDev> &descs,
     const size_t ctr_b =
         align256(2 * sizeof(unsigned long long) + (size_t)tile_counters * sizeof(int));
     const size_t part_b = align256((size_t)partial_floats * sizeof(float));
-    pl.bytes = probs_b + items_b + ctr_b + part_b;
+    const size_t scr_b = align256((size_t)pl.grid * (size_t)pl.scratch_stride * sizeof(float));
+    pl.bytes = probs_b + items_b + ctr_b + part_b + scr_b;
     pl.stream_ordered = stream_ordered;
     if (stream_ordered)
         RBG_CUDA(cudaMallocAsync(&pl.mem, std::max<size_t>(pl.bytes, 256), s));
@@ -527,6 +720,7 @@ void upload_plan(BatchedPlan &pl, const std::vector<ProbDev> &descs,
     pl.counters = reinterpret_cast<int *>(pl.work_counter + 2);
     pl.counter_bytes = 2 * sizeof(unsigned long long) + (size_t)tile_counters * sizeof(int);
     pl.partial = reinterpret_cast<float *>(base + probs_b + items_b + ctr_b);
+    pl.scratch = reinterpret_cast<float *>(base + probs_b + items_b + ctr_b + part_b);
     pl.n_items = (int64_t)items.size();
     pl.n_pairs = n_pairs;
     if (!descs.empty())
@@ -558,7 +752,7 @@ extern "C" int rbg_batched_tile_shape(int32_t config, int32_t *rows, int32_t *co
         if (config < 1 || config > kConfigs)
             fail(RBG_ERROR_INVALID_ARGUMENT, "config must be one of the listed configurations");
         *rows = kTileRows[config];
-        *cols = kTileWidth[config];
+        *cols = config == kRowBlock ? 0 : kTileWidth[config];  // 0: every column
     });
 }
 
@@ -573,10 +767,12 @@ extern "C" int rbg_batched_plan_create(int32_t layout, const rbg_batch_problem *
         int64_t partial_floats = 0, tile_counters = 0;
         int grid = 0;
         int64_t n_pairs = 0;
+        int64_t scratch_stride = 0;
         build_plan(layout, problems, count, tile_config, descs, items, n_pairs, partial_floats,
-                   tile_counters, grid);
+                   tile_counters, grid, scratch_stride);
         auto *pl = new BatchedPlan();
         pl->grid = grid;
+        pl->scratch_stride = scratch_stride;
         try {
             upload_plan(*pl, descs, items, n_pairs, partial_floats, tile_counters, nullptr,
                         false);
@@ -622,11 +818,13 @@ extern "C" int rbg_lskge3_batched(int32_t layout, const rbg_batch_problem *probl
         int64_t partial_floats = 0, tile_counters = 0;
         int grid = 0;
         int64_t n_pairs = 0;
+        int64_t scratch_stride = 0;
         build_plan(layout, problems, count, tile_config, descs, items, n_pairs, partial_floats,
-                   tile_counters, grid);
+                   tile_counters, grid, scratch_stride);
         if (items.empty()) return;
         BatchedPlan pl;
         pl.grid = grid;
+        pl.scratch_stride = scratch_stride;
         upload_plan(pl, descs, items, n_pairs, partial_floats, tile_counters, s, true);
         execute_plan(pl, s);
         RBG_CUDA(cudaFreeAsync(pl.mem, s));

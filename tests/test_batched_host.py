@@ -8,10 +8,12 @@ import pytest
 def test_tile_configs(rb_host):
     from randblas_gb300 import batched
     cfgs = batched.tile_configs()
-    assert cfgs == [1, 2, 3, 4]
-    assert [batched.tile_shape(c) for c in cfgs] == [(128, 128), (128, 64), (128, 32), (64, 256)]
+    assert cfgs == [1, 2, 3, 4, 5]
+    # 5: 128-row blocks over every column (reported as 0 columns)
+    assert [batched.tile_shape(c) for c in cfgs] == [(128, 128), (128, 64), (128, 32), (64, 256),
+                                                     (128, 0)]
     with pytest.raises(rb_host.RandBLASError):
-        batched.tile_shape(5)
+        batched.tile_shape(6)
 
 
 def test_batched_argument_checks(rb_host):
@@ -34,6 +36,7 @@ def test_batched_argument_checks(rb_host):
     assert lib.rbg_batched_plan_create(1, arr, 1, 0, C.byref(h)) == _lib.ERROR_INVALID_ARGUMENT
     assert lib.rbg_batched_plan_create(7, arr, 1, 0, C.byref(h)) == _lib.ERROR_INVALID_ARGUMENT
     assert lib.rbg_batched_plan_create(1, arr, 1, 9, C.byref(h)) == _lib.ERROR_INVALID_ARGUMENT
+    assert lib.rbg_batched_plan_create(1, arr, 1, 6, C.byref(h)) == _lib.ERROR_INVALID_ARGUMENT
 
 
 def test_autotuner_choice_and_cache(rb_host, tmp_path):
@@ -43,8 +46,8 @@ def test_autotuner_choice_and_cache(rb_host, tmp_path):
     def measure(cfg, d, n, m, family):
         calls.append((cfg, n))
         # pretend narrow problems like narrow tiles, wide ones the 64 x 256 tile
-        return {1: 3.0, 2: 2.0, 3: 1.0, 4: 4.0}[cfg] if n <= 32 else \
-            {1: 2.0, 2: 3.0, 3: 4.0, 4: 1.0}[cfg]
+        return {1: 3.0, 2: 2.0, 3: 1.0, 4: 4.0, 5: 5.0}[cfg] if n <= 32 else \
+            {1: 2.0, 2: 3.0, 3: 4.0, 4: 1.0, 5: 5.0}[cfg]
 
     path = str(tmp_path / "tiles.json")
     t = batched.Autotuner(cache_path=path, measure=measure)

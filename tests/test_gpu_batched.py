@@ -34,6 +34,11 @@ SHAPES = [
     # operator tiles of interior row blocks, a last odd column tile on its own, a partial row
     # block
     (257, 300, 9000, 3, 8, 0, 1.0, 0.0, 1),
+    # row blocks over all columns (configuration 5): three passes over a partial last row
+    # block with offsets; two passes with beta and a split K; four passes with long K
+    (300, 300, 9000, 3, 8, 0, 1.0, 0.0, 5),
+    (257, 130, 20000, 0, 0, 1, 0.5, 1.5, 5),
+    (64, 512, 150000, 0, 0, 0, 1.0, 0.0, 5),
 ]
 
 
