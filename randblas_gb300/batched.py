@@ -168,7 +168,7 @@ class Autotuner:
 
     def __init__(self, cache_path: Optional[str] = None,
                  measure: Optional[Callable[[int, int, int, int, int], float]] = None,
-                 m_cap: int = 1 << 16):
+                 m_cap: int = 1 << 14):
         self.cache_path = cache_path or _default_cache_path()
         self._external = measure
         self.m_cap = m_cap
@@ -236,8 +236,10 @@ class Autotuner:
         from .api import DenseDist, RNGState, ScalarDist
         m = min(m, self.m_cap)
         sms = torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
-        tiles = math.ceil(d / 128) * math.ceil(n / 128)
-        count = max(2, min(64, math.ceil(4 * sms / max(tiles, 1))))
+        # enough problems that every configuration's items fill the device several times over,
+        # counting the coarsest (a row block over all columns is one item)
+        row_blocks = math.ceil(d / 128)
+        count = max(2, min(64, math.ceil(4 * sms / max(row_blocks, 1))))
         g = torch.Generator(device="cuda").manual_seed(0)
         probs = []
         for i in range(count):
