@@ -182,11 +182,13 @@ def main():
                     help="skip the 512-problem batching measurement (about 15 s)")
     ap.add_argument("--precision", default="bf16", choices=["bf16", "fp8"],
                     help="tensor-core operand precision for the lowp-small case")
+    ap.add_argument("--tile-config", type=int, default=5,
+                    help="batching tile configuration for the batched-small case")
     ap.add_argument("--m-log2", type=int, default=17,
                     help="log2 of m for the dense small cases")
     ap.add_argument("--case", default="full",
                     choices=["full", "lowp-small", "plain-small", "saso", "convert-small",
-                             "batched", "dense-fp64-small", "more-rows"],
+                             "batched", "batched-small", "dense-fp64-small", "more-rows"],
                     help="full: the benchmark line; the others run one kernel family on a "
                          "smaller case (for profilers) and print a short JSON line")
     args = ap.parse_args()
@@ -704,6 +706,31 @@ def bench_batched(torch, rb, device, args, stream, tune=True):
     return res
 
 
+def bench_batched_small(torch, rb, device, args, stream):
+    """The batching workload's dominant class at a size a full profiler capture handles: 48
+    Gaussian problems, n uniform in [257, 512], d = 4n, m = 2^15, all on tile configuration
+    --tile-config (5: row blocks)."""
+    import numpy as np
+    from randblas_gb300 import batched
+    rng = np.random.default_rng(0)
+    probs, state = [], rb.RNGState(4)
+    for _ in range(48):
+        n = int(rng.integers(257, 513))
+        d, m = 4 * n, 1 << 15
+        A = torch.randn(m, n, device=device)
+        S = rb.DenseSkOp(rb.DenseDist(d, m, rb.ScalarDist.Gaussian), state)
+        state = S.next_state
+        probs.append(batched.BatchProblem(S, A, torch.empty(d, n, device=device), d, n, m,
+                                          tile_config=args.tile_config))
+    flops = sum(2.0 * p.d * p.n * p.m for p in probs)
+    plan = batched.BatchedPlan(probs)
+    ms = event_time(torch, plan.execute, max(1, args.steps), args.warmup, stream)
+    plan.close()
+    return {"workload": "48 Gaussian sketches, n in [257, 512], d = 4n, m = 2^15",
+            "tile_config": args.tile_config, "ms": round(ms, 3),
+            "TFLOP/s": round(flops / ms / 1e9, 2)}
+
+
 def bench_e2e(torch, rb, lowp, have_lowp, S, A_host, args, stream, flops, device):
     """Same sketch through the public API with host buffers.  Precision path: A and B stay in
     pinned host memory and are passed to the call itself (its A conversion pass reads A over
@@ -748,6 +775,8 @@ def run_case(args):
         out.update(bench_saso(torch, rb, dev, args, stream, peaks()[0]))
     elif args.case == "batched":
         out.update(bench_batched(torch, rb, dev, args, stream))
+    elif args.case == "batched-small":
+        out.update(bench_batched_small(torch, rb, dev, args, stream))
     elif args.case == "more-rows":
         out.update(bench_more_rows(torch, rb, dev, stream, peaks()[0]))
     elif args.case == "dense-fp64-small":
