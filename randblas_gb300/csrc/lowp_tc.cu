@@ -1098,12 +1098,36 @@ void lowp_run_streamed(int64_t M, int64_t N, int64_t K, float alpha, const Dense
     const size_t stage_b = ((size_t)kStreamChunk * N * esz + 1023) / 1024 * 1024;
     const size_t at_b = std::max(pc.at_bytes, pt.at_bytes);
     const size_t part_b = std::max(pc.partial_bytes, pt.partial_bytes);
-    Scratch buf(2 * stage_b + at_b + part_b + 1024, s);
+    // B in host memory: the chunks accumulate into a device copy of it (B's orientation,
+    // tight pitch), which goes back once at the end.  Reading and writing host B for every
+    // chunk would take the host link's H2D direction from A's copies.
+    cudaPointerAttributes pb_attr{};
+    bool b_host = false;
+    if (cudaPointerGetAttributes(&pb_attr, out) == cudaSuccess)
+        b_host = pb_attr.type == cudaMemoryTypeHost;
+    else
+        cudaGetLastError();
+    const bool b_rows = os_j == 1;  // rows of B contiguous (else columns)
+    const size_t bdev_b = b_host ? ((size_t)M * N * sizeof(float) + 1023) / 1024 * 1024 : 0;
+    Scratch buf(2 * stage_b + at_b + part_b + bdev_b + 1024, s);
     uint8_t *base = reinterpret_cast<uint8_t *>(
         (reinterpret_cast<uintptr_t>(buf.ptr) + 1023) & ~uintptr_t(1023));
     uint8_t *Af[2] = {base, base + stage_b};
     uint8_t *At = base + 2 * stage_b;
     float *partial = reinterpret_cast<float *>(base + 2 * stage_b + at_b);
+    float *const out_host = out;
+    const int64_t os_i_host = os_i, os_j_host = os_j;
+    if (b_host) {
+        out = reinterpret_cast<float *>(base + 2 * stage_b + at_b + part_b);
+        os_i = b_rows ? N : 1;
+        os_j = b_rows ? 1 : M;
+        if (beta != 0.f)  // the first chunk reads beta * B
+            RBG_CUDA(cudaMemcpy2DAsync(
+                out, (size_t)(b_rows ? N : M) * sizeof(float), out_host,
+                (size_t)(b_rows ? os_i_host : os_j_host) * sizeof(float),
+                (size_t)(b_rows ? N : M) * sizeof(float), (size_t)(b_rows ? M : N),
+                cudaMemcpyHostToDevice, s));
+    }
     cudaEvent_t ready, copied[2], converted[2];
     RBG_CUDA(cudaEventCreateWithFlags(&ready, cudaEventDisableTiming));
     for (int q = 0; q < 2; ++q) {
@@ -1190,6 +1214,11 @@ void lowp_run_streamed(int64_t M, int64_t N, int64_t K, float alpha, const Dense
             RBG_LAUNCHED();
         }
     }
+    if (b_host)
+        RBG_CUDA(cudaMemcpy2DAsync(
+            out_host, (size_t)(b_rows ? os_i_host : os_j_host) * sizeof(float), out,
+            (size_t)(b_rows ? N : M) * sizeof(float), (size_t)(b_rows ? N : M) * sizeof(float),
+            (size_t)(b_rows ? M : N), cudaMemcpyDeviceToHost, s));
     RBG_CUDA(cudaEventDestroy(ready));
     for (int q = 0; q < 2; ++q) {
         RBG_CUDA(cudaEventDestroy(copied[q]));

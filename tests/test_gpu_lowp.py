@@ -131,6 +131,45 @@ def test_lowp_transposed_operator(rb, oracle, case):
     assert r1 <= bound, (case, r1)
 
 
+@pytest.mark.parametrize("lay", [1, 0])
+def test_lowp_host_a_and_b_streamed(rb, lay):
+    """A and B both in pinned host memory, K streamed in five chunks: the chunks accumulate into
+    a device copy of B (read once for beta, written back once), in either layout and with
+    leading-dimension padding, which stays untouched.  Same bound as against device buffers."""
+    import torch
+    from randblas_gb300 import lowp
+    d, n, m = 200, 96, 300000
+    S = rb.DenseSkOp(rb.DenseDist(d, m, rb.ScalarDist.Uniform), rb.RNGState(14))
+    g = torch.Generator(device="cuda").manual_seed(8)
+    Am = torch.randn(m, n, device="cuda", generator=g)
+    Bm = torch.randn(d, n, device="cuda", generator=g)
+    if lay == 1:
+        A, lda = Am.contiguous(), n
+        ldb = n + 5
+        Bbuf = torch.full((d, ldb), 7.0, device="cuda")
+        Bbuf[:, :n] = Bm
+    else:
+        A, lda = Am.T.contiguous(), m
+        ldb = d + 3
+        Bbuf = torch.full((n, ldb), 7.0, device="cuda")
+        Bbuf[:, :d] = Bm.T
+    B_dev = Bbuf.clone()
+    lowp.sketch_lowp(rb.Layout(lay), rb.Op.NoTrans, rb.Op.NoTrans, d, n, m, 0.5, S, 0, 0, A,
+                     lda, 0.25, B_dev.view(-1), ldb)
+    A_host = A.cpu().pin_memory()
+    B_host = Bbuf.cpu().pin_memory()
+    lowp.sketch_lowp(rb.Layout(lay), rb.Op.NoTrans, rb.Op.NoTrans, d, n, m, 0.5, S, 0, 0,
+                     A_host, lda, 0.25, B_host.view(-1), ldb)
+    torch.cuda.synchronize()
+    assert lowp.status() == 0
+    got, want = B_host.double(), B_dev.cpu().double()
+    inner = (slice(None), slice(0, n)) if lay == 1 else (slice(None), slice(0, d))
+    pad = (slice(None), slice(n, ldb)) if lay == 1 else (slice(None), slice(d, ldb))
+    rel = float((got[inner] - want[inner]).norm() / want[inner].norm())
+    assert rel <= 2e-5, rel
+    assert bool((got[pad] == 7.0).all())
+
+
 def test_lowp_workspace_and_errors(rb):
     import torch
     from randblas_gb300 import lowp
