@@ -11,13 +11,13 @@
 //     power-of-two scale of its (K slice, column).
 //  2. sketch: persistent clusters of CN CTAs (one per SM), 16 or 24 warps with fixed roles --
 //       warp 0      TMA producer: A tiles (512 n-rows x 64 bytes of k) into a 5-stage ring;
-//       warp 1      MMA issuer (one thread) and tensor-memory owner (512 columns);
+//       warp 1      MMA issuer (one elected lane issues) and tensor-memory owner (512 columns);
 //       warps 4-7   epilogue: tensor memory -> registers -> FP32 partial tile in HBM;
 //       warps 8-    S producers (8 or 16 warps) in 4 groups taking stages in turn:
-//                   Philox4x32-10 + transform
-//                   for their half of a 128-row S stage (the N-peer makes the other half and
-//                   copies it over with a bulk shared-memory copy), stored in the 64-byte
-//                   swizzled K-major layout the tensor core reads.
+//                   Philox4x32-10 (round keys from the kernel parameters) + transform for
+//                   their half of a 128-row S stage (the N-peer makes the other half and copies
+//                   it over with a bulk shared-memory copy), stored in the 64-byte swizzled
+//                   K-major layout the tensor core reads.
 //     A work unit is one 128 x 512 output tile over one slice of the K range; every unit's
 //     partial goes to its own slot, so the final sum has a fixed order.  S is never written
 //     to HBM.
