@@ -826,6 +826,7 @@ __global__ void __launch_bounds__(256) convert_a_fp8_kernel(const TA *__restrict
     constexpr int BKE = Elem<true>::BK;
     constexpr uintptr_t VEC_ALIGN = 4 * sizeof(TA) - 1;
     __shared__ float tile[64][129];
+    __shared__ float inv_s[128];  // 1 / scale of the tile's columns (K slice g)
     if (sk == 1 && sj != 1) {
         // direct: 16 consecutive k of one row j per thread
         const int64_t kq = kpad / 16;
@@ -867,14 +868,17 @@ __global__ void __launch_bounds__(256) convert_a_fp8_kernel(const TA *__restrict
                                    : 0.f;
             }
         }
-        __syncthreads();
-        // 128 rows j x 4 chunks of 16 k: one 16-byte store each (one K slice per tile, since
-        // slices are whole multiples of 64 k)
+        // one K slice per tile (slices are whole multiples of 64 k): each column's reciprocal
+        // scale once per tile, not once per 16-k chunk
         const int64_t g = k0 / k_per_group;
+        if (threadIdx.x < 128 && j0 + threadIdx.x < npad)
+            inv_s[threadIdx.x] = __fdiv_rn(1.0f, e4m3_scale(amax[g * npad + j0 + threadIdx.x]));
+        __syncthreads();
+        // 128 rows j x 4 chunks of 16 k: one 16-byte store each
         for (int w = threadIdx.x; w < 128 * 4; w += 256) {
             const int jj = w / 4, c = w % 4;
             if (j0 + jj >= npad) continue;
-            const float inv = __fdiv_rn(1.0f, e4m3_scale(amax[g * npad + j0 + jj]));
+            const float inv = inv_s[jj];
             float v[16];
 #pragma unroll
             for (int e = 0; e < 16; ++e) v[e] = tile[16 * c + e][jj] * inv;
