@@ -28,6 +28,9 @@ CASES = [
     (200, 77, 3001, 5, 6, 0, 0, 1, 1.0, 2.0),
     (140, 600, 1000, 7, 1, 1, 1, 1, -1.0, 0.0),
     (96, 40, 777, 0, 3, 1, 0, 0, 1.0, 0.5),
+    # uniform operator over three 512-column tiles (cluster pairs sharing operator rows, the
+    # 8-generator-warp form for BF16), column offset a multiple of 4, partial last tiles
+    (200, 1030, 3000, 3, 4, 0, 1, 1, 1.0, 0.0),
 ]
 
 
