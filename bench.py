@@ -188,7 +188,8 @@ def main():
                     help="log2 of m for the dense small cases")
     ap.add_argument("--case", default="full",
                     choices=["full", "lowp-small", "plain-small", "saso", "convert-small",
-                             "batched", "batched-small", "dense-fp64-small", "more-rows"],
+                             "batched", "batched-small", "dense-fp64-small", "more-rows",
+                             "autograd-small"],
                     help="full: the benchmark line; the others run one kernel family on a "
                          "smaller case (for profilers) and print a short JSON line")
     args = ap.parse_args()
@@ -472,6 +473,28 @@ def bench_autograd(torch, rb, device, stream, bf16_peak):
         if prec is not None and dt == torch.float32:
             out[name + "_graphed"] = autograd_graphed(torch, autograd, S, A, Bt, flops, stream)
     return out
+
+
+def bench_autograd_small(torch, rb, device, args, stream):
+    """The differentiation workload's BF16 forward + backward (Gaussian 2048 x m operator,
+    RNGState(5), A m x 512 FP32) at m = 2^m_log2, with the per-kernel device times."""
+    from randblas_gb300 import autograd
+    d, m, n = 2048, 1 << args.m_log2, 512
+    S = rb.DenseSkOp(rb.DenseDist(d, m, rb.ScalarDist.Gaussian), rb.RNGState(5))
+    g = torch.Generator(device=device).manual_seed(5)
+    A = torch.randn(m, n, device=device, generator=g).requires_grad_(True)
+    Bt = torch.randn(d, n, device=device, generator=g)
+
+    def step():
+        A.grad = None
+        ((autograd.sketch(S, A, precision="bf16") - Bt) ** 2).sum().backward()
+    rb.profile.enable(True)
+    ms = event_time(torch, step, args.steps, args.warmup, stream)
+    prof = rb.profile.read()
+    rb.profile.enable(False)
+    return {"d": d, "m": m, "n": n, "ms_fwd_bwd": round(ms, 4),
+            "TFLOP/s": round(4.0 * d * m * n / (ms * 1e-3) / 1e12, 1),
+            "kernels_ms": {k: round(v["ms"] / max(1, v["launches"]), 4) for k, v in prof.items()}}
 
 
 def autograd_graphed(torch, autograd, S, A, Bt, flops, stream):
@@ -779,6 +802,8 @@ def run_case(args):
         out.update(bench_batched_small(torch, rb, dev, args, stream))
     elif args.case == "more-rows":
         out.update(bench_more_rows(torch, rb, dev, stream, peaks()[0]))
+    elif args.case == "autograd-small":
+        out.update(bench_autograd_small(torch, rb, dev, args, stream))
     elif args.case == "dense-fp64-small":
         rb.profile.enable(True)
         out.update(bench_small_fp64(torch, rb, dev, stream))
