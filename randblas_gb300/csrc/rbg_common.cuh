@@ -115,14 +115,18 @@ __device__ __forceinline__ void boxmuller(uint32_t u0, uint32_t u1, float &first
 // (-pi, pi) and u01 in (0, 1], where their errors (about 1e-6 relative) are far below a BF16
 // ulp (3.9e-3 relative), so at most a BF16 rounding of the entry changes.  The uniform inputs
 // are the exact transforms (each an FMA whose product is exact: one rounding, as above).
+// The logarithm and square root take their flush-to-zero forms: u01 lies in [2^-33, 1] and
+// the square root's argument is 0 or at least 1e-7, so no subnormal ever reaches them, the
+// results are those of the plain forms, and the subnormal handling those forms carry (about
+// 6% of the Gaussian tensor-core producers' time) is gone.
 __device__ __forceinline__ float sqrt_approx(float x) {
     float r;
-    asm("sqrt.approx.f32 %0, %1;" : "=f"(r) : "f"(x));
+    asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
     return r;
 }
 __device__ __forceinline__ float lg2_approx(float x) {
     float r;
-    asm("lg2.approx.f32 %0, %1;" : "=f"(r) : "f"(x));
+    asm("lg2.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
     return r;
 }
 __device__ __forceinline__ void boxmuller_fast(uint32_t u0, uint32_t u1, float &first,
