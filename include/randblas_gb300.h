@@ -397,8 +397,9 @@ int rbg_lskge3_lowp_workspace(int32_t precision, int64_t d, int64_t n, int64_t m
  * A and B may be device memory or host memory the GPU can read (pinned/registered memory, or
  * any host memory where the device reports cudaDevAttrPageableMemoryAccess); B is then written
  * in place.  For BF16 with pinned A, K >= 2^18, op(A) row- or column-contiguous and no
- * workspace given, the call streams A: 2^16-row chunks are copied by the copy engine, converted
- * and sketched on three streams, so the transfer and the sketch overlap.  Otherwise the
+ * workspace given, the call streams A: 2^16-row chunks (the last 2^16 rows in quarters) are
+ * copied by the copy engine on a side stream while the call's stream converts and sketches the
+ * previous chunk, so the transfer and the sketch overlap.  Otherwise the
  * conversion pass reads A over the host link.  Pageable memory on systems without that access
  * is rejected with RBG_ERROR_INVALID_ARGUMENT. */
 int rbg_lskge3_lowp(int32_t precision, int32_t layout, int32_t opS, int32_t opA, int64_t d,

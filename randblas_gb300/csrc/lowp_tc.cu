@@ -31,6 +31,8 @@
 #include <algorithm>
 #include <mutex>
 #include <string>
+#include <utility>
+#include <vector>
 
 #include "rbg_internal.h"
 #include "tc_ptx.cuh"
@@ -1064,8 +1066,23 @@ CUtensorMap encode_at_map(const Plan &pl, const void *At) {
 // into B (beta for the first chunk, 1 after) with its operator columns (or rows) offset by
 // c * kStreamChunk.  The host link then sets the time instead of the sum of the transfer and
 // the sketch.  (Converting beside the sketch instead, on a small grid, made the sketch's
-// clusters wait for SMs and the whole step 30-50 % slower and erratic.)
+// clusters wait for SMs and the whole step 30-50 % slower and erratic.)  The last
+// kStreamChunk rows go in quarter chunks: the work left after the last copy (that chunk's
+// conversion and sketch) is then a quarter as long.
 constexpr int64_t kStreamChunk = 1 << 16;
+constexpr int64_t kStreamTail = kStreamChunk / 4;
+
+// (first row, rows) of each chunk of K rows
+std::vector<std::pair<int64_t, int64_t>> stream_chunks(int64_t K) {
+    std::vector<std::pair<int64_t, int64_t>> ch;
+    int64_t k0 = 0;
+    for (; K - k0 > kStreamChunk; k0 += kStreamChunk) ch.emplace_back(k0, kStreamChunk);
+    for (int64_t kc; k0 < K; k0 += kc) {
+        kc = std::min(kStreamTail, K - k0);
+        ch.emplace_back(k0, kc);
+    }
+    return ch;
+}
 
 bool lowp_streams(bool fp8, int64_t K, const void *A, const Strided &Q, const void *workspace) {
     if (fp8 || workspace || K < 4 * kStreamChunk || (Q.s1 != 1 && Q.s0 != 1)) return false;
@@ -1095,13 +1112,25 @@ void lowp_run_streamed(int64_t M, int64_t N, int64_t K, float alpha, const Dense
                        float beta, float *out, int64_t os_i, int64_t os_j, cudaStream_t s) {
     const cudaStream_t cps = copy_stream();
     const int sms = num_sms();
-    const int64_t nch = (K + kStreamChunk - 1) / kStreamChunk;
-    const Plan pc = make_plan(M, N, kStreamChunk, false);
-    const Plan pt = make_plan(M, N, K - (nch - 1) * kStreamChunk, false);  // last chunk
+    const auto chunks = stream_chunks(K);
+    const int64_t nch = (int64_t)chunks.size();
+    // one plan per chunk length (at most four distinct lengths)
+    std::vector<std::pair<int64_t, Plan>> plans;
+    plans.reserve(4);  // every length is planned below, before any reference is kept
+    auto plan_for = [&](int64_t kc) -> const Plan & {
+        for (const auto &q : plans)
+            if (q.first == kc) return q.second;
+        plans.emplace_back(kc, make_plan(M, N, kc, false));
+        return plans.back().second;
+    };
+    size_t at_b = 0, part_b = 0;
+    for (const auto &c : chunks) {
+        const Plan &q = plan_for(c.second);
+        at_b = std::max(at_b, q.at_bytes);
+        part_b = std::max(part_b, q.partial_bytes);
+    }
     const size_t esz = a_bf16 ? 2 : 4;
     const size_t stage_b = ((size_t)kStreamChunk * N * esz + 1023) / 1024 * 1024;
-    const size_t at_b = std::max(pc.at_bytes, pt.at_bytes);
-    const size_t part_b = std::max(pc.partial_bytes, pt.partial_bytes);
     // B in host memory: the chunks accumulate into a device copy of it (B's orientation,
     // tight pitch), which goes back once at the end.  Reading and writing host B for every
     // chunk would take the host link's H2D direction from A's copies.
@@ -1144,7 +1173,7 @@ void lowp_run_streamed(int64_t M, int64_t N, int64_t K, float alpha, const Dense
     const bool rows = Q.s1 == 1;  // op(A) rows contiguous (else columns)
     auto copy_chunk = [&](int64_t c) -> Strided {
         const int b = (int)(c & 1);
-        const int64_t k0 = c * kStreamChunk, kc = std::min(kStreamChunk, K - k0);
+        const int64_t k0 = chunks[c].first, kc = chunks[c].second;
         // Af[b] is free once chunk c - 2 has been converted
         if (c >= 2) RBG_CUDA(cudaStreamWaitEvent(cps, converted[b], 0));
         const uint8_t *src = static_cast<const uint8_t *>(Q.ptr) + (size_t)k0 * Q.s0 * esz;
@@ -1169,8 +1198,8 @@ void lowp_run_streamed(int64_t M, int64_t N, int64_t K, float alpha, const Dense
     Strided q_next = copy_chunk(0);
     for (int64_t c = 0; c < nch; ++c) {
         const int b = (int)(c & 1);
-        const Plan &pl = c + 1 < nch ? pc : pt;
-        const int64_t k0 = c * kStreamChunk, kc = std::min(kStreamChunk, K - k0);
+        const int64_t k0 = chunks[c].first, kc = chunks[c].second;
+        const Plan &pl = plan_for(kc);
         const Strided q_dev = q_next;
         if (c + 1 < nch) q_next = copy_chunk(c + 1);  // in flight during this chunk's work
         RBG_CUDA(cudaStreamWaitEvent(s, copied[b], 0));
