@@ -12,7 +12,9 @@
 //  2. sketch: persistent clusters of CN CTAs (one per SM), 16 or 24 warps with fixed roles --
 //       warp 0      TMA producer: A tiles (512 n-rows x 64 bytes of k) into a 5-stage ring;
 //       warp 1      MMA issuer (one elected lane issues) and tensor-memory owner (512 columns);
-//       warps 4-7   epilogue: tensor memory -> registers -> FP32 partial tile in HBM;
+//       warps 4-7   epilogue: tensor memory -> registers -> FP32 partial tile (or, with one
+//                   K slice, B itself), through a shared-memory staging buffer and tensor
+//                   stores where the layout allows (plain stores otherwise);
 //       warps 8-    S producers (8 or 16 warps) in 4 groups taking stages in turn:
 //                   Philox4x32-10 (round keys from the kernel parameters) + transform for
 //                   their half of a 128-row S stage (the N-peer makes the other half and copies
@@ -29,6 +31,7 @@
 #include <cuda_fp8.h>
 
 #include <algorithm>
+#include <cstring>
 #include <mutex>
 #include <string>
 #include <utility>
@@ -80,7 +83,15 @@ static_assert(GEN_GROUPS <= STAGES, "generator groups must not outnumber the sta
 // group gi synchronises on named barrier 1 + gi; the hardware has barriers 0 .. 15
 static_assert(GEN_GROUPS + 1 <= 16, "one named barrier per generator group");
 constexpr uint32_t TMEM_COLS = 512;
-constexpr int SMEM_BYTES = STAGES * (S_STAGE_BYTES + A_STAGE_BYTES) + 1024 /*align*/ + 256;
+// Epilogue staging for tensor stores: per epilogue warp two buffers of 32 rows x 16 FP32
+// columns (64-byte rows, 64-byte swizzle), so one store reads a buffer while the warp fills
+// the other.
+constexpr int EPI_COLS = 16;
+constexpr int EPI_BUF_BYTES = 32 * EPI_COLS * 4;               // 2 KiB
+constexpr int EPI_BUFS = 2;
+constexpr int EPI_STAGE_BYTES = 4 * EPI_BUFS * EPI_BUF_BYTES;  // 16 KiB
+constexpr int SMEM_BYTES =
+    STAGES * (S_STAGE_BYTES + A_STAGE_BYTES) + EPI_STAGE_BYTES + 1024 /*align*/ + 256;
 
 struct LowpParams {
     int64_t M, N, K;       // d, n, m
@@ -97,6 +108,10 @@ struct LowpParams {
     float *partial;        // [k_groups][M][N]
     const uint32_t *amax;  // FP8: [k_groups][npad] column maxima (float bits); else null
     int *err;
+    // 0: the epilogue writes with plain stores; 1: tensor stores of alpha * acc into out (one
+    // K slice, beta = 0, out_map over out); 2: tensor stores into the partial buffer (out_map
+    // over [k_groups][M][N])
+    int out_tma;
     // one K slice: the epilogue writes B = alpha * acc + beta * B itself (no partials, no
     // reduce pass)
     int direct;
@@ -337,6 +352,7 @@ __device__ __forceinline__ void produce_s_transposed(uint8_t *tile, const LowpPa
 template <int CN, int kMode, bool kFp8, int kGenWarps>
 __global__ void __launch_bounds__(GenLayout<kGenWarps>::THREADS, 1)
     sketch_tc_kernel(const __grid_constant__ CUtensorMap tmap_a,
+                     const __grid_constant__ CUtensorMap tmap_out,
                      const __grid_constant__ LowpParams p) {
     constexpr int BKE = Elem<kFp8>::BK;
     constexpr int PER_CHUNK = Elem<kFp8>::PER_CHUNK;
@@ -352,7 +368,8 @@ __global__ void __launch_bounds__(GenLayout<kGenWarps>::THREADS, 1)
         (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
     uint8_t *s_tiles = smem;                                 // STAGES x S_STAGE_BYTES
     uint8_t *a_tiles = smem + STAGES * S_STAGE_BYTES;        // STAGES x A_STAGE_BYTES
-    uint64_t *bars = reinterpret_cast<uint64_t *>(a_tiles + STAGES * A_STAGE_BYTES);
+    uint8_t *out_stage = a_tiles + STAGES * A_STAGE_BYTES;   // 4 warps x 2 x EPI_BUF_BYTES
+    uint64_t *bars = reinterpret_cast<uint64_t *>(out_stage + EPI_STAGE_BYTES);
     // full[s]: two arrivals (TMA thread, producing generator group) plus the bytes of the A
     // tile and, with CN = 2, of the peer's S rows; empty[s]: one MMA commit per cluster CTA
     uint64_t *full = bars;
@@ -375,6 +392,7 @@ __global__ void __launch_bounds__(GenLayout<kGenWarps>::THREADS, 1)
         tc::mbar_init(acc_empty, 4);
         tc::fence_barrier_init();
         tc::prefetch_tensormap(&tmap_a);
+        if (p.out_tma) tc::prefetch_tensormap(&tmap_out);
     }
     if (warp == 1) {
         tc::tmem_alloc(tmem_slot, TMEM_COLS);
@@ -517,6 +535,63 @@ __global__ void __launch_bounds__(GenLayout<kGenWarps>::THREADS, 1)
         // ---------------- epilogue: tensor memory -> FP32 partial tile
         const int q = warp - EPI_WARP0;  // tensor-memory lanes 32q .. 32q+31
         int64_t uc = 0;
+        if (p.out_tma) {
+            // tensor stores: 32 columns of tensor memory at a time, in two 16-column halves
+            // that each go registers -> a staging buffer (this lane's row, 64-byte swizzle) ->
+            // one tensor store issued by lane 0; tensor memory is handed back as soon as the
+            // last columns are loaded, while the stores drain.  (Loading 16 columns at a time
+            // measured 1.5% slower on the 2^18 x 512 output; a third buffer gained nothing.)
+            const uint32_t stage0 =
+                tc::smem_addr(out_stage) + (uint32_t)(q * EPI_BUFS * EPI_BUF_BYTES);
+            const uint32_t row_off = (uint32_t)lane * (EPI_COLS * 4);
+            const uint32_t sw = (uint32_t)((lane >> 1) & 3);
+            uint32_t cnt = 0;
+            for (int64_t u = cluster_id; u < p.units; u += num_clusters, ++uc) {
+                int64_t m0, n0, ks0, ks1;
+                const int64_t g = unit_tiles(u, m0, n0, ks0, ks1);
+                if (!tc::mbar_wait(acc_full, (uint32_t)(uc & 1), p.err, 512)) goto done;
+                tc::tc_fence_after();
+                const int y = (int)(m0 + 32 * q);
+#pragma unroll 1
+                for (int c = 0; c < BN / 32; ++c) {
+                    uint32_t r[32];
+                    tc::tmem_ld32(tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(c * 32), r);
+                    tc::tmem_ld_wait();
+                    if (n0 + c * 32 >= p.N) break;
+#pragma unroll
+                    for (int h = 0; h < 2; ++h) {
+                        const int64_t col = n0 + c * 32 + h * EPI_COLS;
+                        if (col >= p.N) break;
+                        float v[EPI_COLS];
+#pragma unroll
+                        for (int j = 0; j < EPI_COLS; ++j) {
+                            float x = __uint_as_float(r[h * EPI_COLS + j]);
+                            if (kFp8) x *= e4m3_scale(p.amax[g * p.npad + col + j]);
+                            v[j] = p.out_tma == 1 ? p.alpha * x : x;
+                        }
+                        const uint32_t buf = stage0 + cnt * EPI_BUF_BYTES;
+                        // the store issued from this buffer two halves ago has read it
+                        if (lane == 0) tc::bulk_wait_read<EPI_BUFS - 1>();
+                        __syncwarp();
+#pragma unroll
+                        for (int j = 0; j < EPI_COLS / 4; ++j)
+                            tc::sts_v4(buf + row_off + ((((uint32_t)j) ^ sw) << 4), v[4 * j],
+                                       v[4 * j + 1], v[4 * j + 2], v[4 * j + 3]);
+                        tc::fence_proxy_async_smem();
+                        __syncwarp();
+                        if (lane == 0) {
+                            if (p.out_tma == 1) tc::tma_store_2d(&tmap_out, buf, (int)col, y);
+                            else tc::tma_store_3d(&tmap_out, buf, (int)col, y, (int)g);
+                            tc::bulk_commit();
+                        }
+                        cnt ^= 1u;
+                    }
+                }
+                tc::tc_fence_before();
+                __syncwarp();
+                if (lane == 0) tc::mbar_arrive(acc_empty);
+            }
+        } else {
         for (int64_t u = cluster_id; u < p.units; u += num_clusters, ++uc) {
             int64_t m0, n0, ks0, ks1;
             const int64_t g = unit_tiles(u, m0, n0, ks0, ks1);
@@ -586,6 +661,7 @@ __global__ void __launch_bounds__(GenLayout<kGenWarps>::THREADS, 1)
             tc::tc_fence_before();
             __syncwarp();
             if (lane == 0) tc::mbar_arrive(acc_empty);
+        }
         }
     } else if (warp >= GEN_WARP0) {
         // ---------------- S producers: GEN_GROUPS groups, group gi takes the stages with
@@ -681,6 +757,8 @@ __global__ void __launch_bounds__(GenLayout<kGenWarps>::THREADS, 1)
         }
     }
 done:
+    // tensor stores still reading the staging buffers finish before the CTA exits
+    if (p.out_tma && warp >= EPI_WARP0 && warp < EPI_WARP0 + 4 && lane == 0) tc::bulk_wait_all();
     tc::tc_fence_before();
     __syncwarp();
     __syncthreads();
@@ -1018,28 +1096,31 @@ int resident_clusters(int cs) {
 }
 
 template <int CN, int kMode, bool kFp8, int kGenWarps>
-void launch_sketch(int clusters, const CUtensorMap &map, const LowpParams &p, cudaStream_t s) {
+void launch_sketch(int clusters, const CUtensorMap &map, const CUtensorMap &out_map,
+                   const LowpParams &p, cudaStream_t s) {
     set_smem_attr<CN, kMode, kFp8, kGenWarps>();
     cudaLaunchAttribute attr[1];
     cudaLaunchConfig_t cfg = cluster_config<CN>(clusters, GenLayout<kGenWarps>::THREADS, attr);
     cfg.stream = s;
-    RBG_CUDA(cudaLaunchKernelEx(&cfg, sketch_tc_kernel<CN, kMode, kFp8, kGenWarps>, map, p));
+    RBG_CUDA(cudaLaunchKernelEx(&cfg, sketch_tc_kernel<CN, kMode, kFp8, kGenWarps>, map, out_map,
+                                p));
     RBG_LAUNCHED();
 }
 
 // Cluster pairs sharing uniform BF16 operator rows that start on counter blocks take the
 // 8-generator-warp form; everything else 16 generator warps.
 template <int kMode, bool kFp8>
-void launch_for(const Plan &pl, const CUtensorMap &map, const LowpParams &p, cudaStream_t s) {
+void launch_for(const Plan &pl, const CUtensorMap &map, const CUtensorMap &out_map,
+                const LowpParams &p, cudaStream_t s) {
     const int clusters = (int)std::min<int64_t>(pl.units, resident_clusters(pl.cn));
     if constexpr (kMode == 1 && !kFp8) {
         if (pl.cn == 2 && p.gen.family == RBG_UNIFORM) {
-            launch_sketch<2, kMode, kFp8, 8>(clusters, map, p, s);
+            launch_sketch<2, kMode, kFp8, 8>(clusters, map, out_map, p, s);
             return;
         }
     }
-    if (pl.cn == 2) launch_sketch<2, kMode, kFp8, 16>(clusters, map, p, s);
-    else launch_sketch<1, kMode, kFp8, 16>(clusters, map, p, s);
+    if (pl.cn == 2) launch_sketch<2, kMode, kFp8, 16>(clusters, map, out_map, p, s);
+    else launch_sketch<1, kMode, kFp8, 16>(clusters, map, out_map, p, s);
 }
 
 
@@ -1056,6 +1137,59 @@ CUtensorMap encode_at_map(const Plan &pl, const void *At) {
         CU_TENSOR_MAP_SWIZZLE_64B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
         CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (cr != CUDA_SUCCESS) fail(RBG_ERROR_CUDA, "cuTensorMapEncodeTiled failed");
+    return map;
+}
+
+bool device_memory_here(const void *ptr) {
+    cudaPointerAttributes pa{};
+    if (cudaPointerGetAttributes(&pa, ptr) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    int dev = -1;
+    RBG_CUDA(cudaGetDevice(&dev));
+    return pa.type == cudaMemoryTypeDevice && pa.device == dev;
+}
+
+// The epilogue's tensor-store target, set in p.out_tma: with one K slice, B itself when
+// beta = 0 and B is device memory of this GPU with contiguous rows at a 16-byte pitch and a
+// 16-byte aligned base (2D map over [M][os_i]); with several slices, the partial buffer when N
+// is a multiple of 4 (3D map over [k_groups][M][N], so a box's rows past M are clipped rather
+// than written into the next slice).  Otherwise the epilogue keeps plain stores.
+CUtensorMap out_tensor_map(const Plan &pl, LowpParams &p) {
+    CUtensorMap map;
+    std::memset(&map, 0, sizeof map);
+    p.out_tma = 0;
+    const cuuint32_t box[3] = {(cuuint32_t)EPI_COLS, 32, 1};
+    const cuuint32_t estr[3] = {1, 1, 1};
+    CUresult cr;
+    int kind;
+    if (pl.groups == 1) {
+        if (p.beta != 0.f || p.os_j != 1 || (p.os_i & 3) != 0 ||
+            (reinterpret_cast<uintptr_t>(p.out) & 15) != 0 || !device_memory_here(p.out))
+            return map;
+        const cuuint64_t dims[2] = {(cuuint64_t)p.N, (cuuint64_t)p.M};
+        const cuuint64_t strides[1] = {(cuuint64_t)p.os_i * 4};
+        cr = tc::tensor_map_encoder()(&map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, p.out, dims,
+                                      strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                                      CU_TENSOR_MAP_SWIZZLE_64B, CU_TENSOR_MAP_L2_PROMOTION_NONE,
+                                      CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+        kind = 1;
+    } else {
+        if ((p.N & 3) != 0) return map;
+        const cuuint64_t dims[3] = {(cuuint64_t)p.N, (cuuint64_t)p.M, (cuuint64_t)pl.groups};
+        const cuuint64_t strides[2] = {(cuuint64_t)p.N * 4, (cuuint64_t)p.M * p.N * 4};
+        cr = tc::tensor_map_encoder()(&map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, p.partial, dims,
+                                      strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                                      CU_TENSOR_MAP_SWIZZLE_64B, CU_TENSOR_MAP_L2_PROMOTION_NONE,
+                                      CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+        kind = 2;
+    }
+    if (cr != CUDA_SUCCESS) {
+        std::memset(&map, 0, sizeof map);
+        return map;
+    }
+    p.out_tma = kind;
     return map;
 }
 
@@ -1230,12 +1364,13 @@ void lowp_run_streamed(int64_t M, int64_t N, int64_t K, float alpha, const Dense
         p.direct = pl.groups == 1;
         p.out = out; p.os_i = os_i; p.os_j = os_j;
         p.alpha = alpha; p.beta = c == 0 ? beta : 1.f;
+        const CUtensorMap out_map = out_tensor_map(pl, p);
         {
             ProfScope prof("lowp_sketch_bf16_tc", s);
             const int mode = (p.c0 % 4) != 0 ? 0 : r_on_i ? 1 : 2;
-            if (mode == 1) launch_for<1, false>(pl, map, p, s);
-            else if (mode == 2) launch_for<2, false>(pl, map, p, s);
-            else launch_for<0, false>(pl, map, p, s);
+            if (mode == 1) launch_for<1, false>(pl, map, out_map, p, s);
+            else if (mode == 2) launch_for<2, false>(pl, map, out_map, p, s);
+            else launch_for<0, false>(pl, map, out_map, p, s);
         }
         if (!p.direct) {
             ProfScope prof("lowp_reduce", s);
@@ -1329,19 +1464,20 @@ void lowp_run(bool fp8, int64_t M, int64_t N, int64_t K, float alpha, const Dens
     p.direct = pl.groups == 1;
     p.out = out; p.os_i = os_i; p.os_j = os_j;
     p.alpha = alpha; p.beta = beta;
+    const CUtensorMap out_map = out_tensor_map(pl, p);
     // fast producers: the operator's natural column offset is a multiple of 4, so chunks
     // (natural row follows i: mode 1) or i-quads (it follows k: mode 2) start on counter blocks
     const int mode = (c0 % 4) != 0 ? 0 : r_on_i ? 1 : 2;
     {
         ProfScope prof(fp8 ? "lowp_sketch_fp8_tc" : "lowp_sketch_bf16_tc", s);
         if (fp8) {
-            if (mode == 1) launch_for<1, true>(pl, map, p, s);
-            else if (mode == 2) launch_for<2, true>(pl, map, p, s);
-            else launch_for<0, true>(pl, map, p, s);
+            if (mode == 1) launch_for<1, true>(pl, map, out_map, p, s);
+            else if (mode == 2) launch_for<2, true>(pl, map, out_map, p, s);
+            else launch_for<0, true>(pl, map, out_map, p, s);
         } else {
-            if (mode == 1) launch_for<1, false>(pl, map, p, s);
-            else if (mode == 2) launch_for<2, false>(pl, map, p, s);
-            else launch_for<0, false>(pl, map, p, s);
+            if (mode == 1) launch_for<1, false>(pl, map, out_map, p, s);
+            else if (mode == 2) launch_for<2, false>(pl, map, out_map, p, s);
+            else launch_for<0, false>(pl, map, out_map, p, s);
         }
     }
     if (!p.direct) {

@@ -31,6 +31,9 @@ CASES = [
     # uniform operator over three 512-column tiles (cluster pairs sharing operator rows, the
     # 8-generator-warp form for BF16), column offset a multiple of 4, partial last tiles
     (200, 1030, 3000, 3, 4, 0, 1, 1, 1.0, 0.0),
+    # several K slices written to the partial buffer by tensor stores: d = 300 leaves a
+    # 32-row box reaching past the last row of each slice, n = 520 a 16-column box past n
+    (300, 520, 6000, 0, 0, 0, 1, 1, 1.0, 0.0),
 ]
 
 
@@ -92,6 +95,32 @@ def test_lowp(rb, oracle, case, prec):
     bound = 1e-3 if prec == "fp8" else (1e-4 if fam == 0 else 2e-5)
     assert r1 <= bound, (case, r1)
     assert r2 <= (1e-2 if prec == "bf16" else 6e-2), (case, r2)
+
+
+@pytest.mark.parametrize("prec", ["bf16", "fp8"])
+def test_lowp_tensor_store_padded_rows(rb, prec):
+    """One K slice with beta = 0 and B's rows at a pitch of n + 4: the epilogue writes B by
+    tensor stores whose boxes reach past row d and column n, which must be clipped there
+    (the pitch padding keeps its value).  The same call with beta != 0 takes plain stores;
+    both results agree to FP32 rounding."""
+    import torch
+    from randblas_gb300 import lowp
+    d, n, m, ldb = 200, 100, 1000, 104
+    S = rb.DenseSkOp(rb.DenseDist(d, m, rb.ScalarDist.Uniform), rb.RNGState(31))
+    g = torch.Generator(device="cuda").manual_seed(9)
+    A = torch.randn(m, n, device="cuda", generator=g)
+    precision = lowp.BF16 if prec == "bf16" else lowp.FP8_E4M3
+    B = torch.full((d + 3, ldb), 7.0, device="cuda")  # three rows past d as a guard
+    lowp.sketch_lowp(rb.Layout.RowMajor, rb.Op.NoTrans, rb.Op.NoTrans, d, n, m, 0.5, S, 0, 0,
+                     A, n, 0.0, B.view(-1), ldb, precision=precision)
+    Bp = torch.zeros((d, ldb), device="cuda")  # beta != 0 on zeros: the plain-store epilogue
+    lowp.sketch_lowp(rb.Layout.RowMajor, rb.Op.NoTrans, rb.Op.NoTrans, d, n, m, 0.5, S, 0, 0,
+                     A, n, 1.0, Bp.view(-1), ldb, precision=precision)
+    torch.cuda.synchronize()
+    assert lowp.status() == 0
+    assert bool((B[:d, n:] == 7.0).all()) and bool((B[d:] == 7.0).all())
+    rel = float((B[:d, :n] - Bp[:, :n]).norm() / Bp[:, :n].norm())
+    assert rel <= 1e-6, rel
 
 
 @pytest.mark.parametrize("case", [
