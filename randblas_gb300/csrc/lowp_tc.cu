@@ -592,76 +592,77 @@ __global__ void __launch_bounds__(GenLayout<kGenWarps>::THREADS, 1)
                 if (lane == 0) tc::mbar_arrive(acc_empty);
             }
         } else {
-        for (int64_t u = cluster_id; u < p.units; u += num_clusters, ++uc) {
-            int64_t m0, n0, ks0, ks1;
-            const int64_t g = unit_tiles(u, m0, n0, ks0, ks1);
-            if (!tc::mbar_wait(acc_full, (uint32_t)(uc & 1), p.err, 512)) goto done;
-            tc::tc_fence_after();
-            const int64_t row = m0 + 32 * q + lane;
-            float *dst = p.partial + (g * p.M + row) * p.N;
+            for (int64_t u = cluster_id; u < p.units; u += num_clusters, ++uc) {
+                int64_t m0, n0, ks0, ks1;
+                const int64_t g = unit_tiles(u, m0, n0, ks0, ks1);
+                if (!tc::mbar_wait(acc_full, (uint32_t)(uc & 1), p.err, 512)) goto done;
+                tc::tc_fence_after();
+                const int64_t row = m0 + 32 * q + lane;
+                float *dst = p.partial + (g * p.M + row) * p.N;
 #pragma unroll 1
-            for (int c = 0; c < BN / 32; ++c) {
-                uint32_t r[32];
-                tc::tmem_ld32(tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(c * 32), r);
-                tc::tmem_ld_wait();
-                const int64_t col = n0 + c * 32;
-                if (kFp8) {
-                    // undo the (K slice, column) scales of A (powers of two: exact)
-                    const uint32_t *am = p.amax + g * p.npad + col;
+                for (int c = 0; c < BN / 32; ++c) {
+                    uint32_t r[32];
+                    tc::tmem_ld32(tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(c * 32), r);
+                    tc::tmem_ld_wait();
+                    const int64_t col = n0 + c * 32;
+                    if (kFp8) {
+                        // undo the (K slice, column) scales of A (powers of two: exact)
+                        const uint32_t *am = p.amax + g * p.npad + col;
 #pragma unroll
-                    for (int v = 0; v < 32; ++v)
-                        r[v] = __float_as_uint(__uint_as_float(r[v]) * e4m3_scale(am[v]));
-                }
-                if (p.direct) {
-                    if (row < p.M && col < p.N) {
-                        float *o = p.out + row * p.os_i;
-                        if (col + 32 <= p.N && p.os_j == 1 &&
-                            ((reinterpret_cast<uintptr_t>(o + col)) & 15) == 0) {
+                        for (int v = 0; v < 32; ++v)
+                            r[v] = __float_as_uint(__uint_as_float(r[v]) * e4m3_scale(am[v]));
+                    }
+                    if (p.direct) {
+                        if (row < p.M && col < p.N) {
+                            float *o = p.out + row * p.os_i;
+                            if (col + 32 <= p.N && p.os_j == 1 &&
+                                ((reinterpret_cast<uintptr_t>(o + col)) & 15) == 0) {
 #pragma unroll
-                            for (int v = 0; v < 8; ++v) {
-                                float4 *o4 = reinterpret_cast<float4 *>(o + col + 4 * v);
-                                float4 b = make_float4(0.f, 0.f, 0.f, 0.f);
-                                if (p.beta != 0.f) b = *o4;
-                                float4 w;
-                                w.x = p.beta == 0.f ? p.alpha * __uint_as_float(r[4 * v])
-                                                    : fmaf(p.alpha, __uint_as_float(r[4 * v]), p.beta * b.x);
-                                w.y = p.beta == 0.f ? p.alpha * __uint_as_float(r[4 * v + 1])
-                                                    : fmaf(p.alpha, __uint_as_float(r[4 * v + 1]), p.beta * b.y);
-                                w.z = p.beta == 0.f ? p.alpha * __uint_as_float(r[4 * v + 2])
-                                                    : fmaf(p.alpha, __uint_as_float(r[4 * v + 2]), p.beta * b.z);
-                                w.w = p.beta == 0.f ? p.alpha * __uint_as_float(r[4 * v + 3])
-                                                    : fmaf(p.alpha, __uint_as_float(r[4 * v + 3]), p.beta * b.w);
-                                *o4 = w;
+                                for (int v = 0; v < 8; ++v) {
+                                    float4 *o4 = reinterpret_cast<float4 *>(o + col + 4 * v);
+                                    float4 b = make_float4(0.f, 0.f, 0.f, 0.f);
+                                    if (p.beta != 0.f) b = *o4;
+                                    const float a0 = __uint_as_float(r[4 * v]);
+                                    const float a1 = __uint_as_float(r[4 * v + 1]);
+                                    const float a2 = __uint_as_float(r[4 * v + 2]);
+                                    const float a3 = __uint_as_float(r[4 * v + 3]);
+                                    const bool b0 = p.beta == 0.f;
+                                    float4 w;
+                                    w.x = b0 ? p.alpha * a0 : fmaf(p.alpha, a0, p.beta * b.x);
+                                    w.y = b0 ? p.alpha * a1 : fmaf(p.alpha, a1, p.beta * b.y);
+                                    w.z = b0 ? p.alpha * a2 : fmaf(p.alpha, a2, p.beta * b.z);
+                                    w.w = b0 ? p.alpha * a3 : fmaf(p.alpha, a3, p.beta * b.w);
+                                    *o4 = w;
+                                }
+                            } else {
+#pragma unroll
+                                for (int v = 0; v < 32; ++v)
+                                    if (col + v < p.N) {
+                                        float &x = o[(col + v) * p.os_j];
+                                        const float a = __uint_as_float(r[v]);
+                                        x = p.beta == 0.f ? p.alpha * a
+                                                          : fmaf(p.alpha, a, p.beta * x);
+                                    }
                             }
+                        }
+                    } else if (row < p.M && col < p.N) {
+                        if (col + 32 <= p.N && (p.N & 3) == 0) {
+#pragma unroll
+                            for (int v = 0; v < 8; ++v)
+                                *reinterpret_cast<float4 *>(dst + col + 4 * v) = make_float4(
+                                    __uint_as_float(r[4 * v]), __uint_as_float(r[4 * v + 1]),
+                                    __uint_as_float(r[4 * v + 2]), __uint_as_float(r[4 * v + 3]));
                         } else {
 #pragma unroll
                             for (int v = 0; v < 32; ++v)
-                                if (col + v < p.N) {
-                                    float &x = o[(col + v) * p.os_j];
-                                    const float a = __uint_as_float(r[v]);
-                                    x = p.beta == 0.f ? p.alpha * a : fmaf(p.alpha, a, p.beta * x);
-                                }
+                                if (col + v < p.N) dst[col + v] = __uint_as_float(r[v]);
                         }
                     }
-                } else if (row < p.M && col < p.N) {
-                    if (col + 32 <= p.N && (p.N & 3) == 0) {
-#pragma unroll
-                        for (int v = 0; v < 8; ++v)
-                            *reinterpret_cast<float4 *>(dst + col + 4 * v) =
-                                make_float4(__uint_as_float(r[4 * v]), __uint_as_float(r[4 * v + 1]),
-                                            __uint_as_float(r[4 * v + 2]),
-                                            __uint_as_float(r[4 * v + 3]));
-                    } else {
-#pragma unroll
-                        for (int v = 0; v < 32; ++v)
-                            if (col + v < p.N) dst[col + v] = __uint_as_float(r[v]);
-                    }
                 }
+                tc::tc_fence_before();
+                __syncwarp();
+                if (lane == 0) tc::mbar_arrive(acc_empty);
             }
-            tc::tc_fence_before();
-            __syncwarp();
-            if (lane == 0) tc::mbar_arrive(acc_empty);
-        }
         }
     } else if (warp >= GEN_WARP0) {
         // ---------------- S producers: GEN_GROUPS groups, group gi takes the stages with
