@@ -774,12 +774,24 @@ def bench_e2e(torch, rb, lowp, have_lowp, S, A_host, args, stream, flops, device
                           1.0, S, A_dev, N_SK, 0.0, B_dev, N_SK)
         B_host.copy_(B_dev, non_blocking=True)
     # three warm-up steps: the first calls on a freshly pinned buffer can take 1.3-3x longer;
-    # up to ten timed steps (single calls of 60-110 ms appear now and then on the host link)
+    # up to ten timed steps (single calls of 60-110 ms appear now and then on the host link).
+    # The value is the mean over the steps; each step's own time is recorded beside it.
     steps = max(1, min(args.steps, 10))
-    ms = event_time(torch, step, steps, 3, stream)
+    for _ in range(3):
+        step()
+    torch.cuda.synchronize()
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(steps + 1)]
+    ev[0].record(stream)
+    for t in range(steps):
+        step()
+        ev[t + 1].record(stream)
+    torch.cuda.synchronize()
+    per = sorted(ev[t].elapsed_time(ev[t + 1]) for t in range(steps))
+    ms = ev[0].elapsed_time(ev[steps]) / steps
     return {"value": round(flops / (ms * 1e-3) / 1e12, 2), "unit": "TFLOP/s",
             "ms_per_step": round(ms, 3), "h2d_bytes_per_step": M_SK * N_SK * 4,
-            "d2h_bytes_per_step": D_SK * N_SK * 4}
+            "d2h_bytes_per_step": D_SK * N_SK * 4,
+            "step_ms_median": round(per[len(per) // 2], 3), "step_ms_max": round(per[-1], 3)}
 
 
 def run_case(args):
