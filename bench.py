@@ -30,9 +30,9 @@ sys.path.insert(0, ROOT)
 
 METRIC = "S·A sketch time and roofline fraction: BF16-TC fused vs FP32 plain, same GPU"
 # DRAM bytes per launch of the BF16 tensor-core sketch at the headline size, from one ncu capture
-# at m = 2^17 (358.6 MB read, 118.1 MB written) with the reads scaled by 8 to m = 2^20 (they
+# at m = 2^17 (344.7 MB read, 83.4 MB written) with the reads scaled by 8 to m = 2^20 (they
 # grow with m; the partial-sum writes do not).
-HEADLINE_TRAFFIC_BYTES = 8 * 358.6e6 + 118.1e6
+HEADLINE_TRAFFIC_BYTES = 8 * 344.7e6 + 83.4e6
 D_SK, M_SK, N_SK = 4096, 1 << 20, 1024
 SASO_D, SASO_M, SASO_N, SASO_K = 1024, 1 << 20, 256, 8
 
