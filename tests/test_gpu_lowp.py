@@ -247,12 +247,15 @@ def test_lowp_workspace_and_errors(rb):
 
 
 @pytest.mark.parametrize("prec", ["bf16", "fp8"])
-def test_lowp_host_buffers(rb, prec):
+@pytest.mark.parametrize("m,beta", [(9000, 0.25), (1500, 0.0)])
+def test_lowp_host_buffers(rb, prec, m, beta):
     """A and B in pinned host memory, passed to the call itself (the A conversion pass reads A
-    over the host link, B is written in place): the same bits as with device buffers."""
+    over the host link, B is written in place): the same bits as with device buffers.  With
+    m = 1500 (one K slice) and beta = 0 the device call writes B by tensor stores and the host
+    call by plain stores, so this also compares the two epilogues."""
     import torch
     from randblas_gb300 import lowp
-    d, n, m = 256, 192, 9000
+    d, n = 256, 192
     S = rb.DenseSkOp(rb.DenseDist(d, m, rb.ScalarDist.Gaussian), rb.RNGState(12))
     g = torch.Generator(device="cuda").manual_seed(4)
     A = torch.randn(m, n, device="cuda", generator=g)
@@ -260,11 +263,11 @@ def test_lowp_host_buffers(rb, prec):
     precision = lowp.BF16 if prec == "bf16" else lowp.FP8_E4M3
     B_dev = B0.clone()
     lowp.sketch_lowp(rb.Layout.RowMajor, rb.Op.NoTrans, rb.Op.NoTrans, d, n, m, 0.5, S, 0, 0, A,
-                     n, 0.25, B_dev, n, precision=precision)
+                     n, beta, B_dev, n, precision=precision)
     A_host = A.cpu().pin_memory()
     B_host = B0.cpu().pin_memory()
     lowp.sketch_lowp(rb.Layout.RowMajor, rb.Op.NoTrans, rb.Op.NoTrans, d, n, m, 0.5, S, 0, 0,
-                     A_host, n, 0.25, B_host, n, precision=precision)
+                     A_host, n, beta, B_host, n, precision=precision)
     torch.cuda.synchronize()
     assert lowp.status() == 0
     assert torch.equal(B_host, B_dev.cpu())
