@@ -169,9 +169,31 @@ __global__ void reduce_splits_kernel(int64_t M, int64_t N, int splits, const T *
 //  * otherwise (a natural row per k): one thread per counter block along the natural row,
 //    i.e. 4 consecutive outputs, walking k.
 template <typename T>
+__device__ __forceinline__ void load4(const T *q, int64_t qs0, bool vec, T out[4]) {
+    if (vec) {  // four consecutive, 16-byte aligned values
+        if constexpr (sizeof(T) == 4) {
+            const float4 w = __ldg(reinterpret_cast<const float4 *>(q));
+            out[0] = w.x; out[1] = w.y; out[2] = w.z; out[3] = w.w;
+        } else {
+            const double2 w0 = __ldg(reinterpret_cast<const double2 *>(q));
+            const double2 w1 = __ldg(reinterpret_cast<const double2 *>(q) + 1);
+            out[0] = w0.x; out[1] = w0.y; out[2] = w1.x; out[3] = w1.y;
+        }
+    } else {
+#pragma unroll
+        for (int l = 0; l < 4; ++l) out[l] = __ldg(q + l * qs0);
+    }
+}
+
+// Philox's round keys come precomputed in the parameters (rk); a lane's counter advances by
+// its stride instead of being recomputed from the entry's coordinates.  vec: Q has unit stride
+// and every counter block's four values start on a 16-byte boundary.
+template <typename T>
 __global__ void __launch_bounds__(256) gemv_gen_kernel(int64_t M, int64_t K, POperand P,
+                                                       const __grid_constant__ RoundKeys rk,
                                                        const T *__restrict__ Q, int64_t qs0,
-                                                       int64_t k_per_split, T *partial) {
+                                                       int vec, int64_t k_per_split,
+                                                       T *partial) {
     const DenseGen &g = P.gen;
     const int64_t kb = (int64_t)blockIdx.y * k_per_split;
     const int64_t ke = min(K, kb + k_per_split);
@@ -180,15 +202,27 @@ __global__ void __launch_bounds__(256) gemv_gen_kernel(int64_t M, int64_t K, POp
         const int lane = threadIdx.x & 31;
         if (i >= M) return;
         const int64_t R = P.r0 + i, cb = P.c0 + kb, ce = P.c0 + ke;  // natural columns
+        // blocks [b_in, b_out) hold four columns inside [cb, ce) each
+        const int64_t b_in = (cb + 3) / 4, b_out = ce / 4;
         T acc = (T)0;
-        for (int64_t b = cb / 4 + lane; 4 * b < ce; b += 32) {
+        int64_t b = cb / 4 + lane;
+        uint4 c = g.counter_of(R, b);
+        for (; 4 * b < ce; b += 32, c = ctr_add(c, 32)) {
             float v[4];
-            gen4(g.family, g.counter_of(R, b), g.key, v);
+            gen4(g.family, c, rk, v);
+            if (b >= b_in && b < b_out) {
+                T q[4];
+                load4(Q + (4 * b - P.c0) * qs0, qs0, vec != 0, q);
 #pragma unroll
-            for (int l = 0; l < 4; ++l) {
-                const int64_t C = 4 * b + l;
-                if (C >= cb && C < ce)
-                    acc = fma(finish_entry<T>(g.family, v[l]), __ldg(Q + (C - P.c0) * qs0), acc);
+                for (int l = 0; l < 4; ++l) acc = fma(finish_entry<T>(g.family, v[l]), q[l], acc);
+            } else {
+#pragma unroll
+                for (int l = 0; l < 4; ++l) {
+                    const int64_t C = 4 * b + l;
+                    if (C >= cb && C < ce)
+                        acc = fma(finish_entry<T>(g.family, v[l]), __ldg(Q + (C - P.c0) * qs0),
+                                  acc);
+                }
             }
         }
 #pragma unroll
@@ -199,9 +233,10 @@ __global__ void __launch_bounds__(256) gemv_gen_kernel(int64_t M, int64_t K, POp
         const int64_t i0 = 4 * b - P.c0;  // output of lane 0 of the block (may be negative)
         if (i0 >= M) return;
         T acc[4] = {(T)0, (T)0, (T)0, (T)0};
-        for (int64_t k = kb; k < ke; ++k) {
+        uint4 c = g.counter_of(P.r0 + kb, b);
+        for (int64_t k = kb; k < ke; ++k, c = ctr_add(c, (uint64_t)g.stride)) {
             float v[4];
-            gen4(g.family, g.counter_of(P.r0 + k, b), g.key, v);
+            gen4(g.family, c, rk, v);
             const T q = __ldg(Q + k * qs0);
 #pragma unroll
             for (int l = 0; l < 4; ++l) acc[l] = fma(finish_entry<T>(g.family, v[l]), q, acc[l]);
@@ -215,27 +250,40 @@ __global__ void __launch_bounds__(256) gemv_gen_kernel(int64_t M, int64_t K, POp
 template <typename T>
 void run_gemv(int64_t M, int64_t K, double alpha, const POperand &P, const Strided &Q,
               double beta, void *out, int64_t os_i, cudaStream_t s) {
-    const int64_t target = (int64_t)num_sms() * 2048 * 2;  // threads in flight
-    int64_t threads, splits;
-    if (P.r_on_i) {
-        threads = M * 32;
-        splits = std::max<int64_t>(1, std::min<int64_t>((target + threads - 1) / threads,
-                                                       (K + 4095) / 4096));
-    } else {
-        threads = (M + 3) / 4 + 1;
-        splits = std::max<int64_t>(1, std::min<int64_t>((target + threads - 1) / threads,
-                                                       (K + 63) / 64));
+    // threads of one K range: a warp per output (r_on_i), else a thread per counter block
+    const int64_t threads = P.r_on_i ? M * 32 : (M + 3) / 4 + 1;
+    const int64_t blocks = (threads + 255) / 256;
+    // K splits: at least one full wave of resident blocks, then the count whose last wave is
+    // fullest (ties to fewer splits), with K ranges of >= 4096 columns (r_on_i) or 64 rows
+    int per_sm = 0;
+    RBG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, gemv_gen_kernel<T>, 256, 0));
+    const int64_t slots = (int64_t)num_sms() * std::max(1, per_sm);
+    const int64_t max_splits = std::max<int64_t>(
+        1, std::min<int64_t>(P.r_on_i ? (K + 4095) / 4096 : (K + 63) / 64, 65535));
+    int64_t splits = 1;
+    double best = -1.0;
+    for (int64_t c = 1; c <= std::min<int64_t>(max_splits, 256); ++c) {
+        const int64_t ctas = blocks * c;
+        const int64_t waves = (ctas + slots - 1) / slots;
+        const double eff = (double)ctas / (double)(waves * slots);
+        if (eff > best + 1e-3) {
+            best = eff;
+            splits = c;
+        }
+        if (ctas >= 8 * slots && eff > 0.95) break;
     }
-    splits = std::min<int64_t>(splits, 65535);
     const int64_t k_per_split = (K + splits - 1) / splits;
     splits = (K + k_per_split - 1) / k_per_split;
     Scratch ws((size_t)splits * M * sizeof(T), s);
-    const int64_t blocks = (threads + 255) / 256;
     if (blocks > INT32_MAX) fail(RBG_ERROR_UNSUPPORTED, "sketch with n = 1: too many rows");
     {
         ProfScope prof("dense_sketch_gemv_generated", s);
+        // 16-byte aligned blocks: Q + (4 b - c0) on a 16-byte boundary for every b
+        const int vec = Q.s0 == 1 && ((reinterpret_cast<uintptr_t>(Q.ptr) -
+                                       (uintptr_t)(P.c0 % 4) * sizeof(T)) & 15) == 0;
         gemv_gen_kernel<T><<<dim3((unsigned)blocks, (unsigned)splits), 256, 0, s>>>(
-            M, K, P, static_cast<const T *>(Q.ptr), Q.s0, k_per_split, ws.as<T>());
+            M, K, P, round_keys(P.gen.key), static_cast<const T *>(Q.ptr), Q.s0, vec,
+            k_per_split, ws.as<T>());
         RBG_LAUNCHED();
     }
     const int grid_r = grid_stride_ctas(M, 256);

@@ -140,10 +140,6 @@ __device__ __forceinline__ uint4 ctr_add_u32(uint4 c, uint32_t v) {
     return c;
 }
 
-// uneg11 as one FMA: the product by 2^-31 is exact, so fma rounds once, like the reference.
-__device__ __forceinline__ float uneg11_fma(uint32_t x) {
-    return __fmaf_rn(__int2float_rn((int32_t)x), 0x1p-31f, 0x1p-32f);
-}
 
 // Four e4m3 values (round to nearest, saturating to +-448) in one word, first value lowest.
 __device__ __forceinline__ uint32_t pack_e4m3x4(float a, float b, float c, float d) {
@@ -187,10 +183,10 @@ __device__ __forceinline__ uint4 gen_chunk_aligned(int family, uint4 c, const Ro
 #pragma unroll
         for (int q = 0; q < E / 4; ++q) {
             const uint4 r = philox(q == 0 ? c : ctr_add_u32(c, (uint32_t)q), key);
-            v[4 * q] = uneg11_fma(r.x);
-            v[4 * q + 1] = uneg11_fma(r.y);
-            v[4 * q + 2] = uneg11_fma(r.z);
-            v[4 * q + 3] = uneg11_fma(r.w);
+            v[4 * q] = uneg11(r.x);
+            v[4 * q + 1] = uneg11(r.y);
+            v[4 * q + 2] = uneg11(r.z);
+            v[4 * q + 3] = uneg11(r.w);
         }
 #pragma unroll
         for (int e = 0; e < E; ++e) v[e] = __fmul_rn(v[e], 1.7320508075688772f);
@@ -278,10 +274,10 @@ __device__ __forceinline__ void gen4_finished(int family, uint4 c, const RoundKe
                                               float v[4]) {
     if (family == RBG_UNIFORM) {
         const uint4 r = philox(c, key);
-        v[0] = __fmul_rn(uneg11_fma(r.x), 1.7320508075688772f);
-        v[1] = __fmul_rn(uneg11_fma(r.y), 1.7320508075688772f);
-        v[2] = __fmul_rn(uneg11_fma(r.z), 1.7320508075688772f);
-        v[3] = __fmul_rn(uneg11_fma(r.w), 1.7320508075688772f);
+        v[0] = __fmul_rn(uneg11(r.x), 1.7320508075688772f);
+        v[1] = __fmul_rn(uneg11(r.y), 1.7320508075688772f);
+        v[2] = __fmul_rn(uneg11(r.z), 1.7320508075688772f);
+        v[3] = __fmul_rn(uneg11(r.w), 1.7320508075688772f);
     } else {
         gen4<true>(family, c, key, v);
     }

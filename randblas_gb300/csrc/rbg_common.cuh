@@ -81,14 +81,14 @@ __host__ __device__ __forceinline__ DevState to_dev(const rbg_state &s) {
 //   uneg11(x) = (int32)x * 2^-31 + 2^-32, u01(x) = x * 2^-32 + 2^-33 (float),
 //   boxmuller(u0, u1) = (sin(pi*uneg11(u0)) * r, cos(pi*uneg11(u0)) * r),
 //   r = sqrt(-2 log(u01(u1))).
-// The products by powers of two are exact, so the single rounding of each transform does
-// not depend on FMA contraction.
+// The products by powers of two are exact, so each transform rounds once, after the addition;
+// one FMA computes exactly that (the same value as a multiply followed by a rounded add).
 __device__ __forceinline__ float uneg11(uint32_t x) {
-    return __fadd_rn(__fmul_rn(__int2float_rn((int32_t)x), 0x1p-31f), 0x1p-32f);
+    return __fmaf_rn(__int2float_rn((int32_t)x), 0x1p-31f, 0x1p-32f);
 }
 
 __device__ __forceinline__ float u01(uint32_t x) {
-    return __fadd_rn(__fmul_rn(__uint2float_rn(x), 0x1p-32f), 0x1p-33f);
+    return __fmaf_rn(__uint2float_rn(x), 0x1p-32f, 0x1p-33f);
 }
 
 // Box-Muller for the plain paths and the explicit fills: sin, cos and log are evaluated in
@@ -131,11 +131,9 @@ __device__ __forceinline__ float lg2_approx(float x) {
 }
 __device__ __forceinline__ void boxmuller_fast(uint32_t u0, uint32_t u1, float &first,
                                                float &second) {
-    const float v0 = __fmaf_rn(__int2float_rn((int32_t)u0), 0x1p-31f, 0x1p-32f);  // uneg11
-    const float v1 = __fmaf_rn(__uint2float_rn(u1), 0x1p-32f, 0x1p-33f);         // u01
     float s, c;
-    __sincosf(__fmul_rn(3.14159265358979323846f, v0), &s, &c);
-    const float r = sqrt_approx(__fmul_rn(lg2_approx(v1), -1.3862943611198906f));
+    __sincosf(__fmul_rn(3.14159265358979323846f, uneg11(u0)), &s, &c);
+    const float r = sqrt_approx(__fmul_rn(lg2_approx(u01(u1)), -1.3862943611198906f));
     first = __fmul_rn(s, r);
     second = __fmul_rn(c, r);
 }

@@ -103,6 +103,32 @@ def test_sketch_vector_golden(rb, oracle):
             assert np.array_equal(to_host(y)[mask], y0[mask])
 
 
+@pytest.mark.parametrize("opS,co,incx", [(0, 0, 1), (0, 3, 1), (0, 4, 2), (1, 0, 1)])
+def test_sketch_vector_large(rb, opS, co, incx):
+    """sketch_vector with a uniform 512 x 2^18 operator (many K ranges, the interior fast path
+    with vector loads when x is contiguous and aligned, scalar loads otherwise, and the
+    transposed orientation), against the FP64 product of the filled operator."""
+    import torch
+    d, m = 512, 1 << 18
+    D = rb.DenseDist(d, m + co + 5, rb.ScalarDist.Uniform)
+    S = rb.DenseSkOp(D, rb.RNGState(21))
+    g = torch.Generator(device="cuda").manual_seed(21)
+    rows, cols = (d, m) if opS == 0 else (m, d)  # op(submat(S)); submat(S) is d x m
+    full = torch.empty(D.n_rows * D.n_cols, device="cuda")
+    rb.fill_dense(D, full, rb.RNGState(21))
+    Sfull = full.view(D.n_rows, D.n_cols) if D.natural_layout == rb.Layout.RowMajor else \
+        full.view(D.n_cols, D.n_rows).T
+    Ssub = Sfull[:d, co:co + m]
+    opSm = Ssub if opS == 0 else Ssub.T
+    x = torch.randn(cols * incx, device="cuda", generator=g)
+    y = torch.zeros(rows, device="cuda")
+    rb.sketch_vector(rb.Op(opS), d, m, 1.0, S, 0, co, x, incx, 0.0, y, 1)
+    ref = opSm.double() @ x[::incx].double()
+    rel = float((y.double() - ref).norm() / ref.norm())
+    # FP32 sums of up to 2^18 terms: about 6e-7 expected; a wrong entry or index gives O(1)
+    assert rel <= 2e-6, rel
+
+
 def test_gaussian_fp64_200x10000_left_sketch(rb, oracle):
     """The 200 x 10000 Gaussian FP64 left sketch of a 10000 x 50 column-major uniform[-1,1]
     matrix (Philox key 0, counter 0; the operator is seeded at the data's next state).  The
