@@ -136,7 +136,8 @@ __device__ __forceinline__ void batched_tile(const ProbDev &pb, int64_t tile, in
             const bool aligned = ((pb.P.r_on_i ? pb.P.c0 + k0 : pb.P.c0 + i0) & 3) == 0;
             if (aligned && i0 + BMT <= pb.M && k0 + BK <= pb.K)
                 simt::gen_p_tile_shared<BMT, 2>(
-                    remote, (uint32_t)(st * BK * (BMT + 4) * sizeof(float)), pb.P, i0, k0, rank);
+                    remote, (uint32_t)(st * BK * (BMT + 4) * sizeof(float)), pb.P, i0, k0, rank,
+                    pb.P.gen.key);
             else
                 simt::gen_p_tile<float, BMT>(Ps, pb.P, pb.M, pb.K, i0, k0);
         } else {

@@ -18,7 +18,9 @@ constexpr int kFillTR = 32;
 constexpr int kFillTC = 128;
 
 template <typename T>
-__global__ void __launch_bounds__(256) fill_dense_kernel(DenseGen g, int64_t R0, int64_t C0,
+__global__ void __launch_bounds__(256) fill_dense_kernel(DenseGen g,
+                                                         const __grid_constant__ RoundKeys rk,
+                                                         int64_t R0, int64_t C0,
                                                          int64_t nr, int64_t nc, int transpose_out,
                                                          T *__restrict__ out) {
     __shared__ T tile[kFillTR][kFillTC + 1];
@@ -36,7 +38,7 @@ __global__ void __launch_bounds__(256) fill_dense_kernel(DenseGen g, int64_t R0,
             const int64_t R = R0 + rb + lr;
             if (rb + lr >= nr) continue;
             float v[4];
-            gen4(g.family, g.counter_of(R, blk0 + b), g.key, v);
+            gen4(g.family, g.counter_of(R, blk0 + b), rk, v);
 #pragma unroll
             for (int l = 0; l < 4; ++l) {
                 const int64_t lc = (blk0 + b) * 4 + l - cabs;  // column inside the tile
@@ -272,11 +274,12 @@ void launch_fill_dense(int dtype, const DenseGen &g, int64_t R0, int64_t C0, int
     if (nr <= 0 || nc <= 0) return;
     const int64_t tiles = ((nr + kFillTR - 1) / kFillTR) * ((nc + kFillTC - 1) / kFillTC);
     const int grid = (int)std::min<int64_t>(tiles, (int64_t)num_sms() * 8);
+    const RoundKeys rk = round_keys(g.key);  // Philox's round keys in the parameters
     if (dtype == RBG_F32)
-        fill_dense_kernel<float><<<grid, 256, 0, s>>>(g, R0, C0, nr, nc, transpose_out,
+        fill_dense_kernel<float><<<grid, 256, 0, s>>>(g, rk, R0, C0, nr, nc, transpose_out,
                                                       (float *)out);
     else
-        fill_dense_kernel<double><<<grid, 256, 0, s>>>(g, R0, C0, nr, nc, transpose_out,
+        fill_dense_kernel<double><<<grid, 256, 0, s>>>(g, rk, R0, C0, nr, nc, transpose_out,
                                                        (double *)out);
     RBG_LAUNCHED();
 }

@@ -34,7 +34,8 @@ using simt::store_tile_regs;
 // instead of __syncthreads); results are the same bits as with CL = 1.  CL must divide BM / 4.
 template <typename T, bool GEN, int TN, int CL = 1>
 __global__ void __launch_bounds__(NT, (sizeof(T) == 4 || TN < BN) ? 2 : 1)
-    dense_sketch_kernel(int64_t M, int64_t N, int64_t K, POperand P, Strided Q, T alpha, T beta,
+    dense_sketch_kernel(int64_t M, int64_t N, int64_t K, POperand P,
+                        const __grid_constant__ RoundKeys rk, Strided Q, T alpha, T beta,
                         T *__restrict__ out, int64_t os_i, int64_t os_j, int64_t kt_per_split,
                         T *__restrict__ partial) {
     static_assert(CL == 1 || (GEN && sizeof(T) == 4), "clusters: FP32, generated operator");
@@ -81,11 +82,11 @@ __global__ void __launch_bounds__(NT, (sizeof(T) == 4 || TN < BN) ? 2 : 1)
                 if (aligned && i0 + BM <= M && k0 + BK <= K)
                     simt::gen_p_tile_shared<BM, CL>(
                         remote, (uint32_t)(buf * BK * (BM + 4) * sizeof(float)), P, i0, k0,
-                        rank);
+                        rank, rk);
                 else
-                    gen_p_tile<T>(Ps[buf], P, M, K, i0, k0);
+                    gen_p_tile<T, BM>(Ps[buf], P, M, K, i0, k0, rk);
             } else {
-                gen_p_tile<T>(Ps[buf], P, M, K, i0, k0);
+                gen_p_tile<T, BM>(Ps[buf], P, M, K, i0, k0, rk);
             }
         } else {
             // P(i, k) = buff[base + i*si + k*sk]
@@ -345,23 +346,26 @@ void launch_dense(int tn, dim3 grid, cudaStream_t s, int64_t M, int64_t N, int64
             const float a = (float)alpha, b = (float)beta;
             float *o = static_cast<float *>(out);
             float *pt = reinterpret_cast<float *>(partial);
+            const RoundKeys rk = round_keys(P.gen.key);
 #define RBG_DENSE_CLUSTER(TNV, CLV)                                                          \
     RBG_CUDA(cudaLaunchKernelEx(&cfg, dense_sketch_kernel<float, true, TNV, CLV>, M, N, K, P, \
-                                Q, a, b, o, os_i, os_j, kt_per_split, pt))
+                                rk, Q, a, b, o, os_i, os_j, kt_per_split, pt))
             if (tn == 64) RBG_DENSE_CLUSTER(64, 2);
             else RBG_DENSE_CLUSTER(BN, 2);
 #undef RBG_DENSE_CLUSTER
             return;
         }
     }
+    // Philox's round keys in the parameters (unused for a materialised operator)
+    const RoundKeys rk = round_keys(P.gen.key);
     if (tn == 64)
-        dense_sketch_kernel<T, GEN, 64><<<grid, NT, 0, s>>>(M, N, K, P, Q, (T)alpha, (T)beta,
-                                                            (T *)out, os_i, os_j, kt_per_split,
-                                                            partial);
+        dense_sketch_kernel<T, GEN, 64><<<grid, NT, 0, s>>>(M, N, K, P, rk, Q, (T)alpha,
+                                                            (T)beta, (T *)out, os_i, os_j,
+                                                            kt_per_split, partial);
     else
-        dense_sketch_kernel<T, GEN, BN><<<grid, NT, 0, s>>>(M, N, K, P, Q, (T)alpha, (T)beta,
-                                                            (T *)out, os_i, os_j, kt_per_split,
-                                                            partial);
+        dense_sketch_kernel<T, GEN, BN><<<grid, NT, 0, s>>>(M, N, K, P, rk, Q, (T)alpha,
+                                                            (T)beta, (T *)out, os_i, os_j,
+                                                            kt_per_split, partial);
 }
 
 template <typename T>

@@ -11,10 +11,13 @@ namespace simt {
 constexpr int BM = 128, BN = 128, BK = 16, NT = 256;  // tile M, max tile N, k step, threads
 
 // P tile, k-major: Ps[k][i] for i in [0, TM), k in [0, BK).  Entries outside M x K are 0.
-// Generated by THREADS threads of the CTA, this one being number tid.
-template <typename T, int TM, int THREADS>
+// Generated by THREADS threads of the CTA, this one being number tid, with Philox keyed by
+// `key`: the operator's key (uint2), or its round keys (RoundKeys) when the caller has them in
+// its kernel parameters.
+template <typename T, int TM, int THREADS, typename Key>
 __device__ __forceinline__ void gen_p_tile_by(T (*Ps)[TM + 4], const POperand &P, int64_t M,
-                                              int64_t K, int64_t i0, int64_t k0, int tid) {
+                                              int64_t K, int64_t i0, int64_t k0, int tid,
+                                              const Key &key) {
     const DenseGen &g = P.gen;
     if (P.r_on_i && ((P.c0 + k0) & 3) == 0 && i0 + TM <= M && k0 + BK <= K) {
         // interior tile, block-aligned: TM rows x BK / 4 whole counter blocks, no bounds
@@ -22,7 +25,7 @@ __device__ __forceinline__ void gen_p_tile_by(T (*Ps)[TM + 4], const POperand &P
         for (int w = tid; w < TM * (BK / 4); w += THREADS) {
             const int i = w / (BK / 4), b = w % (BK / 4);
             float v[4];
-            gen4(g.family, g.counter_of(P.r0 + i0 + i, b0 + b), g.key, v);
+            gen4(g.family, g.counter_of(P.r0 + i0 + i, b0 + b), key, v);
 #pragma unroll
             for (int l = 0; l < 4; ++l) Ps[4 * b + l][i] = finish_entry<T>(g.family, v[l]);
         }
@@ -33,7 +36,7 @@ __device__ __forceinline__ void gen_p_tile_by(T (*Ps)[TM + 4], const POperand &P
         for (int w = tid; w < BK * (TM / 4); w += THREADS) {
             const int k = w / (TM / 4), b = w % (TM / 4);
             float v[4];
-            gen4(g.family, g.counter_of(P.r0 + k0 + k, b0 + b), g.key, v);
+            gen4(g.family, g.counter_of(P.r0 + k0 + k, b0 + b), key, v);
 #pragma unroll
             for (int l = 0; l < 4; ++l) Ps[k][4 * b + l] = finish_entry<T>(g.family, v[l]);
         }
@@ -49,7 +52,7 @@ __device__ __forceinline__ void gen_p_tile_by(T (*Ps)[TM + 4], const POperand &P
             const int i = w / nb, b = w % nb;
             const bool row_ok = i0 + i < M;
             float v[4] = {0.f, 0.f, 0.f, 0.f};
-            if (row_ok) gen4(g.family, g.counter_of(P.r0 + i0 + i, b0 + b), g.key, v);
+            if (row_ok) gen4(g.family, g.counter_of(P.r0 + i0 + i, b0 + b), key, v);
 #pragma unroll
             for (int l = 0; l < 4; ++l) {
                 const int64_t k = (b0 + b) * 4 + l - cfirst;
@@ -67,7 +70,7 @@ __device__ __forceinline__ void gen_p_tile_by(T (*Ps)[TM + 4], const POperand &P
             const int k = w / nb, b = w % nb;
             const bool k_ok = k0 + k < K;
             float v[4] = {0.f, 0.f, 0.f, 0.f};
-            if (k_ok) gen4(g.family, g.counter_of(P.r0 + k0 + k, b0 + b), g.key, v);
+            if (k_ok) gen4(g.family, g.counter_of(P.r0 + k0 + k, b0 + b), key, v);
 #pragma unroll
             for (int l = 0; l < 4; ++l) {
                 const int64_t i = (b0 + b) * 4 + l - cfirst;
@@ -78,11 +81,16 @@ __device__ __forceinline__ void gen_p_tile_by(T (*Ps)[TM + 4], const POperand &P
     }
 }
 
-// gen_p_tile_by with all NT threads of the CTA.
+// gen_p_tile_by with all NT threads of the CTA, keyed by the operator's key or by `key`.
 template <typename T, int TM = BM>
 __device__ __forceinline__ void gen_p_tile(T (*Ps)[TM + 4], const POperand &P, int64_t M,
                                            int64_t K, int64_t i0, int64_t k0) {
-    gen_p_tile_by<T, TM, NT>(Ps, P, M, K, i0, k0, (int)threadIdx.x);
+    gen_p_tile_by<T, TM, NT>(Ps, P, M, K, i0, k0, (int)threadIdx.x, P.gen.key);
+}
+template <typename T, int TM, typename Key>
+__device__ __forceinline__ void gen_p_tile(T (*Ps)[TM + 4], const POperand &P, int64_t M,
+                                           int64_t K, int64_t i0, int64_t k0, const Key &key) {
+    gen_p_tile_by<T, TM, NT>(Ps, P, M, K, i0, k0, (int)threadIdx.x, key);
 }
 
 // ------------------------------------------------------------------ thread-block clusters
@@ -111,14 +119,22 @@ __device__ __forceinline__ void cluster_wait() {
     asm volatile("barrier.cluster.wait.acquire.aligned;" ::: "memory");
 }
 
+// *key when given, else the operator's own key (for callers without round keys).
+template <typename Key>
+__device__ __forceinline__ const Key &key_or(const Key *key, const uint2 &) { return *key; }
+__device__ __forceinline__ const uint2 &key_or(const uint2 *key, const uint2 &own) {
+    return key ? *key : own;
+}
+
 // An interior FP32 operator tile [BK][TM + 4] (whole, block-aligned counter blocks, as in
 // gen_p_tile's fast path) generated by the CL CTAs of a cluster together: CTA `rank`
 // generates 1/CL of it and stores every entry into all CL CTAs' tiles, at remote[q] + off in
-// CTA q.  The caller then runs a cluster barrier before any CTA reads the tile.
-template <int TM, int CL>
+// CTA q.  The caller then runs a cluster barrier before any CTA reads the tile.  `key` as in
+// gen_p_tile_by.
+template <int TM, int CL, typename Key>
 __device__ __forceinline__ void gen_p_tile_shared(const uint32_t (&remote)[CL], uint32_t off0,
                                                   const POperand &P, int64_t i0, int64_t k0,
-                                                  uint32_t rank) {
+                                                  uint32_t rank, const Key &key) {
     const DenseGen &g = P.gen;
     constexpr uint32_t kRowB = (TM + 4) * sizeof(float);
     if (P.r_on_i) {
@@ -127,7 +143,7 @@ __device__ __forceinline__ void gen_p_tile_shared(const uint32_t (&remote)[CL], 
         for (int w = threadIdx.x; w < ROWS * (BK / 4); w += NT) {
             const int i = (int)rank * ROWS + w / (BK / 4), b = w % (BK / 4);
             float v[4];
-            gen4(g.family, g.counter_of(P.r0 + i0 + i, b0 + b), g.key, v);
+            gen4(g.family, g.counter_of(P.r0 + i0 + i, b0 + b), key, v);
 #pragma unroll
             for (int l = 0; l < 4; ++l) {
                 const float e = finish_entry<float>(g.family, v[l]);
@@ -142,7 +158,7 @@ __device__ __forceinline__ void gen_p_tile_shared(const uint32_t (&remote)[CL], 
         for (int w = threadIdx.x; w < BK * BLOCKS; w += NT) {
             const int k = w / BLOCKS, b = (int)rank * BLOCKS + w % BLOCKS;
             float v[4];
-            gen4(g.family, g.counter_of(P.r0 + k0 + k, b0 + b), g.key, v);
+            gen4(g.family, g.counter_of(P.r0 + k0 + k, b0 + b), key, v);
 #pragma unroll
             for (int l = 0; l < 4; ++l) {
                 const float e = finish_entry<float>(g.family, v[l]);

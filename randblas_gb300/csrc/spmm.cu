@@ -1239,7 +1239,8 @@ __device__ __forceinline__ int row_in_iteration(const int64_t *rs, int kn, int64
 
 template <typename T, typename I>
 __global__ void __launch_bounds__(simt::NT)
-    gen_spmm_kernel(int64_t M, int64_t N, int64_t K, POperand P, const I *__restrict__ ptr,
+    gen_spmm_kernel(int64_t M, int64_t N, int64_t K, POperand P,
+                    const __grid_constant__ RoundKeys rk, const I *__restrict__ ptr,
                     const I *__restrict__ idx, const T *__restrict__ val, int64_t nnz,
                     int64_t k_per_split, T alpha, T beta, T *out, int64_t os_i, int64_t os_j,
                     T *partial) {
@@ -1285,7 +1286,7 @@ __global__ void __launch_bounds__(simt::NT)
         // 2. the 32 x 32 operator tile, one 16-wide half per 128 threads
         const int half = tid >> 7;
         simt::gen_p_tile_by<T, kGenRows, simt::NT / 2>(Ps + half * simt::BK, P, M, K, i0,
-                                                       k0 + half * simt::BK, tid & 127);
+                                                       k0 + half * simt::BK, tid & 127, rk);
         // 3. stage, then apply
         if (have) {
             st_j[tid] = (j >= 0 && j < N) ? (int32_t)j : -1;
@@ -1376,7 +1377,8 @@ void gen_spmm_rows(int64_t M, int64_t N, int64_t K, double alpha, const POperand
     {
         ProfScope prof("gen_spmm", s);
         kernel<<<dim3((unsigned)tiles, (unsigned)splits), simt::NT, smem, s>>>(
-            M, N, K, P, static_cast<const I *>(ptr), static_cast<const I *>(idx),
+            M, N, K, P, round_keys(P.gen.key), static_cast<const I *>(ptr),
+            static_cast<const I *>(idx),
             static_cast<const T *>(val), nnz, k_per_split, (T)alpha, (T)beta,
             static_cast<T *>(out), os_i, os_j, partial);
         RBG_LAUNCHED();
