@@ -127,18 +127,21 @@ __global__ void saso_kernel(DevState s, int64_t vec_nnz, int64_t dim_major, int6
 // 32-bit sampler (saso_column), 128 minor indices per block, with the block's entries staged
 // in shared memory so that the stores of all three arrays are contiguous.
 template <typename V, typename I>
-__global__ void __launch_bounds__(128) saso_fast_kernel(DevState s, int vec_nnz,
-                                                        uint32_t dim_major, int64_t dim_minor,
-                                                        I *idx_major, I *idx_minor, V *vals) {
+__global__ void __launch_bounds__(128) saso_fast_kernel(DevState s,
+                                                        const __grid_constant__ RoundKeys rk,
+                                                        int vec_nnz, uint32_t dim_major,
+                                                        int64_t dim_minor, I *idx_major,
+                                                        I *idx_minor, V *vals) {
     __shared__ I smaj[128 * kSasoFastMaxNnz];
     __shared__ V sval[128 * kSasoFastMaxNnz];
     for (int64_t base = blockIdx.x * 128ll; base < dim_minor; base += gridDim.x * 128ll) {
         const int64_t i = base + threadIdx.x;
         if (i < dim_minor)
-            saso_column(s, (uint64_t)i, vec_nnz, dim_major, [&](int j, uint32_t major, bool neg) {
-                smaj[threadIdx.x * vec_nnz + j] = (I)major;
-                sval[threadIdx.x * vec_nnz + j] = neg ? (V)-1 : (V)1;
-            });
+            saso_column(s, rk, (uint64_t)i, vec_nnz, dim_major,
+                        [&](int j, uint32_t major, bool neg) {
+                            smaj[threadIdx.x * vec_nnz + j] = (I)major;
+                            sval[threadIdx.x * vec_nnz + j] = neg ? (V)-1 : (V)1;
+                        });
         __syncthreads();
         const int64_t n = min((int64_t)128, dim_minor - base) * vec_nnz, off = base * vec_nnz;
         for (int64_t t = threadIdx.x; t < n; t += 128) {
@@ -292,7 +295,8 @@ void launch_fill_saso(int dtype, int itype, const DevState &seed, int64_t vec_nn
     int grid = grid_stride_ctas(dim_minor, threads);
     if (dim_major < (int64_t)UINT32_MAX && vec_nnz <= kSasoFastMaxNnz) {
 #define RBG_SASO_FAST(V, I)                                                                  \
-    saso_fast_kernel<V, I><<<grid, 128, 0, s>>>(seed, (int)vec_nnz, (uint32_t)dim_major,     \
+    saso_fast_kernel<V, I><<<grid, 128, 0, s>>>(seed, round_keys(seed.key), (int)vec_nnz,   \
+                                                (uint32_t)dim_major,                         \
                                                 dim_minor, (I *)idx_major, (I *)idx_minor,   \
                                                 (V *)vals)
         if (dtype == RBG_F32 && itype == RBG_I32) RBG_SASO_FAST(float, int32_t);

@@ -183,15 +183,16 @@ constexpr int kSasoFastMaxNnz = 16;
 // Minor index i of a SASO with vec_nnz <= kSasoFastMaxNnz: the partial Fisher-Yates shuffle
 // of sparse_skops.hh:51-106 with 32-bit arithmetic (exact: dim_major < 2^32, x0 % span <
 // span).  emit(j, major, negative) is called for j = 0 .. vec_nnz - 1 in order; counters run
-// seed + i * vec_nnz + j.
-template <typename F>
-__device__ __forceinline__ void saso_column(const DevState &s, uint64_t i, int vec_nnz,
-                                            uint32_t dim_major, F &&emit) {
+// seed + i * vec_nnz + j.  Philox is keyed by `key`: s.key, or its round keys when the caller
+// has them in its kernel parameters.
+template <typename Key, typename F>
+__device__ __forceinline__ void saso_column(const DevState &s, const Key &key, uint64_t i,
+                                            int vec_nnz, uint32_t dim_major, F &&emit) {
     uint32_t mp[kSasoFastMaxNnz], mv[kSasoFastMaxNnz];
     int msize = 0;
     const uint64_t off = i * (uint64_t)vec_nnz;
     for (int j = 0; j < vec_nnz; ++j) {
-        const uint4 r = philox(ctr_add(s.ctr, off + (uint64_t)j), s.key);
+        const uint4 r = philox(ctr_add(s.ctr, off + (uint64_t)j), key);
         const uint32_t ell = (uint32_t)j + r.x % (dim_major - (uint32_t)j);
         uint32_t vj = (uint32_t)j, vl = ell;
         int sj = -1, sl = -1;
@@ -215,6 +216,11 @@ __device__ __forceinline__ void saso_column(const DevState &s, uint64_t i, int v
         }
         emit(j, vl, (r.y & 1u) != 0u);
     }
+}
+template <typename F>
+__device__ __forceinline__ void saso_column(const DevState &s, uint64_t i, int vec_nnz,
+                                            uint32_t dim_major, F &&emit) {
+    saso_column(s, s.key, i, vec_nnz, dim_major, emit);
 }
 
 // ------------------------------------------------------------------ dense operators

@@ -531,6 +531,7 @@ bool rows_plan(int64_t M, int vec_nnz, int ew, RowsPlan &pl) {
 template <typename I>
 struct BucketArgs {
     DevState seed;  // generated operators
+    RoundKeys rk;   // seed.key's round keys
     int vec_nnz;
     uint32_t dim_major;
     int64_t co, K, ro;
@@ -587,7 +588,7 @@ __global__ void __launch_bounds__(kBucketThreads) saso_bucket_kernel(BucketArgs<
                 }
             }
         } else {
-            saso_column(a.seed, (uint64_t)(a.co + c), vec_nnz, a.dim_major,
+            saso_column(a.seed, a.rk, (uint64_t)(a.co + c), vec_nnz, a.dim_major,
                         [&](int j, uint32_t major, bool neg) {
                             const int64_t r = (int64_t)major - a.ro;
 #pragma unroll
@@ -979,6 +980,7 @@ void saso_rows(int64_t M, int64_t N, int64_t K, double alpha, const SparseOperan
     Scratch ovf_count, ovf;
     BucketArgs<I> a{};
     a.seed = Sp.seed;
+    a.rk = round_keys(Sp.seed.key);
     a.vec_nnz = (int)Sp.vec_nnz;
     a.dim_major = (uint32_t)Sp.dim_major;
     a.co = Sp.co; a.K = K; a.ro = Sp.ro;
