@@ -680,20 +680,28 @@ def bench_batched(torch, rb, device, args, stream, tune=True):
                        "[16, 512], d = 4n, FP32", "gflop": round(flops / 1e9, 1),
            "separate_plain_launches": {"ms": round(ms_sep, 2),
                                        "TFLOP/s": round(flops / ms_sep / 1e9, 2)}}
-    tuner = None
+    tuned_plan, tuner = None, None
     if tune:
+        # per-class choices, then checked against the library's choices on this batch
         cache = os.path.join(tempfile.mkdtemp(prefix="rbg_tiles_"), "tiles.json")
         tuner = batched.Autotuner(cache_path=cache)
         t0 = time.perf_counter()
         for p in probs:
-            tuner.choose(p.d, p.n, p.m, int(p.S.dist.family))
+            p.tile_config = 0
+        tuned_plan = tuner.tune_batch(probs)
         torch.cuda.synchronize()
         res["autotune_s"] = round(time.perf_counter() - t0, 1)
-    variants = [("default_tiles", None)] + ([("autotuned", tuner)] if tune else [])
-    for name, tn in variants:
-        for p in probs:
-            p.tile_config = 0
-        plan = batched.BatchedPlan(probs, tuner=tn)
+        tuned_cfg = [p.tile_config for p in probs]
+    variants = [("default_tiles", None)] + ([("autotuned", tuned_plan)] if tune else [])
+    for name, tp in variants:
+        if tp is None:
+            for p in probs:
+                p.tile_config = 0
+            plan = batched.BatchedPlan(probs)
+        else:
+            for p, c in zip(probs, tuned_cfg):
+                p.tile_config = c
+            plan = tp
         graph = plan.capture()
         ms = event_time(torch, graph.replay, steps, 1, stream)
         res[name] = {"ms": round(ms, 2), "TFLOP/s": round(flops / ms / 1e9, 2),

@@ -161,17 +161,20 @@ class Autotuner:
 
     A problem's class is (operator family, d, n rounded up to powers of two, round(log2 m)).
     The first time a class is seen on a device, one synthetic batch of that class (problems
-    enough to fill the device, N(0,1) data) runs once per tile configuration and the fastest
-    is kept.  Choices are stored in a JSON file keyed by device name, so later processes
-    reuse them.  ``measure(config, d, n, m, family) -> seconds`` can replace the device
-    timing (tests)."""
+    enough to fill the device, N(0,1) data, m capped at ``m_cap``) runs once per tile
+    configuration and once with the library's own choice (configuration 0).  A configuration
+    replaces the library's choice only when it is faster by more than ``margin`` (the
+    synthetic batch stands in for the real one, so small differences are not trusted).
+    Choices are stored in a JSON file keyed by device name, so later processes reuse them.
+    ``measure(config, d, n, m, family) -> seconds`` can replace the device timing (tests)."""
 
     def __init__(self, cache_path: Optional[str] = None,
                  measure: Optional[Callable[[int, int, int, int, int], float]] = None,
-                 m_cap: int = 1 << 14):
+                 m_cap: int = 1 << 15, margin: float = 0.03):
         self.cache_path = cache_path or _default_cache_path()
         self._external = measure
         self.m_cap = m_cap
+        self.margin = margin
         self._lock = threading.Lock()
         self.cache: Dict[str, Dict[str, int]] = {}
         if os.path.exists(self.cache_path):
@@ -207,10 +210,12 @@ class Autotuner:
         if hit is not None:
             return int(hit)
         if self._external is not None:
-            times = {c: self._external(c, d, n, m, family) for c in tile_configs()}
+            times = {c: self._external(c, d, n, m, family) for c in [0] + tile_configs()}
         else:
             times = self._time_all(d, n, m, family)
         best = min(times, key=lambda c: (times[c], c))
+        if times[best] > (1.0 - self.margin) * times[0]:
+            best = 0
         with self._lock:
             self.cache.setdefault(dev, {})[key] = best
             self._save()
@@ -220,6 +225,42 @@ class Autotuner:
         for p in problems:
             if p.tile_config == 0:
                 p.tile_config = self.choose(p.d, p.n, p.m, int(p.S.dist.family))
+
+    def tune_batch(self, problems: Sequence[BatchProblem], layout: Layout = Layout.RowMajor,
+                   runs: int = 2) -> "BatchedPlan":
+        """A plan for this batch: the per-class choices (``assign``) checked against the
+        library's own choices on the batch itself.  Both plans run ``runs`` times after one
+        warm-up, and the faster is returned (the other is closed).  The problems'
+        tile_config fields are left as the returned plan uses them."""
+        requested = [p.tile_config for p in problems]
+        self.assign(problems)
+        tuned_cfg = [p.tile_config for p in problems]
+        if all(c == r for c, r in zip(tuned_cfg, requested)):
+            return BatchedPlan(problems, layout)
+
+        def timed(plan: "BatchedPlan") -> float:
+            plan.execute()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            for _ in range(runs):
+                plan.execute()
+            e1.record()
+            torch.cuda.synchronize()
+            return e0.elapsed_time(e1)
+
+        tuned = BatchedPlan(problems, layout)
+        t_tuned = timed(tuned)
+        for p, r in zip(problems, requested):
+            p.tile_config = r
+        library = BatchedPlan(problems, layout)
+        t_library = timed(library)
+        if t_tuned < t_library:
+            library.close()
+            for p, c in zip(problems, tuned_cfg):
+                p.tile_config = c
+            return tuned
+        tuned.close()
+        return library
 
     def _save(self) -> None:
         try:
@@ -232,7 +273,8 @@ class Autotuner:
             pass
 
     def _time_all(self, d: int, n: int, m: int, family: int) -> Dict[int, float]:
-        """Seconds per run of one synthetic batch of the class, for every configuration."""
+        """Seconds per run of one synthetic batch of the class, for every configuration and
+        for the library's choice (0)."""
         from .api import DenseDist, RNGState, ScalarDist
         m = min(m, self.m_cap)
         sms = torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
@@ -247,7 +289,7 @@ class Autotuner:
             A = torch.randn(m, n, device="cuda", generator=g)
             probs.append(BatchProblem(S, A, torch.empty(d, n, device="cuda"), d, n, m))
         times = {}
-        for c in tile_configs():
+        for c in [0] + tile_configs():
             for p in probs:
                 p.tile_config = c
             plan = BatchedPlan(probs)

@@ -163,3 +163,31 @@ def test_benchmark_distribution_sampled(rb):
         rel = float((p.B.double() - want).norm() / want.norm())
         # FP32 sums over up to 2^18 terms, split differently by the two paths
         assert rel < 2e-5, (int(k), rel)
+
+
+def test_tune_batch_plan_matches_plain(rb, tmp_path):
+    """Autotuner.tune_batch on a small mixed batch (beta = 0, so repeated runs give the same
+    output): the plan it returns (per-class choices or the library's, whichever ran faster)
+    computes every problem to FP32 accuracy, and its problems keep the configurations it uses
+    (0 or a valid configuration)."""
+    import torch
+    from randblas_gb300 import batched
+    layout = rb.Layout.RowMajor
+    probs = _batch(rb, layout, seed=5)
+    for p in probs:
+        p.beta = 0.0
+        p.tile_config = 0
+    refs = [_plain(rb, p, layout, p.B.clone()) for p in probs]
+    tuner = batched.Autotuner(cache_path=str(tmp_path / "tiles.json"))
+    plan = tuner.tune_batch(probs, layout)
+    for p in probs:
+        p.B.fill_(float("nan"))
+    plan.execute()
+    torch.cuda.synchronize()
+    plan.close()
+    n_cfg = len(batched.tile_configs())
+    for k, (p, ref) in enumerate(zip(probs, refs)):
+        assert 0 <= p.tile_config <= n_cfg, (k, p.tile_config)
+        rel = float((p.B.double() - ref.double()).norm()) / max(float(ref.double().norm()),
+                                                                 1e-30)
+        assert rel < 2e-6, (k, rel)
