@@ -308,3 +308,34 @@ def test_lowp_host_a_streamed(rb, axis):
     assert launches == 7, launches
     rel = float((B_str.double() - B_dev.double()).norm() / B_dev.double().norm())
     assert rel <= 2e-5, rel
+
+
+@pytest.mark.parametrize("prec", ["bf16", "fp8"])
+@pytest.mark.parametrize("lay", [1, 0])
+def test_lowp_transposed_data(rb, prec, lay):
+    """op(A) = A^T: the data stored transposed and read with opA = Trans gives the same bits
+    as the untransposed data with opA = NoTrans (the conversion pass builds the same k-blocked
+    copy from either layout), in both layouts."""
+    import torch
+    from randblas_gb300 import lowp
+    d, n, m = 200, 96, 3000
+    S = rb.DenseSkOp(rb.DenseDist(d, m, rb.ScalarDist.Uniform), rb.RNGState(41))
+    g = torch.Generator(device="cuda").manual_seed(41)
+    Am = torch.randn(m, n, device="cuda", generator=g)          # op(A), m x n
+    precision = lowp.BF16 if prec == "bf16" else lowp.FP8_E4M3
+    row = lay == 1
+    # NoTrans: A itself in the layout; Trans: A^T (n x m) in the layout
+    A_nt, lda_nt = (Am.contiguous(), n) if row else (Am.T.contiguous(), m)
+    A_t, lda_t = (Am.T.contiguous(), m) if row else (Am.contiguous(), n)
+    shape_b = (d, n) if row else (n, d)
+    ldb = n if row else d
+    B1 = torch.zeros(shape_b, device="cuda")
+    B2 = torch.zeros(shape_b, device="cuda")
+    lowp.sketch_lowp(rb.Layout(lay), rb.Op.NoTrans, rb.Op.NoTrans, d, n, m, 1.0, S, 0, 0, A_nt,
+                     lda_nt, 0.0, B1, ldb, precision=precision)
+    lowp.sketch_lowp(rb.Layout(lay), rb.Op.NoTrans, rb.Op.Trans, d, n, m, 1.0, S, 0, 0, A_t,
+                     lda_t, 0.0, B2, ldb, precision=precision)
+    torch.cuda.synchronize()
+    assert lowp.status() == 0
+    assert torch.equal(B1, B2)
+    assert float(B1.abs().sum()) > 0.0
